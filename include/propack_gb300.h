@@ -1,0 +1,128 @@
+/*
+ * propack_gb300.h -- C ABI of the GB300 Lanczos-bidiagonalisation library.
+ *
+ * The two drivers keep PROPACK 2.1's Fortran argument lists and gfortran's
+ * calling convention (lower-case name + trailing underscore, every scalar by
+ * reference, one hidden size_t length per CHARACTER argument appended after
+ * the last argument, column-major arrays), so a Fortran program that links
+ * against libpropack_gb300.so instead of libdpropack runs unchanged.
+ *
+ * All arithmetic between APROD calls runs in CUDA kernels on the current
+ * device; the library keeps device mirrors of U, V and B and copies the
+ * results back into the caller's arrays on exit.  There is no CPU path: if
+ * no CUDA device is usable the drivers return INFO = PROPACK_ERR_CUDA.
+ */
+#ifndef PROPACK_GB300_H
+#define PROPACK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The user operator, exactly the reference's APROD (double/dlansvd.F:20-33):
+ *   SUBROUTINE APROD(TRANSA, M, N, X, Y, DPARM, IPARM)
+ * TRANSA = 'n': Y(1:M) = A X(1:N);  TRANSA = 't': Y(1:N) = A' X(1:M).
+ * X and Y are HOST arrays when the library calls a user APROD. */
+typedef void (*propack_aprod_t)(const char *transa, const int *m, const int *n,
+                                const double *x, double *y, double *dparm,
+                                int *iparm, size_t transa_len);
+
+/* Negative INFO codes added by this library (the reference's own codes are
+ * INFO = 0, INFO = J > 0 (invariant subspace of dimension J) and INFO = -1
+ * (not converged); double/dlansvd.F:79-83, double/dlansvd_irl.F:93-99). */
+#define PROPACK_ERR_ARG   (-2) /* an argument is out of range            */
+#define PROPACK_ERR_CUDA  (-3) /* a CUDA call failed (no device, OOM, ..) */
+#define PROPACK_ERR_HANDLE (-4) /* iparm does not hold a live operator   */
+#define PROPACK_ERR_WAIT  (-5) /* a bounded device-side wait gave up     */
+
+/* DLANSVD: k largest singular triplets, Krylov dimension grown up to kmax.
+ * Replaces double/dlansvd.F:1-3 (argument meaning: dlansvd.F:10-83).
+ * On exit *k holds the number of converged triplets and doption[2] the
+ * estimate of ||A|| (double/dlanbpro.F:547). */
+void dlansvd_(const char *jobu, const char *jobv, const int *m, const int *n,
+              int *k, const int *kmax, propack_aprod_t aprod,
+              double *U, const int *ldu, double *sigma, double *bnd,
+              double *V, const int *ldv, const double *tolin,
+              double *work, const int *lwork, int *iwork, const int *liwork,
+              double *doption, const int *ioption, int *info,
+              double *dparm, int *iparm, size_t jobu_len, size_t jobv_len);
+
+/* DLANSVD_IRL: neig triplets by implicitly restarted Lanczos
+ * bidiagonalisation with fixed dimension dim and p shifts per restart.
+ * Replaces double/dlansvd_irl.F:1-3 (argument meaning: :10-99).
+ * On exit *neig holds the number of converged triplets. */
+void dlansvd_irl_(const char *which, const char *jobu, const char *jobv,
+                  const int *m, const int *n, const int *dim, const int *p,
+                  int *neig, const int *maxiter, propack_aprod_t aprod,
+                  double *U, const int *ldu, double *sigma, double *bnd,
+                  double *V, const int *ldv, const double *tolin,
+                  double *work, const int *lwork, int *iwork,
+                  const int *liwork, double *doption, const int *ioption,
+                  int *info, double *dparm, int *iparm, size_t which_len,
+                  size_t jobu_len, size_t jobv_len);
+
+/* The counters of double/stat.h:6-15 for the calling host thread:
+ * clearstat replaces double/printstat.F:4-32, printstat :35-75. */
+void clearstat_(void);
+void printstat_(void);
+
+/* ---------------------------------------------------------------------
+ * Device-resident sparse operator (the library's own APROD).
+ *
+ * A = S + L diag(w) R'   with S (m x n), L (m x r), R (n x r) given as
+ * host CSR arrays (0-based, int64 row pointers, int32 column indices,
+ * float64 values); r = 0 for a plain CSR matrix.  The library copies them
+ * to the device and builds A' there.  A Lanczos driver that receives
+ * propack_gpu_csr_aprod_ as its APROD argument recognises it by address
+ * and applies the operator on the device with no host traffic; the
+ * operator's handle travels in iparm[0..1] (low, high 32 bits).  No
+ * counterpart exists in the reference: it supplies the APROD that the
+ * reference leaves to the user (double/dlanbpro.F:288, :420).
+ * Returns 0 and writes the handle, or a negative PROPACK_ERR_* code. */
+int propack_csr_create(int m, int n, const int64_t *s_rowptr,
+                       const int32_t *s_colidx, const double *s_val,
+                       int r, const int64_t *l_rowptr, const int32_t *l_colidx,
+                       const double *l_val, const int64_t *r_rowptr,
+                       const int32_t *r_colidx, const double *r_val,
+                       const double *w, int64_t *handle);
+int propack_csr_destroy(int64_t handle);
+/* Store a handle in iparm[0..1] (helper for C callers). */
+void propack_handle_to_iparm(int64_t handle, int *iparm);
+
+/* APROD-compatible entry: with HOST x, y it copies x in, applies the
+ * device operator named by iparm[0..1] and copies y out.  Passed as the
+ * APROD argument of dlansvd_/dlansvd_irl_ it is never called through the
+ * pointer: the drivers apply the operator on device vectors directly. */
+void propack_gpu_csr_aprod_(const char *transa, const int *m, const int *n,
+                            const double *x, double *y, double *dparm,
+                            int *iparm, size_t transa_len);
+
+/* ---------------------------------------------------------------------
+ * Per-thread call statistics of the last driver call on this host thread
+ * (the reference keeps these in COMMON /timing/; here they are
+ * thread-local so the library is reentrant).  No reference counterpart. */
+typedef struct {
+    int64_t nopx;      /* operator applications (matvecs)       */
+    int64_t nreorth;   /* reorthogonalisations                  */
+    int64_t ndot;      /* inner products in reorthogonalisation */
+    int64_t nrestart;  /* implicit restarts                     */
+    int64_t nbsvd;     /* bidiagonal SVDs                       */
+    int64_t nlandim;   /* final Lanczos dimension               */
+    double device_ms;  /* device time between entry and exit    */
+    double lanczos_ms; /* of which inside Lanczos steps         */
+    double bsvd_ms;    /* of which bidiagonal SVD + shifts      */
+    double gemm_ms;    /* of which restart / Ritz products      */
+    int64_t kernel_launches; /* kernels this library launched   */
+} propack_stats_t;
+void propack_get_stats(propack_stats_t *out);
+
+/* Last error message for the calling thread ("" if none). */
+const char *propack_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PROPACK_GB300_H */

@@ -1,0 +1,274 @@
+// pgb.cuh -- shared definitions of the GB300 Lanczos-bidiagonalisation
+// library: error handling, the device-resident Lanczos state, the device
+// CSR operator, and warp/CTA reduction helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+namespace pgb {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string &msg);
+#define PGB_CUDA(call)                                                              \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            ::pgb::set_error(std::string(#call " failed: ") + cudaGetErrorString(e_)); \
+            throw ::pgb::CudaFailure();                                             \
+        }                                                                           \
+    } while (0)
+struct CudaFailure {};
+struct ArgFailure {};
+struct WaitFailure {};
+
+// kernel launch accounting (for the stats struct)
+extern thread_local int64_t g_launches;
+#define PGB_LAUNCHED() (++::pgb::g_launches)
+
+// ------------------------------------------------------------- constants
+constexpr double EPS = 1.1102230246251565e-16;      // dlamch('e') = 2^-53
+constexpr double SFMIN = 2.2250738585072014e-308;   // dlamch('s')
+constexpr double KAPPA = 0.717;                     // dlanbpro.F:118
+constexpr double KAPPA_GETU0 = (double)0.717f;      // dgetu0.F:30 (REAL literal)
+constexpr double FUDGE = 1.01;                      // dlanbpro.F:117
+constexpr int NTRY = 5;                             // dreorth.F:64
+constexpr int BS = 256;                             // threads per CTA of the vector kernels
+constexpr int NNZ_PB = 2048;                        // nnz staged per CTA in the SpMV
+constexpr int ROWS_PB = 256;                        // rows per SpMV row block (<= BS)
+
+// ------------------------------------------------------- device operator
+// CSR with int32 row pointers (nnz < 2^31) and CSR-adaptive row blocks.
+struct Csr {
+    int rows = 0, cols = 0;   // cols counts the low-rank tail columns too
+    int ncol0 = 0;            // columns < ncol0 gather x; the rest gather z
+    int64_t nnz = 0;
+    int *ptr = nullptr;       // rows+1
+    int *idx = nullptr;       // nnz
+    double *val = nullptr;    // nnz
+    float *valf = nullptr;    // nnz (FP32 copy for the mixed-precision path)
+    int nblk = 0;             // row blocks
+    int *blk = nullptr;       // nblk+1 row boundaries
+    int segs = 0;             // thin matrices: segments per row for the split reduction
+};
+
+// A = S + L diag(w) R'.  fwd = [S | L] (m x (n+r)), adj = [S' | R]
+// (n x (m+r)); thin_r = R' (r x n), thin_l = L' (r x m).
+struct Operator {
+    int m = 0, n = 0, r = 0;
+    Csr fwd, adj, thin_r, thin_l;
+    double *w = nullptr;
+    double *zbuf = nullptr;      // r: the low-rank coefficients of the current product
+    double *zpart = nullptr;     // r * segs partials
+    unsigned int *zticket = nullptr;
+    int64_t id = 0;
+    int device = 0;
+};
+Operator *lookup_operator(int64_t handle);
+
+// ------------------------------------------------- Lanczos device state
+// Deferred scaling of a Lanczos vector (dsafescal, dsafescal.F:49-53):
+// mode 0 = none, 1 = multiply by val (= 1/alpha), 2 = divide by val
+// (|alpha| < sfmin), 3 = zero the vector (reorthogonalisation collapse,
+// dreorth.F:96-98).
+struct Pend {
+    int mode;
+    double val;
+};
+
+struct LbCtl {
+    // parameters of the current dlanbpro call
+    int m, n, k;            // rows, cols, target dimension
+    int ldu, ldv;
+    int icgs, ielr;
+    double delta, eta, epsn, epsn2;
+    // recurrence state (dlanbpro.F:123-126)
+    int j;                  // current step, 1-based
+    int full_reorth, force_reorth;
+    int ierr;
+    double alpha, beta, anorm, amax, numax, mumax, rnorm;
+    // per half-step phase state
+    int elr_active, elr_iter;
+    double elr_s;           // ELR inner product for the coming iteration
+    int reorth_active, reorth_iter, reorth_count;
+    double reorth_nrm0;
+    int nsel;               // columns selected for reorthogonalisation
+    int collapsed;          // the last reorthogonalisation zeroed the vector
+    int ndot_iter;          // inner products counted per CGS pass (dreorth.F:91, :164)
+    Pend pend_u, pend_v;    // deferred scaling of the newest u / v column
+    int pend_u_col, pend_v_col;
+    // suspension: the device met a case the enqueued sequence cannot finish
+    int status;             // 0 running, 1 suspended, 2 finished early (invariant subspace)
+    int susp_reason;        // 1 = getu0 needed (invariant subspace test), 2 = reorth iterations
+    int susp_side;          // 0 = V half, 1 = U half
+    int susp_j;
+    // statistics (double/stat.h)
+    long long nopx, nreorth, ndot;
+    // last-CTA tickets
+    unsigned int ticket;
+};
+
+// Everything a Lanczos kernel needs, passed by value.
+struct LbArgs {
+    LbCtl *ctl;
+    double *U, *V;          // device Lanczos vectors, column-major
+    int ldu, ldv;
+    double *balpha, *bbeta; // B(:,1), B(:,2)
+    double *mu, *nu;
+    int *index;             // reorthogonalisation intervals (1-based)
+    int *sel;               // expanded column list (0-based)
+    double *h;              // CGS coefficients
+    double *part_sq, *part_dot;   // per-CTA partial sums (nb)
+    double *part_cols;            // (kmax+1) * nb partial CGS dots, column c at c*nb
+    int nb;                 // CTAs of the vector kernels
+    int kmax;               // capacity of the column arrays
+    Csr fwd, adj;           // device operator (fwd = [S|L], adj = [S'|R])
+    const double *z;        // low-rank coefficients of the current product
+};
+
+// --------------------------------------------------------- helpers
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+// Deterministic CTA sum (fixed tree); all threads get the result.
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (w == 0) {
+        t = (lane < NT / 32) ? sh[lane] : 0.0;
+        t = warp_sum(t);
+        if (lane == 0) sh[0] = t;
+    }
+    __syncthreads();
+    t = sh[0];
+    __syncthreads();
+    return t;
+}
+template <int NT>
+__device__ __forceinline__ double block_max(double v, double *sh)
+{
+    v = warp_max(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (w == 0) {
+        t = (lane < NT / 32) ? sh[lane] : 0.0;
+        t = warp_max(t);
+        if (lane == 0) sh[0] = t;
+    }
+    __syncthreads();
+    t = sh[0];
+    __syncthreads();
+    return t;
+}
+
+// Last-CTA election after every CTA has published its partials.
+__device__ __forceinline__ bool last_cta(unsigned int *ticket)
+{
+    __shared__ bool amlast;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int t = atomicAdd(ticket, 1u);
+        amlast = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (amlast) {
+        __threadfence();
+        if (threadIdx.x == 0) *ticket = 0u;
+    }
+    return amlast;
+}
+
+__device__ __forceinline__ double apply_pend(double x, Pend p)
+{
+    switch (p.mode) {
+    case 1: return x * p.val;
+    case 2: return x / p.val;
+    case 3: return 0.0;
+    default: return x;
+    }
+}
+
+
+// ------------------------------------------------ small dense kernels
+struct AnaArgs {
+    const double *balpha, *bbeta;  // B of the Lanczos run
+    double *a1, *b1, *bnd;         // scratch: sigma(B), bounds (dim+1)
+    double *w;                     // 4*(dim+1) scratch
+    const LbCtl *ctl;              // rnorm of the run
+    double *sigma_out, *bnd_out;   // neig / k
+    int *nconv_out;
+    double *anorm_drv;             // the driver's local anorm
+    int dim, m, n, neig, kk;       // kk: k = dim - p (IRL) or k (lansvd)
+    int irl, small_side;
+    double tol;
+};
+
+struct SweepArgs {
+    double *balpha, *bbeta;   // modified in place
+    const double *a1, *bnd;   // from k_analyse
+    double *P, *Q;            // (dim+1)^2, dim^2
+    double *shifts;           // dim
+    double *w;                // 4*(dim+1)
+    LbCtl *ctl;               // rnorm <- beta_k, nrestart counted by the host
+    int dim, k, neig, small_side;
+    double min_relgap;
+};
+
+struct RitzArgs {
+    const double *balpha, *bbeta;
+    double *D, *E;      // dim+1 scratch copies
+    double *Mt;         // (dim+1)^2 : Q' of dbdqr
+    double *P;          // dim^2 : left vectors of R
+    double *Qt;         // dim^2 : right vectors' transpose
+    double *w;          // 4*(dim+1)
+    int dim, m, n;
+};
+
+void launch_analyse(const AnaArgs &a, cudaStream_t s);
+void launch_sweeps(const SweepArgs &a, cudaStream_t s);
+void launch_ritz_prep(const RitzArgs &a, cudaStream_t s);
+void gemm(int mr, int nc, int kk, const double *A, int lda, bool ta, const double *B, int ldb, bool tb, double *C,
+          int ldc, cudaStream_t s);
+void copy_cols(const double *src, int lds, double *dst, int ldd, int rows, int cols, cudaStream_t s);
+
+// ------------------------------------------------ Lanczos step enqueue
+void lb_set_smem_limits(int kmax);
+void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int ielr, int ntry_spec,
+                     bool host_product, cudaStream_t s);
+void lb_enqueue_cgs_more(const LbArgs &a, int side, int j, int passes, cudaStream_t s);
+void lb_enqueue_flush(const LbArgs &a, cudaStream_t s);
+void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s);
+int64_t handle_from_iparm(const int *iparm);
+const char *last_error();
+
+// --------------------------------------------------------- host helpers
+struct Dev {
+    int device = 0;
+    int sms = 0;
+    int nb = 0;            // CTAs for the streaming kernels
+};
+const Dev &device_info();
+
+// operator application on device vectors (no Lanczos fusion)
+void op_apply(const Operator &op, bool trans, const double *x, double *y, cudaStream_t s);
+
+}  // namespace pgb

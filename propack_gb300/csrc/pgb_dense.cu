@@ -1,0 +1,640 @@
+// pgb_dense.cu -- the small dense part of the IRL/Ritz machinery, on device:
+//
+//   k_analyse      dbdqr + bidiagonal QR SVD (values + last row of the left
+//                  vectors) + error bounds + drefinebounds + convergence
+//                  count (double/dlansvd_irl.F:218-290, dlansvd.F:192-236)
+//   k_irl_sweeps   exact-shift selection and dbsvdstep sweeps accumulating
+//                  P and Q (dlansvd_irl.F:304-363)
+//   k_ritz_prep    dbdqr with Q' + full SVD of R (the role of dbdsdc in
+//                  double/dritzvec.F:116-124)
+//   k_gemm         C = op(A) op(B) in FP64 for the restart and Ritz
+//                  products (dlansvd_irl.F:371-398, dritzvec.F:130-198)
+//
+// The bidiagonal SVD is one CTA: thread 0 runs the implicit zero-shift /
+// shifted QR iteration (Demmel & Kahan 1990; the algorithm of LAPACK
+// dbdsqr) and records each sweep's rotation chain in shared memory; the
+// whole CTA then applies the chain to the singular-vector matrices, one row
+// (or column) per thread.
+#include "pgb.cuh"
+
+namespace pgb {
+
+// --------------------------------------------------------- scalar helpers
+// plane rotation [c s; -s c][f; g] = [r; 0]; cosine made positive when
+// |f| > |g| (the dlartg convention)
+__device__ __forceinline__ void lartg(double f, double g, double &c, double &s, double &r)
+{
+    if (g == 0.0) { c = 1.0; s = 0.0; r = f; return; }
+    if (f == 0.0) { c = 0.0; s = 1.0; r = g; return; }
+    double rr = hypot(f, g);
+    double cc = f / rr, ss = g / rr;
+    if (fabs(f) > fabs(g) && cc < 0.0) { cc = -cc; ss = -ss; rr = -rr; }
+    c = cc; s = ss; r = rr;
+}
+
+// singular values of [f g; 0 h]: smax + smin = hypot(|f|+|h|, g),
+// smax - smin = hypot(|f|-|h|, g), smin = |f h| / smax
+__device__ __forceinline__ void sv2x2(double f, double g, double h, double &smin, double &smax)
+{
+    const double fa = fabs(f), ga = fabs(g), ha = fabs(h);
+    const double mx = 0.5 * (hypot(fa + ha, ga) + hypot(fa - ha, ga));
+    smax = mx;
+    smin = mx > 0.0 ? (fa / mx) * ha : 0.0;
+}
+
+// dbdqr (double/dbsvd.F:87-157); thread 0.  With Qt != nullptr the
+// (n+1) x (n+1) matrix Q' is formed (ldq).
+__device__ void bdqr_dev(int ignorelast, int n, double *D, double *E, double *c1, double *c2, double *Qt, int ldq)
+{
+    double cs, sn, r;
+    if (n < 1) return;
+#define QT(a, b) Qt[(size_t)((b)-1) * ldq + ((a)-1)]
+    if (Qt) {
+        for (int j = 1; j <= n + 1; j++) {
+            for (int i = 1; i <= n + 1; i++) QT(i, j) = 0.0;
+            QT(j, j) = 1.0;
+        }
+    }
+    int i;
+    for (i = 1; i <= n - 1; i++) {
+        lartg(D[i - 1], E[i - 1], cs, sn, r);
+        D[i - 1] = r;
+        E[i - 1] = sn * D[i];
+        D[i] = cs * D[i];
+        if (Qt) {
+            for (int j = 1; j <= i; j++) {
+                QT(i + 1, j) = -sn * QT(i, j);
+                QT(i, j) = cs * QT(i, j);
+            }
+            QT(i, i + 1) = sn;
+            QT(i + 1, i + 1) = cs;
+        }
+    }
+    if (!ignorelast) {
+        lartg(D[n - 1], E[n - 1], cs, sn, r);
+        D[n - 1] = r;
+        E[n - 1] = 0.0;
+        *c1 = sn;
+        *c2 = cs;
+        if (Qt) {
+            for (int j = 1; j <= i; j++) {
+                QT(i + 1, j) = -sn * QT(i, j);
+                QT(i, j) = cs * QT(i, j);
+            }
+            QT(i, i + 1) = sn;
+            QT(i + 1, i + 1) = cs;
+        }
+    }
+#undef QT
+}
+
+// drefinebounds (double/dbsvd.F:162-231); thread 0
+__device__ void refinebounds_dev(int n, int k, const double *theta, double *bound, double tol, double eps34)
+{
+    if (k <= 1) return;
+    for (int i = 1; i <= k; i++) {
+        for (int l = -1; l <= 1; l += 2) {
+            if ((l == 1 && i < k) || (l == -1 && i > 1)) {
+                if (fabs(theta[i - 1] - theta[i + l - 1]) < eps34 * theta[i - 1]) {
+                    if (bound[i - 1] > tol && bound[i + l - 1] > tol) {
+                        bound[i + l - 1] = hypot(bound[i - 1], bound[i + l - 1]);
+                        bound[i - 1] = 0.0;
+                    }
+                }
+            }
+        }
+    }
+    for (int i = 1; i <= k; i++) {
+        if (i < k || k == n) {
+            double gap;
+            if (i == 1) {
+                gap = fabs(theta[i - 1] - theta[i]) - fmax(bound[i - 1], bound[i]);
+            } else if (i == n) {
+                gap = fabs(theta[i - 2] - theta[i - 1]) - fmax(bound[i - 2], bound[i - 1]);
+            } else {
+                gap = fabs(theta[i - 1] - theta[i]) - fmax(bound[i - 1], bound[i]);
+                const double g2 = fabs(theta[i - 2] - theta[i - 1]) - fmax(bound[i - 2], bound[i - 1]);
+                if (g2 < gap) gap = g2;
+            }
+            if (gap > bound[i - 1]) bound[i - 1] = bound[i - 1] * (bound[i - 1] / gap);
+        }
+    }
+}
+
+// ---------------------------------------------------- CTA bidiagonal SVD
+struct QrShared {
+    int ll, cnt, vt_fwd, u_fwd, apply, done, info;
+};
+
+// apply a recorded chain: VT rows (pair i: rows lo+i, lo+i+1), U columns
+__device__ void apply_chain(int ncvt, double *vt, int ldvt, int nru, double *u, int ldu, int lo, int cnt,
+                            const double *cv, const double *sv, int vfwd, const double *cu, const double *su, int ufwd)
+{
+    for (int col = threadIdx.x; col < ncvt; col += blockDim.x) {
+        double *A = vt + (size_t)col * ldvt + lo;
+        for (int t = 0; t < cnt; t++) {
+            const int i = vfwd ? t : cnt - 1 - t;
+            const double c = cv[i], s = sv[i];
+            const double x = A[i], y = A[i + 1];
+            A[i + 1] = c * y - s * x;
+            A[i] = s * y + c * x;
+        }
+    }
+    for (int row = threadIdx.x; row < nru; row += blockDim.x) {
+        for (int t = 0; t < cnt; t++) {
+            const int i = ufwd ? t : cnt - 1 - t;
+            const double c = cu[i], s = su[i];
+            double *x = u + (size_t)(lo + i) * ldu + row, *y = x + ldu;
+            const double xv = *x, yv = *y;
+            *y = c * yv - s * xv;
+            *x = s * yv + c * xv;
+        }
+    }
+}
+
+// Upper bidiagonal SVD by implicit QR, executed by the whole CTA.  d[n],
+// e[n] (e[n-1] unused); VT n x ncvt (ldvt), U nru x n (ldu).  w: 4n doubles
+// of shared or global scratch.  Singular values end up non-negative and
+// sorted decreasingly.  Returns 0 or >0 (no convergence).
+__device__ int bdsqr_cta(int n, double *d, double *e, int ncvt, double *vt, int ldvt, int nru, double *u, int ldu,
+                         double *w, QrShared &q)
+{
+    double *c1 = w, *s1 = w + n, *c2 = w + 2 * n, *s2 = w + 3 * n;
+    const int tid = threadIdx.x;
+    // per-thread-0 state
+    double tol = 0, thresh = 0, sminl = 0, smax = 0;
+    long maxit = 0, iter = 0;
+    int oldll = -1, oldm = -1, idir = 0, m = n - 1;
+    if (tid == 0) {
+        q.info = 0;
+        q.done = (n <= 1);
+        if (n > 1) {
+            const double tolmul = fmax(10.0, fmin(100.0, pow(EPS, -0.125)));
+            tol = tolmul * EPS;
+            for (int i = 0; i < n; i++) smax = fmax(smax, fabs(d[i]));
+            for (int i = 0; i < n - 1; i++) smax = fmax(smax, fabs(e[i]));
+            double sminoa = fabs(d[0]);
+            if (sminoa != 0.0) {
+                double mu = sminoa;
+                for (int i = 1; i < n; i++) {
+                    mu = fabs(d[i]) * (mu / (mu + fabs(e[i - 1])));
+                    sminoa = fmin(sminoa, mu);
+                    if (sminoa == 0.0) break;
+                }
+            }
+            sminoa = sminoa / sqrt((double)n);
+            thresh = fmax(tol * sminoa, 6.0 * (double)n * (double)n * SFMIN);
+            maxit = 6L * n * n;
+        }
+    }
+    __syncthreads();
+    while (true) {
+        if (tid == 0) {
+            q.apply = 0;
+            while (!q.done && !q.apply) {
+                if (m <= 0) { q.done = 1; break; }
+                if (iter > maxit) { q.info = 1; q.done = 1; break; }
+                int ll, split = -1;
+                smax = fabs(d[m]);
+                for (ll = m - 1; ll >= 0; ll--) {
+                    const double abss = fabs(d[ll]), abse = fabs(e[ll]);
+                    if (abse <= thresh) { split = ll; break; }
+                    smax = fmax(smax, fmax(abss, abse));
+                }
+                if (split >= 0) {
+                    e[split] = 0.0;
+                    if (split == m - 1) { m -= 1; continue; }
+                    ll = split + 1;
+                } else {
+                    ll = 0;
+                }
+                if (ll > oldm || m < oldll) idir = (fabs(d[ll]) >= fabs(d[m])) ? 1 : 2;
+                bool defl = false;
+                if (idir == 1) {
+                    if (fabs(e[m - 1]) <= tol * fabs(d[m])) { e[m - 1] = 0.0; continue; }
+                    double mu = fabs(d[ll]);
+                    sminl = mu;
+                    for (int l3 = ll; l3 <= m - 1; l3++) {
+                        if (fabs(e[l3]) <= tol * mu) { e[l3] = 0.0; defl = true; break; }
+                        mu = fabs(d[l3 + 1]) * (mu / (mu + fabs(e[l3])));
+                        sminl = fmin(sminl, mu);
+                    }
+                } else {
+                    if (fabs(e[ll]) <= tol * fabs(d[ll])) { e[ll] = 0.0; continue; }
+                    double mu = fabs(d[m]);
+                    sminl = mu;
+                    for (int l3 = m - 1; l3 >= ll; l3--) {
+                        if (fabs(e[l3]) <= tol * mu) { e[l3] = 0.0; defl = true; break; }
+                        mu = fabs(d[l3]) * (mu / (mu + fabs(e[l3])));
+                        sminl = fmin(sminl, mu);
+                    }
+                }
+                if (defl) continue;
+                oldll = ll;
+                oldm = m;
+                double shift, sll, rdum;
+                if ((double)n * tol * (sminl / smax) <= fmax(EPS, 0.01 * tol)) {
+                    shift = 0.0;
+                } else {
+                    if (idir == 1) { sll = fabs(d[ll]); sv2x2(d[m - 1], e[m - 1], d[m], shift, rdum); }
+                    else { sll = fabs(d[m]); sv2x2(d[ll], e[ll], d[ll + 1], shift, rdum); }
+                    if (sll > 0.0 && (shift / sll) * (shift / sll) < EPS) shift = 0.0;
+                }
+                iter += m - ll;
+                const int cnt = m - ll;
+                double cs, sn, r, oldcs, oldsn, f, g, h;
+                if (shift == 0.0) {
+                    if (idir == 1) {
+                        cs = 1.0; oldcs = 1.0; oldsn = 0.0;
+                        for (int i = ll; i <= m - 1; i++) {
+                            lartg(d[i] * cs, e[i], cs, sn, r);
+                            if (i > ll) e[i - 1] = oldsn * r;
+                            lartg(oldcs * r, d[i + 1] * sn, oldcs, oldsn, d[i]);
+                            c1[i - ll] = cs; s1[i - ll] = sn; c2[i - ll] = oldcs; s2[i - ll] = oldsn;
+                        }
+                        h = d[m] * cs;
+                        d[m] = h * oldcs;
+                        e[m - 1] = h * oldsn;
+                        q.vt_fwd = 1; q.u_fwd = 1;
+                        if (fabs(e[m - 1]) <= thresh) e[m - 1] = 0.0;
+                        // VT gets (c1,s1), U gets (c2,s2)
+                    } else {
+                        cs = 1.0; oldcs = 1.0; oldsn = 0.0;
+                        for (int i = m; i >= ll + 1; i--) {
+                            lartg(d[i] * cs, e[i - 1], cs, sn, r);
+                            if (i < m) e[i] = oldsn * r;
+                            lartg(oldcs * r, d[i - 1] * sn, oldcs, oldsn, d[i]);
+                            // U gets (cs,-sn) -> stored in (c2,s2); VT gets (oldcs,-oldsn) -> (c1,s1)
+                            c2[i - ll - 1] = cs; s2[i - ll - 1] = -sn;
+                            c1[i - ll - 1] = oldcs; s1[i - ll - 1] = -oldsn;
+                        }
+                        h = d[ll] * cs;
+                        d[ll] = h * oldcs;
+                        e[ll] = h * oldsn;
+                        q.vt_fwd = 0; q.u_fwd = 0;
+                        if (fabs(e[ll]) <= thresh) e[ll] = 0.0;
+                    }
+                } else {
+                    double cosr, sinr, cosl, sinl;
+                    if (idir == 1) {
+                        f = (fabs(d[ll]) - shift) * (copysign(1.0, d[ll]) + shift / d[ll]);
+                        g = e[ll];
+                        for (int i = ll; i <= m - 1; i++) {
+                            lartg(f, g, cosr, sinr, r);
+                            if (i > ll) e[i - 1] = r;
+                            f = cosr * d[i] + sinr * e[i];
+                            e[i] = cosr * e[i] - sinr * d[i];
+                            g = sinr * d[i + 1];
+                            d[i + 1] = cosr * d[i + 1];
+                            lartg(f, g, cosl, sinl, r);
+                            d[i] = r;
+                            f = cosl * e[i] + sinl * d[i + 1];
+                            d[i + 1] = cosl * d[i + 1] - sinl * e[i];
+                            if (i < m - 1) { g = sinl * e[i + 1]; e[i + 1] = cosl * e[i + 1]; }
+                            c1[i - ll] = cosr; s1[i - ll] = sinr; c2[i - ll] = cosl; s2[i - ll] = sinl;
+                        }
+                        e[m - 1] = f;
+                        q.vt_fwd = 1; q.u_fwd = 1;
+                        if (fabs(e[m - 1]) <= thresh) e[m - 1] = 0.0;
+                    } else {
+                        f = (fabs(d[m]) - shift) * (copysign(1.0, d[m]) + shift / d[m]);
+                        g = e[m - 1];
+                        for (int i = m; i >= ll + 1; i--) {
+                            lartg(f, g, cosr, sinr, r);
+                            if (i < m) e[i] = r;
+                            f = cosr * d[i] + sinr * e[i - 1];
+                            e[i - 1] = cosr * e[i - 1] - sinr * d[i];
+                            g = sinr * d[i - 1];
+                            d[i - 1] = cosr * d[i - 1];
+                            lartg(f, g, cosl, sinl, r);
+                            d[i] = r;
+                            f = cosl * e[i - 1] + sinl * d[i - 1];
+                            d[i - 1] = cosl * d[i - 1] - sinl * e[i - 1];
+                            if (i > ll + 1) { g = sinl * e[i - 2]; e[i - 2] = cosl * e[i - 2]; }
+                            // U gets (cosr,-sinr) -> (c2,s2); VT gets (cosl,-sinl) -> (c1,s1)
+                            c2[i - ll - 1] = cosr; s2[i - ll - 1] = -sinr;
+                            c1[i - ll - 1] = cosl; s1[i - ll - 1] = -sinl;
+                        }
+                        e[ll] = f;
+                        q.vt_fwd = 0; q.u_fwd = 0;
+                        if (fabs(e[ll]) <= thresh) e[ll] = 0.0;
+                    }
+                }
+                q.ll = ll;
+                q.cnt = cnt;
+                q.apply = (ncvt > 0 || nru > 0);
+            }
+        }
+        __syncthreads();
+        if (q.done && !q.apply) break;
+        if (q.apply) apply_chain(ncvt, vt, ldvt, nru, u, ldu, q.ll, q.cnt, c1, s1, q.vt_fwd, c2, s2, q.u_fwd);
+        __syncthreads();
+    }
+    // non-negative values
+    for (int i = 0; i < n; i++) {
+        if (d[i] < 0.0) {
+            __syncthreads();
+            for (int c = tid; c < ncvt; c += blockDim.x) vt[(size_t)c * ldvt + i] = -vt[(size_t)c * ldvt + i];
+            __syncthreads();
+            if (tid == 0) d[i] = -d[i];
+            __syncthreads();
+        }
+    }
+    // sort decreasingly
+    __shared__ int isub_s;
+    for (int i = 0; i < n - 1; i++) {
+        if (tid == 0) {
+            int isub = i;
+            double smx = d[i];
+            for (int j = i + 1; j < n; j++)
+                if (d[j] > smx) { smx = d[j]; isub = j; }
+            isub_s = isub;
+            if (isub != i) { d[isub] = d[i]; d[i] = smx; }
+        }
+        __syncthreads();
+        const int isub = isub_s;
+        if (isub != i) {
+            for (int c = tid; c < ncvt; c += blockDim.x) {
+                const double t = vt[(size_t)c * ldvt + i];
+                vt[(size_t)c * ldvt + i] = vt[(size_t)c * ldvt + isub];
+                vt[(size_t)c * ldvt + isub] = t;
+            }
+            for (int r = tid; r < nru; r += blockDim.x) {
+                const double t = u[(size_t)i * ldu + r];
+                u[(size_t)i * ldu + r] = u[(size_t)isub * ldu + r];
+                u[(size_t)isub * ldu + r] = t;
+            }
+        }
+        __syncthreads();
+    }
+    return q.info;
+}
+
+// ----------------------------------------------------------------- analysis
+
+// IRL: dlansvd_irl.F:218-290.  lansvd: dlansvd.F:192-236.
+__global__ void k_analyse(AnaArgs a)
+{
+    __shared__ QrShared q;
+    const int dim = a.dim;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) { a.a1[i] = a.balpha[i]; a.b1[i] = a.bbeta[i]; }
+    for (int i = threadIdx.x; i <= dim; i += blockDim.x) a.bnd[i] = 0.0;
+    __syncthreads();
+    const int mn = a.m < a.n ? a.m : a.n;
+    if (threadIdx.x == 0) bdqr_dev(dim == mn, dim, a.a1, a.b1, &a.bnd[dim - 1], &a.bnd[dim], nullptr, 0);
+    __syncthreads();
+    bdsqr_cta(dim, a.a1, a.b1, 0, nullptr, 1, 1, a.bnd, 1, a.w, q);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double eps34 = pow(EPS, 0.75);
+        const double epsn = (double)(a.m > a.n ? a.m : a.n) * EPS / 2.0;
+        double anorm = *a.anorm_drv;
+        if (dim > 5) anorm = a.a1[0];
+        else anorm = fmax(anorm, a.a1[0]);
+        *a.anorm_drv = anorm;
+        const double rnorm = a.ctl->rnorm;
+        for (int i = 0; i < dim; i++) a.bnd[i] = fabs(rnorm * a.bnd[i]);
+        int nconv = 0;
+        if (a.irl) {
+            const int neig = a.neig;
+            if (a.small_side) refinebounds_dev(mn, dim, a.a1, a.bnd, epsn * anorm, eps34);
+            else refinebounds_dev(mn, dim < neig ? dim : neig, a.a1, a.bnd, epsn * anorm, eps34);
+            if (a.small_side) {
+                for (int i = dim - neig + 1; i <= dim; i++) {
+                    if (a.bnd[i - 1] <= a.tol * a.a1[0]) {
+                        a.sigma_out[nconv] = a.a1[i - 1];
+                        a.bnd_out[nconv] = a.bnd[i - 1];
+                        nconv++;
+                    }
+                }
+            } else {
+                int i = 1;
+                const int lim = dim < neig ? dim : neig;
+                while (i <= lim) {
+                    if (a.bnd[i - 1] <= a.tol * a.a1[i - 1]) {
+                        a.sigma_out[nconv] = a.a1[i - 1];
+                        a.bnd_out[nconv] = a.bnd[i - 1];
+                        nconv++;
+                        i++;
+                    } else {
+                        i = a.kk + 1;
+                    }
+                }
+            }
+        } else {
+            // dlansvd: k = a.kk
+            refinebounds_dev(mn, dim, a.a1, a.bnd, epsn * anorm, eps34);
+            const int lim = dim < a.kk ? dim : a.kk;
+            for (int i = 0; i < lim; i++) a.bnd_out[i] = a.bnd[i];
+            int i = 0;
+            while (i < lim) {
+                if (a.bnd[i] <= a.tol * a.a1[i]) { a.sigma_out[nconv] = a.a1[i]; nconv++; i++; }
+                else i = a.kk;
+            }
+        }
+        *a.nconv_out = nconv;
+    }
+}
+
+// ------------------------------------------------------------ IRL sweeps
+
+// dbsvdstep chain (double/dbsvd.F:5-82) for sweep length kk: thread 0
+// computes the rotations (U side in cu/su, V side in cv/sv).
+__device__ void bsvdstep_chain(int kk, double sigma, double *D, double *E, double *cu, double *su, double *cv,
+                               double *sv)
+{
+    double c, s, x, y, r;
+    x = D[0] * D[0] - sigma * sigma;
+    y = E[0] * D[0];
+    for (int i = 1; i <= kk - 1; i++) {
+        if (i > 1) lartg(x, y, c, s, E[i - 2]);
+        else lartg(x, y, c, s, r);
+        x = c * D[i - 1] + s * E[i - 1];
+        E[i - 1] = -s * D[i - 1] + c * E[i - 1];
+        D[i - 1] = x;
+        y = s * D[i];
+        D[i] = c * D[i];
+        cu[i - 1] = c; su[i - 1] = s;
+        lartg(x, y, c, s, D[i - 1]);
+        x = c * E[i - 1] + s * D[i];
+        D[i] = -s * E[i - 1] + c * D[i];
+        E[i - 1] = x;
+        y = s * E[i];
+        E[i] = c * E[i];
+        cv[i - 1] = c; sv[i - 1] = s;
+    }
+    lartg(x, y, c, s, E[kk - 2]);
+    x = c * D[kk - 1] + s * E[kk - 1];
+    E[kk - 1] = -s * D[kk - 1] + c * E[kk - 1];
+    D[kk - 1] = x;
+    cu[kk - 1] = c; su[kk - 1] = s;
+}
+
+__global__ void k_irl_sweeps(SweepArgs a)
+{
+    const int dim = a.dim, k = a.k, dp1 = dim + 1;
+    double *cu = a.w, *su = a.w + dp1, *cv = a.w + 2 * dp1, *sv = a.w + 3 * dp1;
+    // shifts (dlansvd_irl.F:304-344)
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < dim - k; i++) a.shifts[i] = 0.0;
+        int nshft = 0;
+        if (a.small_side) {
+            const double ref = a.a1[dim - a.neig - 1];
+            for (int i = 1; i <= k; i++) {
+                const double relgap = a.a1[i - 1] - a.bnd[i - 1] - ref;
+                a.shifts[nshft++] = (relgap > a.min_relgap * ref) ? a.a1[i - 1] : a.a1[0];
+            }
+        } else {
+            for (int i = dim; i >= k + 1; i--) {
+                const double relgap = a.a1[k - 1] - (a.a1[i - 1] + a.bnd[i - 1]);
+                a.shifts[nshft++] = (relgap > a.min_relgap * a.a1[k - 1]) ? a.a1[i - 1] : 0.0;
+            }
+        }
+    }
+    // P = I, Q = I
+    for (size_t t = threadIdx.x; t < (size_t)dp1 * dp1; t += blockDim.x) a.P[t] = (t % (dp1 + 1) == 0) ? 1.0 : 0.0;
+    for (size_t t = threadIdx.x; t < (size_t)dim * dim; t += blockDim.x) a.Q[t] = (t % (dim + 1) == 0) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int i = dim; i >= k + 1; i--) {
+        const double shift = a.shifts[dim - i];
+        if (i <= 1) continue;  // dbsvdstep returns for k <= 1
+        if (threadIdx.x == 0) bsvdstep_chain(i, shift, a.balpha, a.bbeta, cu, su, cv, sv);
+        __syncthreads();
+        // the U rotations act on columns (t, t+1) of P, t = 0..i-1; the V
+        // rotations on columns (t, t+1) of Q, t = 0..i-2; one row per thread
+        for (int row = threadIdx.x; row < dp1; row += blockDim.x) {
+            double *Pr = a.P + row;
+            double xc = Pr[0];
+            for (int t = 0; t < i; t++) {
+                const double c = cu[t], s = su[t];
+                const double yc = Pr[(size_t)(t + 1) * dp1];
+                Pr[(size_t)t * dp1] = c * xc + s * yc;
+                xc = c * yc - s * xc;
+            }
+            Pr[(size_t)i * dp1] = xc;
+        }
+        for (int row = threadIdx.x; row < dim; row += blockDim.x) {
+            double *Qr = a.Q + row;
+            double xc = Qr[0];
+            for (int t = 0; t < i - 1; t++) {
+                const double c = cv[t], s = sv[t];
+                const double yc = Qr[(size_t)(t + 1) * dim];
+                Qr[(size_t)t * dim] = c * xc + s * yc;
+                xc = c * yc - s * xc;
+            }
+            Qr[(size_t)(i - 1) * dim] = xc;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.ctl->rnorm = a.bbeta[k - 1];
+}
+
+// -------------------------------------------------------------- Ritz prep
+__global__ void k_ritz_prep(RitzArgs a)
+{
+    __shared__ QrShared q;
+    const int dim = a.dim;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) { a.D[i] = a.balpha[i]; a.E[i] = a.bbeta[i]; }
+    for (size_t t = threadIdx.x; t < (size_t)dim * dim; t += blockDim.x) {
+        const double v = (t % (dim + 1) == 0) ? 1.0 : 0.0;
+        a.P[t] = v;
+        a.Qt[t] = v;
+    }
+    __syncthreads();
+    const int mn = a.m < a.n ? a.m : a.n;
+    if (threadIdx.x == 0) {
+        double c1 = 0, c2 = 0;
+        bdqr_dev(dim == mn, dim, a.D, a.E, &c1, &c2, a.Mt, dim + 1);
+    }
+    __syncthreads();
+    bdsqr_cta(dim, a.D, a.E, dim, a.Qt, dim, dim, a.P, dim, a.w, q);
+}
+
+// ------------------------------------------------------------------ GEMM
+// C(mr x nc) = op(A) op(B), FP64, 64 x 64 tiles, 256 threads x 4 x 4.
+// op(A)(i,l) = ta ? A[i*lda + l] : A[l*lda + i]; same for B with (l, j).
+__global__ void __launch_bounds__(256) k_gemm(int mr, int nc, int kk, const double *__restrict__ A, int lda, int ta,
+                                             const double *__restrict__ B, int ldb, int tb, double *__restrict__ C,
+                                             int ldc)
+{
+    __shared__ double As[16][64 + 1];
+    __shared__ double Bs[16][64 + 1];
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
+    double acc[4][4] = {};
+    for (int l0 = 0; l0 < kk; l0 += 16) {
+        for (int t = threadIdx.x; t < 16 * 64; t += 256) {
+            const int l = t / 64, i = t % 64;
+            const int gi = i0 + i, gl = l0 + l;
+            double v = 0.0;
+            if (gi < mr && gl < kk) v = ta ? A[(size_t)gi * lda + gl] : A[(size_t)gl * lda + gi];
+            As[l][i] = v;
+            const int gj = j0 + i;
+            double u = 0.0;
+            if (gj < nc && gl < kk) u = tb ? B[(size_t)gl * ldb + gj] : B[(size_t)gj * ldb + gl];
+            Bs[l][i] = u;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int l = 0; l < 16; l++) {
+            double av[4], bv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) { av[q] = As[l][tx + 16 * q]; bv[q] = Bs[l][ty + 16 * q]; }
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) acc[p][q] = fma(av[p], bv[q], acc[p][q]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int gi = i0 + tx + 16 * p, gj = j0 + ty + 16 * q;
+            if (gi < mr && gj < nc) C[(size_t)gj * ldc + gi] = acc[p][q];
+        }
+}
+
+__global__ void k_copy_cols(const double *src, int lds, double *dst, int ldd, int rows, int cols)
+{
+    const size_t total = (size_t)rows * cols;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = t / rows, r = t % rows;
+        dst[c * ldd + r] = src[c * lds + r];
+    }
+}
+
+// ------------------------------------------------------------ host wrappers
+void launch_analyse(const AnaArgs &a, cudaStream_t s)
+{
+    k_analyse<<<1, 256, 0, s>>>(a);
+    PGB_LAUNCHED();
+}
+void launch_sweeps(const SweepArgs &a, cudaStream_t s)
+{
+    k_irl_sweeps<<<1, 256, 0, s>>>(a);
+    PGB_LAUNCHED();
+}
+void launch_ritz_prep(const RitzArgs &a, cudaStream_t s)
+{
+    k_ritz_prep<<<1, 256, 0, s>>>(a);
+    PGB_LAUNCHED();
+}
+// C = op(A) op(B) (out of place)
+void gemm(int mr, int nc, int kk, const double *A, int lda, bool ta, const double *B, int ldb, bool tb, double *C,
+          int ldc, cudaStream_t s)
+{
+    if (mr <= 0 || nc <= 0) return;
+    dim3 grid((mr + 63) / 64, (nc + 63) / 64);
+    k_gemm<<<grid, 256, 0, s>>>(mr, nc, kk, A, lda, ta ? 1 : 0, B, ldb, tb ? 1 : 0, C, ldc);
+    PGB_LAUNCHED();
+}
+void copy_cols(const double *src, int lds, double *dst, int ldd, int rows, int cols, cudaStream_t s)
+{
+    if (rows <= 0 || cols <= 0) return;
+    k_copy_cols<<<device_info().nb, 256, 0, s>>>(src, lds, dst, ldd, rows, cols);
+    PGB_LAUNCHED();
+}
+
+}  // namespace pgb

@@ -1,0 +1,983 @@
+// pgb_driver.cu -- the DLANSVD / DLANSVD_IRL drivers behind the C ABI.
+//
+// Control flow follows double/dlansvd_irl.F:160-419 and double/dlansvd.F:
+// 131-291; the Lanczos recurrence follows double/dlanbpro.F:146-549.  The
+// host only orchestrates: the Lanczos vectors, B, the omega recurrences, the
+// bidiagonal SVD, the shifts and the restart/Ritz products all live and run
+// on the device.  One host/device round trip per restart reads the number of
+// converged values.  Rare cases (a random restart vector after an
+// invariant subspace, dgetu0.F; the resume prologue of dlanbpro.F:231-275)
+// are driven from the host with device kernels.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/propack_gb300.h"
+#include "pgb.cuh"
+
+namespace pgb {
+
+// ------------------------------------------------------------- statistics
+struct Stats {
+    int64_t nopx = 0, nreorth = 0, ndot = 0, nrestart = 0, nbsvd = 0, nlandim = 0, nsing = 0;
+    double device_ms = 0, lanczos_ms = 0, bsvd_ms = 0, gemm_ms = 0;
+    int64_t launches = 0;
+};
+static thread_local Stats g_stat;       // cumulative (clearstat_/printstat_)
+static thread_local Stats g_last;       // last driver call (propack_get_stats)
+
+// ------------------------------------------------------------ small kernels
+#define LCG_A 33952834046453ULL
+#define LCG_MASK ((1ULL << 48) - 1ULL)
+
+__device__ __forceinline__ unsigned long long mulmod48(unsigned long long a, unsigned long long b)
+{
+    return (a * b) & LCG_MASK;
+}
+// x[i] = 2 * (seed * a^(offset+i+1) mod 2^48) / 2^48 - 1: dlarnv(2, ...) with
+// dlaruv's generator (Lapack_Util/dlarnv.f, dlaruv.f), 64 values per thread.
+__global__ void k_rng_pm1(double *x, int n, unsigned long long seed, long long offset)
+{
+    const double r48 = 1.0 / 281474976710656.0;
+    const long long nchunk = (n + 63) / 64;
+    for (long long cidx = blockIdx.x * (long long)blockDim.x + threadIdx.x; cidx < nchunk;
+         cidx += (long long)gridDim.x * blockDim.x) {
+        unsigned long long e = (unsigned long long)(offset + cidx * 64 + 1), p = 1, b = LCG_A;
+        while (e) {
+            if (e & 1) p = mulmod48(p, b);
+            b = mulmod48(b, b);
+            e >>= 1;
+        }
+        unsigned long long s = mulmod48(seed, p);
+        const int i0 = (int)(cidx * 64);
+        for (int q = 0; q < 64 && i0 + q < n; q++) {
+            x[i0 + q] = 2.0 * ((double)s * r48) - 1.0;
+            s = mulmod48(s, LCG_A);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BS) k_sumsq_part(const double *x, int n, double *part)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) s = fma(x[i], x[i], s);
+    s = block_sum<BS>(s, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void __launch_bounds__(BS) k_sum_final(const double *part, int nb, double *out)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += BS) s += part[b];
+    s = block_sum<BS>(s, red);
+    if (threadIdx.x == 0) *out = s;
+}
+// partial W(:,0:kk)' x per CTA (contiguous row chunks), column c at c*nb
+__global__ void __launch_bounds__(BS) k_gemvt_part(const double *W, size_t ld, int len, int kk, const double *x,
+                                                   double *part)
+{
+    const int chunk = (len + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * chunk, r1 = min(len, r0 + chunk);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c = w; c < kk; c += BS / 32) {
+        const double *col = W + (size_t)c * ld;
+        double acc = 0.0;
+        for (int r = r0 + lane; r < r1; r += 32) acc = fma(col[r], x[r], acc);
+        acc = warp_sum(acc);
+        if (lane == 0) part[(size_t)c * gridDim.x + blockIdx.x] = acc;
+    }
+}
+__global__ void __launch_bounds__(BS) k_gemvt_final(const double *part, int nb, int kk, double *h)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c = w; c < kk; c += BS / 32) {
+        double s = 0.0;
+        for (int b = lane; b < nb; b += 32) s += part[(size_t)c * nb + b];
+        s = warp_sum(s);
+        if (lane == 0) h[c] = s;
+    }
+}
+__global__ void __launch_bounds__(BS) k_gemvn_upd(const double *W, size_t ld, int len, int kk, const double *h,
+                                                  double *x)
+{
+    for (int r = blockIdx.x * BS + threadIdx.x; r < len; r += gridDim.x * BS) {
+        double acc = 0.0;
+        for (int c = 0; c < kk; c++) acc = fma(W[(size_t)c * ld + r], h[c], acc);
+        x[r] -= acc;
+    }
+}
+__global__ void k_scale(double *x, int n, int mode, double val)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (mode == 1) x[i] *= val;
+        else if (mode == 2) x[i] /= val;
+        else if (mode == 3) x[i] = 0.0;
+    }
+}
+// apply the deferred scale of u (which=0) or v (which=1) to its column now
+__global__ void k_apply_pend_col(LbCtl *ctl, double *U, int ldu, double *V, int ldv, int m, int n, int which)
+{
+    const Pend p = which == 0 ? ctl->pend_u : ctl->pend_v;
+    const int col = which == 0 ? ctl->pend_u_col : ctl->pend_v_col;
+    if (p.mode != 0 && col >= 0) {
+        double *x = which == 0 ? U + (size_t)col * ldu : V + (size_t)col * ldv;
+        const int len = which == 0 ? m : n;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x)
+            x[i] = apply_pend(x[i], p);
+    }
+}
+__global__ void k_clear_pend(LbCtl *ctl, int which)
+{
+    if (which == 0) ctl->pend_u.mode = 0;
+    else ctl->pend_v.mode = 0;
+}
+
+// ------------------------------------------------------------- context
+struct Ctx {
+    int m = 0, n = 0, kmax = 0, ldu = 0, ldv = 0;
+    cudaStream_t s = nullptr;
+    double *U = nullptr, *V = nullptr;
+    LbCtl *ctl = nullptr;
+    LbCtl *hctl = nullptr;  // pinned host copy
+    double *balpha = nullptr, *bbeta = nullptr, *mu = nullptr, *nu = nullptr, *h = nullptr;
+    double *part_sq = nullptr, *part_dot = nullptr, *part_cols = nullptr;
+    int *index = nullptr, *sel = nullptr;
+    double *xr = nullptr, *yr = nullptr;    // max(m,n) scratch
+    double *scal = nullptr;                 // device scalar slots
+    double *hscal = nullptr;                // pinned host scalars
+    // dense
+    double *a1 = nullptr, *b1 = nullptr, *bnd = nullptr, *w = nullptr, *P = nullptr, *Q = nullptr;
+    double *shifts = nullptr, *sig_out = nullptr, *bnd_out = nullptr, *anorm_drv = nullptr;
+    int *nconv = nullptr;
+    double *D = nullptr, *E = nullptr, *Mt = nullptr, *Pr = nullptr, *Qt = nullptr, *X = nullptr;
+    double *gout = nullptr;                 // GEMM output scratch
+    // operator
+    const Operator *op = nullptr;
+    propack_aprod_t aprod = nullptr;
+    double *dparm = nullptr;
+    int *iparm = nullptr;
+    double *hx = nullptr, *hy = nullptr;    // pinned host vectors for a host APROD
+    int nb = 0;
+    int ntry_spec = 2;
+    std::vector<void *> allocs;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    template <typename T>
+    T *dalloc(size_t count)
+    {
+        void *p = nullptr;
+        PGB_CUDA(cudaMalloc(&p, sizeof(T) * std::max<size_t>(count, 1)));
+        PGB_CUDA(cudaMemsetAsync(p, 0, sizeof(T) * std::max<size_t>(count, 1), s));
+        allocs.push_back(p);
+        return (T *)p;
+    }
+    ~Ctx()
+    {
+        if (s) cudaStreamSynchronize(s);
+        for (void *p : allocs) cudaFree(p);
+        if (hctl) cudaFreeHost(hctl);
+        if (hscal) cudaFreeHost(hscal);
+        if (hx) cudaFreeHost(hx);
+        if (hy) cudaFreeHost(hy);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (s) cudaStreamDestroy(s);
+    }
+    LbArgs args() const
+    {
+        LbArgs a;
+        a.ctl = ctl; a.U = U; a.V = V; a.ldu = ldu; a.ldv = ldv;
+        a.balpha = balpha; a.bbeta = bbeta; a.mu = mu; a.nu = nu;
+        a.index = index; a.sel = sel; a.h = h;
+        a.part_sq = part_sq; a.part_dot = part_dot; a.part_cols = part_cols;
+        a.nb = nb; a.kmax = kmax;
+        if (op) { a.fwd = op->fwd; a.adj = op->adj; a.z = op->zbuf; }
+        else {
+            a.fwd.rows = m; a.adj.rows = n; a.z = nullptr;
+        }
+        return a;
+    }
+    void sync() { PGB_CUDA(cudaStreamSynchronize(s)); }
+    void get_ctl()
+    {
+        PGB_CUDA(cudaMemcpyAsync(hctl, ctl, sizeof(LbCtl), cudaMemcpyDeviceToHost, s));
+        sync();
+    }
+    void put_ctl() { PGB_CUDA(cudaMemcpyAsync(ctl, hctl, sizeof(LbCtl), cudaMemcpyHostToDevice, s)); }
+};
+
+static void init_ctx(Ctx &c, int m, int n, int kmax)
+{
+    const Dev &d = device_info();
+    c.m = m; c.n = n; c.kmax = kmax;
+    c.ldu = (m + 31) / 32 * 32;
+    c.ldv = (n + 31) / 32 * 32;
+    c.nb = d.nb;
+    PGB_CUDA(cudaStreamCreateWithFlags(&c.s, cudaStreamNonBlocking));
+    PGB_CUDA(cudaEventCreate(&c.ev0));
+    PGB_CUDA(cudaEventCreate(&c.ev1));
+    c.U = c.dalloc<double>((size_t)c.ldu * (kmax + 1));
+    c.V = c.dalloc<double>((size_t)c.ldv * (kmax + 1));
+    c.ctl = c.dalloc<LbCtl>(1);
+    PGB_CUDA(cudaMallocHost(&c.hctl, sizeof(LbCtl)));
+    memset(c.hctl, 0, sizeof(LbCtl));
+    c.balpha = c.dalloc<double>(kmax + 2);
+    c.bbeta = c.dalloc<double>(kmax + 2);
+    c.mu = c.dalloc<double>(kmax + 2);
+    c.nu = c.dalloc<double>(kmax + 2);
+    c.h = c.dalloc<double>(kmax + 2);
+    c.part_sq = c.dalloc<double>(c.nb);
+    c.part_dot = c.dalloc<double>(c.nb);
+    c.part_cols = c.dalloc<double>((size_t)c.nb * (kmax + 2));
+    c.index = c.dalloc<int>(2 * (size_t)kmax + 8);
+    c.sel = c.dalloc<int>(kmax + 2);
+    const int mn = std::max(m, n);
+    c.xr = c.dalloc<double>(mn);
+    c.yr = c.dalloc<double>(mn);
+    c.scal = c.dalloc<double>(8);
+    PGB_CUDA(cudaMallocHost(&c.hscal, sizeof(double) * 8));
+    const size_t d1 = kmax + 2;
+    c.a1 = c.dalloc<double>(d1); c.b1 = c.dalloc<double>(d1); c.bnd = c.dalloc<double>(d1);
+    c.w = c.dalloc<double>(4 * d1);
+    c.P = c.dalloc<double>(d1 * d1); c.Q = c.dalloc<double>(d1 * d1);
+    c.shifts = c.dalloc<double>(d1);
+    c.sig_out = c.dalloc<double>(d1); c.bnd_out = c.dalloc<double>(d1);
+    c.anorm_drv = c.dalloc<double>(1);
+    c.nconv = c.dalloc<int>(1);
+    c.D = c.dalloc<double>(d1); c.E = c.dalloc<double>(d1);
+    c.Mt = c.dalloc<double>(d1 * d1); c.Pr = c.dalloc<double>(d1 * d1); c.Qt = c.dalloc<double>(d1 * d1);
+    c.X = c.dalloc<double>(d1 * d1);
+    c.gout = c.dalloc<double>((size_t)std::max(c.ldu, c.ldv) * (kmax + 1));
+    lb_set_smem_limits(kmax);
+}
+
+// ----------------------------------------------------- device utilities
+static double dev_nrm2(Ctx &c, const double *x, int n)
+{
+    k_sumsq_part<<<c.nb, BS, 0, c.s>>>(x, n, c.part_sq);
+    PGB_LAUNCHED();
+    k_sum_final<<<1, BS, 0, c.s>>>(c.part_sq, c.nb, c.scal);
+    PGB_LAUNCHED();
+    PGB_CUDA(cudaMemcpyAsync(c.hscal, c.scal, sizeof(double), cudaMemcpyDeviceToHost, c.s));
+    c.sync();
+    return std::sqrt(c.hscal[0]);
+}
+static void dev_scale(Ctx &c, double *x, int n, int mode, double val)
+{
+    if (mode == 0 || n <= 0) return;
+    k_scale<<<c.nb, 256, 0, c.s>>>(x, n, mode, val);
+    PGB_LAUNCHED();
+}
+// dsafescal on the device
+static void dev_safescal(Ctx &c, double *x, int n, double alpha)
+{
+    if (std::fabs(alpha) >= SFMIN) dev_scale(c, x, n, 1, 1.0 / alpha);
+    else dev_scale(c, x, n, 2, alpha);
+}
+
+// y = op(A) x on device vectors, through the device operator or the
+// caller's host APROD
+static void dev_aprod(Ctx &c, bool trans, const double *x, double *y)
+{
+    const int nin = trans ? c.m : c.n, nout = trans ? c.n : c.m;
+    if (c.op) {
+        op_apply(*c.op, trans, x, y, c.s);
+        return;
+    }
+    PGB_CUDA(cudaMemcpyAsync(c.hx, x, sizeof(double) * nin, cudaMemcpyDeviceToHost, c.s));
+    c.sync();
+    const char ta = trans ? 't' : 'n';
+    c.aprod(&ta, &c.m, &c.n, c.hx, c.hy, c.dparm, c.iparm, 1);
+    PGB_CUDA(cudaMemcpyAsync(y, c.hy, sizeof(double) * nout, cudaMemcpyHostToDevice, c.s));
+}
+
+// dreorth against all of W(:,0:kk) (index = [1, kk, kk+1]), iterated CGS;
+// host-driven (resume prologue and dgetu0 only)
+static void dev_reorth_full(Ctx &c, const double *W, size_t ld, int len, int kk, double *x, double *nrm, double kappa)
+{
+    if (kk <= 0 || len <= 0) return;
+    for (int itry = 0; itry < NTRY; itry++) {
+        const double nrm0 = *nrm;
+        k_gemvt_part<<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, x, c.part_cols);
+        PGB_LAUNCHED();
+        k_gemvt_final<<<1, BS, 0, c.s>>>(c.part_cols, c.nb, kk, c.h);
+        PGB_LAUNCHED();
+        k_gemvn_upd<<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, c.h, x);
+        PGB_LAUNCHED();
+        g_last.ndot += 2 * (int64_t)kk;
+        *nrm = dev_nrm2(c, x, len);
+        if (*nrm > kappa * nrm0) { g_last.nreorth++; return; }
+    }
+    *nrm = 0.0;
+    dev_scale(c, x, len, 3, 0.0);
+    g_last.nreorth++;
+}
+
+// dgetu0 (double/dgetu0.F:11-89): a random vector in span(op(A)) orthogonal
+// to the first j columns of W; returns u0norm, anormest, ierr.
+static int dev_getu0(Ctx &c, bool trans, int j, int ntry, double *u0, double *u0norm, const double *W, size_t ld,
+                     double *anormest)
+{
+    const unsigned long long seed = (1ull << 36) | (3ull << 24) | (5ull << 12) | 7ull;
+    const int rsize = trans ? c.m : c.n, usize = trans ? c.n : c.m;
+    for (int itry = 0; itry < ntry; itry++) {
+        const int nch = (rsize + 63) / 64;
+        k_rng_pm1<<<std::max(1, std::min(c.nb, (nch + 255) / 256)), 256, 0, c.s>>>(c.xr, rsize, seed,
+                                                                                   (long long)itry * rsize);
+        PGB_LAUNCHED();
+        const double nrm = dev_nrm2(c, c.xr, rsize);
+        dev_aprod(c, trans, c.xr, u0);
+        g_last.nopx++;
+        *u0norm = dev_nrm2(c, u0, usize);
+        *anormest = *u0norm / nrm;
+        if (j >= 1) dev_reorth_full(c, W, ld, usize, j, u0, u0norm, KAPPA_GETU0);
+        if (*u0norm > 0) return 0;
+    }
+    return -1;
+}
+
+// ------------------------------------------------------------ dlanbpro
+struct LbResult {
+    int ierr;
+};
+
+// Run dlanbpro (double/dlanbpro.F:1-549) from k0 to *kp on the device.
+static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption, const int *ioption, int *ierr)
+{
+    const int m = c.m, n = c.n;
+    int k = *kp;
+    LbCtl &h = *c.hctl;
+    // the device holds the authoritative control block between calls;
+    // refresh the host copy (counters, pending scales)
+    c.get_ctl();
+    const int mn = std::max(m, n);
+    h.m = m; h.n = n; h.k = k; h.ldu = c.ldu; h.ldv = c.ldv;
+    h.icgs = ioption[0]; h.ielr = ioption[1];
+    h.epsn = (double)mn * EPS;
+    h.epsn2 = std::sqrt((double)mn) * EPS;
+    h.delta = doption[0] < 0 ? std::sqrt(EPS / k) : doption[0];
+    h.eta = doption[1] < 0 ? std::pow(EPS, 0.75) / std::sqrt((double)k) : doption[1];
+    h.full_reorth = (h.delta <= h.eta || h.delta == 0.0);
+    h.status = 0;
+    h.elr_active = 0;
+    h.reorth_active = 0;
+    h.collapsed = 0;
+    double anorm;
+    std::vector<double> hb(2 * (size_t)(k + 2), 0.0);
+    if (k0 > 0) {
+        PGB_CUDA(cudaMemcpyAsync(hb.data(), c.balpha, sizeof(double) * k0, cudaMemcpyDeviceToHost, c.s));
+        PGB_CUDA(cudaMemcpyAsync(hb.data() + k + 2, c.bbeta, sizeof(double) * k0, cudaMemcpyDeviceToHost, c.s));
+        c.sync();
+    }
+    double *ba = hb.data(), *bb = hb.data() + k + 2;
+    if (doption[2] > 0) {
+        anorm = doption[2];
+    } else if (k0 > 0) {
+        anorm = std::hypot(ba[0], bb[0]);
+        if (anorm <= 0) { *ierr = -1; doption[2] = anorm; return; }
+    } else {
+        anorm = 0.0;
+    }
+    *ierr = 0;
+    PGB_CUDA(cudaMemsetAsync(c.mu, 0, sizeof(double) * (k + 2), c.s));
+    PGB_CUDA(cudaMemsetAsync(c.nu, 0, sizeof(double) * (k + 2), c.s));
+    PGB_CUDA(cudaMemsetAsync(c.index, 0, sizeof(int) * (2 * (size_t)k + 4), c.s));
+    double anormest = 0.0;
+    if (*rnorm == 0.0) {
+        int e = dev_getu0(c, false, k0, 3, c.U + (size_t)k0 * c.ldu, rnorm, c.U, c.ldu, &anormest);
+        *ierr = e;
+        anorm = std::max(anorm, anormest);
+    }
+    int j0;
+    h.pend_u.mode = 0; h.pend_v.mode = 0; h.pend_u_col = -1; h.pend_v_col = -1;
+    if (k0 == 0) {
+        h.amax = 0.0;
+        h.alpha = 0.0;
+        h.beta = *rnorm;
+        h.force_reorth = 0;
+        double s;
+        int e;
+        if (n > m) e = dev_getu0(c, false, 0, 1, c.yr, &s, c.U, c.ldu, &anormest);
+        else e = dev_getu0(c, true, 0, 1, c.yr, &s, c.V, c.ldv, &anormest);
+        *ierr = e;
+        anorm = std::max(anorm, FUDGE * anormest);
+        j0 = 1;
+        if (h.beta != 0.0) {
+            // deferred dsafescal of u_1
+            if (std::fabs(h.beta) >= SFMIN) { h.pend_u.mode = 1; h.pend_u.val = 1.0 / h.beta; }
+            else { h.pend_u.mode = 2; h.pend_u.val = h.beta; }
+            h.pend_u_col = 0;
+        }
+        const double one = 1.0;
+        PGB_CUDA(cudaMemcpyAsync(c.mu, &one, sizeof(double), cudaMemcpyHostToDevice, c.s));
+        PGB_CUDA(cudaMemcpyAsync(c.nu, &one, sizeof(double), cudaMemcpyHostToDevice, c.s));
+    } else {
+        h.force_reorth = 1;
+        h.alpha = ba[k0 - 1];
+        h.beta = *rnorm;
+        if (k0 < k && h.beta * h.delta < anorm * EPS) { h.full_reorth = 1; *ierr = k0; }
+        const int idx3[3] = {1, k0, k0 + 1};
+        PGB_CUDA(cudaMemcpyAsync(c.index, idx3, sizeof(idx3), cudaMemcpyHostToDevice, c.s));
+        double *uk = c.U + (size_t)k0 * c.ldu;
+        dev_scale(c, uk, m, 1, *rnorm);
+        dev_reorth_full(c, c.U, c.ldu, m, k0, uk, rnorm, KAPPA);
+        dev_safescal(c, uk, m, *rnorm);
+        std::vector<double> mus(k0, h.epsn2);
+        PGB_CUDA(cudaMemcpyAsync(c.mu, mus.data(), sizeof(double) * k0, cudaMemcpyHostToDevice, c.s));
+        PGB_CUDA(cudaMemcpyAsync(c.nu, mus.data(), sizeof(double) * k0, cudaMemcpyHostToDevice, c.s));
+        h.beta = *rnorm;
+        bb[k0 - 1] = h.beta;
+        PGB_CUDA(cudaMemcpyAsync(c.bbeta + k0 - 1, &bb[k0 - 1], sizeof(double), cudaMemcpyHostToDevice, c.s));
+        h.amax = 0.0;
+        for (int j = 1; j <= k0; j++) {
+            h.amax = std::max(h.amax, std::max(ba[j - 1], bb[j - 1]));
+            double a1, b1;
+            if (j == 1) {
+                anorm = std::max(anorm, FUDGE * h.alpha);
+            } else if (j == 2) {
+                a1 = bb[0] / h.amax;
+                a1 = FUDGE * h.amax * std::sqrt((ba[0] / h.amax) * (ba[0] / h.amax) + a1 * a1 + ba[1] / h.amax * a1);
+                anorm = std::max(anorm, a1);
+            } else {
+                a1 = ba[j - 2] / h.amax;
+                b1 = bb[j - 2] / h.amax;
+                a1 = FUDGE * h.amax * std::sqrt(a1 * a1 + b1 * b1 + a1 * bb[j - 3] / h.amax + ba[j - 1] / h.amax * b1);
+                anorm = std::max(anorm, a1);
+            }
+        }
+        j0 = k0 + 1;
+    }
+    h.anorm = anorm;
+    h.numax = 0.0;
+    h.mumax = 0.0;
+    h.rnorm = *rnorm;
+    h.ierr = *ierr;
+    h.j = j0;
+    h.ticket = 0;
+    c.put_ctl();
+
+    // the step loop: enqueue everything, then look for a suspension
+    const bool host_ap = (c.op == nullptr);
+    int j = j0, side = 0;
+    bool finished = false;
+    int rounds = 0;
+    while (!finished) {
+        if (++rounds > 4 * (k + 2)) {
+            set_error("dlanbpro: too many suspensions");
+            throw WaitFailure();
+        }
+        LbArgs a = c.args();
+        if (!host_ap) {
+            for (; j <= k; j++) {
+                for (; side < 2; side++) lb_enqueue_half(a, c.op, side, j, h.ielr, c.ntry_spec, false, c.s);
+                side = 0;
+            }
+            c.get_ctl();
+        } else {
+            // host APROD: one synchronous product per half step
+            bool susp = false;
+            for (; j <= k && !susp; j++) {
+                for (; side < 2 && !susp; side++) {
+                    double *x = side == 0 ? c.U + (size_t)(j - 1) * c.ldu : c.V + (size_t)(j - 1) * c.ldv;
+                    double *y = side == 0 ? c.V + (size_t)(j - 1) * c.ldv : c.U + (size_t)j * c.ldu;
+                    // the product must see the scaled input
+                    k_apply_pend_col<<<c.nb, 256, 0, c.s>>>(c.ctl, c.U, c.ldu, c.V, c.ldv, m, n, side == 0 ? 0 : 1);
+                    PGB_LAUNCHED();
+                    k_clear_pend<<<1, 1, 0, c.s>>>(c.ctl, side == 0 ? 0 : 1);
+                    PGB_LAUNCHED();
+                    dev_aprod(c, side == 0, x, y);
+                    lb_enqueue_half(a, nullptr, side, j, h.ielr, c.ntry_spec, true, c.s);
+                    c.get_ctl();
+                    if (h.status != 0) susp = true;
+                    if (susp) break;
+                }
+                if (susp) break;
+                side = 0;
+            }
+            if (!susp) c.get_ctl();
+        }
+        if (h.status == 0) {
+            finished = true;
+            break;
+        }
+        // ---- a suspension: finish the case on the host side, then resume
+        const int sj = h.susp_j, ss = h.susp_side;
+        if (h.susp_reason == 2) {
+            h.status = 0;
+            c.put_ctl();
+            lb_enqueue_cgs_more(c.args(), ss, sj, NTRY - c.ntry_spec, c.s);
+            c.get_ctl();
+            if (h.status != 0 && h.susp_reason == 2) {
+                set_error("reorthogonalisation did not finish within NTRY passes");
+                throw WaitFailure();
+            }
+            if (h.status == 0) {
+                // continue after the finished half step
+                if (ss == 0) { j = sj; side = 1; }
+                else { j = sj + 1; side = 0; }
+                continue;
+            }
+            // fell into an invariant-subspace suspension: handled below
+        }
+        if (h.susp_reason != 1) {
+            set_error("device control block reports an unknown suspension");
+            throw WaitFailure();
+        }
+        if (h.susp_reason == 1) {
+            const int jj = h.susp_j;
+            h.status = 0;
+            if (h.susp_side == 0) {
+                // dlanbpro.F:372-405: new random v_j orthogonal to V(:,1:j-1)
+                // (u_j may still carry its deferred scale: apply it first)
+                c.put_ctl();
+                k_apply_pend_col<<<c.nb, 256, 0, c.s>>>(c.ctl, c.U, c.ldu, c.V, c.ldv, m, n, 0);
+                PGB_LAUNCHED();
+                k_clear_pend<<<1, 1, 0, c.s>>>(c.ctl, 0);
+                PGB_LAUNCHED();
+                c.get_ctl();
+                double alpha = 0.0;
+                double *vj = c.V + (size_t)(jj - 1) * c.ldv;
+                int e = dev_getu0(c, true, jj - 1, 3, vj, &alpha, c.V, c.ldv, &anormest);
+                h.ierr = e;
+                if (alpha == 0.0) {
+                    k = jj - 1;
+                    h.ierr = -jj;
+                    c.put_ctl();
+                    finished = true;
+                    break;
+                }
+                dev_safescal(c, vj, n, alpha);
+                h.alpha = 0.0;
+                h.force_reorth = 1;
+                if (h.delta > 0) h.full_reorth = 0;
+                const double z0 = 0.0;
+                PGB_CUDA(cudaMemcpyAsync(c.balpha + jj - 1, &z0, sizeof(double), cudaMemcpyHostToDevice, c.s));
+                h.pend_v.mode = 0;
+                h.pend_v_col = jj - 1;
+                c.put_ctl();
+                j = jj; side = 1;
+            } else {
+                // dlanbpro.F:503-535: new random u_{j+1} orthogonal to U(:,1:j)
+                c.put_ctl();
+                k_apply_pend_col<<<c.nb, 256, 0, c.s>>>(c.ctl, c.U, c.ldu, c.V, c.ldv, m, n, 1);
+                PGB_LAUNCHED();
+                k_clear_pend<<<1, 1, 0, c.s>>>(c.ctl, 1);
+                PGB_LAUNCHED();
+                c.get_ctl();
+                double beta = 0.0;
+                double *uj1 = c.U + (size_t)jj * c.ldu;
+                int e = dev_getu0(c, false, jj, 3, uj1, &beta, c.U, c.ldu, &anormest);
+                h.ierr = e;
+                if (beta == 0.0) {
+                    k = jj;
+                    h.ierr = -jj;
+                    c.put_ctl();
+                    finished = true;
+                    break;
+                }
+                dev_safescal(c, uj1, m, beta);
+                h.beta = 0.0;
+                h.force_reorth = 1;
+                if (h.delta > 0) h.full_reorth = 0;
+                const double z0 = 0.0;
+                PGB_CUDA(cudaMemcpyAsync(c.bbeta + jj - 1, &z0, sizeof(double), cudaMemcpyHostToDevice, c.s));
+                h.pend_u.mode = 0;
+                h.pend_u_col = jj;
+                h.rnorm = 0.0;
+                c.put_ctl();
+                j = jj + 1; side = 0;
+            }
+            continue;
+        }
+    }
+    // apply the deferred scaling of the newest columns
+    lb_enqueue_flush(c.args(), c.s);
+    c.get_ctl();
+    *kp = k;
+    *rnorm = h.rnorm;
+    *ierr = h.ierr;
+    doption[2] = h.anorm;
+}
+
+// ------------------------------------------------------------- drivers
+static inline bool yes(const char *c) { return c && (c[0] == 'y' || c[0] == 'Y'); }
+
+static void copy_in_u1(Ctx &c, const double *U)
+{
+    PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(double) * c.m, cudaMemcpyHostToDevice, c.s));
+}
+
+static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, bool du, bool dv)
+{
+    if (ncols <= 0) return;
+    if (du)
+        PGB_CUDA(cudaMemcpy2DAsync(U, sizeof(double) * ldu, c.U, sizeof(double) * c.ldu, sizeof(double) * c.m, ncols,
+                                   cudaMemcpyDeviceToHost, c.s));
+    if (dv)
+        PGB_CUDA(cudaMemcpy2DAsync(V, sizeof(double) * ldv, c.V, sizeof(double) * c.ldv, sizeof(double) * c.n, ncols,
+                                   cudaMemcpyDeviceToHost, c.s));
+}
+
+// U(:,0:nc) <- U(:,0:kk) op(B)   (dgemm_ovwr_left)
+static void ovwr_left(Ctx &c, double *A, int lda, int rows, int nc, int kk, const double *B, int ldb, bool tb)
+{
+    gemm(rows, nc, kk, A, lda, false, B, ldb, tb, c.gout, lda, c.s);
+    copy_cols(c.gout, lda, A, lda, rows, nc, c.s);
+}
+
+// dritzvec (double/dritzvec.F:1-199)
+static void dev_ritzvec(Ctx &c, bool small_side, bool du, bool dv, int k, int dim)
+{
+    RitzArgs r;
+    r.balpha = c.balpha; r.bbeta = c.bbeta; r.D = c.D; r.E = c.E; r.Mt = c.Mt; r.P = c.Pr; r.Qt = c.Qt;
+    r.w = c.w; r.dim = dim; r.m = c.m; r.n = c.n;
+    launch_ritz_prep(r, c.s);
+    const int dp1 = dim + 1;
+    // X = P' Mt(1:dim, 1:dim+1)   (dim x dim+1, ld dim+1)
+    gemm(dim, dp1, dim, c.Pr, dim, true, c.Mt, dp1, false, c.X, dp1, c.s);
+    const int mstart = small_side ? dim - k + 1 : 1;
+    if (du) ovwr_left(c, c.U, c.ldu, c.m, k, dp1, c.X + (mstart - 1), dp1, true);
+    if (dv) ovwr_left(c, c.V, c.ldv, c.n, k, dim, c.Qt + (mstart - 1), dim, true);
+}
+
+struct Timer {
+    Ctx &c;
+    double &acc;
+    cudaEvent_t a, b;
+    Timer(Ctx &cc, double &ac) : c(cc), acc(ac)
+    {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, c.s);
+    }
+    ~Timer()
+    {
+        cudaEventRecord(b, c.s);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        acc += ms;
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+};
+
+static void finish_stats(Ctx &c, int64_t launches0)
+{
+    g_last.nopx += c.hctl->nopx;
+    g_last.nreorth += c.hctl->nreorth;
+    g_last.ndot += c.hctl->ndot;
+    g_last.launches = g_launches - launches0;
+    g_stat.nopx += g_last.nopx;
+    g_stat.nreorth += g_last.nreorth;
+    g_stat.ndot += g_last.ndot;
+    g_stat.nrestart += g_last.nrestart;
+    g_stat.nbsvd += g_last.nbsvd;
+    g_stat.nlandim = g_last.nlandim;
+    g_stat.nsing = g_last.nsing;
+    g_stat.device_ms += g_last.device_ms;
+    g_stat.launches += g_last.launches;
+}
+
+static void setup_operator(Ctx &c, propack_aprod_t aprod, double *dparm, int *iparm)
+{
+    if (aprod == propack_gpu_csr_aprod_) {
+        const Operator *op = lookup_operator(handle_from_iparm(iparm));
+        if (!op) {
+            set_error("APROD is propack_gpu_csr_aprod_ but iparm holds no live operator handle");
+            throw ArgFailure();
+        }
+        if (op->m != c.m || op->n != c.n) {
+            set_error("operator shape does not match m, n");
+            throw ArgFailure();
+        }
+        c.op = op;
+    } else {
+        c.aprod = aprod;
+        c.dparm = dparm;
+        c.iparm = iparm;
+        PGB_CUDA(cudaMallocHost(&c.hx, sizeof(double) * std::max(c.m, c.n)));
+        PGB_CUDA(cudaMallocHost(&c.hy, sizeof(double) * std::max(c.m, c.n)));
+    }
+}
+
+static void run_irl(const char *which, const char *jobu, const char *jobv, int m, int n, int dim, int p, int *neig,
+                    int maxiter, propack_aprod_t aprod, double *U, int ldu, double *sigma, double *bnd, double *V,
+                    int ldv, double tolin, double *doption, const int *ioption, int *info, double *dparm, int *iparm)
+{
+    if (m <= 0 || n <= 0 || dim <= 0 || p < 0 || *neig < 0 || ldu < m || ldv < n || !aprod || !U || !V || !sigma ||
+        !bnd || !doption || !ioption) {
+        set_error("dlansvd_irl_: invalid argument");
+        throw ArgFailure();
+    }
+    const int64_t l0 = g_launches;
+    g_last = Stats();
+    const bool small_side = which && (which[0] == 's' || which[0] == 'S');
+    dim = std::min(dim, std::min(n + 1, m + 1));
+    const int k = dim - p;
+    if (k < 1 || *neig > k) {
+        set_error("dlansvd_irl_: need 1 <= neig <= dim - p");
+        throw ArgFailure();
+    }
+    const double tol = std::min(1.0, std::max(16.0 * EPS, tolin));
+    Ctx c;
+    init_ctx(c, m, n, dim);
+    setup_operator(c, aprod, dparm, iparm);
+    const int neig0 = *neig;
+    PGB_CUDA(cudaEventRecord(c.ev0, c.s));
+    copy_in_u1(c, U);
+    double rnorm = dev_nrm2(c, c.U, m);
+    int ierr = 0;
+    double anorm_drv = 0.0;
+    if (rnorm == 0.0) {
+        double est = 0.0;
+        ierr = dev_getu0(c, false, 0, 1, c.U, &rnorm, c.U, c.ldu, &est);
+        anorm_drv = est;
+    }
+    PGB_CUDA(cudaMemcpyAsync(c.anorm_drv, &anorm_drv, sizeof(double), cudaMemcpyHostToDevice, c.s));
+    *info = 0;
+    int iter = 0, nconv = 0, kold = 0;
+    std::vector<double> hs(dim + 2), hb(dim + 2);
+    while (nconv < neig0 && iter < maxiter) {
+        {
+            Timer t(c, g_last.lanczos_ms);
+            dev_lanbpro(c, kold, &dim, &rnorm, doption, ioption, &ierr);
+        }
+        kold = k;
+        {
+            Timer t(c, g_last.bsvd_ms);
+            AnaArgs a;
+            a.balpha = c.balpha; a.bbeta = c.bbeta; a.a1 = c.a1; a.b1 = c.b1; a.bnd = c.bnd; a.w = c.w;
+            a.ctl = c.ctl; a.sigma_out = c.sig_out; a.bnd_out = c.bnd_out; a.nconv_out = c.nconv;
+            a.anorm_drv = c.anorm_drv; a.dim = dim; a.m = m; a.n = n; a.neig = neig0; a.kk = k;
+            a.irl = 1; a.small_side = small_side; a.tol = tol;
+            launch_analyse(a, c.s);
+            g_last.nbsvd++;
+            PGB_CUDA(cudaMemcpyAsync(c.hscal, c.nconv, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+            c.sync();
+            int nc = 0;
+            memcpy(&nc, c.hscal, sizeof(int));
+            nconv = nc;
+        }
+        if (ierr < 0) {
+            if (dim < k) *info = dim;
+            break;
+        }
+        if (nconv < neig0) {
+            {
+                Timer t(c, g_last.bsvd_ms);
+                SweepArgs s;
+                s.balpha = c.balpha; s.bbeta = c.bbeta; s.a1 = c.a1; s.bnd = c.bnd; s.P = c.P; s.Q = c.Q;
+                s.shifts = c.shifts; s.w = c.w; s.ctl = c.ctl; s.dim = dim; s.k = k; s.neig = neig0;
+                s.small_side = small_side; s.min_relgap = doption[3];
+                launch_sweeps(s, c.s);
+            }
+            {
+                Timer t(c, g_last.gemm_ms);
+                ovwr_left(c, c.U, c.ldu, m, k + 1, dim + 1, c.P, dim + 1, false);
+                ovwr_left(c, c.V, c.ldv, n, k, dim, c.Q, dim, false);
+            }
+            // rnorm = beta_k after the sweeps (written into the control block)
+            c.get_ctl();
+            rnorm = c.hctl->rnorm;
+            g_last.nrestart++;
+        }
+        iter++;
+    }
+    PGB_CUDA(cudaMemcpyAsync(hs.data(), c.sig_out, sizeof(double) * std::max(nconv, 1), cudaMemcpyDeviceToHost, c.s));
+    PGB_CUDA(cudaMemcpyAsync(hb.data(), c.bnd_out, sizeof(double) * std::max(nconv, 1), cudaMemcpyDeviceToHost, c.s));
+    c.sync();
+    for (int i = 0; i < nconv && i < neig0; i++) { sigma[i] = hs[i]; bnd[i] = hb[i]; }
+    const bool du = yes(jobu), dv = yes(jobv);
+    if ((nconv >= neig0 || *info > 0) && (du || dv)) {
+        Timer t(c, g_last.gemm_ms);
+        dev_ritzvec(c, small_side, du, dv, nconv, dim);
+    }
+    copy_out(c, U, ldu, V, ldv, nconv, du, dv);
+    PGB_CUDA(cudaEventRecord(c.ev1, c.s));
+    c.sync();
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    g_last.device_ms = ms;
+    *neig = nconv;
+    g_last.nlandim = dim;
+    c.get_ctl();
+    finish_stats(c, l0);
+}
+
+static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp, int kmax, propack_aprod_t aprod,
+                       double *U, int ldu, double *sigma, double *bnd, double *V, int ldv, double tolin,
+                       double *doption, const int *ioption, int *info, double *dparm, int *iparm)
+{
+    const int k = *kp;
+    if (m <= 0 || n <= 0 || k <= 0 || kmax <= 0 || ldu < m || ldv < n || !aprod || !U || !V || !sigma || !bnd ||
+        !doption || !ioption) {
+        set_error("dlansvd_: invalid argument");
+        throw ArgFailure();
+    }
+    const int64_t l0 = g_launches;
+    g_last = Stats();
+    const int lanmax = std::min(std::min(n + 1, m + 1), kmax);
+    const double tol = std::min(1.0, std::max(16.0 * EPS, tolin));
+    Ctx c;
+    init_ctx(c, m, n, lanmax);
+    setup_operator(c, aprod, dparm, iparm);
+    PGB_CUDA(cudaEventRecord(c.ev0, c.s));
+    copy_in_u1(c, U);
+    double rnorm = dev_nrm2(c, c.U, m);
+    int ierr = 0;
+    double anorm_drv = 0.0;
+    if (rnorm == 0.0) {
+        double est = 0.0;
+        ierr = dev_getu0(c, false, 0, 1, c.U, &rnorm, c.U, c.ldu, &est);
+        anorm_drv = est;
+    }
+    PGB_CUDA(cudaMemcpyAsync(c.anorm_drv, &anorm_drv, sizeof(double), cudaMemcpyHostToDevice, c.s));
+    g_last.nsing = k;
+    *info = 0;
+    int neig = 0, jold = 0;
+    int j = std::min(k + std::max(8, k) + 1, lanmax);
+    std::vector<double> hs(lanmax + 2), hb(lanmax + 2);
+    while (neig < k) {
+        {
+            Timer t(c, g_last.lanczos_ms);
+            dev_lanbpro(c, jold, &j, &rnorm, doption, ioption, &ierr);
+        }
+        jold = j;
+        {
+            Timer t(c, g_last.bsvd_ms);
+            AnaArgs a;
+            a.balpha = c.balpha; a.bbeta = c.bbeta; a.a1 = c.a1; a.b1 = c.b1; a.bnd = c.bnd; a.w = c.w;
+            a.ctl = c.ctl; a.sigma_out = c.sig_out; a.bnd_out = c.bnd_out; a.nconv_out = c.nconv;
+            a.anorm_drv = c.anorm_drv; a.dim = j; a.m = m; a.n = n; a.neig = k; a.kk = k;
+            a.irl = 0; a.small_side = 0; a.tol = tol;
+            launch_analyse(a, c.s);
+            g_last.nbsvd++;
+            PGB_CUDA(cudaMemcpyAsync(c.hscal, c.nconv, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+            c.sync();
+            memcpy(&neig, c.hscal, sizeof(int));
+        }
+        if (ierr < 0) {
+            if (j < k) *info = j;
+            break;
+        }
+        if (j >= lanmax) {
+            if (neig < k) *info = -1;
+            break;
+        }
+        int dj;
+        if (neig > 1) {
+            dj = std::min(j / 2, ((k - neig) * (j - 6)) / (2 * neig + 1));
+            dj = std::min(100, std::max(2, dj));
+        } else {
+            dj = j / 2;
+            dj = std::min(100, std::max(10, dj));
+        }
+        j = std::min(j + dj, lanmax);
+    }
+    const int lim = std::min(j, k);
+    PGB_CUDA(cudaMemcpyAsync(hs.data(), c.sig_out, sizeof(double) * std::max(neig, 1), cudaMemcpyDeviceToHost, c.s));
+    PGB_CUDA(cudaMemcpyAsync(hb.data(), c.bnd_out, sizeof(double) * std::max(lim, 1), cudaMemcpyDeviceToHost, c.s));
+    c.sync();
+    for (int i = 0; i < neig; i++) sigma[i] = hs[i];
+    for (int i = 0; i < lim; i++) bnd[i] = hb[i];
+    const bool du = yes(jobu), dv = yes(jobv);
+    if ((neig >= k || *info > 0) && (du || dv)) {
+        Timer t(c, g_last.gemm_ms);
+        dev_ritzvec(c, false, du, dv, neig, jold);
+    }
+    copy_out(c, U, ldu, V, ldv, neig, du, dv);
+    PGB_CUDA(cudaEventRecord(c.ev1, c.s));
+    c.sync();
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    g_last.device_ms = ms;
+    *kp = neig;
+    g_last.nlandim = j;
+    c.get_ctl();
+    finish_stats(c, l0);
+}
+
+}  // namespace pgb
+
+// ------------------------------------------------------------------ C ABI
+using namespace pgb;
+
+extern "C" void dlansvd_irl_(const char *which, const char *jobu, const char *jobv, const int *m, const int *n,
+                             const int *dim, const int *p, int *neig, const int *maxiter, propack_aprod_t aprod,
+                             double *U, const int *ldu, double *sigma, double *bnd, double *V, const int *ldv,
+                             const double *tolin, double *work, const int *lwork, int *iwork, const int *liwork,
+                             double *doption, const int *ioption, int *info, double *dparm, int *iparm,
+                             size_t which_len, size_t jobu_len, size_t jobv_len)
+{
+    (void)work; (void)lwork; (void)iwork; (void)liwork; (void)which_len; (void)jobu_len; (void)jobv_len;
+    set_error("");
+    try {
+        run_irl(which, jobu, jobv, *m, *n, *dim, *p, neig, *maxiter, aprod, U, *ldu, sigma, bnd, V, *ldv, *tolin,
+                doption, ioption, info, dparm, iparm);
+    } catch (const CudaFailure &) {
+        *info = PROPACK_ERR_CUDA;
+    } catch (const ArgFailure &) {
+        *info = PROPACK_ERR_ARG;
+    } catch (const WaitFailure &) {
+        *info = PROPACK_ERR_WAIT;
+    }
+}
+
+extern "C" void dlansvd_(const char *jobu, const char *jobv, const int *m, const int *n, int *k, const int *kmax,
+                         propack_aprod_t aprod, double *U, const int *ldu, double *sigma, double *bnd, double *V,
+                         const int *ldv, const double *tolin, double *work, const int *lwork, int *iwork,
+                         const int *liwork, double *doption, const int *ioption, int *info, double *dparm, int *iparm,
+                         size_t jobu_len, size_t jobv_len)
+{
+    (void)work; (void)lwork; (void)iwork; (void)liwork; (void)jobu_len; (void)jobv_len;
+    set_error("");
+    try {
+        run_lansvd(jobu, jobv, *m, *n, k, *kmax, aprod, U, *ldu, sigma, bnd, V, *ldv, *tolin, doption, ioption, info,
+                   dparm, iparm);
+    } catch (const CudaFailure &) {
+        *info = PROPACK_ERR_CUDA;
+    } catch (const ArgFailure &) {
+        *info = PROPACK_ERR_ARG;
+    } catch (const WaitFailure &) {
+        *info = PROPACK_ERR_WAIT;
+    }
+}
+
+extern "C" void clearstat_(void) { g_stat = Stats(); }
+
+extern "C" void printstat_(void)
+{
+    const Stats &s = g_stat;
+    printf("+-----------------------------------------------------------+\n");
+    printf(" Dimension of Lanczos basis                  = %12lld\n", (long long)s.nlandim);
+    printf(" Number of singular values requested         = %12lld\n", (long long)s.nsing);
+    printf(" Number of restarts                          = %12lld\n", (long long)s.nrestart);
+    printf(" Number of matrix-vector multiplications     = %12lld\n", (long long)s.nopx);
+    printf(" Number of reorthogonalizations              = %12lld\n", (long long)s.nreorth);
+    printf(" Number of inner products in reorth.         = %12lld\n", (long long)s.ndot);
+    printf(" Number of bidiagonal SVDs                   = %12lld\n", (long long)s.nbsvd);
+    printf(" Device time (ms)                            = %12.3f\n", s.device_ms);
+    printf(" Kernel launches                             = %12lld\n", (long long)s.launches);
+    printf("+-----------------------------------------------------------+\n");
+}
+
+extern "C" void propack_get_stats(propack_stats_t *out)
+{
+    const Stats &s = g_last;
+    out->nopx = s.nopx;
+    out->nreorth = s.nreorth;
+    out->ndot = s.ndot;
+    out->nrestart = s.nrestart;
+    out->nbsvd = s.nbsvd;
+    out->nlandim = s.nlandim;
+    out->device_ms = s.device_ms;
+    out->lanczos_ms = s.lanczos_ms;
+    out->bsvd_ms = s.bsvd_ms;
+    out->gemm_ms = s.gemm_ms;
+    out->kernel_launches = s.launches;
+}

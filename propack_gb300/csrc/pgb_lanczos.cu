@@ -1,0 +1,752 @@
+// pgb_lanczos.cu -- device-resident steps of dlanbpro (double/dlanbpro.F:283-546).
+//
+// One Lanczos step is a fixed sequence of kernels per half step (V half:
+// alpha_j v_j = A' u_j - beta_j v_{j-1}; U half: beta_{j+1} u_{j+1} =
+// A v_j - alpha_j u_j):
+//
+//   k_lb_spmv     fused SpMV + axpy with the previous vector + partial
+//                 sums of ||y||^2 and <prev, y>  (dlanbpro.F:288-296, :420-424)
+//   k_lb_elr      one extended-local-reorthogonalisation pass (:301-316, :429-443)
+//   k_lb_cgs_dots first classical Gram-Schmidt projection (dreorth.F:174)
+//   k_lb_cgs_upd  v -= W h fused with the projections of the updated
+//                 vector for the next pass (dreorth.F:85-95, dcgs :199)
+//
+// Every kernel ends with a last-CTA tail that reduces the partial sums in a
+// fixed order and runs the scalar logic of dlanbpro on the device: the
+// alpha/beta bookkeeping, the ||A|| estimate, the omega recurrences
+// (dupdate_nu/mu, parallel over k), dcompute_int, the reorthogonalisation
+// decision and the invariant-subspace test.  The host never reads a scalar
+// between kernels: a kernel whose phase is not needed (no ELR, no
+// reorthogonalisation) sees that in the control block and returns at once.
+// Cases that the fixed sequence cannot finish (an invariant subspace that
+// needs a fresh random vector, more Gram-Schmidt passes than were enqueued)
+// set status = 1 and every later kernel of the sequence returns; the host
+// finishes the case and resumes.
+//
+// dsafescal (dsafescal.F:4-55) is deferred: the new vector is left
+// unscaled, the product that reads it through the operator is scaled
+// instead (A(v/a) = (Av)/a), and the next same-side SpMV, which reads it
+// row by row, writes the scaled value back.
+#include "pgb.cuh"
+#include "pgb_spmv.cuh"
+
+namespace pgb {
+
+struct Tail {
+    LbCtl c;
+    int go;
+    double red[32];
+};
+
+__device__ __forceinline__ Pend make_scale(double a)
+{
+    Pend p;
+    if (fabs(a) >= SFMIN) { p.mode = 1; p.val = 1.0 / a; }
+    else { p.mode = 2; p.val = a; }
+    return p;
+}
+
+// ---------------------------------------------------------------- tails
+__device__ void tail_load(const LbArgs &a, Tail &t)
+{
+    if (threadIdx.x == 0) t.c = *a.ctl;
+    __syncthreads();
+}
+__device__ void tail_store(const LbArgs &a, Tail &t)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *a.ctl = t.c;
+        __threadfence();
+    }
+}
+// fixed-order sum of the per-CTA partials
+__device__ double sum_parts(const double *p, int nb, double *red)
+{
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += BS) s += p[b];
+    return block_sum<BS>(s, red);
+}
+
+// dset_mu (dlanbpro.F:555-577), thread 0
+__device__ void set_mu(int k, double *mu, const int *index, double val)
+{
+    int i = 0;
+    while (index[i] <= k && index[i] > 0) {
+        const int p = index[i], q = index[i + 1];
+        for (int j = p; j <= q; j++) mu[j - 1] = val;
+        i += 2;
+    }
+}
+
+// dcompute_int (dlanbpro.F:581-624), thread 0.  Fortran DO-variable exit
+// values are reproduced (s = lo-1 and i = j+1 when a search runs out).
+__device__ void compute_int(const double *mu, int j, double delta, double eta, int *index)
+{
+    if (delta < eta) return;
+    int ip = 0, i = 0, k, s;
+    index[0] = 0;
+    while (i < j) {
+        for (k = i + 1; k <= j; k++)
+            if (fabs(mu[k - 1]) > delta) break;
+        if (k > j) break;
+        const int lo = i > 1 ? i : 1;
+        for (s = k; s >= lo; s--)
+            if (fabs(mu[s - 1]) < eta) break;
+        index[ip++] = s + 1;
+        for (i = s + 1; i <= j; i++)
+            if (fabs(mu[i - 1]) < eta) break;
+        index[ip++] = i - 1;
+    }
+    index[ip] = j + 1;
+}
+
+// expand index[] into the 0-based column list walked by dcgs (CGS) or
+// dmgs (MGS stops at an empty range); thread 0.  Returns the ndot count
+// of one pass.
+__device__ int build_sel(const int *index, int kk, int icgs, int *sel, int *nsel)
+{
+    int ns = 0, nd = 0, i = 0;
+    if (icgs) {
+        while (index[i] <= kk && index[i] > 0) {
+            const int p = index[i], q = index[i + 1];
+            nd += q - p + 1;
+            for (int c = p; c <= q; c++) sel[ns++] = c - 1;
+            i += 2;
+        }
+    } else {
+        int p = index[0], q = index[1];
+        while (p <= kk && p > 0 && p <= q) {
+            nd += q - p + 1;
+            for (int c = p; c <= q; c++) sel[ns++] = c - 1;
+            i += 2;
+            p = index[i];
+            q = index[i + 1];
+        }
+    }
+    *nsel = ns;
+    return nd + kk;
+}
+
+// dupdate_nu (dlanbpro.F:684-723), all threads; j > 1
+__device__ void update_nu_par(Tail &t, const LbArgs &a, int j)
+{
+    const double *ba = a.balpha, *bb = a.bbeta;
+    double *mu = a.mu, *nu = a.nu;
+    const double e1 = t.c.epsn2, an = t.c.anorm;
+    const double aj = ba[j - 1], bjm = bb[j - 2];
+    const double hj = hypot(aj, bjm);
+    double loc = 0.0;
+    for (int k = 1 + threadIdx.x; k <= j - 1; k += BS) {
+        double v = bb[k - 1] * mu[k] + ba[k - 1] * mu[k - 1] - bjm * nu[k - 1];
+        const double d = e1 * (hypot(ba[k - 1], bb[k - 1]) + hj) + e1 * an;
+        v = (v + copysign(d, v)) / aj;
+        nu[k - 1] = v;
+        loc = fmax(loc, fabs(v));
+    }
+    const double mx = block_max<BS>(loc, t.red);
+    if (threadIdx.x == 0) {
+        nu[j - 1] = 1.0;
+        t.c.numax = mx;
+    }
+    __syncthreads();
+}
+
+// dupdate_mu (dlanbpro.F:628-679), all threads
+__device__ void update_mu_par(Tail &t, const LbArgs &a, int j)
+{
+    const double *ba = a.balpha, *bb = a.bbeta;
+    double *mu = a.mu;
+    const double *nu = a.nu;
+    const double e1 = t.c.epsn2, an = t.c.anorm;
+    double loc = 0.0;
+    if (j == 1) {
+        if (threadIdx.x == 0) {
+            mu[0] = e1 / bb[0];
+            loc = fabs(mu[0]);
+        }
+    } else {
+        const double aj = ba[j - 1], bj = bb[j - 1];
+        const double hj = hypot(aj, bj);
+        for (int k = 1 + threadIdx.x; k <= j; k += BS) {
+            double v, d;
+            if (k == 1) {
+                v = ba[0] * nu[0] - aj * mu[0];
+                d = e1 * (hj + ba[0]) + e1 * an;
+            } else if (k < j) {
+                v = ba[k - 1] * nu[k - 1] + bb[k - 2] * nu[k - 2] - aj * mu[k - 1];
+                d = e1 * (hj + hypot(ba[k - 1], bb[k - 2])) + e1 * an;
+            } else {
+                v = bb[j - 2] * nu[j - 2];
+                d = e1 * (hj + hypot(aj, bb[j - 2])) + e1 * an;
+            }
+            v = (v + copysign(d, v)) / bj;
+            mu[k - 1] = v;
+            loc = fmax(loc, fabs(v));
+        }
+    }
+    const double mx = block_max<BS>(loc, t.red);
+    if (threadIdx.x == 0) {
+        mu[j] = 1.0;
+        t.c.mumax = mx;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------- V half logic
+__device__ void v_post(Tail &t, const LbArgs &a, int j)
+{
+    if (threadIdx.x != 0) return;
+    LbCtl &c = t.c;
+    if (c.alpha < c.anorm * c.epsn && j < c.k) {
+        c.rnorm = c.alpha;
+        c.alpha = 0.0;
+        c.status = 1;
+        c.susp_reason = 1;
+        c.susp_side = 0;
+        c.susp_j = j;
+        return;
+    } else if (j > 1 && !c.full_reorth && j < c.k && (c.delta * c.alpha < c.anorm * EPS)) {
+        c.ierr = j;
+    }
+    a.balpha[j - 1] = c.alpha;
+    if (c.alpha != 0.0) c.pend_v = make_scale(c.alpha);
+    else { c.pend_v.mode = c.collapsed ? 3 : 0; c.pend_v.val = 0.0; }
+    c.pend_v_col = j - 1;
+}
+__device__ void v_post_reorth(Tail &t, const LbArgs &a, int j)
+{
+    if (threadIdx.x != 0) return;
+    set_mu(j - 1, a.nu, a.index, EPS);
+    t.c.numax = t.c.eta;
+    t.c.force_reorth = !t.c.force_reorth;
+}
+// dlanbpro.F:340-367: nu recurrence and the reorthogonalisation decision
+__device__ void v_reorth_decide(Tail &t, const LbArgs &a, int j)
+{
+    __syncthreads();
+    const bool do_nu = !t.c.full_reorth && t.c.alpha != 0.0;
+    if (do_nu && j > 1) update_nu_par(t, a, j);
+    if (threadIdx.x == 0) {
+        LbCtl &c = t.c;
+        t.go = 4;
+        c.collapsed = 0;
+        if ((c.full_reorth || c.numax > c.delta || c.force_reorth) && c.alpha != 0.0) {
+            if (c.full_reorth || c.eta == 0.0) {
+                a.index[0] = 1; a.index[1] = j - 1; a.index[2] = j;
+            } else if (!c.force_reorth) {
+                compute_int(a.nu, j - 1, c.delta, c.eta, a.index);
+            }
+            if (j - 1 <= 0) {
+                t.go = 3;  // dreorth returns at once for k <= 0
+            } else {
+                c.ndot_iter = build_sel(a.index, j - 1, c.icgs, a.sel, &c.nsel);
+                c.reorth_active = 1;
+                c.reorth_iter = 0;
+                c.reorth_nrm0 = c.alpha;
+                t.go = 0;
+            }
+        }
+    }
+    __syncthreads();
+    if (t.go == 3) { v_post_reorth(t, a, j); v_post(t, a, j); }
+    else if (t.go == 4) v_post(t, a, j);
+}
+// B(j,1), amax and the ||A|| estimate (dlanbpro.F:318-334), then the decision
+__device__ void v_finish_alpha(Tail &t, const LbArgs &a, int j)
+{
+    if (threadIdx.x == 0) {
+        LbCtl &c = t.c;
+        const double *ba = a.balpha, *bb = a.bbeta;
+        a.balpha[j - 1] = c.alpha;
+        c.amax = fmax(c.amax, c.alpha);
+        double a1, b1;
+        if (j == 2) {
+            a1 = bb[0] / c.amax;
+            a1 = FUDGE * c.amax * sqrt((ba[0] / c.amax) * (ba[0] / c.amax) + a1 * a1 + ba[1] / c.amax * a1);
+        } else {
+            a1 = ba[j - 2] / c.amax;
+            b1 = bb[j - 2] / c.amax;
+            a1 = FUDGE * c.amax * sqrt(a1 * a1 + b1 * b1 + a1 * bb[j - 3] / c.amax + ba[j - 1] / c.amax * b1);
+        }
+        c.anorm = fmax(c.anorm, a1);
+    }
+    v_reorth_decide(t, a, j);
+}
+
+// ---------------------------------------------------------- U half logic
+__device__ void u_post(Tail &t, const LbArgs &a, int j)
+{
+    if (threadIdx.x != 0) return;
+    LbCtl &c = t.c;
+    if (c.beta < c.anorm * c.epsn && j < c.k) {
+        c.rnorm = c.beta;
+        c.beta = 0.0;
+        c.status = 1;
+        c.susp_reason = 1;
+        c.susp_side = 1;
+        c.susp_j = j;
+        return;
+    } else if (!c.full_reorth && j < c.k && (c.delta * c.beta < c.anorm * EPS)) {
+        c.ierr = j;
+    }
+    a.bbeta[j - 1] = c.beta;
+    if (c.beta != 0.0 && c.beta != 1.0) c.pend_u = make_scale(c.beta);
+    else { c.pend_u.mode = c.collapsed ? 3 : 0; c.pend_u.val = 0.0; }
+    c.pend_u_col = j;
+    c.rnorm = c.beta;
+    c.j = j + 1;
+}
+__device__ void u_post_reorth(Tail &t, const LbArgs &a, int j)
+{
+    if (threadIdx.x != 0) return;
+    set_mu(j, a.mu, a.index, EPS);
+    t.c.mumax = t.c.eta;
+    t.c.force_reorth = !t.c.force_reorth;
+}
+// dlanbpro.F:463-498
+__device__ void u_reorth_decide(Tail &t, const LbArgs &a, int j)
+{
+    __syncthreads();
+    const bool do_mu = !t.c.full_reorth && t.c.beta != 0.0;
+    if (do_mu) update_mu_par(t, a, j);
+    if (threadIdx.x == 0) {
+        LbCtl &c = t.c;
+        t.go = 4;
+        c.collapsed = 0;
+        if ((c.full_reorth || c.mumax > c.delta || c.force_reorth) && c.beta != 0.0) {
+            if (c.full_reorth || c.eta == 0.0) {
+                a.index[0] = 1; a.index[1] = j; a.index[2] = j + 1;
+            } else if (!c.force_reorth) {
+                compute_int(a.mu, j, c.delta, c.eta, a.index);
+            } else {
+                for (int i = 0; i < 2 * j + 1; i++)
+                    if (a.index[i] == j) { a.index[i] = j + 1; break; }
+            }
+            c.ndot_iter = build_sel(a.index, j, c.icgs, a.sel, &c.nsel);
+            c.reorth_active = 1;
+            c.reorth_iter = 0;
+            c.reorth_nrm0 = c.beta;
+            t.go = 0;
+        }
+    }
+    __syncthreads();
+    if (t.go == 4) u_post(t, a, j);
+}
+// B(j,2), amax and the ||A|| estimate (dlanbpro.F:445-458)
+__device__ void u_finish_beta(Tail &t, const LbArgs &a, int j)
+{
+    if (threadIdx.x == 0) {
+        LbCtl &c = t.c;
+        const double *ba = a.balpha, *bb = a.bbeta;
+        a.bbeta[j - 1] = c.beta;
+        c.amax = fmax(c.amax, c.beta);
+        double a1;
+        if (j <= 1) {
+            a1 = hypot(ba[0], bb[0]);
+        } else {
+            a1 = ba[j - 1] / c.amax;
+            a1 = c.amax * sqrt(a1 * a1 + (bb[j - 1] / c.amax) * (bb[j - 1] / c.amax) + a1 * bb[j - 2] / c.amax);
+        }
+        c.anorm = fmax(c.anorm, a1);
+    }
+    u_reorth_decide(t, a, j);
+}
+
+// ------------------------------------------------ continuations by phase
+template <int SIDE>
+__device__ void after_spmv(Tail &t, const LbArgs &a, int j, double nrm, double dotp)
+{
+    if (threadIdx.x == 0) {
+        LbCtl &c = t.c;
+        c.nopx++;
+        t.go = 1;
+        if (SIDE == 0) {
+            if (j > 1) c.pend_v.mode = 0;  // v_{j-1} was scaled in place by the SpMV
+            c.alpha = nrm;
+            if (j == 1) {
+                c.anorm = fmax(c.anorm, FUDGE * c.alpha);
+                t.go = 2;
+            } else if (c.ielr > 0 && c.alpha < KAPPA * c.beta) {
+                c.elr_active = 1;
+                c.elr_iter = 1;
+                c.elr_s = dotp;
+                if (c.beta != 0.0) { c.beta += dotp; a.bbeta[j - 2] = c.beta; }
+                t.go = 0;
+            }
+        } else {
+            c.pend_u.mode = 0;  // u_j was scaled in place by the SpMV
+            c.beta = nrm;
+            if (c.ielr > 0 && c.beta < KAPPA * c.alpha) {
+                c.elr_active = 1;
+                c.elr_iter = 1;
+                c.elr_s = dotp;
+                if (c.alpha != 0.0) { c.alpha += dotp; a.balpha[j - 1] = c.alpha; }
+                t.go = 0;
+            }
+        }
+    }
+    __syncthreads();
+    if (SIDE == 0) {
+        if (t.go == 1) v_finish_alpha(t, a, j);
+        else if (t.go == 2) v_reorth_decide(t, a, j);
+    } else {
+        if (t.go == 1) u_finish_beta(t, a, j);
+    }
+}
+
+template <int SIDE>
+__device__ void after_elr(Tail &t, const LbArgs &a, int j, double snrm, double dotp)
+{
+    if (threadIdx.x == 0) {
+        LbCtl &c = t.c;
+        double &cur = SIDE == 0 ? c.alpha : c.beta;
+        double &oth = SIDE == 0 ? c.beta : c.alpha;
+        t.go = 0;
+        if (snrm >= KAPPA * cur || c.elr_iter >= c.ielr) {
+            if (SIDE == 0) a.nu[j - 2] = EPS;
+            else a.mu[j - 1] = EPS;
+            cur = snrm;
+            c.elr_active = 0;
+            t.go = 1;
+        } else {
+            cur = snrm;
+            c.elr_iter++;
+            c.elr_s = dotp;
+            if (oth != 0.0) {
+                oth += dotp;
+                if (SIDE == 0) a.bbeta[j - 2] = oth;
+                else a.balpha[j - 1] = oth;
+            }
+        }
+    }
+    __syncthreads();
+    if (t.go == 1) {
+        if (SIDE == 0) v_finish_alpha(t, a, j);
+        else u_finish_beta(t, a, j);
+    }
+}
+
+// h[c] = sum over CTAs of part_cols[c*nb + b] (one warp per column)
+__device__ void reduce_cols(const LbArgs &a, int L)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c = w; c < L; c += BS / 32) {
+        const double *p = a.part_cols + (size_t)c * a.nb;
+        double s = 0.0;
+        for (int b = lane; b < a.nb; b += 32) s += p[b];
+        s = warp_sum(s);
+        if (lane == 0) a.h[c] = s;
+    }
+    __syncthreads();
+}
+
+template <int SIDE>
+__device__ void after_cgs(Tail &t, const LbArgs &a, int j, double nrm, int last)
+{
+    if (threadIdx.x == 0) {
+        LbCtl &c = t.c;
+        double &cur = SIDE == 0 ? c.alpha : c.beta;
+        c.ndot += c.ndot_iter;
+        t.go = 0;
+        if (nrm > KAPPA * c.reorth_nrm0) {
+            cur = nrm;
+            c.nreorth++;
+            c.reorth_active = 0;
+            t.go = 1;
+        } else {
+            c.reorth_nrm0 = nrm;
+            c.reorth_iter++;
+            if (c.reorth_iter >= NTRY) {
+                cur = 0.0;
+                c.collapsed = 1;
+                c.nreorth++;
+                c.reorth_active = 0;
+                t.go = 1;
+            } else if (last) {
+                c.status = 1;
+                c.susp_reason = 2;
+                c.susp_side = SIDE;
+                c.susp_j = j;
+                cur = nrm;
+                t.go = 2;
+            } else {
+                cur = nrm;
+                t.go = 2;
+            }
+        }
+    }
+    __syncthreads();
+    if (t.go == 1) {
+        if (SIDE == 0) { v_post_reorth(t, a, j); v_post(t, a, j); }
+        else { u_post_reorth(t, a, j); u_post(t, a, j); }
+    } else if (t.go == 2) {
+        reduce_cols(a, t.c.nsel);
+    }
+}
+
+// ----------------------------------------------------------------- kernels
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_spmv(LbArgs a, int j, int host_product)
+{
+    __shared__ SpmvStage<double> st;
+    __shared__ double sred[32];
+    __shared__ Tail t;
+    if (a.ctl->status != 0) return;
+    const Pend pin = SIDE == 0 ? a.ctl->pend_u : a.ctl->pend_v;
+    const Pend pprev = SIDE == 0 ? a.ctl->pend_v : a.ctl->pend_u;
+    const bool has_prev = SIDE == 1 || j > 1;
+    const double coef = SIDE == 0 ? a.ctl->beta : a.ctl->alpha;
+    const double *x = SIDE == 0 ? a.U + (size_t)(j - 1) * a.ldu : a.V + (size_t)(j - 1) * a.ldv;
+    double *out = SIDE == 0 ? a.V + (size_t)(j - 1) * a.ldv : a.U + (size_t)j * a.ldu;
+    double *prev = SIDE == 0 ? (j > 1 ? a.V + (size_t)(j - 2) * a.ldv : nullptr) : a.U + (size_t)(j - 1) * a.ldu;
+    const Csr &A = SIDE == 0 ? a.adj : a.fwd;
+    const double *z = a.z;
+    const int n0 = A.ncol0;
+    double sq = 0.0, dt = 0.0;
+    auto epi = [&](int r, double acc) {
+        double y = apply_pend(acc, pin);
+        if (has_prev) {
+            double pv = prev[r];
+            if (pprev.mode) {
+                pv = apply_pend(pv, pprev);
+                prev[r] = pv;
+            }
+            y = fma(-coef, pv, y);
+            dt = fma(pv, y, dt);
+        }
+        out[r] = y;
+        sq = fma(y, y, sq);
+    };
+    if (!host_product) {
+        auto xl = [&](int c) -> double { return c < n0 ? x[c] : z[c - n0]; };
+        csr_rows<double, double>(A.ptr, A.idx, A.val, A.blk, A.nblk, xl, epi, st, sred);
+    } else {
+        // the caller's APROD already wrote the product into out
+        for (int r = blockIdx.x * BS + threadIdx.x; r < A.rows; r += gridDim.x * BS) epi(r, out[r]);
+    }
+    sq = block_sum<BS>(sq, sred);
+    dt = block_sum<BS>(dt, sred);
+    if (threadIdx.x == 0) {
+        a.part_sq[blockIdx.x] = sq;
+        a.part_dot[blockIdx.x] = dt;
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
+        const double d2 = sum_parts(a.part_dot, gridDim.x, t.red);
+        after_spmv<SIDE>(t, a, j, sqrt(s2), d2);
+        tail_store(a, t);
+    }
+}
+
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_elr(LbArgs a, int j)
+{
+    __shared__ double sred[32];
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->elr_active) return;
+    const double s = a.ctl->elr_s;
+    const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
+    double *x = SIDE == 0 ? a.V + (size_t)(j - 1) * a.ldv : a.U + (size_t)j * a.ldu;
+    const double *p = SIDE == 0 ? a.V + (size_t)(j - 2) * a.ldv : a.U + (size_t)(j - 1) * a.ldu;
+    double sq = 0.0, dt = 0.0;
+    for (int r = blockIdx.x * BS + threadIdx.x; r < len; r += gridDim.x * BS) {
+        const double pv = p[r];
+        const double y = fma(-s, pv, x[r]);
+        x[r] = y;
+        sq = fma(y, y, sq);
+        dt = fma(pv, y, dt);
+    }
+    sq = block_sum<BS>(sq, sred);
+    dt = block_sum<BS>(dt, sred);
+    if (threadIdx.x == 0) {
+        a.part_sq[blockIdx.x] = sq;
+        a.part_dot[blockIdx.x] = dt;
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
+        const double d2 = sum_parts(a.part_dot, gridDim.x, t.red);
+        after_elr<SIDE>(t, a, j, sqrt(s2), d2);
+        tail_store(a, t);
+    }
+}
+
+// projections W(:,sel)' x: each CTA owns a contiguous row chunk, each warp
+// a subset of the columns.
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_cgs_dots(LbArgs a, int j)
+{
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active) return;
+    const int L = a.ctl->nsel;
+    const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
+    const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
+    const double *W = SIDE == 0 ? a.V : a.U;
+    const double *x = SIDE == 0 ? a.V + (size_t)(j - 1) * a.ldv : a.U + (size_t)j * a.ldu;
+    const int chunk = (len + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * chunk, r1 = min(len, r0 + chunk);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c = w; c < L; c += BS / 32) {
+        const double *col = W + (size_t)a.sel[c] * ld;
+        double acc = 0.0;
+        for (int r = r0 + lane; r < r1; r += 32) acc = fma(col[r], x[r], acc);
+        acc = warp_sum(acc);
+        if (lane == 0) a.part_cols[(size_t)c * a.nb + blockIdx.x] = acc;
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        reduce_cols(a, L);
+        tail_store(a, t);
+    }
+}
+
+// x -= W(:,sel) h, then the projections of the new x for the next pass
+constexpr int CGS_TR = 64;
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
+{
+    extern __shared__ double dyn[];  // h[L] | acc[L]
+    __shared__ double red4[4][CGS_TR];
+    __shared__ double xn[CGS_TR];
+    __shared__ double sred[32];
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active) return;
+    const int L = a.ctl->nsel;
+    double *hs = dyn, *acc = dyn + L;
+    for (int c = threadIdx.x; c < L; c += BS) { hs[c] = a.h[c]; acc[c] = 0.0; }
+    __syncthreads();
+    const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
+    const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
+    const double *W = SIDE == 0 ? a.V : a.U;
+    double *x = SIDE == 0 ? a.V + (size_t)(j - 1) * a.ldv : a.U + (size_t)j * a.ldu;
+    const int chunk = (len + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * chunk, r1 = min(len, r0 + chunk);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int rr = threadIdx.x % CGS_TR, g = threadIdx.x / CGS_TR;
+    double sq = 0.0;
+    for (int tb = r0; tb < r1; tb += CGS_TR) {
+        const int r = tb + rr;
+        double part = 0.0;
+        if (r < r1)
+            for (int c = g; c < L; c += 4) part = fma(W[(size_t)a.sel[c] * ld + r], hs[c], part);
+        red4[g][rr] = part;
+        __syncthreads();
+        if (g == 0) {
+            double v = 0.0;
+            if (r < r1) {
+                v = x[r] - (((red4[0][rr] + red4[1][rr]) + red4[2][rr]) + red4[3][rr]);
+                x[r] = v;
+                sq = fma(v, v, sq);
+            }
+            xn[rr] = v;
+        }
+        __syncthreads();
+        const int ra = tb + lane, rb = tb + lane + 32;
+        const double xa = xn[lane], xb = xn[lane + 32];
+        for (int c = w; c < L; c += BS / 32) {
+            const double *col = W + (size_t)a.sel[c] * ld;
+            double v = 0.0;
+            if (ra < r1) v = col[ra] * xa;
+            if (rb < r1) v = fma(col[rb], xb, v);
+            v = warp_sum(v);
+            if (lane == 0) acc[c] += v;
+        }
+        __syncthreads();
+    }
+    for (int c = threadIdx.x; c < L; c += BS) a.part_cols[(size_t)c * a.nb + blockIdx.x] = acc[c];
+    sq = block_sum<BS>(sq, sred);
+    if (threadIdx.x == 0) a.part_sq[blockIdx.x] = sq;
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
+        after_cgs<SIDE>(t, a, j, sqrt(s2), last);
+        tail_store(a, t);
+    }
+}
+
+// apply the deferred scaling of the newest u and v columns
+__global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
+{
+    if (a.ctl->status != 0) return;
+    const Pend pu = a.ctl->pend_u, pv = a.ctl->pend_v;
+    const int cu = a.ctl->pend_u_col, cv = a.ctl->pend_v_col;
+    const int m = a.fwd.rows, n = a.adj.rows;
+    const int len = m > n ? m : n;
+    for (int r = blockIdx.x * BS + threadIdx.x; r < len; r += gridDim.x * BS) {
+        if (pu.mode && cu >= 0 && r < m) a.U[(size_t)cu * a.ldu + r] = apply_pend(a.U[(size_t)cu * a.ldu + r], pu);
+        if (pv.mode && cv >= 0 && r < n) a.V[(size_t)cv * a.ldv + r] = apply_pend(a.V[(size_t)cv * a.ldv + r], pv);
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        if (threadIdx.x == 0) {
+            a.ctl->pend_u.mode = 0;
+            a.ctl->pend_v.mode = 0;
+            __threadfence();
+        }
+    }
+}
+
+// ------------------------------------------------------------ host side
+void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s);
+
+static size_t cgs_smem(const LbArgs &a) { return sizeof(double) * 2 * (size_t)(a.kmax + 1); }
+
+void lb_set_smem_limits(int kmax)
+{
+    const size_t need = sizeof(double) * 2 * (size_t)(kmax + 1);
+    if (need > 48 * 1024) {
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    }
+}
+
+// Enqueue the kernels of one half step.  host_product: the product was
+// written into the output column by a host APROD call.
+void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int ielr, int ntry_spec,
+                     bool host_product, cudaStream_t s)
+{
+    const int nb = a.nb;
+    if (side == 0) {
+        if (!host_product && op && op->r > 0) op_thin(*op, true, a.U + (size_t)(j - 1) * a.ldu, s);
+        k_lb_spmv<0><<<nb, BS, 0, s>>>(a, j, host_product ? 1 : 0);
+        PGB_LAUNCHED();
+        if (j > 1)
+            for (int i = 0; i < ielr; i++) { k_lb_elr<0><<<nb, BS, 0, s>>>(a, j); PGB_LAUNCHED(); }
+        k_lb_cgs_dots<0><<<nb, BS, 0, s>>>(a, j);
+        PGB_LAUNCHED();
+        for (int i = 0; i < ntry_spec; i++) {
+            k_lb_cgs_upd<0><<<nb, BS, cgs_smem(a), s>>>(a, j, i == ntry_spec - 1);
+            PGB_LAUNCHED();
+        }
+    } else {
+        if (!host_product && op && op->r > 0) op_thin(*op, false, a.V + (size_t)(j - 1) * a.ldv, s);
+        k_lb_spmv<1><<<nb, BS, 0, s>>>(a, j, host_product ? 1 : 0);
+        PGB_LAUNCHED();
+        for (int i = 0; i < ielr; i++) { k_lb_elr<1><<<nb, BS, 0, s>>>(a, j); PGB_LAUNCHED(); }
+        k_lb_cgs_dots<1><<<nb, BS, 0, s>>>(a, j);
+        PGB_LAUNCHED();
+        for (int i = 0; i < ntry_spec; i++) {
+            k_lb_cgs_upd<1><<<nb, BS, cgs_smem(a), s>>>(a, j, i == ntry_spec - 1);
+            PGB_LAUNCHED();
+        }
+    }
+}
+
+// more Gram-Schmidt passes after a suspension with reason 2
+void lb_enqueue_cgs_more(const LbArgs &a, int side, int j, int passes, cudaStream_t s)
+{
+    for (int i = 0; i < passes; i++) {
+        if (side == 0) k_lb_cgs_upd<0><<<a.nb, BS, cgs_smem(a), s>>>(a, j, i == passes - 1);
+        else k_lb_cgs_upd<1><<<a.nb, BS, cgs_smem(a), s>>>(a, j, i == passes - 1);
+        PGB_LAUNCHED();
+    }
+}
+
+void lb_enqueue_flush(const LbArgs &a, cudaStream_t s)
+{
+    k_lb_flush<<<a.nb, BS, 0, s>>>(a);
+    PGB_LAUNCHED();
+}
+
+}  // namespace pgb

@@ -1,0 +1,636 @@
+// pgb_operator.cu -- the device-resident sparse operator A = S + L diag(w) R'
+// (the library's APROD): upload, device-side transpose, CSR-adaptive row
+// blocking, and the plain (unfused) application used by the random start
+// vector (dgetu0.F:71) and by the APROD-compatible C entry point.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "../../include/propack_gb300.h"
+#include "pgb.cuh"
+#include "pgb_spmv.cuh"
+
+namespace pgb {
+
+thread_local int64_t g_launches = 0;
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+const char *last_error() { return g_err.c_str(); }
+
+const Dev &device_info()
+{
+    static thread_local Dev d;
+    static thread_local int cached = -1;
+    int cur = 0;
+    PGB_CUDA(cudaGetDevice(&cur));
+    if (cached != cur) {
+        cudaDeviceProp p;
+        PGB_CUDA(cudaGetDeviceProperties(&p, cur));
+        d.device = cur;
+        d.sms = p.multiProcessorCount;
+        d.nb = d.sms * 4;
+        cached = cur;
+    }
+    return d;
+}
+
+// ------------------------------------------------------------ scans
+// Exclusive prefix sum of n int counts into out[0..n] (out[n] = total).
+__global__ void k_scan_blocks(const int *in, int n, int *bsum)
+{
+    __shared__ int sh[1024];
+    const int base = blockIdx.x * 4096;
+    int s = 0;
+    for (int q = 0; q < 4; q++) {
+        const int i = base + q * 1024 + threadIdx.x;
+        s += (i < n) ? in[i] : 0;
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 512; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) bsum[blockIdx.x] = sh[0];
+}
+__global__ void k_scan_sums(int *bsum, int nblk, int *total_out)
+{
+    // single CTA, sequential over chunks of 1024 with a running carry
+    __shared__ int sh[1024];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < nblk; c0 += 1024) {
+        const int i = c0 + threadIdx.x;
+        const int v = (i < nblk) ? bsum[i] : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            const int t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < nblk) bsum[i] = carry + sh[threadIdx.x] - v;  // exclusive
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += sh[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total_out = carry;
+}
+__global__ void k_scan_final(const int *in, int n, const int *boff, int *out)
+{
+    __shared__ int sh[1024];
+    const int base = blockIdx.x * 4096;
+    int v[4], s = 0;
+    for (int q = 0; q < 4; q++) {
+        const int i = base + threadIdx.x * 4 + q;
+        v[q] = (i < n) ? in[i] : 0;
+        s += v[q];
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += t;
+        __syncthreads();
+    }
+    int run = boff[blockIdx.x] + sh[threadIdx.x] - s;
+    for (int q = 0; q < 4; q++) {
+        const int i = base + threadIdx.x * 4 + q;
+        if (i < n) out[i] = run;
+        run += v[q];
+    }
+}
+// out has n+1 entries; returns the total on the host.
+static int scan_excl(const int *in, int *out, int n, cudaStream_t s)
+{
+    const int nblk = std::max(1, (n + 4095) / 4096);
+    int *bsum = nullptr;
+    PGB_CUDA(cudaMallocAsync(&bsum, sizeof(int) * (nblk + 1), s));
+    k_scan_blocks<<<nblk, 1024, 0, s>>>(in, n, bsum);
+    PGB_LAUNCHED();
+    k_scan_sums<<<1, 1024, 0, s>>>(bsum, nblk, out + n);
+    PGB_LAUNCHED();
+    k_scan_final<<<nblk, 1024, 0, s>>>(in, n, bsum, out);
+    PGB_LAUNCHED();
+    int total = 0;
+    PGB_CUDA(cudaMemcpyAsync(&total, out + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PGB_CUDA(cudaFreeAsync(bsum, s));
+    PGB_CUDA(cudaStreamSynchronize(s));
+    return total;
+}
+
+// ------------------------------------------------------ row blocks
+__global__ void k_blk_flags(const int *ptr, int rows, int half, int *flag)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        int f = (r == 0) || (r % ROWS_PB == 0);
+        const int len = ptr[r + 1] - ptr[r];
+        if (r > 0) {
+            const int lenp = ptr[r] - ptr[r - 1];
+            if (ptr[r] / half != ptr[r - 1] / half) f = 1;
+            if (lenp > half) f = 1;
+        }
+        if (len > half) f = 1;
+        flag[r] = f;
+    }
+}
+__global__ void k_blk_emit(const int *flag, const int *pos, int rows, int *blk)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+        if (flag[r]) blk[pos[r]] = r;
+    if (blockIdx.x == 0 && threadIdx.x == 0) blk[pos[rows]] = rows;
+}
+static void build_blocks(Csr &A, cudaStream_t s)
+{
+    int *flag = nullptr, *pos = nullptr;
+    const int rows = A.rows;
+    PGB_CUDA(cudaMallocAsync(&flag, sizeof(int) * (rows + 1), s));
+    PGB_CUDA(cudaMallocAsync(&pos, sizeof(int) * (rows + 1), s));
+    const int g = std::min(4096, std::max(1, (rows + 255) / 256));
+    if (rows > 0) {
+        k_blk_flags<<<g, 256, 0, s>>>(A.ptr, rows, NNZ_PB / 2, flag);
+        PGB_LAUNCHED();
+    }
+    A.nblk = scan_excl(flag, pos, rows, s);
+    PGB_CUDA(cudaMalloc(&A.blk, sizeof(int) * (A.nblk + 1)));
+    k_blk_emit<<<g, 256, 0, s>>>(flag, pos, rows, A.blk);
+    PGB_LAUNCHED();
+    PGB_CUDA(cudaFreeAsync(flag, s));
+    PGB_CUDA(cudaFreeAsync(pos, s));
+}
+
+// -------------------------------------------------------- transpose
+// T = [A' | X] where X (A.cols x xcols) contributes extra entries appended
+// to every row of A' with column index xoff + col.  Entries of a row of
+// A' come out in increasing original position, i.e. increasing row of A,
+// so the transposed SpMV sums in a fixed order.
+__global__ void k_count_cols(const int *idx, int64_t nnz, int *cnt)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[idx[e]], 1);
+}
+__global__ void k_add_extra(int *tot, const int *cnt, const int *xptr, int cols)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x)
+        tot[c] = cnt[c] + (xptr ? (xptr[c + 1] - xptr[c]) : 0);
+}
+__global__ void k_scatter(const int *ptr, const int *idx, int rows, const int *optr, int *fill,
+                          unsigned long long *key)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+        for (int e = ptr[i]; e < ptr[i + 1]; e++) {
+            const int c = idx[e];
+            const int p = optr[c] + atomicAdd(&fill[c], 1);
+            key[p] = ((unsigned long long)(unsigned)e << 32) | (unsigned)i;
+        }
+    }
+}
+// one warp per segment of length <= 1024: bitonic sort in shared memory;
+// longer segments are listed for k_segsort_long.
+__global__ void k_segsort_warp(unsigned long long *key, const int *optr, const int *cnt, int cols,
+                               int *longlist, int *nlong)
+{
+    __shared__ unsigned long long sh[4][1024];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned long long *s = sh[w];
+    for (int c = blockIdx.x * 4 + w; c < cols; c += gridDim.x * 4) {
+        const int len = cnt[c], off = optr[c];
+        if (len <= 1) continue;
+        if (len > 1024) {
+            if (lane == 0) longlist[atomicAdd(nlong, 1)] = c;
+            continue;
+        }
+        int P = 2;
+        while (P < len) P <<= 1;
+        for (int i = lane; i < P; i += 32) s[i] = (i < len) ? key[off + i] : ~0ull;
+        __syncwarp();
+        for (int k = 2; k <= P; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = lane; i < P; i += 32) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const unsigned long long a = s[i], b = s[ixj];
+                        const bool up = ((i & k) == 0);
+                        if ((a > b) == up) { s[i] = b; s[ixj] = a; }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        for (int i = lane; i < len; i += 32) key[off + i] = s[i];
+        __syncwarp();
+    }
+}
+// one CTA per long segment: bitonic sort in a padded global scratch area
+__global__ void k_segsort_long(unsigned long long *key, const int *optr, const int *cnt, const int *list,
+                               const int64_t *soff, unsigned long long *scratch)
+{
+    const int c = list[blockIdx.x];
+    const int len = cnt[c], off = optr[c];
+    unsigned long long *s = scratch + soff[blockIdx.x];
+    int P = 2;
+    while (P < len) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) s[i] = (i < len) ? key[off + i] : ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = s[i], b = s[ixj];
+                    const bool up = ((i & k) == 0);
+                    if ((a > b) == up) { s[i] = b; s[ixj] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < len; i += blockDim.x) key[off + i] = s[i];
+}
+__global__ void k_finish_t(const unsigned long long *key, const int *optr, const int *cnt, int cols,
+                           const double *val, const int *xptr, const int *xidx, const double *xval, int xoff,
+                           int *oidx, double *oval)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
+        const int off = optr[c], len = cnt[c];
+        for (int q = 0; q < len; q++) {
+            const unsigned long long k = key[off + q];
+            oidx[off + q] = (int)(k & 0xffffffffull);
+            oval[off + q] = val[(int)(k >> 32)];
+        }
+        if (xptr) {
+            int p = off + len;
+            for (int e = xptr[c]; e < xptr[c + 1]; e++, p++) {
+                oidx[p] = xoff + xidx[e];
+                oval[p] = xval[e];
+            }
+        }
+    }
+}
+
+// A: rows x cols device CSR (ptr/idx/val); X optional (cols rows).
+static void transpose_into(Csr &T, const int *ptr, const int *idx, const double *val, int rows, int cols,
+                           int64_t nnz, const int *xptr, const int *xidx, const double *xval, int xoff, int xcols,
+                           cudaStream_t s)
+{
+    int *cnt = nullptr, *tot = nullptr, *fill = nullptr, *longlist = nullptr, *nlong = nullptr;
+    unsigned long long *key = nullptr;
+    PGB_CUDA(cudaMallocAsync(&cnt, sizeof(int) * (cols + 1), s));
+    PGB_CUDA(cudaMallocAsync(&tot, sizeof(int) * (cols + 1), s));
+    PGB_CUDA(cudaMallocAsync(&fill, sizeof(int) * (cols + 1), s));
+    PGB_CUDA(cudaMallocAsync(&longlist, sizeof(int) * (cols + 1), s));
+    PGB_CUDA(cudaMallocAsync(&nlong, sizeof(int), s));
+    PGB_CUDA(cudaMallocAsync(&key, sizeof(unsigned long long) * std::max<int64_t>(nnz, 1), s));
+    PGB_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (cols + 1), s));
+    PGB_CUDA(cudaMemsetAsync(fill, 0, sizeof(int) * (cols + 1), s));
+    PGB_CUDA(cudaMemsetAsync(nlong, 0, sizeof(int), s));
+    const int g = 4096;
+    if (nnz > 0) { k_count_cols<<<g, 256, 0, s>>>(idx, nnz, cnt); PGB_LAUNCHED(); }
+    if (cols > 0) { k_add_extra<<<g, 256, 0, s>>>(tot, cnt, xptr, cols); PGB_LAUNCHED(); }
+    T.rows = cols;
+    T.cols = rows + xcols;
+    T.ncol0 = rows;
+    PGB_CUDA(cudaMalloc(&T.ptr, sizeof(int) * (cols + 1)));
+    const int total = scan_excl(tot, T.ptr, cols, s);
+    T.nnz = total;
+    PGB_CUDA(cudaMalloc(&T.idx, sizeof(int) * std::max(total, 1)));
+    PGB_CUDA(cudaMalloc(&T.val, sizeof(double) * std::max(total, 1)));
+    // the scan wrote T.ptr; optr == T.ptr, the A' part of row c is [ptr[c], ptr[c]+cnt[c])
+    if (rows > 0 && nnz > 0) { k_scatter<<<g, 256, 0, s>>>(ptr, idx, rows, T.ptr, fill, key); PGB_LAUNCHED(); }
+    if (cols > 0) { k_segsort_warp<<<g, 128, 0, s>>>(key, T.ptr, cnt, cols, longlist, nlong); PGB_LAUNCHED(); }
+    int hlong = 0;
+    PGB_CUDA(cudaMemcpyAsync(&hlong, nlong, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PGB_CUDA(cudaStreamSynchronize(s));
+    if (hlong > 0) {
+        std::vector<int> hl(hlong), hc(hlong);
+        PGB_CUDA(cudaMemcpy(hl.data(), longlist, sizeof(int) * hlong, cudaMemcpyDeviceToHost));
+        std::sort(hl.begin(), hl.end());
+        std::vector<int64_t> soff(hlong + 1, 0);
+        for (int q = 0; q < hlong; q++) {
+            int len = 0;
+            PGB_CUDA(cudaMemcpy(&len, cnt + hl[q], sizeof(int), cudaMemcpyDeviceToHost));
+            int64_t P = 2;
+            while (P < len) P <<= 1;
+            soff[q + 1] = soff[q] + P;
+        }
+        int *dl = nullptr;
+        int64_t *doff = nullptr;
+        unsigned long long *scr = nullptr;
+        PGB_CUDA(cudaMalloc(&dl, sizeof(int) * hlong));
+        PGB_CUDA(cudaMalloc(&doff, sizeof(int64_t) * (hlong + 1)));
+        PGB_CUDA(cudaMalloc(&scr, sizeof(unsigned long long) * soff[hlong]));
+        PGB_CUDA(cudaMemcpy(dl, hl.data(), sizeof(int) * hlong, cudaMemcpyHostToDevice));
+        PGB_CUDA(cudaMemcpy(doff, soff.data(), sizeof(int64_t) * (hlong + 1), cudaMemcpyHostToDevice));
+        k_segsort_long<<<hlong, 1024, 0, s>>>(key, T.ptr, cnt, dl, doff, scr);
+        PGB_LAUNCHED();
+        PGB_CUDA(cudaStreamSynchronize(s));
+        PGB_CUDA(cudaFree(dl));
+        PGB_CUDA(cudaFree(doff));
+        PGB_CUDA(cudaFree(scr));
+    }
+    if (cols > 0) {
+        k_finish_t<<<g, 256, 0, s>>>(key, T.ptr, cnt, cols, val, xptr, xidx, xval, rows, T.idx, T.val);
+        PGB_LAUNCHED();
+    }
+    PGB_CUDA(cudaFreeAsync(cnt, s));
+    PGB_CUDA(cudaFreeAsync(tot, s));
+    PGB_CUDA(cudaFreeAsync(fill, s));
+    PGB_CUDA(cudaFreeAsync(longlist, s));
+    PGB_CUDA(cudaFreeAsync(nlong, s));
+    PGB_CUDA(cudaFreeAsync(key, s));
+    (void)xoff;
+}
+
+// fwd = [S | L]: row i holds S's row then L's row (columns n + c)
+__global__ void k_count_merge(const int *sp, const int *lp, int rows, int *tot)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x)
+        tot[i] = (sp[i + 1] - sp[i]) + (lp ? (lp[i + 1] - lp[i]) : 0);
+}
+__global__ void k_merge_rows(const int *sp, const int *si, const double *sv, const int *lp, const int *li,
+                             const double *lv, int rows, int loff, const int *optr, int *oi, double *ov)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+        int p = optr[i];
+        for (int e = sp[i]; e < sp[i + 1]; e++, p++) { oi[p] = si[e]; ov[p] = sv[e]; }
+        if (lp)
+            for (int e = lp[i]; e < lp[i + 1]; e++, p++) { oi[p] = loff + li[e]; ov[p] = lv[e]; }
+    }
+}
+__global__ void k_to_float(const double *a, float *b, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+// ------------------------------------------------------ application
+// z[c] = w[c] * sum(thin row c . x), split into segments of NNZ_PB.
+__global__ void __launch_bounds__(BS) k_thin(Csr T, const double *__restrict__ x, const double *w,
+                                             double *zpart, double *z, unsigned int *ticket, double xscale_dummy)
+{
+    __shared__ double sred[32];
+    (void)xscale_dummy;
+    const int nseg = T.segs;
+    double part_total = 0.0;
+    for (int t = blockIdx.x; t < T.rows * nseg; t += gridDim.x) {
+        const int c = t / nseg, sg = t % nseg;
+        const int a = T.ptr[c] + sg * NNZ_PB;
+        const int b = min(T.ptr[c + 1], a + NNZ_PB);
+        double acc = 0.0;
+        for (int e = a + threadIdx.x; e < b; e += BS) acc += T.val[e] * x[T.idx[e]];
+        acc = block_sum<BS>(acc, sred);
+        if (threadIdx.x == 0) zpart[t] = acc;
+        part_total += acc;
+    }
+    (void)part_total;
+    if (last_cta(ticket)) {
+        for (int c = threadIdx.x; c < T.rows; c += BS) {
+            double s = 0.0;
+            for (int sg = 0; sg < nseg; sg++) s += zpart[c * nseg + sg];
+            z[c] = w[c] * s;
+        }
+    }
+}
+
+// y = A x (A = fwd or adj) with x already carrying z for the tail columns
+__global__ void __launch_bounds__(BS) k_spmv_plain(Csr A, const double *__restrict__ x,
+                                                   const double *__restrict__ z, double *__restrict__ y)
+{
+    __shared__ SpmvStage<double> st;
+    __shared__ double sred[32];
+    const int n0 = A.ncol0;
+    auto xl = [&](int c) -> double { return c < n0 ? __ldg(x + c) : z[c - n0]; };
+    auto epi = [&](int r, double acc) { y[r] = acc; };
+    csr_rows<double, double>(A.ptr, A.idx, A.val, A.blk, A.nblk, xl, epi, st, sred);
+}
+
+void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s)
+{
+    if (op.r <= 0) return;
+    const Csr &T = trans ? op.thin_l : op.thin_r;
+    const int nt = std::max(1, T.rows * T.segs);
+    k_thin<<<std::min(nt, device_info().nb), BS, 0, s>>>(T, x, op.w, op.zpart, op.zbuf, op.zticket, 1.0);
+    PGB_LAUNCHED();
+}
+
+void op_apply(const Operator &op, bool trans, const double *x, double *y, cudaStream_t s)
+{
+    op_thin(op, trans, x, s);
+    const Csr &A = trans ? op.adj : op.fwd;
+    k_spmv_plain<<<device_info().nb, BS, 0, s>>>(A, x, op.zbuf, y);
+    PGB_LAUNCHED();
+}
+
+// ------------------------------------------------------- registry
+static std::mutex g_reg_mu;
+static std::map<int64_t, Operator *> g_reg;
+static int64_t g_next_id = 1;
+
+Operator *lookup_operator(int64_t handle)
+{
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    auto it = g_reg.find(handle);
+    return it == g_reg.end() ? nullptr : it->second;
+}
+
+static void free_csr(Csr &A)
+{
+    cudaFree(A.ptr); cudaFree(A.idx); cudaFree(A.val); cudaFree(A.valf); cudaFree(A.blk);
+    A = Csr();
+}
+
+static int *upload_ptr(const int64_t *p, int rows, cudaStream_t s)
+{
+    std::vector<int> h(rows + 1);
+    for (int i = 0; i <= rows; i++) h[i] = (int)p[i];
+    int *d = nullptr;
+    PGB_CUDA(cudaMalloc(&d, sizeof(int) * (rows + 1)));
+    PGB_CUDA(cudaMemcpyAsync(d, h.data(), sizeof(int) * (rows + 1), cudaMemcpyHostToDevice, s));
+    PGB_CUDA(cudaStreamSynchronize(s));
+    return d;
+}
+template <typename T>
+static T *upload(const T *p, int64_t n, cudaStream_t s)
+{
+    T *d = nullptr;
+    PGB_CUDA(cudaMalloc(&d, sizeof(T) * std::max<int64_t>(n, 1)));
+    if (n > 0) PGB_CUDA(cudaMemcpyAsync(d, p, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+    return d;
+}
+
+static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, const double *sv, int r,
+                           const int64_t *lp, const int32_t *li, const double *lv, const int64_t *rp,
+                           const int32_t *ri, const double *rv, const double *w, int64_t *handle)
+{
+    if (m <= 0 || n <= 0 || r < 0 || !sp || !handle) throw ArgFailure();
+    const int64_t snnz = sp[m];
+    const int64_t lnnz = r > 0 ? lp[m] : 0, rnnz = r > 0 ? rp[n] : 0;
+    if (snnz < 0 || snnz + lnnz >= (int64_t)INT32_MAX || snnz + rnnz >= (int64_t)INT32_MAX) {
+        set_error("operator has 2^31 or more nonzeros");
+        throw ArgFailure();
+    }
+    if (r > 0 && (!lp || !li || !lv || !rp || !ri || !rv || !w)) throw ArgFailure();
+    // column indices must be in range (checked on the host, once)
+    for (int64_t e = 0; e < snnz; e++)
+        if (si[e] < 0 || si[e] >= n) { set_error("S column index out of range"); throw ArgFailure(); }
+    for (int64_t e = 0; e < lnnz; e++)
+        if (li[e] < 0 || li[e] >= r) { set_error("L column index out of range"); throw ArgFailure(); }
+    for (int64_t e = 0; e < rnnz; e++)
+        if (ri[e] < 0 || ri[e] >= r) { set_error("R column index out of range"); throw ArgFailure(); }
+    device_info();
+    cudaStream_t s;
+    PGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    Operator *op = new Operator();
+    op->m = m; op->n = n; op->r = r;
+    PGB_CUDA(cudaGetDevice(&op->device));
+    int *dsp = upload_ptr(sp, m, s);
+    int *dsi = upload<int>(si, snnz, s);
+    double *dsv = upload<double>(sv, snnz, s);
+    int *dlp = nullptr, *dli = nullptr, *drp = nullptr, *dri = nullptr;
+    double *dlv = nullptr, *drv = nullptr;
+    if (r > 0) {
+        dlp = upload_ptr(lp, m, s); dli = upload<int>(li, lnnz, s); dlv = upload<double>(lv, lnnz, s);
+        drp = upload_ptr(rp, n, s); dri = upload<int>(ri, rnnz, s); drv = upload<double>(rv, rnnz, s);
+        op->w = upload<double>(w, r, s);
+    }
+    const int g = 4096;
+    // fwd = [S | L]
+    {
+        Csr &A = op->fwd;
+        A.rows = m; A.cols = n + r; A.ncol0 = n;
+        int *tot = nullptr;
+        PGB_CUDA(cudaMallocAsync(&tot, sizeof(int) * (m + 1), s));
+        k_count_merge<<<g, 256, 0, s>>>(dsp, dlp, m, tot);
+        PGB_LAUNCHED();
+        PGB_CUDA(cudaMalloc(&A.ptr, sizeof(int) * (m + 1)));
+        A.nnz = scan_excl(tot, A.ptr, m, s);
+        PGB_CUDA(cudaMalloc(&A.idx, sizeof(int) * std::max<int64_t>(A.nnz, 1)));
+        PGB_CUDA(cudaMalloc(&A.val, sizeof(double) * std::max<int64_t>(A.nnz, 1)));
+        k_merge_rows<<<g, 256, 0, s>>>(dsp, dsi, dsv, dlp, dli, dlv, m, n, A.ptr, A.idx, A.val);
+        PGB_LAUNCHED();
+        PGB_CUDA(cudaFreeAsync(tot, s));
+        build_blocks(A, s);
+    }
+    // adj = [S' | R]
+    transpose_into(op->adj, dsp, dsi, dsv, m, n, snnz, drp, dri, drv, m, r, s);
+    build_blocks(op->adj, s);
+    if (r > 0) {
+        // thin_r = R' (r x n), thin_l = L' (r x m)
+        transpose_into(op->thin_r, drp, dri, drv, n, r, rnnz, nullptr, nullptr, nullptr, 0, 0, s);
+        transpose_into(op->thin_l, dlp, dli, dlv, m, r, lnnz, nullptr, nullptr, nullptr, 0, 0, s);
+        for (Csr *T : {&op->thin_r, &op->thin_l}) {
+            std::vector<int> hp(r + 1);
+            PGB_CUDA(cudaMemcpy(hp.data(), T->ptr, sizeof(int) * (r + 1), cudaMemcpyDeviceToHost));
+            int mx = 0;
+            for (int c = 0; c < r; c++) mx = std::max(mx, hp[c + 1] - hp[c]);
+            T->segs = std::max(1, (mx + NNZ_PB - 1) / NNZ_PB);
+        }
+        const int segs = std::max(op->thin_r.segs, op->thin_l.segs);
+        PGB_CUDA(cudaMalloc(&op->zbuf, sizeof(double) * r));
+        PGB_CUDA(cudaMalloc(&op->zpart, sizeof(double) * (size_t)r * segs));
+        PGB_CUDA(cudaMemset(op->zbuf, 0, sizeof(double) * r));
+    }
+    PGB_CUDA(cudaMalloc(&op->zticket, sizeof(unsigned int)));
+    PGB_CUDA(cudaMemset(op->zticket, 0, sizeof(unsigned int)));
+    // FP32 copies of the values for the mixed-precision path
+    for (Csr *A : {&op->fwd, &op->adj}) {
+        PGB_CUDA(cudaMalloc(&A->valf, sizeof(float) * std::max<int64_t>(A->nnz, 1)));
+        k_to_float<<<g, 256, 0, s>>>(A->val, A->valf, A->nnz);
+        PGB_LAUNCHED();
+    }
+    PGB_CUDA(cudaStreamSynchronize(s));
+    cudaFree(dsp); cudaFree(dsi); cudaFree(dsv);
+    if (r > 0) { cudaFree(dlp); cudaFree(dli); cudaFree(dlv); cudaFree(drp); cudaFree(dri); cudaFree(drv); }
+    PGB_CUDA(cudaStreamDestroy(s));
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mu);
+        op->id = g_next_id++;
+        g_reg[op->id] = op;
+    }
+    *handle = op->id;
+    return 0;
+}
+
+static int destroy_operator(int64_t handle)
+{
+    Operator *op = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_reg_mu);
+        auto it = g_reg.find(handle);
+        if (it == g_reg.end()) return PROPACK_ERR_HANDLE;
+        op = it->second;
+        g_reg.erase(it);
+    }
+    cudaDeviceSynchronize();
+    free_csr(op->fwd); free_csr(op->adj); free_csr(op->thin_r); free_csr(op->thin_l);
+    cudaFree(op->w); cudaFree(op->zbuf); cudaFree(op->zpart); cudaFree(op->zticket);
+    delete op;
+    return 0;
+}
+
+int64_t handle_from_iparm(const int *iparm)
+{
+    if (!iparm) return 0;
+    return (int64_t)((uint64_t)(uint32_t)iparm[0] | ((uint64_t)(uint32_t)iparm[1] << 32));
+}
+
+}  // namespace pgb
+
+// ------------------------------------------------------------ C ABI
+using namespace pgb;
+
+extern "C" int propack_csr_create(int m, int n, const int64_t *s_rowptr, const int32_t *s_colidx,
+                                  const double *s_val, int r, const int64_t *l_rowptr, const int32_t *l_colidx,
+                                  const double *l_val, const int64_t *r_rowptr, const int32_t *r_colidx,
+                                  const double *r_val, const double *w, int64_t *handle)
+{
+    try {
+        return create_operator(m, n, s_rowptr, s_colidx, s_val, r, l_rowptr, l_colidx, l_val, r_rowptr, r_colidx,
+                               r_val, w, handle);
+    } catch (const CudaFailure &) {
+        return PROPACK_ERR_CUDA;
+    } catch (const ArgFailure &) {
+        if (g_err.empty()) set_error("invalid argument to propack_csr_create");
+        return PROPACK_ERR_ARG;
+    }
+}
+
+extern "C" int propack_csr_destroy(int64_t handle) { return destroy_operator(handle); }
+
+extern "C" void propack_handle_to_iparm(int64_t handle, int *iparm)
+{
+    iparm[0] = (int)(uint32_t)((uint64_t)handle & 0xffffffffu);
+    iparm[1] = (int)(uint32_t)((uint64_t)handle >> 32);
+}
+
+extern "C" void propack_gpu_csr_aprod_(const char *transa, const int *m, const int *n, const double *x, double *y,
+                                       double *dparm, int *iparm, size_t transa_len)
+{
+    (void)dparm; (void)transa_len;
+    Operator *op = lookup_operator(handle_from_iparm(iparm));
+    if (!op) { set_error("propack_gpu_csr_aprod_: iparm holds no live operator"); return; }
+    const bool t = (transa[0] == 't' || transa[0] == 'T');
+    const int nin = t ? *m : *n, nout = t ? *n : *m;
+    try {
+        cudaStream_t s;
+        PGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        double *dx = nullptr, *dy = nullptr;
+        PGB_CUDA(cudaMallocAsync(&dx, sizeof(double) * nin, s));
+        PGB_CUDA(cudaMallocAsync(&dy, sizeof(double) * nout, s));
+        PGB_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * nin, cudaMemcpyHostToDevice, s));
+        op_apply(*op, t, dx, dy, s);
+        PGB_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
+        PGB_CUDA(cudaFreeAsync(dx, s));
+        PGB_CUDA(cudaFreeAsync(dy, s));
+        PGB_CUDA(cudaStreamSynchronize(s));
+        PGB_CUDA(cudaStreamDestroy(s));
+    } catch (...) {
+    }
+}
+
+extern "C" const char *propack_last_error(void) { return pgb::last_error(); }

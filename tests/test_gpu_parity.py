@@ -1,0 +1,188 @@
+"""Parity of the GPU library (called through its C ABI) with the oracle and
+with the reference's outputs (scipy's PROPACK golden fixtures).
+
+Tolerances (FP64 path): singular values 1e-10 relative, singular vectors
+|<u_gpu, u_ref>| within 1e-8 of 1 (sin-angle ~1e-8), operator products
+1e-12 relative."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+from scipy.sparse.linalg import aslinearoperator
+
+import oracle
+import propack_gb300 as pg
+from propack_gb300 import workloads
+from conftest import csr_from, illc1850, subspace_err
+
+pytestmark = pytest.mark.gpu
+
+SIG_RTOL = 1e-10
+VEC_TOL = 1e-8
+
+
+def rng0():
+    return np.random.default_rng(0)
+
+
+# ------------------------------------------------------------ operator
+@pytest.mark.parametrize("kind", ["plain", "lowrank", "zipf", "longcols"])
+def test_operator_products(kind):
+    rng = np.random.default_rng(3)
+    if kind == "plain":
+        S = workloads.plain_lansvd(0)
+        L = R = w = None
+        Ad = S.toarray()
+    elif kind == "lowrank":
+        S, L, R, w = workloads.lowrank_irl(seed=5, m=3000, n=800, nnz_row=7, rank=6, udens=0.05, vdens=0.2)
+        Ad = workloads.dense_of(S, L, R, w)
+    elif kind == "zipf":
+        S = workloads.zipf_mixed(seed=4, m=20000, hi=5000)
+        L = R = w = None
+        Ad = None
+    else:
+        # dense columns and long rows: exercises the long-segment transpose and single-row blocks
+        m, n = 3000, 50
+        X = rng.standard_normal((m, n))
+        X[rng.random((m, n)) > 0.9] = 0.0
+        S = sp.csr_array(X)
+        L = R = w = None
+        Ad = S.toarray()
+    op = pg.CsrOperator(S, L, R, w)
+    m, n = op.shape
+    x = rng.standard_normal(n)
+    y = rng.standard_normal(m)
+    if Ad is not None:
+        ref_n, ref_t = Ad @ x, Ad.T @ y
+    else:
+        ref_n, ref_t = S @ x, S.T @ y
+    got_n, got_t = op.matvec(x), op.rmatvec(y)
+    np.testing.assert_allclose(got_n, ref_n, rtol=1e-12, atol=1e-12 * np.abs(ref_n).max())
+    np.testing.assert_allclose(got_t, ref_t, rtol=1e-12, atol=1e-12 * np.abs(ref_t).max())
+    # bit-reproducible: same inputs give the same bits
+    assert np.array_equal(op.rmatvec(y), got_t)
+    op.close()
+
+
+# -------------------------------------------------- golden (reference) cases
+def test_plain_lansvd_vs_golden(golden):
+    A = csr_from(golden, "plain")
+    u, s, vt, bnd = pg.svdp(A, 10, irl_mode=False, kmax=200, tol=1e-12, rng=rng0())
+    np.testing.assert_allclose(s, golden["plain_lansvd_sigma"], rtol=SIG_RTOL)
+    np.testing.assert_allclose(s, golden["plain_dense_sigma"][:10], rtol=SIG_RTOL)
+    assert subspace_err(u, golden["plain_lansvd_u"]) < VEC_TOL
+    assert subspace_err(vt.T, golden["plain_lansvd_vt"].T) < VEC_TOL
+
+
+def test_plain_irl_vs_golden(golden):
+    A = csr_from(golden, "plain")
+    u, s, vt, bnd = pg.svdp(A, 10, irl_mode=True, kmax=30, tol=1e-12, rng=rng0())
+    st = pg.get_stats()
+    assert st["nrestart"] > 0
+    np.testing.assert_allclose(s, golden["plain_irl_sigma"], rtol=SIG_RTOL)
+    assert subspace_err(u, golden["plain_irl_u"]) < VEC_TOL
+    assert subspace_err(vt.T, golden["plain_irl_vt"].T) < VEC_TOL
+
+
+@pytest.mark.parametrize("case,kw", [("small_irl_lm", dict(irl_mode=True, which="LM")),
+                                     ("small_irl_sm", dict(irl_mode=True, which="SM")),
+                                     ("small_lansvd", dict(irl_mode=False))])
+@pytest.mark.parametrize("ctor", ["dense", "csr", "linop"])
+def test_small_cases_vs_golden(golden, case, kw, ctor):
+    M = csr_from(golden, "small").toarray()
+    A = {"dense": M, "csr": sp.csr_array(M), "linop": aslinearoperator(M)}[ctor]
+    u, s, vt, bnd = pg.svdp(A, 3, tol=1e-8, rng=rng0(), **kw)
+    np.testing.assert_allclose(s, golden[case + "_sigma"], rtol=1e-8, atol=1e-8)
+    u1, s1, vt1 = np.linalg.svd(M, full_matrices=False)
+    if kw.get("which") == "SM":
+        u1, vt1 = np.roll(u1, 3, 1), np.roll(vt1, 3, 0)
+    np.testing.assert_allclose(np.abs(u1.T @ u), np.eye(10, 3), atol=1e-8)
+    np.testing.assert_allclose(np.abs(vt1 @ vt.T), np.eye(10, 3), atol=1e-8)
+
+
+def test_lowrank_irl_vs_golden(golden):
+    S, L, R = csr_from(golden, "lr_S"), csr_from(golden, "lr_L"), csr_from(golden, "lr_R")
+    op = pg.CsrOperator(S, L, R, golden["lr_w"])
+    u, s, vt, bnd = pg.svdp(op, 10, irl_mode=True, kmax=30, tol=1e-10, rng=rng0())
+    np.testing.assert_allclose(s, golden["lowrank_irl_sigma"], rtol=SIG_RTOL)
+    np.testing.assert_allclose(s, golden["lowrank_dense_sigma"][:10], rtol=SIG_RTOL)
+    # residuals against the operator itself
+    res = max(np.linalg.norm(op.matvec(vt[i]) - s[i] * u[:, i]) for i in range(10))
+    assert res < 1e-8 * s[0]
+    op.close()
+
+
+def test_illc1850_vs_golden(golden):
+    A = illc1850()
+    if A is None or "illc_sigma" not in golden:
+        pytest.skip("illc1850 not available")
+    u, s, vt, bnd = pg.svdp(A, 200, irl_mode=False, rng=rng0())
+    np.testing.assert_allclose(s, golden["illc_sigma"], rtol=1e-10)
+    np.testing.assert_allclose(u.T @ u, np.eye(200), atol=1e-9)
+    np.testing.assert_allclose(vt @ vt.T, np.eye(200), atol=1e-9)
+
+
+# ----------------------------------------------------- GPU vs oracle, same inputs
+OPTS = [dict(), dict(cgs=True), dict(elr=False), dict(delta=1e-20, eta=1e-10),  # full reorthogonalisation
+        dict(delta=-1.0, eta=-1.0)]                                           # PROPACK's own defaults
+
+
+@pytest.mark.parametrize("opts", OPTS, ids=["default", "cgs", "noelr", "full", "propack_defaults"])
+@pytest.mark.parametrize("irl", [True, False])
+def test_vs_oracle_same_trajectory(golden, opts, irl):
+    S, L, R = csr_from(golden, "lr_S"), csr_from(golden, "lr_L"), csr_from(golden, "lr_R")
+    w = golden["lr_w"]
+    op = pg.CsrOperator(S, L, R, w)
+    oop = oracle.Operator(S, L, R, w)
+    kw = dict(irl_mode=irl, kmax=30 if irl else 120, tol=1e-10, **opts)
+    u, s, vt, bnd = pg.svdp(op, 10, rng=rng0(), **kw)
+    st = pg.get_stats()
+    oracle.clearstat()
+    uo, so, vto, bo, info, kc = oracle.svdp(None, 10, rng=rng0(), op=oop, **kw)
+    sto = oracle.getstat()
+    assert info == 0 and kc == 10
+    np.testing.assert_allclose(s, so, rtol=SIG_RTOL)
+    assert subspace_err(u, uo) < VEC_TOL
+    assert subspace_err(vt.T, vto.T) < VEC_TOL
+    # the same Lanczos trajectory: matvec counts agree within a few steps
+    assert abs(st["nopx"] - sto["nopx"]) <= 0.05 * sto["nopx"] + 4
+    op.close()
+
+
+def test_zero_start_vector_uses_dlarnv(golden):
+    """v0 = 0 makes the driver draw PROPACK's own dlarnv start vector (dgetu0)."""
+    A = csr_from(golden, "plain")
+    z = np.zeros(A.shape[0])
+    u, s, vt, bnd = pg.svdp(A, 10, irl_mode=False, kmax=200, tol=1e-12, v0=z, rng=rng0())
+    uo, so, vto, bo, info, kc = oracle.svdp(A, 10, irl_mode=False, kmax=200, tol=1e-12, v0=z, rng=rng0())
+    np.testing.assert_allclose(s, so, rtol=SIG_RTOL)
+    np.testing.assert_allclose(s, golden["plain_dense_sigma"][:10], rtol=SIG_RTOL)
+
+
+def test_invariant_subspace_rank_deficient():
+    """A rank-6 matrix: the Lanczos run meets an invariant subspace
+    (dlanbpro.F:372-409 / :503-539) and the drivers report it as the
+    reference does."""
+    rng = np.random.default_rng(7)
+    X = rng.standard_normal((60, 6)) @ rng.standard_normal((6, 40))
+    A = sp.csr_array(X)
+    res = {}
+    for name, fn in (("gpu", lambda: pg.svdp(A, 4, irl_mode=False, kmax=30, tol=1e-10, rng=rng0())),
+                     ("oracle", lambda: oracle.svdp(A, 4, irl_mode=False, kmax=30, tol=1e-10, rng=rng0()))):
+        try:
+            out = fn()
+            res[name] = ("ok", out[1])
+        except Exception as e:  # LinAlgError on INFO > 0
+            res[name] = ("err", type(e).__name__)
+    if res["oracle"][0] == "ok":
+        assert res["gpu"][0] == "ok"
+        np.testing.assert_allclose(res["gpu"][1], np.linalg.svd(X, compute_uv=False)[:4], rtol=1e-10)
+    else:
+        assert res["gpu"] == res["oracle"]
+
+
+def test_bad_operator_handle_is_an_error():
+    A = np.ones((5, 4))
+    op = pg.CsrOperator(A)
+    op.close()
+    with pytest.raises(pg.PropackError):
+        pg.svdp(op, 2, rng=rng0())

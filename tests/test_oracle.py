@@ -1,0 +1,112 @@
+"""The oracle (CPU restatement of PROPACK) pinned against the reference's
+outputs: scipy's packaging of PROPACK (golden fixtures), dense LAPACK, and
+the generator table of LAPACK's dlaruv."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import csr_from, illc1850, subspace_err
+
+
+def test_lcg_matches_dlaruv_table():
+    # rows 1, 2, 3, 4, 64, 117, 128 of dlaruv's multiplier table (base-4096 digits)
+    table = {1: (494, 322, 2508, 2549), 2: (2637, 789, 3754, 1145), 3: (255, 1440, 1766, 2253),
+             4: (2008, 752, 3572, 305), 64: (2770, 1238, 1956, 2817), 117: (2785, 1832, 1836, 3365),
+             128: (545, 2366, 3801, 1537)}
+    a = 33952834046453
+    for i, dig in table.items():
+        x = pow(a, i, 2 ** 48)
+        assert ((x >> 36) & 4095, (x >> 24) & 4095, (x >> 12) & 4095, x & 4095) == dig
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 10, 57, 150])
+def test_bdsqr_vs_numpy(n):
+    rng = np.random.default_rng(n)
+    d = rng.standard_normal(n)
+    e = rng.standard_normal(n - 1)
+    B = np.diag(d) + np.diag(e, 1)
+    s_ref = np.linalg.svd(B, compute_uv=False)
+    dd, U, VT, info = oracle.bdsqr(d, e, nru_vectors=True, ncvt_vectors=True)
+    assert info == 0
+    np.testing.assert_allclose(dd, s_ref, rtol=1e-13, atol=1e-14 * s_ref[0])
+    np.testing.assert_allclose(U @ np.diag(dd) @ VT, B, atol=1e-13 * s_ref[0])
+    np.testing.assert_allclose(U.T @ U, np.eye(n), atol=1e-13)
+    # last row of the left vectors, as used for the Ritz bounds
+    urow = np.zeros(n)
+    urow[-1] = 1.0
+    d2, U2, _, _ = oracle.bdsqr(d, e, urow=urow)
+    np.testing.assert_allclose(np.abs(U2[0]), np.abs(U[-1]), atol=1e-12)
+
+
+def test_bdsqr_graded_relative_accuracy():
+    d = 10.0 ** (-np.arange(20.0))
+    e = 10.0 ** (-np.arange(19.0) - 0.5)
+    B = np.diag(d) + np.diag(e, 1)
+    s_ref = np.linalg.svd(B, compute_uv=False)
+    dd, _, _, _ = oracle.bdsqr(d, e)
+    np.testing.assert_allclose(dd, s_ref, rtol=1e-12)
+
+
+def test_plain_lansvd_vs_golden(golden):
+    A = csr_from(golden, "plain")
+    u, s, vt, bnd, info, kc = oracle.svdp(A, 10, irl_mode=False, kmax=200, tol=1e-12,
+                                          rng=np.random.default_rng(0))
+    assert info == 0 and kc == 10
+    np.testing.assert_allclose(s, golden["plain_lansvd_sigma"], rtol=1e-12)
+    np.testing.assert_allclose(s, golden["plain_dense_sigma"][:10], rtol=1e-12)
+    assert subspace_err(u, golden["plain_lansvd_u"]) < 1e-10
+    assert subspace_err(vt.T, golden["plain_lansvd_vt"].T) < 1e-10
+
+
+def test_plain_irl_vs_golden(golden):
+    A = csr_from(golden, "plain")
+    u, s, vt, bnd, info, kc = oracle.svdp(A, 10, irl_mode=True, kmax=30, tol=1e-12,
+                                          rng=np.random.default_rng(0))
+    st = oracle.getstat()
+    oracle.clearstat()
+    assert info == 0 and kc == 10
+    assert st["nrestart"] > 0
+    np.testing.assert_allclose(s, golden["plain_irl_sigma"], rtol=1e-12)
+    assert subspace_err(u, golden["plain_irl_u"]) < 1e-9
+
+
+@pytest.mark.parametrize("case,kw", [("small_irl_lm", dict(irl_mode=True, which="LM")),
+                                     ("small_irl_sm", dict(irl_mode=True, which="SM")),
+                                     ("small_lansvd", dict(irl_mode=False))])
+def test_small_cases_vs_golden(golden, case, kw):
+    A = csr_from(golden, "small")
+    which = kw.pop("which", "LM")
+    u, s, vt, bnd, info, kc = oracle.svdp(A.toarray(), 3, which=which, tol=1e-8, rng=np.random.default_rng(0), **kw)
+    assert info == 0
+    np.testing.assert_allclose(s, golden[case + "_sigma"], rtol=1e-8, atol=1e-8)
+
+
+def test_lowrank_irl_vs_golden(golden):
+    S, L, R = csr_from(golden, "lr_S"), csr_from(golden, "lr_L"), csr_from(golden, "lr_R")
+    w = golden["lr_w"]
+    op = oracle.Operator(S, L, R, w)
+    u, s, vt, bnd, info, kc = oracle.svdp(None, 10, irl_mode=True, kmax=30, tol=1e-10,
+                                          rng=np.random.default_rng(0), op=op)
+    assert info == 0 and kc == 10
+    np.testing.assert_allclose(s, golden["lowrank_irl_sigma"], rtol=1e-10)
+    np.testing.assert_allclose(s, golden["lowrank_dense_sigma"][:10], rtol=1e-10)
+
+
+def test_python_callback_equals_builtin_operator(golden):
+    A = csr_from(golden, "plain")
+    r1 = oracle.svdp(A, 10, irl_mode=False, kmax=200, tol=1e-12, rng=np.random.default_rng(0))
+    from scipy.sparse.linalg import aslinearoperator
+    r2 = oracle.svdp(aslinearoperator(A), 10, irl_mode=False, kmax=200, tol=1e-12, rng=np.random.default_rng(0))
+    np.testing.assert_allclose(r1[1], r2[1], rtol=1e-13)
+
+
+@pytest.mark.slow
+def test_illc1850_vs_golden(golden):
+    A = illc1850()
+    if A is None or "illc_sigma" not in golden:
+        pytest.skip("illc1850 not available")
+    u, s, vt, bnd, info, kc = oracle.svdp(A, 200, irl_mode=False, rng=np.random.default_rng(0))
+    assert info == 0
+    np.testing.assert_allclose(s, golden["illc_sigma"], rtol=1e-11)
+    np.testing.assert_allclose(u.T @ u, np.eye(200), atol=1e-9)
+    np.testing.assert_allclose(vt @ vt.T, np.eye(200), atol=1e-9)
