@@ -116,8 +116,20 @@ typedef struct {
     double bsvd_ms;    /* of which bidiagonal SVD + shifts      */
     double gemm_ms;    /* of which restart / Ritz products      */
     int64_t kernel_launches; /* kernels this library launched   */
+    double solve_ms;   /* device time from the start vector in HBM
+                          to the Ritz vectors in HBM (no host copies) */
 } propack_stats_t;
 void propack_get_stats(propack_stats_t *out);
+
+/* Per-kernel device timing: with profiling on, CUDA events are recorded
+ * on the launching stream around every launch of the main kernels and
+ * propack_get_profile returns, per kernel class, the summed milliseconds
+ * and launch counts accumulated since propack_set_profiling(1).  Classes
+ * in order: SpMV A'u (fused), SpMV Av (fused), ELR pass, CGS projection,
+ * CGS update, low-rank prepass, bidiagonal analysis, IRL sweeps, GEMM.
+ * Returns the number of classes.  No reference counterpart. */
+void propack_set_profiling(int on);
+int propack_get_profile(double *total_ms, int64_t *launches, int n);
 
 /* Last error message for the calling thread ("" if none). */
 const char *propack_last_error(void);

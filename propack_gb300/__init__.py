@@ -39,7 +39,11 @@ class _Stats(C.Structure):
     _fields_ = [("nopx", C.c_int64), ("nreorth", C.c_int64), ("ndot", C.c_int64), ("nrestart", C.c_int64),
                 ("nbsvd", C.c_int64), ("nlandim", C.c_int64), ("device_ms", C.c_double),
                 ("lanczos_ms", C.c_double), ("bsvd_ms", C.c_double), ("gemm_ms", C.c_double),
-                ("kernel_launches", C.c_int64)]
+                ("kernel_launches", C.c_int64), ("solve_ms", C.c_double)]
+
+
+PROFILE_KINDS = ("spmv_adj", "spmv_fwd", "elr", "cgs_dots", "cgs_upd", "lowrank_prepass", "analyse", "sweeps",
+                 "gemm")
 
 
 _lib = None
@@ -78,6 +82,20 @@ def get_stats():
 
 def clearstat():
     load().clearstat_()
+
+
+def set_profiling(on):
+    load().propack_set_profiling(1 if on else 0)
+
+
+def get_profile():
+    """{kernel class: (launches, total ms)} since set_profiling(True)."""
+    L = load()
+    n = len(PROFILE_KINDS)
+    ms = (C.c_double * n)()
+    cnt = (C.c_int64 * n)()
+    L.propack_get_profile(ms, cnt, n)
+    return {k: (int(cnt[i]), float(ms[i])) for i, k in enumerate(PROFILE_KINDS)}
 
 
 def printstat():

@@ -26,6 +26,20 @@ struct WaitFailure {};
 extern thread_local int64_t g_launches;
 #define PGB_LAUNCHED() (++::pgb::g_launches)
 
+// Optional per-kernel timing with CUDA events recorded on the launching
+// stream (propack_set_profiling); off by default.
+enum ProfKind { PK_SPMV_ADJ, PK_SPMV_FWD, PK_ELR, PK_CGS_DOTS, PK_CGS_UPD, PK_THIN, PK_ANALYSE, PK_SWEEPS,
+                PK_GEMM, PK_N };
+extern thread_local int g_prof_on;
+void prof_mark(int kind, cudaStream_t s, bool begin);
+void prof_collect();
+#define PGB_PROF(kind, s, ...)                                     \
+    do {                                                           \
+        if (::pgb::g_prof_on) ::pgb::prof_mark((kind), (s), true); \
+        __VA_ARGS__;                                               \
+        if (::pgb::g_prof_on) ::pgb::prof_mark((kind), (s), false);\
+    } while (0)
+
 // ------------------------------------------------------------- constants
 constexpr double EPS = 1.1102230246251565e-16;      // dlamch('e') = 2^-53
 constexpr double SFMIN = 2.2250738585072014e-308;   // dlamch('s')

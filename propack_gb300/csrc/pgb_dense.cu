@@ -608,12 +608,12 @@ __global__ void k_copy_cols(const double *src, int lds, double *dst, int ldd, in
 // ------------------------------------------------------------ host wrappers
 void launch_analyse(const AnaArgs &a, cudaStream_t s)
 {
-    k_analyse<<<1, 256, 0, s>>>(a);
+    PGB_PROF(PK_ANALYSE, s, k_analyse<<<1, 256, 0, s>>>(a));
     PGB_LAUNCHED();
 }
 void launch_sweeps(const SweepArgs &a, cudaStream_t s)
 {
-    k_irl_sweeps<<<1, 256, 0, s>>>(a);
+    PGB_PROF(PK_SWEEPS, s, k_irl_sweeps<<<1, 256, 0, s>>>(a));
     PGB_LAUNCHED();
 }
 void launch_ritz_prep(const RitzArgs &a, cudaStream_t s)
@@ -627,7 +627,7 @@ void gemm(int mr, int nc, int kk, const double *A, int lda, bool ta, const doubl
 {
     if (mr <= 0 || nc <= 0) return;
     dim3 grid((mr + 63) / 64, (nc + 63) / 64);
-    k_gemm<<<grid, 256, 0, s>>>(mr, nc, kk, A, lda, ta ? 1 : 0, B, ldb, tb ? 1 : 0, C, ldc);
+    PGB_PROF(PK_GEMM, s, k_gemm<<<grid, 256, 0, s>>>(mr, nc, kk, A, lda, ta ? 1 : 0, B, ldb, tb ? 1 : 0, C, ldc));
     PGB_LAUNCHED();
 }
 void copy_cols(const double *src, int lds, double *dst, int ldd, int rows, int cols, cudaStream_t s)

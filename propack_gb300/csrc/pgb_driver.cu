@@ -25,6 +25,7 @@ struct Stats {
     int64_t nopx = 0, nreorth = 0, ndot = 0, nrestart = 0, nbsvd = 0, nlandim = 0, nsing = 0;
     double device_ms = 0, lanczos_ms = 0, bsvd_ms = 0, gemm_ms = 0;
     int64_t launches = 0;
+    double solve_ms = 0;
 };
 static thread_local Stats g_stat;       // cumulative (clearstat_/printstat_)
 static thread_local Stats g_last;       // last driver call (propack_get_stats)
@@ -164,7 +165,7 @@ struct Ctx {
     int nb = 0;
     int ntry_spec = 2;
     std::vector<void *> allocs;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
 
     template <typename T>
     T *dalloc(size_t count)
@@ -185,6 +186,8 @@ struct Ctx {
         if (hy) cudaFreeHost(hy);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (evs0) cudaEventDestroy(evs0);
+        if (evs1) cudaEventDestroy(evs1);
         if (s) cudaStreamDestroy(s);
     }
     LbArgs args() const
@@ -220,6 +223,8 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
     PGB_CUDA(cudaStreamCreateWithFlags(&c.s, cudaStreamNonBlocking));
     PGB_CUDA(cudaEventCreate(&c.ev0));
     PGB_CUDA(cudaEventCreate(&c.ev1));
+    PGB_CUDA(cudaEventCreate(&c.evs0));
+    PGB_CUDA(cudaEventCreate(&c.evs1));
     c.U = c.dalloc<double>((size_t)c.ldu * (kmax + 1));
     c.V = c.dalloc<double>((size_t)c.ldv * (kmax + 1));
     c.ctl = c.dalloc<LbCtl>(1);
@@ -730,6 +735,7 @@ static void run_irl(const char *which, const char *jobu, const char *jobv, int m
     const int neig0 = *neig;
     PGB_CUDA(cudaEventRecord(c.ev0, c.s));
     copy_in_u1(c, U);
+    PGB_CUDA(cudaEventRecord(c.evs0, c.s));
     double rnorm = dev_nrm2(c, c.U, m);
     int ierr = 0;
     double anorm_drv = 0.0;
@@ -797,12 +803,16 @@ static void run_irl(const char *which, const char *jobu, const char *jobv, int m
         Timer t(c, g_last.gemm_ms);
         dev_ritzvec(c, small_side, du, dv, nconv, dim);
     }
+    PGB_CUDA(cudaEventRecord(c.evs1, c.s));
     copy_out(c, U, ldu, V, ldv, nconv, du, dv);
     PGB_CUDA(cudaEventRecord(c.ev1, c.s));
     c.sync();
     float ms = 0;
     cudaEventElapsedTime(&ms, c.ev0, c.ev1);
     g_last.device_ms = ms;
+    cudaEventElapsedTime(&ms, c.evs0, c.evs1);
+    g_last.solve_ms = ms;
+    prof_collect();
     *neig = nconv;
     g_last.nlandim = dim;
     c.get_ctl();
@@ -828,6 +838,7 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
     setup_operator(c, aprod, dparm, iparm);
     PGB_CUDA(cudaEventRecord(c.ev0, c.s));
     copy_in_u1(c, U);
+    PGB_CUDA(cudaEventRecord(c.evs0, c.s));
     double rnorm = dev_nrm2(c, c.U, m);
     int ierr = 0;
     double anorm_drv = 0.0;
@@ -890,12 +901,16 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
         Timer t(c, g_last.gemm_ms);
         dev_ritzvec(c, false, du, dv, neig, jold);
     }
+    PGB_CUDA(cudaEventRecord(c.evs1, c.s));
     copy_out(c, U, ldu, V, ldv, neig, du, dv);
     PGB_CUDA(cudaEventRecord(c.ev1, c.s));
     c.sync();
     float ms = 0;
     cudaEventElapsedTime(&ms, c.ev0, c.ev1);
     g_last.device_ms = ms;
+    cudaEventElapsedTime(&ms, c.evs0, c.evs1);
+    g_last.solve_ms = ms;
+    prof_collect();
     *kp = neig;
     g_last.nlandim = j;
     c.get_ctl();
@@ -980,4 +995,5 @@ extern "C" void propack_get_stats(propack_stats_t *out)
     out->bsvd_ms = s.bsvd_ms;
     out->gemm_ms = s.gemm_ms;
     out->kernel_launches = s.launches;
+    out->solve_ms = s.solve_ms;
 }

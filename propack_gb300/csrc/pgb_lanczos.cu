@@ -708,26 +708,34 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
 {
     const int nb = a.nb;
     if (side == 0) {
-        if (!host_product && op && op->r > 0) op_thin(*op, true, a.U + (size_t)(j - 1) * a.ldu, s);
-        k_lb_spmv<0><<<nb, BS, 0, s>>>(a, j, host_product ? 1 : 0);
+        if (!host_product && op && op->r > 0)
+            PGB_PROF(PK_THIN, s, op_thin(*op, true, a.U + (size_t)(j - 1) * a.ldu, s));
+        PGB_PROF(PK_SPMV_ADJ, s, k_lb_spmv<0><<<nb, BS, 0, s>>>(a, j, host_product ? 1 : 0));
         PGB_LAUNCHED();
         if (j > 1)
-            for (int i = 0; i < ielr; i++) { k_lb_elr<0><<<nb, BS, 0, s>>>(a, j); PGB_LAUNCHED(); }
-        k_lb_cgs_dots<0><<<nb, BS, 0, s>>>(a, j);
+            for (int i = 0; i < ielr; i++) {
+                PGB_PROF(PK_ELR, s, k_lb_elr<0><<<nb, BS, 0, s>>>(a, j));
+                PGB_LAUNCHED();
+            }
+        PGB_PROF(PK_CGS_DOTS, s, k_lb_cgs_dots<0><<<nb, BS, 0, s>>>(a, j));
         PGB_LAUNCHED();
         for (int i = 0; i < ntry_spec; i++) {
-            k_lb_cgs_upd<0><<<nb, BS, cgs_smem(a), s>>>(a, j, i == ntry_spec - 1);
+            PGB_PROF(PK_CGS_UPD, s, k_lb_cgs_upd<0><<<nb, BS, cgs_smem(a), s>>>(a, j, i == ntry_spec - 1));
             PGB_LAUNCHED();
         }
     } else {
-        if (!host_product && op && op->r > 0) op_thin(*op, false, a.V + (size_t)(j - 1) * a.ldv, s);
-        k_lb_spmv<1><<<nb, BS, 0, s>>>(a, j, host_product ? 1 : 0);
+        if (!host_product && op && op->r > 0)
+            PGB_PROF(PK_THIN, s, op_thin(*op, false, a.V + (size_t)(j - 1) * a.ldv, s));
+        PGB_PROF(PK_SPMV_FWD, s, k_lb_spmv<1><<<nb, BS, 0, s>>>(a, j, host_product ? 1 : 0));
         PGB_LAUNCHED();
-        for (int i = 0; i < ielr; i++) { k_lb_elr<1><<<nb, BS, 0, s>>>(a, j); PGB_LAUNCHED(); }
-        k_lb_cgs_dots<1><<<nb, BS, 0, s>>>(a, j);
+        for (int i = 0; i < ielr; i++) {
+            PGB_PROF(PK_ELR, s, k_lb_elr<1><<<nb, BS, 0, s>>>(a, j));
+            PGB_LAUNCHED();
+        }
+        PGB_PROF(PK_CGS_DOTS, s, k_lb_cgs_dots<1><<<nb, BS, 0, s>>>(a, j));
         PGB_LAUNCHED();
         for (int i = 0; i < ntry_spec; i++) {
-            k_lb_cgs_upd<1><<<nb, BS, cgs_smem(a), s>>>(a, j, i == ntry_spec - 1);
+            PGB_PROF(PK_CGS_UPD, s, k_lb_cgs_upd<1><<<nb, BS, cgs_smem(a), s>>>(a, j, i == ntry_spec - 1));
             PGB_LAUNCHED();
         }
     }

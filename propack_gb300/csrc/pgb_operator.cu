@@ -15,6 +15,67 @@
 namespace pgb {
 
 thread_local int64_t g_launches = 0;
+
+// ------------------------------------------------------- event profiling
+thread_local int g_prof_on = 0;
+struct ProfRec {
+    int kind;
+    cudaEvent_t a, b;
+};
+static thread_local std::vector<ProfRec> g_prof_open;
+static thread_local std::vector<cudaEvent_t> g_prof_pool;
+static thread_local double g_prof_ms[PK_N];
+static thread_local int64_t g_prof_cnt[PK_N];
+
+static cudaEvent_t prof_event()
+{
+    if (!g_prof_pool.empty()) {
+        cudaEvent_t e = g_prof_pool.back();
+        g_prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+void prof_mark(int kind, cudaStream_t s, bool begin)
+{
+    if (begin) {
+        ProfRec r;
+        r.kind = kind;
+        r.a = prof_event();
+        r.b = nullptr;
+        cudaEventRecord(r.a, s);
+        g_prof_open.push_back(r);
+    } else if (!g_prof_open.empty()) {
+        ProfRec &r = g_prof_open.back();
+        r.b = prof_event();
+        cudaEventRecord(r.b, s);
+    }
+}
+void prof_collect()
+{
+    for (ProfRec &r : g_prof_open) {
+        if (!r.b) continue;
+        cudaEventSynchronize(r.b);
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            g_prof_ms[r.kind] += ms;
+            g_prof_cnt[r.kind] += 1;
+        }
+        g_prof_pool.push_back(r.a);
+        g_prof_pool.push_back(r.b);
+    }
+    g_prof_open.clear();
+}
+void prof_reset()
+{
+    for (int i = 0; i < PK_N; i++) { g_prof_ms[i] = 0.0; g_prof_cnt[i] = 0; }
+}
+void prof_get(double *ms, int64_t *cnt, int n)
+{
+    for (int i = 0; i < n && i < PK_N; i++) { ms[i] = g_prof_ms[i]; cnt[i] = g_prof_cnt[i]; }
+}
 static thread_local std::string g_err;
 void set_error(const std::string &msg) { g_err = msg; }
 const char *last_error() { return g_err.c_str(); }
@@ -634,3 +695,19 @@ extern "C" void propack_gpu_csr_aprod_(const char *transa, const int *m, const i
 }
 
 extern "C" const char *propack_last_error(void) { return pgb::last_error(); }
+
+namespace pgb {
+void prof_reset();
+void prof_get(double *ms, int64_t *cnt, int n);
+}
+extern "C" void propack_set_profiling(int on)
+{
+    pgb::g_prof_on = on ? 1 : 0;
+    pgb::prof_reset();
+}
+extern "C" int propack_get_profile(double *total_ms, int64_t *launches, int n)
+{
+    pgb::prof_collect();
+    pgb::prof_get(total_ms, launches, n);
+    return pgb::PK_N;
+}
