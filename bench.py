@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--workload", default="lowrank_irl", choices=sorted(WORKLOADS))
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="shrink m and n by this factor (profiling captures only; not a bench line)")
     return ap.parse_args()
 
 
@@ -73,10 +75,10 @@ def dist_env():
     return rank, world, local
 
 
-def make_workload(name):
+def make_workload(name, scale=1.0):
     from propack_gb300 import workloads
     if name == "lowrank_irl":
-        return workloads.lowrank_irl(seed=1)
+        return workloads.lowrank_irl(seed=1, m=int(2_000_000 * scale), n=int(500_000 * scale))
     raise ValueError(name)
 
 
@@ -207,10 +209,12 @@ def run_ours(args, wl):
         import torch.distributed as dist
         dist.init_process_group("gloo")
         barrier = dist.barrier
-    S, L, R, w = make_workload(args.workload)
+    S, L, R, w = make_workload(args.workload, args.scale)
     m, n = S.shape
     r = L.shape[1]
     k, kmax, tol = wl["k"], wl["kmax"], wl["tol"]
+    # reduced-scale runs only feed profiler captures: bound their restarts
+    maxiter = 1000 if args.scale == 1.0 else 20
 
     def solve(op, u0=None):
         u = np.zeros((m, kmax + 1), order="F")
@@ -219,7 +223,7 @@ def run_ours(args, wl):
         u[:, 0] = np.random.default_rng(0).uniform(size=m) if u0 is None else u0
         dop = np.array([np.sqrt(np.finfo(float).eps), np.finfo(float).eps ** 0.75, 0.0, 0.002])
         iop = np.array([0, 1], dtype=np.int32)
-        kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, 1000, op.aprod, u, sig, bnd, v, tol,
+        kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, op.aprod, u, sig, bnd, v, tol,
                                  dop, iop, iparm=op.iparm)
         return kc, info, sig, u, v
 
@@ -239,7 +243,8 @@ def run_ours(args, wl):
         launches += st["kernel_launches"]
         matvecs.append(st["nopx"])
         restarts.append(st["nrestart"])
-        assert info == 0 and kc == k, (info, kc)
+        if args.scale == 1.0:
+            assert info == 0 and kc == k, (info, kc)
     wall_ms = (time.perf_counter() - t0) * 1e3
     barrier()
     clocks = sampler.stop() if sampler else None
@@ -291,9 +296,10 @@ def run_ours(args, wl):
         sig, bnd = np.zeros(k), np.zeros(k)
         dop = np.array([np.sqrt(np.finfo(float).eps), np.finfo(float).eps ** 0.75, 0.0, 0.002])
         iop = np.array([0, 1], dtype=np.int32)
-        kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, 1000, o.aprod, u_pin, sig, bnd, v_pin,
+        kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, o.aprod, u_pin, sig, bnd, v_pin,
                                  tol, dop, iop, iparm=o.iparm)
-        assert info == 0 and kc == k
+        if args.scale == 1.0:
+            assert info == 0 and kc == k
         lib.propack_csr_destroy(h.value)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     barrier()
@@ -333,7 +339,7 @@ def run_ours(args, wl):
             "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded numpy default_rng(1))",
-            "config": {"workload": args.workload, "desc": wl["desc"], "form": "plain FP64",
+            "config": {"workload": args.workload, "desc": wl["desc"], "form": "plain FP64", "scale": args.scale,
                        "l2": "inputs larger than L2 (operator ~1 GB, basis ~3 GB); no flush"},
             "matvecs": statistics.mean(matvecs), "restarts": statistics.mean(restarts),
             "max_rel_residual": rel_resid, "wall_ms_per_step": wall_ms / args.steps,

@@ -346,7 +346,6 @@ static void transpose_into(Csr &T, const int *ptr, const int *idx, const double 
     PGB_CUDA(cudaMallocAsync(&fill, sizeof(int) * (cols + 1), s));
     PGB_CUDA(cudaMallocAsync(&longlist, sizeof(int) * (cols + 1), s));
     PGB_CUDA(cudaMallocAsync(&nlong, sizeof(int), s));
-    PGB_CUDA(cudaMallocAsync(&key, sizeof(unsigned long long) * std::max<int64_t>(nnz, 1), s));
     PGB_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (cols + 1), s));
     PGB_CUDA(cudaMemsetAsync(fill, 0, sizeof(int) * (cols + 1), s));
     PGB_CUDA(cudaMemsetAsync(nlong, 0, sizeof(int), s));
@@ -361,6 +360,10 @@ static void transpose_into(Csr &T, const int *ptr, const int *idx, const double 
     T.nnz = total;
     PGB_CUDA(cudaMalloc(&T.idx, sizeof(int) * std::max(total, 1)));
     PGB_CUDA(cudaMalloc(&T.val, sizeof(double) * std::max(total, 1)));
+    // the sort keys live at the output positions of row c of A', whose
+    // offsets T.ptr include the appended X entries: size them by `total`,
+    // not by nnz(A)
+    PGB_CUDA(cudaMallocAsync(&key, sizeof(unsigned long long) * std::max(total, 1), s));
     // the scan wrote T.ptr; optr == T.ptr, the A' part of row c is [ptr[c], ptr[c]+cnt[c])
     if (rows > 0 && nnz > 0) { k_scatter<<<g, 256, 0, s>>>(ptr, idx, rows, T.ptr, fill, key); PGB_LAUNCHED(); }
     if (cols > 0) { k_segsort_warp<<<g, 128, 0, s>>>(key, T.ptr, cnt, cols, longlist, nlong); PGB_LAUNCHED(); }
