@@ -100,6 +100,25 @@ void propack_gpu_csr_aprod_(const char *transa, const int *m, const int *n,
                             const double *x, double *y, double *dparm,
                             int *iparm, size_t transa_len);
 
+/* Apply the device operator to DEVICE vectors without allocating any
+ * device memory: y = A x (trans = 0; x has n entries, y has m) or
+ * y = A' x (trans != 0; x has m, y has n), enqueued on `stream` (a
+ * cudaStream_t; NULL for the default stream) and not synchronised.
+ * For callers that must not call cudaMalloc/cudaFree while they run.
+ * The only scratch is a fixed array of PROPACK_NOALLOC_MAX_DOUBLES
+ * doubles (512 KiB) in device memory, held by every GPU that loads the
+ * library until the process exits; an operator whose low-rank term needs
+ * r*(1+segments)+1 > PROPACK_NOALLOC_MAX_DOUBLES doubles is rejected with
+ * PROPACK_ERR_ARG.  All calls share that array: calls that may overlap on
+ * the GPU (different streams, different host threads) race and must be
+ * serialised by the caller.  The first call on each device looks up the
+ * array's device address (no allocation); make that first call before
+ * any stream capture.  No counterpart exists in the reference.
+ * Returns 0 or a negative PROPACK_ERR_* code. */
+#define PROPACK_NOALLOC_MAX_DOUBLES 65536
+int propack_csr_apply_noalloc(int64_t handle, int trans, const double *x,
+                              double *y, void *stream);
+
 /* ---------------------------------------------------------------------
  * Per-thread call statistics of the last driver call on this host thread
  * (the reference keeps these in COMMON /timing/; here they are

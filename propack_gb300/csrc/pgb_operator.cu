@@ -482,6 +482,13 @@ void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s)
     PGB_LAUNCHED();
 }
 
+// y = A x with a caller-supplied z (the low-rank coefficients); no scratch
+void op_spmv_plain_launch(const Csr &A, const double *x, const double *z, double *y, cudaStream_t s)
+{
+    k_spmv_plain<<<device_info().nb, BS, 0, s>>>(A, x, z, y);
+    PGB_LAUNCHED();
+}
+
 void op_apply(const Operator &op, bool trans, const double *x, double *y, cudaStream_t s)
 {
     op_thin(op, trans, x, s);
