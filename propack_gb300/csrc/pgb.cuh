@@ -48,8 +48,9 @@ constexpr double KAPPA_GETU0 = (double)0.717f;      // dgetu0.F:30 (REAL literal
 constexpr double FUDGE = 1.01;                      // dlanbpro.F:117
 constexpr int NTRY = 5;                             // dreorth.F:64
 constexpr int BS = 256;                             // threads per CTA of the vector kernels
-constexpr int NNZ_PB = 2048;                        // nnz staged per CTA in the SpMV
-constexpr int ROWS_PB = 256;                        // rows per SpMV row block (<= BS)
+constexpr int NNZ_PB = 2048;                        // nnz per CTA segment of the low-rank prepass
+constexpr int NNZ_W = 256;                          // nnz staged per warp in the SpMV (multiple of 32)
+constexpr int ROWS_W = 32;                          // rows per SpMV row block (<= 32)
 
 // ------------------------------------------------------- device operator
 // CSR with int32 row pointers (nnz < 2^31) and CSR-adaptive row blocks.

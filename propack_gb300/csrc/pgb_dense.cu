@@ -26,8 +26,10 @@ __device__ __forceinline__ void lartg(double f, double g, double &c, double &s, 
 {
     if (g == 0.0) { c = 1.0; s = 0.0; r = f; return; }
     if (f == 0.0) { c = 0.0; s = 1.0; r = g; return; }
-    double rr = hypot(f, g);
-    double cc = f / rr, ss = g / rr;
+    // one reciprocal hypotenuse (overflow-safe) instead of hypot + 2 divides
+    const double rh = rhypot(f, g);
+    double cc = f * rh, ss = g * rh;
+    double rr = fma(f, cc, g * ss);
     if (fabs(f) > fabs(g) && cc < 0.0) { cc = -cc; ss = -ss; rr = -rr; }
     c = cc; s = ss; r = rr;
 }
@@ -372,38 +374,46 @@ __device__ int bdsqr_cta(int n, double *d, double *e, int ncvt, double *vt, int 
 
 // ----------------------------------------------------------------- analysis
 
-// IRL: dlansvd_irl.F:218-290.  lansvd: dlansvd.F:192-236.
-__global__ void k_analyse(AnaArgs a)
+// IRL: dlansvd_irl.F:218-290.  lansvd: dlansvd.F:192-236.  The bidiagonal,
+// the bound row and the rotation chains live in shared memory when they
+// fit (use_smem), so the sequential QR iteration of thread 0 runs at
+// shared-memory latency.
+__global__ void k_analyse(AnaArgs a, int use_smem)
 {
     __shared__ QrShared q;
+    extern __shared__ double dsm[];
     const int dim = a.dim;
-    for (int i = threadIdx.x; i < dim; i += blockDim.x) { a.a1[i] = a.balpha[i]; a.b1[i] = a.bbeta[i]; }
-    for (int i = threadIdx.x; i <= dim; i += blockDim.x) a.bnd[i] = 0.0;
+    double *d = use_smem ? dsm : a.a1;
+    double *e = use_smem ? dsm + (dim + 1) : a.b1;
+    double *bnd = use_smem ? dsm + 2 * (dim + 1) : a.bnd;
+    double *w = use_smem ? dsm + 3 * (dim + 1) + 1 : a.w;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) { d[i] = a.balpha[i]; e[i] = a.bbeta[i]; }
+    for (int i = threadIdx.x; i <= dim; i += blockDim.x) bnd[i] = 0.0;
     __syncthreads();
     const int mn = a.m < a.n ? a.m : a.n;
-    if (threadIdx.x == 0) bdqr_dev(dim == mn, dim, a.a1, a.b1, &a.bnd[dim - 1], &a.bnd[dim], nullptr, 0);
+    if (threadIdx.x == 0) bdqr_dev(dim == mn, dim, d, e, &bnd[dim - 1], &bnd[dim], nullptr, 0);
     __syncthreads();
-    bdsqr_cta(dim, a.a1, a.b1, 0, nullptr, 1, 1, a.bnd, 1, a.w, q);
+    bdsqr_cta(dim, d, e, 0, nullptr, 1, 1, bnd, 1, w, q);
     __syncthreads();
     if (threadIdx.x == 0) {
         const double eps34 = pow(EPS, 0.75);
         const double epsn = (double)(a.m > a.n ? a.m : a.n) * EPS / 2.0;
         double anorm = *a.anorm_drv;
-        if (dim > 5) anorm = a.a1[0];
-        else anorm = fmax(anorm, a.a1[0]);
+        if (dim > 5) anorm = d[0];
+        else anorm = fmax(anorm, d[0]);
         *a.anorm_drv = anorm;
         const double rnorm = a.ctl->rnorm;
-        for (int i = 0; i < dim; i++) a.bnd[i] = fabs(rnorm * a.bnd[i]);
+        for (int i = 0; i < dim; i++) bnd[i] = fabs(rnorm * bnd[i]);
         int nconv = 0;
         if (a.irl) {
             const int neig = a.neig;
-            if (a.small_side) refinebounds_dev(mn, dim, a.a1, a.bnd, epsn * anorm, eps34);
-            else refinebounds_dev(mn, dim < neig ? dim : neig, a.a1, a.bnd, epsn * anorm, eps34);
+            if (a.small_side) refinebounds_dev(mn, dim, d, bnd, epsn * anorm, eps34);
+            else refinebounds_dev(mn, dim < neig ? dim : neig, d, bnd, epsn * anorm, eps34);
             if (a.small_side) {
                 for (int i = dim - neig + 1; i <= dim; i++) {
-                    if (a.bnd[i - 1] <= a.tol * a.a1[0]) {
-                        a.sigma_out[nconv] = a.a1[i - 1];
-                        a.bnd_out[nconv] = a.bnd[i - 1];
+                    if (bnd[i - 1] <= a.tol * d[0]) {
+                        a.sigma_out[nconv] = d[i - 1];
+                        a.bnd_out[nconv] = bnd[i - 1];
                         nconv++;
                     }
                 }
@@ -411,9 +421,9 @@ __global__ void k_analyse(AnaArgs a)
                 int i = 1;
                 const int lim = dim < neig ? dim : neig;
                 while (i <= lim) {
-                    if (a.bnd[i - 1] <= a.tol * a.a1[i - 1]) {
-                        a.sigma_out[nconv] = a.a1[i - 1];
-                        a.bnd_out[nconv] = a.bnd[i - 1];
+                    if (bnd[i - 1] <= a.tol * d[i - 1]) {
+                        a.sigma_out[nconv] = d[i - 1];
+                        a.bnd_out[nconv] = bnd[i - 1];
                         nconv++;
                         i++;
                     } else {
@@ -423,16 +433,22 @@ __global__ void k_analyse(AnaArgs a)
             }
         } else {
             // dlansvd: k = a.kk
-            refinebounds_dev(mn, dim, a.a1, a.bnd, epsn * anorm, eps34);
+            refinebounds_dev(mn, dim, d, bnd, epsn * anorm, eps34);
             const int lim = dim < a.kk ? dim : a.kk;
-            for (int i = 0; i < lim; i++) a.bnd_out[i] = a.bnd[i];
+            for (int i = 0; i < lim; i++) a.bnd_out[i] = bnd[i];
             int i = 0;
             while (i < lim) {
-                if (a.bnd[i] <= a.tol * a.a1[i]) { a.sigma_out[nconv] = a.a1[i]; nconv++; i++; }
+                if (bnd[i] <= a.tol * d[i]) { a.sigma_out[nconv] = d[i]; nconv++; i++; }
                 else i = a.kk;
             }
         }
         *a.nconv_out = nconv;
+    }
+    __syncthreads();
+    if (use_smem) {
+        // the sweeps read the Ritz values and bounds from global memory
+        for (int i = threadIdx.x; i < dim; i += blockDim.x) { a.a1[i] = d[i]; a.bnd[i] = bnd[i]; }
+        if (threadIdx.x == 0) a.bnd[dim] = bnd[dim];
     }
 }
 
@@ -470,10 +486,16 @@ __device__ void bsvdstep_chain(int kk, double sigma, double *D, double *E, doubl
     cu[kk - 1] = c; su[kk - 1] = s;
 }
 
-__global__ void k_irl_sweeps(SweepArgs a)
+__global__ void k_irl_sweeps(SweepArgs a, int use_smem)
 {
+    extern __shared__ double dsm[];
     const int dim = a.dim, k = a.k, dp1 = dim + 1;
-    double *cu = a.w, *su = a.w + dp1, *cv = a.w + 2 * dp1, *sv = a.w + 3 * dp1;
+    double *cu = use_smem ? dsm : a.w, *su = cu + dp1, *cv = cu + 2 * dp1, *sv = cu + 3 * dp1;
+    double *D = use_smem ? dsm + 4 * dp1 : a.balpha;
+    double *E = use_smem ? dsm + 5 * dp1 : a.bbeta;
+    if (use_smem) {
+        for (int i = threadIdx.x; i < dim; i += blockDim.x) { D[i] = a.balpha[i]; E[i] = a.bbeta[i]; }
+    }
     // shifts (dlansvd_irl.F:304-344)
     if (threadIdx.x == 0) {
         for (int i = 0; i < dim - k; i++) a.shifts[i] = 0.0;
@@ -498,7 +520,7 @@ __global__ void k_irl_sweeps(SweepArgs a)
     for (int i = dim; i >= k + 1; i--) {
         const double shift = a.shifts[dim - i];
         if (i <= 1) continue;  // dbsvdstep returns for k <= 1
-        if (threadIdx.x == 0) bsvdstep_chain(i, shift, a.balpha, a.bbeta, cu, su, cv, sv);
+        if (threadIdx.x == 0) bsvdstep_chain(i, shift, D, E, cu, su, cv, sv);
         __syncthreads();
         // the U rotations act on columns (t, t+1) of P, t = 0..i-1; the V
         // rotations on columns (t, t+1) of Q, t = 0..i-2; one row per thread
@@ -526,15 +548,22 @@ __global__ void k_irl_sweeps(SweepArgs a)
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) a.ctl->rnorm = a.bbeta[k - 1];
+    if (use_smem) {
+        for (int i = threadIdx.x; i < dim; i += blockDim.x) { a.balpha[i] = D[i]; a.bbeta[i] = E[i]; }
+    }
+    if (threadIdx.x == 0) a.ctl->rnorm = E[k - 1];
 }
 
 // -------------------------------------------------------------- Ritz prep
-__global__ void k_ritz_prep(RitzArgs a)
+__global__ void k_ritz_prep(RitzArgs a, int use_smem)
 {
     __shared__ QrShared q;
+    extern __shared__ double dsm[];
     const int dim = a.dim;
-    for (int i = threadIdx.x; i < dim; i += blockDim.x) { a.D[i] = a.balpha[i]; a.E[i] = a.bbeta[i]; }
+    double *D = use_smem ? dsm : a.D;
+    double *E = use_smem ? dsm + (dim + 1) : a.E;
+    double *w = use_smem ? dsm + 2 * (dim + 1) : a.w;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) { D[i] = a.balpha[i]; E[i] = a.bbeta[i]; }
     for (size_t t = threadIdx.x; t < (size_t)dim * dim; t += blockDim.x) {
         const double v = (t % (dim + 1) == 0) ? 1.0 : 0.0;
         a.P[t] = v;
@@ -544,10 +573,10 @@ __global__ void k_ritz_prep(RitzArgs a)
     const int mn = a.m < a.n ? a.m : a.n;
     if (threadIdx.x == 0) {
         double c1 = 0, c2 = 0;
-        bdqr_dev(dim == mn, dim, a.D, a.E, &c1, &c2, a.Mt, dim + 1);
+        bdqr_dev(dim == mn, dim, D, E, &c1, &c2, a.Mt, dim + 1);
     }
     __syncthreads();
-    bdsqr_cta(dim, a.D, a.E, dim, a.Qt, dim, dim, a.P, dim, a.w, q);
+    bdsqr_cta(dim, D, E, dim, a.Qt, dim, dim, a.P, dim, w, q);
 }
 
 // ------------------------------------------------------------------ GEMM
@@ -606,19 +635,38 @@ __global__ void k_copy_cols(const double *src, int lds, double *dst, int ldd, in
 }
 
 // ------------------------------------------------------------ host wrappers
+// dynamic shared memory for the single-CTA kernels, when it fits
+static int smem_for(const void *fn, size_t bytes)
+{
+    static thread_local int max_optin = -1;
+    if (max_optin < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    if (bytes + 1024 > (size_t)max_optin) return 0;
+    if (bytes > 48 * 1024) PGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return 1;
+}
 void launch_analyse(const AnaArgs &a, cudaStream_t s)
 {
-    PGB_PROF(PK_ANALYSE, s, k_analyse<<<1, 256, 0, s>>>(a));
+    const size_t bytes = sizeof(double) * (7 * (size_t)(a.dim + 1) + 2);
+    const int use = smem_for((const void *)k_analyse, bytes);
+    PGB_PROF(PK_ANALYSE, s, k_analyse<<<1, 32, use ? bytes : 0, s>>>(a, use));
     PGB_LAUNCHED();
 }
 void launch_sweeps(const SweepArgs &a, cudaStream_t s)
 {
-    PGB_PROF(PK_SWEEPS, s, k_irl_sweeps<<<1, 256, 0, s>>>(a));
+    const size_t bytes = sizeof(double) * 6 * (size_t)(a.dim + 1);
+    const int use = smem_for((const void *)k_irl_sweeps, bytes);
+    PGB_PROF(PK_SWEEPS, s, k_irl_sweeps<<<1, 256, use ? bytes : 0, s>>>(a, use));
     PGB_LAUNCHED();
 }
 void launch_ritz_prep(const RitzArgs &a, cudaStream_t s)
 {
-    k_ritz_prep<<<1, 256, 0, s>>>(a);
+    const size_t bytes = sizeof(double) * 6 * (size_t)(a.dim + 1);
+    const int use = smem_for((const void *)k_ritz_prep, bytes);
+    k_ritz_prep<<<1, 256, use ? bytes : 0, s>>>(a, use);
     PGB_LAUNCHED();
 }
 // C = op(A) op(B) (out of place)

@@ -489,7 +489,7 @@ __device__ void after_cgs(Tail &t, const LbArgs &a, int j, double nrm, int last)
 template <int SIDE>
 __global__ void __launch_bounds__(BS) k_lb_spmv(LbArgs a, int j, int host_product)
 {
-    __shared__ SpmvStage<double> st;
+    __shared__ SpmvStage<double, double> st[SPMV_WARPS];
     __shared__ double sred[32];
     __shared__ Tail t;
     if (a.ctl->status != 0) return;
@@ -504,10 +504,9 @@ __global__ void __launch_bounds__(BS) k_lb_spmv(LbArgs a, int j, int host_produc
     const double *z = a.z;
     const int n0 = A.ncol0;
     double sq = 0.0, dt = 0.0;
-    auto epi = [&](int r, double acc) {
+    auto epi = [&](int r, double acc, double pv) {
         double y = apply_pend(acc, pin);
         if (has_prev) {
-            double pv = prev[r];
             if (pprev.mode) {
                 pv = apply_pend(pv, pprev);
                 prev[r] = pv;
@@ -518,12 +517,13 @@ __global__ void __launch_bounds__(BS) k_lb_spmv(LbArgs a, int j, int host_produc
         out[r] = y;
         sq = fma(y, y, sq);
     };
+    auto pre = [&](int r) -> double { return has_prev ? prev[r] : 0.0; };
     if (!host_product) {
         auto xl = [&](int c) -> double { return c < n0 ? x[c] : z[c - n0]; };
-        csr_rows<double, double>(A.ptr, A.idx, A.val, A.blk, A.nblk, xl, epi, st, sred);
+        csr_rows<double, double>(A.ptr, A.idx, A.val, A.blk, A.nblk, xl, pre, epi, st);
     } else {
         // the caller's APROD already wrote the product into out
-        for (int r = blockIdx.x * BS + threadIdx.x; r < A.rows; r += gridDim.x * BS) epi(r, out[r]);
+        for (int r = blockIdx.x * BS + threadIdx.x; r < A.rows; r += gridDim.x * BS) epi(r, out[r], pre(r));
     }
     sq = block_sum<BS>(sq, sred);
     dt = block_sum<BS>(dt, sred);
@@ -590,8 +590,16 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_dots(LbArgs a, int j)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int c = w; c < L; c += BS / 32) {
         const double *col = W + (size_t)a.sel[c] * ld;
-        double acc = 0.0;
-        for (int r = r0 + lane; r < r1; r += 32) acc = fma(col[r], x[r], acc);
+        double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
+        int r = r0 + lane;
+        for (; r + 96 < r1; r += 128) {
+            acc0 = fma(col[r], x[r], acc0);
+            acc1 = fma(col[r + 32], x[r + 32], acc1);
+            acc2 = fma(col[r + 64], x[r + 64], acc2);
+            acc3 = fma(col[r + 96], x[r + 96], acc3);
+        }
+        for (; r < r1; r += 32) acc0 = fma(col[r], x[r], acc0);
+        double acc = (acc0 + acc1) + (acc2 + acc3);
         acc = warp_sum(acc);
         if (lane == 0) a.part_cols[(size_t)c * a.nb + blockIdx.x] = acc;
     }
@@ -604,10 +612,15 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_dots(LbArgs a, int j)
 
 // x -= W(:,sel) h, then the projections of the new x for the next pass
 constexpr int CGS_TR = 64;
-template <int SIDE>
+// CPW > 0: each warp owns columns w, w+8, ..., w+8*(CPW-1) and every lane
+// keeps one register accumulator per owned column across all of the CTA's
+// row tiles (one FP64 FMA per element, one warp reduction per column per
+// CTA).  CPW == 0: any number of columns, one warp reduction per column
+// per tile (used when the selection can exceed 8*24 columns).
+template <int SIDE, int CPW>
 __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
 {
-    extern __shared__ double dyn[];  // h[L] | acc[L]
+    extern __shared__ double dyn[];  // h[L] | acc[L] | sel[L] (ints)
     __shared__ double red4[4][CGS_TR];
     __shared__ double xn[CGS_TR];
     __shared__ double sred[32];
@@ -615,7 +628,12 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
     if (a.ctl->status != 0 || !a.ctl->reorth_active) return;
     const int L = a.ctl->nsel;
     double *hs = dyn, *acc = dyn + L;
-    for (int c = threadIdx.x; c < L; c += BS) { hs[c] = a.h[c]; acc[c] = 0.0; }
+    int *ssel = reinterpret_cast<int *>(dyn + 2 * L);
+    for (int c = threadIdx.x; c < L; c += BS) {
+        hs[c] = a.h[c];
+        acc[c] = 0.0;
+        ssel[c] = a.sel[c];
+    }
     __syncthreads();
     const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
     const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
@@ -626,12 +644,21 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int rr = threadIdx.x % CGS_TR, g = threadIdx.x / CGS_TR;
     double sq = 0.0;
+    double accr[CPW > 0 ? CPW : 1];
+#pragma unroll
+    for (int q = 0; q < (CPW > 0 ? CPW : 1); q++) accr[q] = 0.0;
     for (int tb = r0; tb < r1; tb += CGS_TR) {
         const int r = tb + rr;
-        double part = 0.0;
-        if (r < r1)
-            for (int c = g; c < L; c += 4) part = fma(W[(size_t)a.sel[c] * ld + r], hs[c], part);
-        red4[g][rr] = part;
+        double p0 = 0.0, p1 = 0.0;
+        if (r < r1) {
+            int c = g;
+            for (; c + 4 < L; c += 8) {
+                p0 = fma(W[(size_t)ssel[c] * ld + r], hs[c], p0);
+                p1 = fma(W[(size_t)ssel[c + 4] * ld + r], hs[c + 4], p1);
+            }
+            if (c < L) p0 = fma(W[(size_t)ssel[c] * ld + r], hs[c], p0);
+        }
+        red4[g][rr] = p0 + p1;
         __syncthreads();
         if (g == 0) {
             double v = 0.0;
@@ -645,13 +672,34 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
         __syncthreads();
         const int ra = tb + lane, rb = tb + lane + 32;
         const double xa = xn[lane], xb = xn[lane + 32];
-        for (int c = w; c < L; c += BS / 32) {
-            const double *col = W + (size_t)a.sel[c] * ld;
-            double v = 0.0;
-            if (ra < r1) v = col[ra] * xa;
-            if (rb < r1) v = fma(col[rb], xb, v);
-            v = warp_sum(v);
-            if (lane == 0) acc[c] += v;
+        if (CPW > 0) {
+#pragma unroll
+            for (int q = 0; q < (CPW > 0 ? CPW : 1); q++) {
+                const int c = w + 8 * q;
+                if (c < L) {
+                    const double *col = W + (size_t)ssel[c] * ld;
+                    if (ra < r1) accr[q] = fma(col[ra], xa, accr[q]);
+                    if (rb < r1) accr[q] = fma(col[rb], xb, accr[q]);
+                }
+            }
+        } else {
+            for (int c = w; c < L; c += BS / 32) {
+                const double *col = W + (size_t)ssel[c] * ld;
+                double v = 0.0;
+                if (ra < r1) v = col[ra] * xa;
+                if (rb < r1) v = fma(col[rb], xb, v);
+                v = warp_sum(v);
+                if (lane == 0) acc[c] += v;
+            }
+        }
+        __syncthreads();
+    }
+    if (CPW > 0) {
+#pragma unroll
+        for (int q = 0; q < (CPW > 0 ? CPW : 1); q++) {
+            const int c = w + 8 * q;
+            const double v = warp_sum(accr[q]);
+            if (c < L && lane == 0) acc[c] = v;
         }
         __syncthreads();
     }
@@ -690,15 +738,51 @@ __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
 // ------------------------------------------------------------ host side
 void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s);
 
-static size_t cgs_smem(const LbArgs &a) { return sizeof(double) * 2 * (size_t)(a.kmax + 1); }
+static size_t cgs_smem(const LbArgs &a) { return (sizeof(double) * 2 + sizeof(int)) * (size_t)(a.kmax + 1) + 16; }
 
+template <int SIDE>
+static void set_upd_limits(size_t need)
+{
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+}
 void lb_set_smem_limits(int kmax)
 {
-    const size_t need = sizeof(double) * 2 * (size_t)(kmax + 1);
+    const size_t need = (sizeof(double) * 2 + sizeof(int)) * (size_t)(kmax + 1) + 16;
     if (need > 48 * 1024) {
-        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+        set_upd_limits<0>(need);
+        set_upd_limits<1>(need);
     }
+}
+
+// one CGS update pass; the template is chosen from an upper bound of the
+// number of selected columns (j-1 on the V side, j on the U side)
+template <int SIDE>
+static void launch_upd(const LbArgs &a, int j, int last, int maxcols, cudaStream_t s)
+{
+    const size_t sm = cgs_smem(a);
+    const int cpw = (maxcols + 7) / 8;
+    if (cpw <= 4) k_lb_cgs_upd<SIDE, 4><<<a.nb, BS, sm, s>>>(a, j, last);
+    else if (cpw <= 8) k_lb_cgs_upd<SIDE, 8><<<a.nb, BS, sm, s>>>(a, j, last);
+    else if (cpw <= 16) k_lb_cgs_upd<SIDE, 16><<<a.nb, BS, sm, s>>>(a, j, last);
+    else if (cpw <= 24) k_lb_cgs_upd<SIDE, 24><<<a.nb, BS, sm, s>>>(a, j, last);
+    else k_lb_cgs_upd<SIDE, 0><<<a.nb, BS, sm, s>>>(a, j, last);
+}
+
+// one wave of CTAs at the fused SpMV's occupancy (partials are summed over gridDim)
+template <int SIDE>
+static int spmv_grid(int nb)
+{
+    static thread_local int g = 0;
+    if (g == 0) {
+        int per = 0;
+        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lb_spmv<SIDE>, BS, 0));
+        g = std::max(1, per) * device_info().sms;
+    }
+    return std::min(g, nb);
 }
 
 // Enqueue the kernels of one half step.  host_product: the product was
@@ -710,7 +794,7 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
     if (side == 0) {
         if (!host_product && op && op->r > 0)
             PGB_PROF(PK_THIN, s, op_thin(*op, true, a.U + (size_t)(j - 1) * a.ldu, s));
-        PGB_PROF(PK_SPMV_ADJ, s, k_lb_spmv<0><<<nb, BS, 0, s>>>(a, j, host_product ? 1 : 0));
+        PGB_PROF(PK_SPMV_ADJ, s, k_lb_spmv<0><<<spmv_grid<0>(nb), BS, 0, s>>>(a, j, host_product ? 1 : 0));
         PGB_LAUNCHED();
         if (j > 1)
             for (int i = 0; i < ielr; i++) {
@@ -720,13 +804,13 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
         PGB_PROF(PK_CGS_DOTS, s, k_lb_cgs_dots<0><<<nb, BS, 0, s>>>(a, j));
         PGB_LAUNCHED();
         for (int i = 0; i < ntry_spec; i++) {
-            PGB_PROF(PK_CGS_UPD, s, k_lb_cgs_upd<0><<<nb, BS, cgs_smem(a), s>>>(a, j, i == ntry_spec - 1));
+            PGB_PROF(PK_CGS_UPD, s, launch_upd<0>(a, j, i == ntry_spec - 1, j - 1, s));
             PGB_LAUNCHED();
         }
     } else {
         if (!host_product && op && op->r > 0)
             PGB_PROF(PK_THIN, s, op_thin(*op, false, a.V + (size_t)(j - 1) * a.ldv, s));
-        PGB_PROF(PK_SPMV_FWD, s, k_lb_spmv<1><<<nb, BS, 0, s>>>(a, j, host_product ? 1 : 0));
+        PGB_PROF(PK_SPMV_FWD, s, k_lb_spmv<1><<<spmv_grid<1>(nb), BS, 0, s>>>(a, j, host_product ? 1 : 0));
         PGB_LAUNCHED();
         for (int i = 0; i < ielr; i++) {
             PGB_PROF(PK_ELR, s, k_lb_elr<1><<<nb, BS, 0, s>>>(a, j));
@@ -735,7 +819,7 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
         PGB_PROF(PK_CGS_DOTS, s, k_lb_cgs_dots<1><<<nb, BS, 0, s>>>(a, j));
         PGB_LAUNCHED();
         for (int i = 0; i < ntry_spec; i++) {
-            PGB_PROF(PK_CGS_UPD, s, k_lb_cgs_upd<1><<<nb, BS, cgs_smem(a), s>>>(a, j, i == ntry_spec - 1));
+            PGB_PROF(PK_CGS_UPD, s, launch_upd<1>(a, j, i == ntry_spec - 1, j, s));
             PGB_LAUNCHED();
         }
     }
@@ -745,8 +829,8 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
 void lb_enqueue_cgs_more(const LbArgs &a, int side, int j, int passes, cudaStream_t s)
 {
     for (int i = 0; i < passes; i++) {
-        if (side == 0) k_lb_cgs_upd<0><<<a.nb, BS, cgs_smem(a), s>>>(a, j, i == passes - 1);
-        else k_lb_cgs_upd<1><<<a.nb, BS, cgs_smem(a), s>>>(a, j, i == passes - 1);
+        if (side == 0) launch_upd<0>(a, j, i == passes - 1, j - 1, s);
+        else launch_upd<1>(a, j, i == passes - 1, j, s);
         PGB_LAUNCHED();
     }
 }

@@ -189,7 +189,7 @@ static int scan_excl(const int *in, int *out, int n, cudaStream_t s)
 __global__ void k_blk_flags(const int *ptr, int rows, int half, int *flag)
 {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
-        int f = (r == 0) || (r % ROWS_PB == 0);
+        int f = (r == 0) || (r % ROWS_W == 0);
         const int len = ptr[r + 1] - ptr[r];
         if (r > 0) {
             const int lenp = ptr[r] - ptr[r - 1];
@@ -214,7 +214,7 @@ static void build_blocks(Csr &A, cudaStream_t s)
     PGB_CUDA(cudaMallocAsync(&pos, sizeof(int) * (rows + 1), s));
     const int g = std::min(4096, std::max(1, (rows + 255) / 256));
     if (rows > 0) {
-        k_blk_flags<<<g, 256, 0, s>>>(A.ptr, rows, NNZ_PB / 2, flag);
+        k_blk_flags<<<g, 256, 0, s>>>(A.ptr, rows, NNZ_W / 2, flag);
         PGB_LAUNCHED();
     }
     A.nblk = scan_excl(flag, pos, rows, s);
@@ -465,12 +465,24 @@ __global__ void __launch_bounds__(BS) k_thin(Csr T, const double *__restrict__ x
 __global__ void __launch_bounds__(BS) k_spmv_plain(Csr A, const double *__restrict__ x,
                                                    const double *__restrict__ z, double *__restrict__ y)
 {
-    __shared__ SpmvStage<double> st;
-    __shared__ double sred[32];
+    __shared__ SpmvStage<double, double> st[SPMV_WARPS];
     const int n0 = A.ncol0;
     auto xl = [&](int c) -> double { return c < n0 ? __ldg(x + c) : z[c - n0]; };
-    auto epi = [&](int r, double acc) { y[r] = acc; };
-    csr_rows<double, double>(A.ptr, A.idx, A.val, A.blk, A.nblk, xl, epi, st, sred);
+    auto pre = [&](int r) -> double { return 0.0; };
+    auto epi = [&](int r, double acc, double) { y[r] = acc; };
+    csr_rows<double, double>(A.ptr, A.idx, A.val, A.blk, A.nblk, xl, pre, epi, st);
+}
+
+// one wave of CTAs at the kernel's occupancy
+static int spmv_plain_grid()
+{
+    static thread_local int g = 0;
+    if (g == 0) {
+        int per = 0;
+        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv_plain, BS, 0));
+        g = std::max(1, per) * device_info().sms;
+    }
+    return g;
 }
 
 void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s)
@@ -485,7 +497,7 @@ void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s)
 // y = A x with a caller-supplied z (the low-rank coefficients); no scratch
 void op_spmv_plain_launch(const Csr &A, const double *x, const double *z, double *y, cudaStream_t s)
 {
-    k_spmv_plain<<<device_info().nb, BS, 0, s>>>(A, x, z, y);
+    k_spmv_plain<<<spmv_plain_grid(), BS, 0, s>>>(A, x, z, y);
     PGB_LAUNCHED();
 }
 
@@ -493,7 +505,7 @@ void op_apply(const Operator &op, bool trans, const double *x, double *y, cudaSt
 {
     op_thin(op, trans, x, s);
     const Csr &A = trans ? op.adj : op.fwd;
-    k_spmv_plain<<<device_info().nb, BS, 0, s>>>(A, x, op.zbuf, y);
+    k_spmv_plain<<<spmv_plain_grid(), BS, 0, s>>>(A, x, op.zbuf, y);
     PGB_LAUNCHED();
 }
 

@@ -143,8 +143,11 @@ def test_vs_oracle_same_trajectory(golden, opts, irl):
     np.testing.assert_allclose(s, so, rtol=SIG_RTOL)
     assert subspace_err(u, uo) < VEC_TOL
     assert subspace_err(vt.T, vto.T) < VEC_TOL
-    # the same Lanczos trajectory: matvec counts agree within a few steps
-    assert abs(st["nopx"] - sto["nopx"]) <= 0.05 * sto["nopx"] + 4
+    # the same Lanczos trajectory up to rounding: partial reorthogonalisation
+    # and the convergence test are threshold decisions, so one restart more or
+    # less (2 * shifts matvecs) is within parity
+    shifts = kw["kmax"] - 10 if irl else 0
+    assert abs(st["nopx"] - sto["nopx"]) <= 0.05 * sto["nopx"] + 2 * shifts + 4
     op.close()
 
 
