@@ -1,30 +1,38 @@
 #!/usr/bin/env python
-"""Benchmark: time to k converged singular triplets on one GB300.
+"""Benchmark: ms and matvecs to k converged singular triplets on one GB300,
+chosen (mixed) form vs plain FP64.
 
-Workload (default ``lowrank_irl``): DLANSVD_IRL in FP64 on a 2,000,000 x
-500,000 sparse operator (20 N(0,1) nonzeros per row at uniform columns)
-plus a rank-64 term sum_i 100*0.9^i u_i v_i' with sparse unit-norm u_i (1%
-dense) and v_i (5% dense), kept factored; k = 50, Lanczos dimension 150
-(p = 100 shifts), tol = 1e-10.  Seeded synthetic data (numpy default_rng(1)).
+Workloads (seeded synthetic data, numpy default_rng):
+* zipf_mixed (default): 4,000,000 x 4,000,000 CSR, nnz per row Zipf(2)
+  clipped to [4, 2000] (31 M nonzeros), uniform columns, values
+  N(0,1) * (1 + i mod 1000)^-0.7 (FP32-representable); k = 50, Lanczos
+  dimension 150, tol = 1e-8 (residual <= 1e-8 * ||A||).
+* lowrank_irl: 2,000,000 x 500,000, 20 N(0,1) nonzeros per row plus a
+  rank-64 term sum_i 100*0.9^i u_i v_i' (sparse unit-norm u_i, v_i; kept
+  factored); k = 50, dimension 150, tol = 1e-10.
 
-A step is one complete solve (start vector -> k converged Ritz triplets).
+A step is one complete DLANSVD_IRL solve (start vector -> k converged Ritz
+triplets), run in each form of --forms (the first is the chosen form):
+* mixed: FP32 Lanczos vectors / SpMV / Gram-Schmidt with compensated
+  reductions, FP64 scalars, then a short FP64 refinement to tol;
+* fp64: the reference's FP64 method.
 
-* value    device ms per solve with the operator already resident in HBM,
-           from CUDA events the library records on the stream its kernels
-           run on (start vector in HBM -> Ritz vectors in HBM).
-* e2e      ms per solve through the public C ABI with HOST inputs: upload of
+* value    chosen form, device ms per solve with the operator already in
+           HBM (CUDA events the library records on its own stream, start
+           vector in HBM -> Ritz vectors in HBM); `forms` gives every form.
+* e2e      chosen form through the public C ABI with HOST inputs: upload of
            the CSR arrays from pinned memory + device transpose + solve +
            copy of sigma, U(:,1:k), V(:,1:k) back to pinned memory.
-* roofline the fused SpMV pair (the dominant HBM-bound kernel): algorithmic
-           bytes per launch / mean launch time, from events around every
-           launch in one profiled solve.
+* roofline the fused SpMV pair of the chosen form (the HBM-bound kernel):
+           algorithmic bytes per launch / mean launch time, from events
+           around every launch in one profiled solve.
 * cpu_baseline / --impl reference: the oracle (the C restatement of
-           PROPACK with OpenMP) on the host cores, timing one complete IRL
-           cycle (maxiter=1) of the same workload and scaling it to the
-           matvec count of a full solve.
+           PROPACK, FP64, OpenMP) on the host cores, timing one complete IRL
+           cycle (maxiter=1) of the same workload and scaling it by matvecs
+           to a full FP64 solve.
 
-Inputs (operator ~1 GB, Lanczos basis 3 GB) are far larger than the 129 MB
-L2, so no L2 flush is needed between steps.
+Inputs (operators of hundreds of MB, Lanczos bases of GBs) are far larger
+than the 129 MB L2, so no L2 flush is needed between steps.
 """
 import argparse
 import json
@@ -41,17 +49,24 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "lowrank_irl": dict(
         desc="2000000x500000 CSR 20nnz/row N(0,1) + rank-64 sparse factored term (w_i=100*0.9^i), "
-             "DLANSVD_IRL FP64 k=50 dim=150 p=100 tol=1e-10",
+             "DLANSVD_IRL k=50 dim=150 p=100 tol=1e-10",
         k=50, kmax=150, tol=1e-10,
-        # matvecs of a complete solve of this seeded workload, measured on GB300
-        # (the GPU path and the oracle follow the same Lanczos trajectory);
-        # used to scale the oracle's one-cycle sample to a full solve
+        # matvecs of a complete FP64 solve of this seeded workload, measured on
+        # GB300 (the GPU path and the oracle follow the same Lanczos trajectory
+        # up to rounding); used to scale the oracle's one-cycle sample when the
+        # FP64 form is not timed in the same run
         matvecs_full=1901,
+    ),
+    "zipf_mixed": dict(
+        desc="4000000x4000000 CSR, nnz/row Zipf(2) clipped to [4,2000], uniform columns, "
+             "N(0,1)*(1+i mod 1000)^-0.7 values (FP32-representable), DLANSVD_IRL k=50 dim=150 p=100 tol=1e-8",
+        k=50, kmax=150, tol=1e-8,
+        matvecs_full=None,
     ),
 }
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the fused SpMV
-# pair, from ncu on this workload (None until captured)
-SPMV_TRAFFIC_BYTES = None
+# pair, from ncu on this workload and form ({workload: {form: bytes}})
+SPMV_TRAFFIC_BYTES = {}
 
 
 def parse():
@@ -60,7 +75,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lowrank_irl", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="zipf_mixed", choices=sorted(WORKLOADS))
+    ap.add_argument("--forms", default="mixed,fp64",
+                    help="comma list; the first is the chosen form reported as value")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--scale", type=float, default=1.0,
@@ -76,9 +93,12 @@ def dist_env():
 
 
 def make_workload(name, scale=1.0):
+    """(S, L, R, w) with A = S + L diag(w) R' (L = R = w = None for plain CSR)."""
     from propack_gb300 import workloads
     if name == "lowrank_irl":
         return workloads.lowrank_irl(seed=1, m=int(2_000_000 * scale), n=int(500_000 * scale))
+    if name == "zipf_mixed":
+        return workloads.zipf_mixed(seed=2, m=int(4_000_000 * scale)), None, None, None
     raise ValueError(name)
 
 
@@ -143,22 +163,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def spmv_bytes(m, n, r, nnz_s, nnz_l, nnz_r):
-    """Algorithmic bytes of one fused SpMV launch, FP64 values / int32 indices:
-    values+indices, row pointers, gathered input, written output, previous
-    Lanczos vector read for the axpy and written back once scaled."""
-    fwd = (nnz_s + nnz_l) * 12 + (m + 1) * 4 + (n + r) * 8 + 3 * m * 8
-    adj = (nnz_s + nnz_r) * 12 + (n + 1) * 4 + (m + r) * 8 + 3 * n * 8
+def spmv_bytes(m, n, r, nnz_s, nnz_l, nnz_r, vb=8):
+    """Algorithmic bytes of one fused SpMV launch with vb-byte values and
+    vectors (8: FP64 form, 4: mixed form) and int32 indices: values+indices,
+    row pointers, gathered input, written output, previous Lanczos vector
+    read for the axpy and written back once scaled."""
+    fwd = (nnz_s + nnz_l) * (vb + 4) + (m + 1) * 4 + (n + r) * vb + 3 * m * vb
+    adj = (nnz_s + nnz_r) * (vb + 4) + (n + 1) * 4 + (m + r) * vb + 3 * n * vb
     return fwd, adj
 
 
-def cpu_sample(S, L, R, w, wl, cores):
-    """One complete IRL cycle of the oracle on the host cores, scaled to a full solve."""
+def cpu_sample(S, L, R, w, wl, cores, matvecs_full=None):
+    """One complete IRL cycle of the oracle on the host cores, scaled by
+    matvecs to a full FP64 solve."""
     import numpy as np
     import oracle
     oracle.build()
     oracle.lib().oracle_set_threads(cores)
-    op = oracle.Operator(S, L, R, w)
+    op = oracle.Operator(S, L, R, w) if L is not None else oracle.Operator(S)
     oracle.clearstat()
     t0 = time.perf_counter()
     u, s, vt, bnd, info, kc = oracle.svdp(None, wl["k"], irl_mode=True, kmax=wl["kmax"], tol=wl["tol"],
@@ -166,8 +188,9 @@ def cpu_sample(S, L, R, w, wl, cores):
                                           compute_v=False)
     dt = (time.perf_counter() - t0) * 1e3
     st = oracle.getstat()
-    scale = wl["matvecs_full"] / max(st["nopx"], 1)
-    return dt * scale, dict(cycle_ms=dt, cycle_matvecs=st["nopx"], scale=scale)
+    full = matvecs_full or wl["matvecs_full"] or st["nopx"]
+    scale = full / max(st["nopx"], 1)
+    return dt * scale, dict(cycle_ms=dt, cycle_matvecs=st["nopx"], scale=scale, matvecs_full=full)
 
 
 def run_reference(args, wl):
@@ -177,6 +200,10 @@ def run_reference(args, wl):
     cores = os.cpu_count() or 1
     S, L, R, w = make_workload(args.workload)
     vals = []
+    if wl["matvecs_full"] is None:
+        print(json.dumps({"impl": "reference", "unavailable": "matvec count of a full solve of this workload "
+                          "not yet measured"}))
+        return 0
     for it in range(args.warmup + args.steps):
         v, info = cpu_sample(S, L, R, w, wl, cores)
         if it >= args.warmup:
@@ -185,7 +212,8 @@ def run_reference(args, wl):
     sample = (f"oracle (C restatement of PROPACK dlansvd_irl, OpenMP) on {cores} host cores: one full IRL cycle "
               f"(maxiter=1: {info['cycle_matvecs']} matvecs, {info['cycle_ms']:.0f} ms) of the same workload, "
               f"scaled by matvecs to a full solve ({wl['matvecs_full']} matvecs)")
-    line = {"impl": "reference", "metric": "ms to k=50 converged triplets (DLANSVD_IRL, resid<=1e-8*||A||)",
+    line = {"impl": "reference",
+            "metric": "ms & matvecs to k=50 triplets at resid<=1e-8*||A||: chosen form vs plain FP64, 1 GB300",
             "value": value, "unit": "ms", "higher_is_better": False, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded)",
@@ -211,141 +239,171 @@ def run_ours(args, wl):
         barrier = dist.barrier
     S, L, R, w = make_workload(args.workload, args.scale)
     m, n = S.shape
-    r = L.shape[1]
+    r = 0 if L is None else L.shape[1]
+    nnz_l = 0 if L is None else L.nnz
+    nnz_r = 0 if R is None else R.nnz
     k, kmax, tol = wl["k"], wl["kmax"], wl["tol"]
+    forms = [f.strip() for f in args.forms.split(",") if f.strip()]
+    chosen = forms[0]
     # reduced-scale runs only feed profiler captures: bound their restarts
     maxiter = 1000 if args.scale == 1.0 else 20
+    dop0 = [np.sqrt(np.finfo(float).eps), np.finfo(float).eps ** 0.75, 0.0, 0.002]  # scipy's defaults
 
     def solve(op, u0=None):
         u = np.zeros((m, kmax + 1), order="F")
         v = np.zeros((n, kmax), order="F")
         sig, bnd = np.zeros(k), np.zeros(k)
         u[:, 0] = np.random.default_rng(0).uniform(size=m) if u0 is None else u0
-        dop = np.array([np.sqrt(np.finfo(float).eps), np.finfo(float).eps ** 0.75, 0.0, 0.002])
+        dop = np.array(dop0)
         iop = np.array([0, 1], dtype=np.int32)
         kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, op.aprod, u, sig, bnd, v, tol,
                                  dop, iop, iparm=op.iparm)
         return kc, info, sig, u, v
 
     op = pg.CsrOperator(S, L, R, w)
-    for _ in range(args.warmup):
-        solve(op)
+    results = {}
     sampler = ClockSampler(0) if rank == 0 else None
     if sampler:
         sampler.start()
-    barrier()
-    t0 = time.perf_counter()
-    dev_ms, launches, matvecs, restarts = 0.0, 0, [], []
-    for _ in range(args.steps):
-        kc, info, sig, u, v = solve(op)
-        st = pg.get_stats()
-        dev_ms += st["solve_ms"]
-        launches += st["kernel_launches"]
-        matvecs.append(st["nopx"])
-        restarts.append(st["nrestart"])
-        if args.scale == 1.0:
-            assert info == 0 and kc == k, (info, kc)
-    wall_ms = (time.perf_counter() - t0) * 1e3
-    barrier()
+    for form in forms:
+        pg.set_precision(form)
+        for _ in range(args.warmup):
+            solve(op)
+        barrier()
+        t0 = time.perf_counter()
+        dev_ms, launches, matvecs, restarts, low = 0.0, 0, [], [], []
+        for _ in range(args.steps):
+            kc, info, sig, u, v = solve(op)
+            st = pg.get_stats()
+            dev_ms += st["solve_ms"]
+            launches += st["kernel_launches"]
+            matvecs.append(st["nopx"])
+            restarts.append(st["nrestart"])
+            low.append(st["nopx_low"])
+            if args.scale == 1.0:
+                assert info == 0 and kc == k, (form, info, kc)
+        wall_ms = (time.perf_counter() - t0) * 1e3
+        barrier()
+        # residual check of the last solve (not timed)
+        res = 0.0
+        for i in range(k):
+            res = max(res, np.linalg.norm(op.matvec(v[:, i]) - sig[i] * u[:, i]),
+                      np.linalg.norm(op.rmatvec(u[:, i]) - sig[i] * v[:, i]))
+        results[form] = dict(dev_ms=dev_ms, wall_ms=wall_ms, launches=launches,
+                             matvecs=statistics.mean(matvecs), restarts=statistics.mean(restarts),
+                             matvecs_fp32=statistics.mean(low), rel_resid=res / sig[0], sigma=sig.copy())
     clocks = sampler.stop() if sampler else None
-    # residual check of the last solve (not timed): max ||A v - s u||, ||A' u - s v|| / ||A||
-    res = 0.0
-    for i in range(k):
-        res = max(res, np.linalg.norm(op.matvec(v[:, i]) - sig[i] * u[:, i]),
-                  np.linalg.norm(op.rmatvec(u[:, i]) - sig[i] * v[:, i]))
-    rel_resid = res / sig[0]
-    # per-kernel profile of one more solve (events around every launch)
+    # per-kernel profile of one more solve of the chosen form
+    pg.set_precision(chosen)
     pg.set_profiling(True)
     solve(op)
     prof = pg.get_profile()
     pg.set_profiling(False)
     op.close()
 
-    # e2e through the public API with pinned host buffers
+    # e2e of the chosen form through the public API with pinned host buffers
     import torch
-    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     import scipy.sparse as sp
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     h_parts = {}
     for nm, M in (("S", S), ("L", L), ("R", R)):
+        if M is None:
+            continue
         M = sp.csr_array(M)
         h_parts[nm] = (pin(M.indptr.astype(np.int64)), pin(M.indices.astype(np.int32)), pin(M.data))
-    h_w = pin(w)
+    h_w = pin(w) if w is not None else None
     u_pin = torch.zeros((kmax + 1, m), dtype=torch.float64).pin_memory().numpy().T  # Fortran order
     v_pin = torch.zeros((kmax, n), dtype=torch.float64).pin_memory().numpy().T
     u0 = np.random.default_rng(0).uniform(size=m)
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 2))
-
-    class _Op:  # an operator built from the pinned host arrays through the C ABI
-        pass
-
     lib = pg.load()
     import ctypes as C
+    nul64, nul32, nuld = C.POINTER(C.c_int64)(), C.POINTER(C.c_int)(), C.POINTER(C.c_double)()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         h = C.c_int64(0)
-        (sp_, si, sv), (lp, li, lv), (rp, ri, rv) = h_parts["S"], h_parts["L"], h_parts["R"]
-        P = pg._i64p
-        rc = lib.propack_csr_create(m, n, P(sp_), pg._ip(si), pg._dp(sv), r, P(lp), pg._ip(li), pg._dp(lv),
-                                    P(rp), pg._ip(ri), pg._dp(rv), pg._dp(h_w), C.byref(h))
+        sp_, si, sv = h_parts["S"]
+        if r:
+            (lp, li, lv), (rp, ri, rv) = h_parts["L"], h_parts["R"]
+            rc = lib.propack_csr_create(m, n, pg._i64p(sp_), pg._ip(si), pg._dp(sv), r, pg._i64p(lp), pg._ip(li),
+                                        pg._dp(lv), pg._i64p(rp), pg._ip(ri), pg._dp(rv), pg._dp(h_w), C.byref(h))
+        else:
+            rc = lib.propack_csr_create(m, n, pg._i64p(sp_), pg._ip(si), pg._dp(sv), 0, nul64, nul32, nuld, nul64,
+                                        nul32, nuld, nuld, C.byref(h))
         assert rc == 0, pg.last_error()
-        o = _Op()
-        o.iparm = np.array([h.value & 0xFFFFFFFF, (h.value >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
-        o.aprod = C.cast(lib.propack_gpu_csr_aprod_, pg.APROD)
+        iparm = np.array([h.value & 0xFFFFFFFF, (h.value >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
+        aprod = C.cast(lib.propack_gpu_csr_aprod_, pg.APROD)
         u_pin[:, 0] = u0
         sig, bnd = np.zeros(k), np.zeros(k)
-        dop = np.array([np.sqrt(np.finfo(float).eps), np.finfo(float).eps ** 0.75, 0.0, 0.002])
+        dop = np.array(dop0)
         iop = np.array([0, 1], dtype=np.int32)
-        kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, o.aprod, u_pin, sig, bnd, v_pin,
-                                 tol, dop, iop, iparm=o.iparm)
+        kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, aprod, u_pin, sig, bnd, v_pin,
+                                 tol, dop, iop, iparm=iparm)
         if args.scale == 1.0:
             assert info == 0 and kc == k
         lib.propack_csr_destroy(h.value)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     barrier()
-    h2d = sum(a.nbytes for t in h_parts.values() for a in t) + h_w.nbytes + m * 8
+    pg.set_precision("fp64")
+    h2d = sum(a.nbytes for t in h_parts.values() for a in t) + (h_w.nbytes if h_w is not None else 0) + m * 8
     d2h = 2 * k * 8 + k * (m + n) * 8
 
     # whole job: max over ranks
-    total_dev = dev_ms
+    tot = {f: results[f]["dev_ms"] for f in forms}
     if world > 1:
-        import torch
-        t = torch.tensor([total_dev, wall_ms, e2e_ms], dtype=torch.float64)
+        t = torch.tensor([tot[f] for f in forms] + [e2e_ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_dev, wall_ms, e2e_ms = t.tolist()
-    value = total_dev / (args.steps * world)
+        vals = t.tolist()
+        tot = dict(zip(forms, vals[:-1]))
+        e2e_ms = vals[-1]
+    per = {f: tot[f] / (args.steps * world) for f in forms}
+    value = per[chosen]
 
     if rank != 0:
         return 0
-    fwd_b, adj_b = spmv_bytes(m, n, r, S.nnz, L.nnz, R.nnz)
-    n_adj, t_adj = prof["spmv_adj"]
-    n_fwd, t_fwd = prof["spmv_fwd"]
-    achieved = (fwd_b * n_fwd + adj_b * n_adj) / ((t_fwd + t_adj) * 1e-3) / 1e9
+    vb = 4 if chosen == "mixed" else 8
+    kadj, kfwd = ("spmv_adj_fp32", "spmv_fwd_fp32") if chosen == "mixed" else ("spmv_adj", "spmv_fwd")
+    fwd_b, adj_b = spmv_bytes(m, n, r, S.nnz, nnz_l, nnz_r, vb)
+    n_adj, t_adj = prof[kadj]
+    n_fwd, t_fwd = prof[kfwd]
+    achieved = (fwd_b * n_fwd + adj_b * n_adj) / max((t_fwd + t_adj) * 1e-3, 1e-12) / 1e9
     peak, peak_kind = peaks()
-    roof = {"bound": "hbm", "kernel": "fused SpMV pair (k_lb_spmv<0>/<1>)", "achieved": achieved, "peak": peak,
-            "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": SPMV_TRAFFIC_BYTES,
+    roof = {"bound": "hbm", "kernel": f"fused SpMV pair ({'FP32, mixed form' if vb == 4 else 'FP64'})",
+            "achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": SPMV_TRAFFIC_BYTES.get(args.workload, {}).get(chosen) if SPMV_TRAFFIC_BYTES else None,
             "algorithmic_bytes_per_launch": {"fwd": fwd_b, "adj": adj_b},
             "mean_launch_ms": {"fwd": t_fwd / max(n_fwd, 1), "adj": t_adj / max(n_adj, 1)}}
     cpu = None
     if not args.no_cpu:
         cores = os.cpu_count() or 1
-        cv, info = cpu_sample(S, L, R, w, wl, cores)
+        mv_full = results["fp64"]["matvecs"] if "fp64" in results else None
+        cv, info = cpu_sample(S, L, R, w, wl, cores, mv_full)
         cpu = {"value": cv, "unit": "ms", "cores": cores, "kind": "port",
-               "sample": f"oracle one IRL cycle ({info['cycle_matvecs']} matvecs, {info['cycle_ms']:.0f} ms) "
-                         f"scaled by matvecs to a full solve ({wl['matvecs_full']})"}
+               "sample": f"oracle (FP64 reference algorithm, OpenMP) one IRL cycle ({info['cycle_matvecs']} matvecs, "
+                         f"{info['cycle_ms']:.0f} ms) scaled by matvecs to a full FP64 solve "
+                         f"({info['matvecs_full']:.0f} matvecs)"}
     breakdown = {kk: {"launches": c, "ms": t} for kk, (c, t) in prof.items() if c}
-    line = {"metric": "ms to k=50 converged triplets (DLANSVD_IRL, resid<=1e-8*||A||)", "value": value,
-            "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value,
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded numpy default_rng(1))",
-            "config": {"workload": args.workload, "desc": wl["desc"], "form": "plain FP64", "scale": args.scale,
-                       "l2": "inputs larger than L2 (operator ~1 GB, basis ~3 GB); no flush"},
-            "matvecs": statistics.mean(matvecs), "restarts": statistics.mean(restarts),
-            "max_rel_residual": rel_resid, "wall_ms_per_step": wall_ms / args.steps,
+    forms_out = {f: {"ms": per[f], "matvecs": results[f]["matvecs"], "matvecs_fp32": results[f]["matvecs_fp32"],
+                     "restarts": results[f]["restarts"], "max_rel_residual": results[f]["rel_resid"],
+                     "wall_ms_per_step": results[f]["wall_ms"] / args.steps} for f in forms}
+    sig_err = None
+    if "fp64" in results and chosen != "fp64":
+        s1, s2 = results["fp64"]["sigma"], results[chosen]["sigma"]
+        sig_err = float(np.max(np.abs(s1 - s2) / s1))
+    line = {"metric": "ms & matvecs to k=50 triplets at resid<=1e-8*||A||: chosen form vs plain FP64, 1 GB300",
+            "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 vectors + f64 scalars" if chosen == "mixed" else "f64",
+            "data": "synthetic (seeded numpy default_rng)",
+            "config": {"workload": args.workload, "desc": wl["desc"], "chosen_form": chosen, "scale": args.scale,
+                       "l2": "inputs larger than L2 (operator and Lanczos basis are GBs); no flush"},
+            "matvecs": results[chosen]["matvecs"], "forms": forms_out,
+            "speedup_vs_plain_fp64": (per["fp64"] / per[chosen]) if "fp64" in per and chosen != "fp64" else None,
+            "max_rel_sigma_diff_vs_fp64": sig_err,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-            "kernel_breakdown": breakdown}
+            "gpu_launches": int(sum(results[f]["launches"] for f in forms)), "roofline": roof,
+            "cpu_baseline": cpu, "clocks": clocks, "kernel_breakdown": breakdown}
     print(json.dumps(line))
     return 0
 

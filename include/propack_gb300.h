@@ -137,15 +137,33 @@ typedef struct {
     int64_t kernel_launches; /* kernels this library launched   */
     double solve_ms;   /* device time from the start vector in HBM
                           to the Ritz vectors in HBM (no host copies) */
+    int64_t nopx_low;  /* mixed form: matvecs of the FP32 phase        */
+    double low_ms;     /* mixed form: device ms of the FP32 phase      */
 } propack_stats_t;
 void propack_get_stats(propack_stats_t *out);
+
+/* Precision of dlansvd_irl_ for the calling host thread.  mode 0 (the
+ * default) is the reference's FP64 method.  mode 1 is the mixed form:
+ * Lanczos vectors, SpMV (on an FP32 copy of the values) and Gram-Schmidt
+ * in FP32 with compensated (two-sum / two-product) reductions, while
+ * alpha, beta, the omega recurrences (with FP32 unit roundoff), the
+ * bidiagonal SVD and the shifts stay FP64; the FP32 run stops at
+ * max(tol, 1e-6) (or after 8 restarts without a new converged value) and
+ * an FP64 run with the same dim and p, started from the sum of the top
+ * neig FP32 Ritz vectors, refines the triplets to the requested tol.
+ * which = 'S' always runs in FP64.
+ * Returns 0, or PROPACK_ERR_ARG for another mode.  No reference
+ * counterpart. */
+int propack_set_precision(int mode);
+int propack_get_precision(void);
 
 /* Per-kernel device timing: with profiling on, CUDA events are recorded
  * on the launching stream around every launch of the main kernels and
  * propack_get_profile returns, per kernel class, the summed milliseconds
  * and launch counts accumulated since propack_set_profiling(1).  Classes
  * in order: SpMV A'u (fused), SpMV Av (fused), ELR pass, CGS projection,
- * CGS update, low-rank prepass, bidiagonal analysis, IRL sweeps, GEMM.
+ * CGS update, low-rank prepass, bidiagonal analysis, IRL sweeps, GEMM,
+ * then the FP32 (mixed form) SpMV A'u, SpMV Av, CGS projection, CGS update.
  * Returns the number of classes.  No reference counterpart. */
 void propack_set_profiling(int on);
 int propack_get_profile(double *total_ms, int64_t *launches, int n);

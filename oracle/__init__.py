@@ -71,7 +71,8 @@ class Operator:
 
     def __init__(self, S, L=None, R=None, w=None):
         import scipy.sparse as sp
-        S = sp.csr_array(S, dtype=np.float64)
+        # copy: sorting the indices of a view would permute the caller's data
+        S = sp.csr_array(S, dtype=np.float64, copy=True)
         S.sort_indices()
         self.shape = S.shape
         self._keep = []

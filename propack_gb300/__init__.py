@@ -39,11 +39,12 @@ class _Stats(C.Structure):
     _fields_ = [("nopx", C.c_int64), ("nreorth", C.c_int64), ("ndot", C.c_int64), ("nrestart", C.c_int64),
                 ("nbsvd", C.c_int64), ("nlandim", C.c_int64), ("device_ms", C.c_double),
                 ("lanczos_ms", C.c_double), ("bsvd_ms", C.c_double), ("gemm_ms", C.c_double),
-                ("kernel_launches", C.c_int64), ("solve_ms", C.c_double)]
+                ("kernel_launches", C.c_int64), ("solve_ms", C.c_double), ("nopx_low", C.c_int64),
+                ("low_ms", C.c_double)]
 
 
 PROFILE_KINDS = ("spmv_adj", "spmv_fwd", "elr", "cgs_dots", "cgs_upd", "lowrank_prepass", "analyse", "sweeps",
-                 "gemm")
+                 "gemm", "spmv_adj_fp32", "spmv_fwd_fp32", "cgs_dots_fp32", "cgs_upd_fp32")
 
 
 _lib = None
@@ -236,14 +237,32 @@ def lansvd(jobu, jobv, m, n, k, kmax, aprod, U, sigma, bnd, V, tol, doption, iop
 _which_converter = {"LM": b"L", "SM": b"S"}
 
 
+PRECISIONS = {"fp64": 0, "mixed": 1}
+
+
+def set_precision(precision):
+    """'fp64' (the reference's method) or 'mixed' (FP32 Lanczos vectors with
+    FP64 scalars, then a short FP64 refinement) for this host thread."""
+    rc = load().propack_set_precision(PRECISIONS[precision])
+    if rc != 0:
+        raise PropackError(f"propack_set_precision failed ({rc})")
+
+
+def get_precision():
+    mode = load().propack_get_precision()
+    return {v: k for k, v in PRECISIONS.items()}[mode]
+
+
 def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=True, v0=None,
          full_output=False, tol=0, delta=None, eta=None, anorm=0, cgs=False, elr=True, min_relgap=0.002,
-         shifts=None, maxiter=None, rng=None):
+         shifts=None, maxiter=None, rng=None, precision="fp64"):
     """Singular triplets of A by Lanczos bidiagonalisation on the GPU.
 
     Argument semantics, defaults, validation and return values follow
     scipy.sparse.linalg._svdp._svdp (scipy/sparse/linalg/_svdp.py); the
     Fortran-level call follows double/dlansvd_irl.F:1-3 / dlansvd.F:1-3.
+    precision: 'fp64' (default; the reference's method) or 'mixed' (FP32
+    Lanczos vectors, FP64 scalars, FP64 refinement to the requested tol).
     Returns (u, sigma, vt, bnd) like scipy's _svdp."""
     from scipy.linalg import LinAlgError
     if rng is None:
@@ -306,6 +325,8 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
         aprod, iparm = op.aprod, op.iparm
     else:
         aprod, iparm = _host_aprod(A), None
+    previous = get_precision()
+    set_precision(precision)
     try:
         if irl_mode:
             kc, info = lansvd_irl(_which_converter[which], jobu, jobv, m, n, kmax, shifts, k, maxiter, aprod,
@@ -314,6 +335,7 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
             kc, info = lansvd(jobu, jobv, m, n, k, kmax, aprod, u, sigma, bnd, v, tol, doption, ioption,
                               iparm=iparm)
     finally:
+        set_precision(previous)
         if own_op is not None:
             own_op.close()
     if info <= ERR_ARG:

@@ -29,7 +29,7 @@ extern thread_local int64_t g_launches;
 // Optional per-kernel timing with CUDA events recorded on the launching
 // stream (propack_set_profiling); off by default.
 enum ProfKind { PK_SPMV_ADJ, PK_SPMV_FWD, PK_ELR, PK_CGS_DOTS, PK_CGS_UPD, PK_THIN, PK_ANALYSE, PK_SWEEPS,
-                PK_GEMM, PK_N };
+                PK_GEMM, PK_SPMV_ADJ32, PK_SPMV_FWD32, PK_CGS_DOTS32, PK_CGS_UPD32, PK_N };
 extern thread_local int g_prof_on;
 void prof_mark(int kind, cudaStream_t s, bool begin);
 void prof_collect();
@@ -97,6 +97,7 @@ struct LbCtl {
     int ldu, ldv;
     int icgs, ielr;
     double delta, eta, epsn, epsn2;
+    double eps_vec;         // unit roundoff of the Lanczos vectors (2^-53 FP64, 2^-24 FP32)
     // recurrence state (dlanbpro.F:123-126)
     int j;                  // current step, 1-based
     int full_reorth, force_reorth;
@@ -126,7 +127,7 @@ struct LbCtl {
 // Everything a Lanczos kernel needs, passed by value.
 struct LbArgs {
     LbCtl *ctl;
-    double *U, *V;          // device Lanczos vectors, column-major
+    void *U, *V;            // device Lanczos vectors (double or float), column-major
     int ldu, ldv;
     double *balpha, *bbeta; // B(:,1), B(:,2)
     double *mu, *nu;
@@ -139,6 +140,43 @@ struct LbArgs {
     int kmax;               // capacity of the column arrays
     Csr fwd, adj;           // device operator (fwd = [S|L], adj = [S'|R])
     const double *z;        // low-rank coefficients of the current product
+};
+template <typename T>
+__host__ __device__ __forceinline__ T *ucol(const LbArgs &a, int c) { return (T *)a.U + (size_t)c * a.ldu; }
+template <typename T>
+__host__ __device__ __forceinline__ T *vcol(const LbArgs &a, int c) { return (T *)a.V + (size_t)c * a.ldv; }
+
+// FP64 accumulation, or FP32 with compensated (two-sum / two-product)
+// accumulation; value() returns the sum in double.
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ void add(double a) { s += a; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct Acc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float p)
+    {
+        const float t = s + p;
+        const float bp = t - s;
+        c += (s - (t - bp)) + (p - bp);
+        s = t;
+    }
+    __device__ __forceinline__ void add_prod(float a, float b)
+    {
+        const float p = a * b;
+        const float pe = fmaf(a, b, -p);
+        const float t = s + p;
+        const float bp = t - s;
+        c += ((s - (t - bp)) + (p - bp)) + pe;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
 // --------------------------------------------------------- helpers
@@ -221,6 +259,15 @@ __device__ __forceinline__ double apply_pend(double x, Pend p)
     default: return x;
     }
 }
+__device__ __forceinline__ float apply_pend(float x, Pend p)
+{
+    switch (p.mode) {
+    case 1: return x * (float)p.val;
+    case 2: return (float)((double)x / p.val);
+    case 3: return 0.f;
+    default: return x;
+    }
+}
 
 
 // ------------------------------------------------ small dense kernels
@@ -261,17 +308,23 @@ struct RitzArgs {
 void launch_analyse(const AnaArgs &a, cudaStream_t s);
 void launch_sweeps(const SweepArgs &a, cudaStream_t s);
 void launch_ritz_prep(const RitzArgs &a, cudaStream_t s);
-void gemm(int mr, int nc, int kk, const double *A, int lda, bool ta, const double *B, int ldb, bool tb, double *C,
-          int ldc, cudaStream_t s);
-void copy_cols(const double *src, int lds, double *dst, int ldd, int rows, int cols, cudaStream_t s);
+template <typename T>
+void gemm(int mr, int nc, int kk, const T *A, int lda, bool ta, const double *B, int ldb, bool tb, T *C, int ldc,
+          cudaStream_t s);
+template <typename T>
+void copy_cols(const T *src, int lds, T *dst, int ldd, int rows, int cols, cudaStream_t s);
 
 // ------------------------------------------------ Lanczos step enqueue
 void lb_set_smem_limits(int kmax);
+template <typename T>
 void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int ielr, int ntry_spec,
                      bool host_product, cudaStream_t s);
+template <typename T>
 void lb_enqueue_cgs_more(const LbArgs &a, int side, int j, int passes, cudaStream_t s);
+template <typename T>
 void lb_enqueue_flush(const LbArgs &a, cudaStream_t s);
-void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s);
+template <typename T>
+void op_thin(const Operator &op, bool trans, const T *x, cudaStream_t s);
 int64_t handle_from_iparm(const int *iparm);
 const char *last_error();
 
@@ -284,6 +337,7 @@ struct Dev {
 const Dev &device_info();
 
 // operator application on device vectors (no Lanczos fusion)
-void op_apply(const Operator &op, bool trans, const double *x, double *y, cudaStream_t s);
+template <typename T>
+void op_apply(const Operator &op, bool trans, const T *x, T *y, cudaStream_t s);
 
 }  // namespace pgb

@@ -580,33 +580,36 @@ __global__ void k_ritz_prep(RitzArgs a, int use_smem)
 }
 
 // ------------------------------------------------------------------ GEMM
-// C(mr x nc) = op(A) op(B), FP64, 64 x 64 tiles, 256 threads x 4 x 4.
+// C(mr x nc) = op(A) op(B), 64 x 64 tiles, 256 threads x 4 x 4.  A and C
+// hold T (the Lanczos vector type), B is FP64 (the small restart / Ritz
+// factors); the product is formed in T.
 // op(A)(i,l) = ta ? A[i*lda + l] : A[l*lda + i]; same for B with (l, j).
-__global__ void __launch_bounds__(256) k_gemm(int mr, int nc, int kk, const double *__restrict__ A, int lda, int ta,
-                                             const double *__restrict__ B, int ldb, int tb, double *__restrict__ C,
+template <typename T>
+__global__ void __launch_bounds__(256) k_gemm(int mr, int nc, int kk, const T *__restrict__ A, int lda, int ta,
+                                             const double *__restrict__ B, int ldb, int tb, T *__restrict__ C,
                                              int ldc)
 {
-    __shared__ double As[16][64 + 1];
-    __shared__ double Bs[16][64 + 1];
+    __shared__ T As[16][64 + 1];
+    __shared__ T Bs[16][64 + 1];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
-    double acc[4][4] = {};
+    T acc[4][4] = {};
     for (int l0 = 0; l0 < kk; l0 += 16) {
         for (int t = threadIdx.x; t < 16 * 64; t += 256) {
             const int l = t / 64, i = t % 64;
             const int gi = i0 + i, gl = l0 + l;
-            double v = 0.0;
+            T v = 0;
             if (gi < mr && gl < kk) v = ta ? A[(size_t)gi * lda + gl] : A[(size_t)gl * lda + gi];
             As[l][i] = v;
             const int gj = j0 + i;
-            double u = 0.0;
-            if (gj < nc && gl < kk) u = tb ? B[(size_t)gl * ldb + gj] : B[(size_t)gj * ldb + gl];
+            T u = 0;
+            if (gj < nc && gl < kk) u = (T)(tb ? B[(size_t)gl * ldb + gj] : B[(size_t)gj * ldb + gl]);
             Bs[l][i] = u;
         }
         __syncthreads();
 #pragma unroll
         for (int l = 0; l < 16; l++) {
-            double av[4], bv[4];
+            T av[4], bv[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) { av[q] = As[l][tx + 16 * q]; bv[q] = Bs[l][ty + 16 * q]; }
 #pragma unroll
@@ -625,7 +628,8 @@ __global__ void __launch_bounds__(256) k_gemm(int mr, int nc, int kk, const doub
         }
 }
 
-__global__ void k_copy_cols(const double *src, int lds, double *dst, int ldd, int rows, int cols)
+template <typename T>
+__global__ void k_copy_cols(const T *src, int lds, T *dst, int ldd, int rows, int cols)
 {
     const size_t total = (size_t)rows * cols;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
@@ -670,19 +674,27 @@ void launch_ritz_prep(const RitzArgs &a, cudaStream_t s)
     PGB_LAUNCHED();
 }
 // C = op(A) op(B) (out of place)
-void gemm(int mr, int nc, int kk, const double *A, int lda, bool ta, const double *B, int ldb, bool tb, double *C,
-          int ldc, cudaStream_t s)
+template <typename T>
+void gemm(int mr, int nc, int kk, const T *A, int lda, bool ta, const double *B, int ldb, bool tb, T *C, int ldc,
+          cudaStream_t s)
 {
     if (mr <= 0 || nc <= 0) return;
     dim3 grid((mr + 63) / 64, (nc + 63) / 64);
-    PGB_PROF(PK_GEMM, s, k_gemm<<<grid, 256, 0, s>>>(mr, nc, kk, A, lda, ta ? 1 : 0, B, ldb, tb ? 1 : 0, C, ldc));
+    PGB_PROF(PK_GEMM, s, k_gemm<T><<<grid, 256, 0, s>>>(mr, nc, kk, A, lda, ta ? 1 : 0, B, ldb, tb ? 1 : 0, C, ldc));
     PGB_LAUNCHED();
 }
-void copy_cols(const double *src, int lds, double *dst, int ldd, int rows, int cols, cudaStream_t s)
+template <typename T>
+void copy_cols(const T *src, int lds, T *dst, int ldd, int rows, int cols, cudaStream_t s)
 {
     if (rows <= 0 || cols <= 0) return;
-    k_copy_cols<<<device_info().nb, 256, 0, s>>>(src, lds, dst, ldd, rows, cols);
+    k_copy_cols<T><<<device_info().nb, 256, 0, s>>>(src, lds, dst, ldd, rows, cols);
     PGB_LAUNCHED();
 }
+template void gemm<double>(int, int, int, const double *, int, bool, const double *, int, bool, double *, int,
+                           cudaStream_t);
+template void gemm<float>(int, int, int, const float *, int, bool, const double *, int, bool, float *, int,
+                          cudaStream_t);
+template void copy_cols<double>(const double *, int, double *, int, int, int, cudaStream_t);
+template void copy_cols<float>(const float *, int, float *, int, int, int, cudaStream_t);
 
 }  // namespace pgb

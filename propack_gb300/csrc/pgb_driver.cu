@@ -26,6 +26,8 @@ struct Stats {
     double device_ms = 0, lanczos_ms = 0, bsvd_ms = 0, gemm_ms = 0;
     int64_t launches = 0;
     double solve_ms = 0;
+    int64_t nopx_low = 0;   // matvecs of the FP32 phase (mixed form)
+    double low_ms = 0;      // device ms of the FP32 phase (mixed form)
 };
 static thread_local Stats g_stat;       // cumulative (clearstat_/printstat_)
 static thread_local Stats g_last;       // last driver call (propack_get_stats)
@@ -40,7 +42,8 @@ __device__ __forceinline__ unsigned long long mulmod48(unsigned long long a, uns
 }
 // x[i] = 2 * (seed * a^(offset+i+1) mod 2^48) / 2^48 - 1: dlarnv(2, ...) with
 // dlaruv's generator (Lapack_Util/dlarnv.f, dlaruv.f), 64 values per thread.
-__global__ void k_rng_pm1(double *x, int n, unsigned long long seed, long long offset)
+template <typename T>
+__global__ void k_rng_pm1(T *x, int n, unsigned long long seed, long long offset)
 {
     const double r48 = 1.0 / 281474976710656.0;
     const long long nchunk = (n + 63) / 64;
@@ -55,18 +58,19 @@ __global__ void k_rng_pm1(double *x, int n, unsigned long long seed, long long o
         unsigned long long s = mulmod48(seed, p);
         const int i0 = (int)(cidx * 64);
         for (int q = 0; q < 64 && i0 + q < n; q++) {
-            x[i0 + q] = 2.0 * ((double)s * r48) - 1.0;
+            x[i0 + q] = (T)(2.0 * ((double)s * r48) - 1.0);
             s = mulmod48(s, LCG_A);
         }
     }
 }
 
-__global__ void __launch_bounds__(BS) k_sumsq_part(const double *x, int n, double *part)
+template <typename T>
+__global__ void __launch_bounds__(BS) k_sumsq_part(const T *x, int n, double *part)
 {
     __shared__ double red[32];
-    double s = 0.0;
-    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) s = fma(x[i], x[i], s);
-    s = block_sum<BS>(s, red);
+    Acc<T> a;
+    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) a.add_prod(x[i], x[i]);
+    const double s = block_sum<BS>(a.value(), red);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 __global__ void __launch_bounds__(BS) k_sum_final(const double *part, int nb, double *out)
@@ -78,18 +82,18 @@ __global__ void __launch_bounds__(BS) k_sum_final(const double *part, int nb, do
     if (threadIdx.x == 0) *out = s;
 }
 // partial W(:,0:kk)' x per CTA (contiguous row chunks), column c at c*nb
-__global__ void __launch_bounds__(BS) k_gemvt_part(const double *W, size_t ld, int len, int kk, const double *x,
-                                                   double *part)
+template <typename T>
+__global__ void __launch_bounds__(BS) k_gemvt_part(const T *W, size_t ld, int len, int kk, const T *x, double *part)
 {
     const int chunk = (len + gridDim.x - 1) / gridDim.x;
     const int r0 = blockIdx.x * chunk, r1 = min(len, r0 + chunk);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int c = w; c < kk; c += BS / 32) {
-        const double *col = W + (size_t)c * ld;
-        double acc = 0.0;
-        for (int r = r0 + lane; r < r1; r += 32) acc = fma(col[r], x[r], acc);
-        acc = warp_sum(acc);
-        if (lane == 0) part[(size_t)c * gridDim.x + blockIdx.x] = acc;
+        const T *col = W + (size_t)c * ld;
+        Acc<T> acc;
+        for (int r = r0 + lane; r < r1; r += 32) acc.add_prod(col[r], x[r]);
+        const double v = warp_sum(acc.value());
+        if (lane == 0) part[(size_t)c * gridDim.x + blockIdx.x] = v;
     }
 }
 __global__ void __launch_bounds__(BS) k_gemvt_final(const double *part, int nb, int kk, double *h)
@@ -102,30 +106,31 @@ __global__ void __launch_bounds__(BS) k_gemvt_final(const double *part, int nb, 
         if (lane == 0) h[c] = s;
     }
 }
-__global__ void __launch_bounds__(BS) k_gemvn_upd(const double *W, size_t ld, int len, int kk, const double *h,
-                                                  double *x)
+template <typename T>
+__global__ void __launch_bounds__(BS) k_gemvn_upd(const T *W, size_t ld, int len, int kk, const double *h, T *x)
 {
     for (int r = blockIdx.x * BS + threadIdx.x; r < len; r += gridDim.x * BS) {
-        double acc = 0.0;
-        for (int c = 0; c < kk; c++) acc = fma(W[(size_t)c * ld + r], h[c], acc);
+        T acc = 0;
+        for (int c = 0; c < kk; c++) acc = fma(W[(size_t)c * ld + r], (T)h[c], acc);
         x[r] -= acc;
     }
 }
-__global__ void k_scale(double *x, int n, int mode, double val)
+template <typename T>
+__global__ void k_scale(T *x, int n, int mode, double val)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (mode == 1) x[i] *= val;
-        else if (mode == 2) x[i] /= val;
-        else if (mode == 3) x[i] = 0.0;
-    }
+    Pend p;
+    p.mode = mode;
+    p.val = val;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = apply_pend(x[i], p);
 }
 // apply the deferred scale of u (which=0) or v (which=1) to its column now
-__global__ void k_apply_pend_col(LbCtl *ctl, double *U, int ldu, double *V, int ldv, int m, int n, int which)
+template <typename T>
+__global__ void k_apply_pend_col(LbCtl *ctl, T *U, int ldu, T *V, int ldv, int m, int n, int which)
 {
     const Pend p = which == 0 ? ctl->pend_u : ctl->pend_v;
     const int col = which == 0 ? ctl->pend_u_col : ctl->pend_v_col;
     if (p.mode != 0 && col >= 0) {
-        double *x = which == 0 ? U + (size_t)col * ldu : V + (size_t)col * ldv;
+        T *x = which == 0 ? U + (size_t)col * ldu : V + (size_t)col * ldv;
         const int len = which == 0 ? m : n;
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x)
             x[i] = apply_pend(x[i], p);
@@ -136,18 +141,35 @@ __global__ void k_clear_pend(LbCtl *ctl, int which)
     if (which == 0) ctl->pend_u.mode = 0;
     else ctl->pend_v.mode = 0;
 }
+template <typename TS, typename TD>
+__global__ void k_convert(const TS *src, TD *dst, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = (TD)src[i];
+}
+// out[r] = sum over the first ncols columns of U (the warm start of the
+// FP64 refinement: a vector in the span of the FP32 Ritz vectors)
+template <typename T>
+__global__ void k_sum_cols(const T *U, size_t ldu, int m, int ncols, double *out)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < ncols; c++) s += (double)U[(size_t)c * ldu + r];
+        out[r] = s;
+    }
+}
 
 // ------------------------------------------------------------- context
 struct Ctx {
-    int m = 0, n = 0, kmax = 0, ldu = 0, ldv = 0;
+    int m = 0, n = 0, kmax = 0, ldu = 0, ldv = 0, es = 8;
     cudaStream_t s = nullptr;
-    double *U = nullptr, *V = nullptr;
+    void *U = nullptr, *V = nullptr;        // Lanczos vectors (double or float)
     LbCtl *ctl = nullptr;
     LbCtl *hctl = nullptr;  // pinned host copy
     double *balpha = nullptr, *bbeta = nullptr, *mu = nullptr, *nu = nullptr, *h = nullptr;
     double *part_sq = nullptr, *part_dot = nullptr, *part_cols = nullptr;
     int *index = nullptr, *sel = nullptr;
-    double *xr = nullptr, *yr = nullptr;    // max(m,n) scratch
+    void *xr = nullptr, *yr = nullptr;      // max(m,n) scratch of the vector type
+    double *dx = nullptr, *dy = nullptr;    // max(m,n) FP64 scratch
     double *scal = nullptr;                 // device scalar slots
     double *hscal = nullptr;                // pinned host scalars
     // dense
@@ -155,7 +177,7 @@ struct Ctx {
     double *shifts = nullptr, *sig_out = nullptr, *bnd_out = nullptr, *anorm_drv = nullptr;
     int *nconv = nullptr;
     double *D = nullptr, *E = nullptr, *Mt = nullptr, *Pr = nullptr, *Qt = nullptr, *X = nullptr;
-    double *gout = nullptr;                 // GEMM output scratch
+    void *gout = nullptr;                   // GEMM output scratch (vector type)
     // operator
     const Operator *op = nullptr;
     propack_aprod_t aprod = nullptr;
@@ -167,15 +189,17 @@ struct Ctx {
     std::vector<void *> allocs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
 
-    template <typename T>
-    T *dalloc(size_t count)
+    void *dbytes(size_t bytes)
     {
         void *p = nullptr;
-        PGB_CUDA(cudaMalloc(&p, sizeof(T) * std::max<size_t>(count, 1)));
-        PGB_CUDA(cudaMemsetAsync(p, 0, sizeof(T) * std::max<size_t>(count, 1), s));
+        bytes = std::max<size_t>(bytes, 16);
+        PGB_CUDA(cudaMalloc(&p, bytes));
+        PGB_CUDA(cudaMemsetAsync(p, 0, bytes, s));
         allocs.push_back(p);
-        return (T *)p;
+        return p;
     }
+    template <typename T>
+    T *dalloc(size_t count) { return (T *)dbytes(sizeof(T) * count); }
     ~Ctx()
     {
         if (s) cudaStreamSynchronize(s);
@@ -204,6 +228,10 @@ struct Ctx {
         }
         return a;
     }
+    template <typename T>
+    T *Ucol(int c) const { return (T *)U + (size_t)c * ldu; }
+    template <typename T>
+    T *Vcol(int c) const { return (T *)V + (size_t)c * ldv; }
     void sync() { PGB_CUDA(cudaStreamSynchronize(s)); }
     void get_ctl()
     {
@@ -213,10 +241,11 @@ struct Ctx {
     void put_ctl() { PGB_CUDA(cudaMemcpyAsync(ctl, hctl, sizeof(LbCtl), cudaMemcpyHostToDevice, s)); }
 };
 
+template <typename T>
 static void init_ctx(Ctx &c, int m, int n, int kmax)
 {
     const Dev &d = device_info();
-    c.m = m; c.n = n; c.kmax = kmax;
+    c.m = m; c.n = n; c.kmax = kmax; c.es = (int)sizeof(T);
     c.ldu = (m + 31) / 32 * 32;
     c.ldv = (n + 31) / 32 * 32;
     c.nb = d.nb;
@@ -225,8 +254,8 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
     PGB_CUDA(cudaEventCreate(&c.ev1));
     PGB_CUDA(cudaEventCreate(&c.evs0));
     PGB_CUDA(cudaEventCreate(&c.evs1));
-    c.U = c.dalloc<double>((size_t)c.ldu * (kmax + 1));
-    c.V = c.dalloc<double>((size_t)c.ldv * (kmax + 1));
+    c.U = c.dalloc<T>((size_t)c.ldu * (kmax + 1));
+    c.V = c.dalloc<T>((size_t)c.ldv * (kmax + 1));
     c.ctl = c.dalloc<LbCtl>(1);
     PGB_CUDA(cudaMallocHost(&c.hctl, sizeof(LbCtl)));
     memset(c.hctl, 0, sizeof(LbCtl));
@@ -241,8 +270,10 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
     c.index = c.dalloc<int>(2 * (size_t)kmax + 8);
     c.sel = c.dalloc<int>(kmax + 2);
     const int mn = std::max(m, n);
-    c.xr = c.dalloc<double>(mn);
-    c.yr = c.dalloc<double>(mn);
+    c.xr = c.dalloc<T>(mn);
+    c.yr = c.dalloc<T>(mn);
+    c.dx = c.dalloc<double>(mn);
+    c.dy = c.dalloc<double>(mn);
     c.scal = c.dalloc<double>(8);
     PGB_CUDA(cudaMallocHost(&c.hscal, sizeof(double) * 8));
     const size_t d1 = kmax + 2;
@@ -256,14 +287,15 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
     c.D = c.dalloc<double>(d1); c.E = c.dalloc<double>(d1);
     c.Mt = c.dalloc<double>(d1 * d1); c.Pr = c.dalloc<double>(d1 * d1); c.Qt = c.dalloc<double>(d1 * d1);
     c.X = c.dalloc<double>(d1 * d1);
-    c.gout = c.dalloc<double>((size_t)std::max(c.ldu, c.ldv) * (kmax + 1));
+    c.gout = c.dalloc<T>((size_t)std::max(c.ldu, c.ldv) * (kmax + 1));
     lb_set_smem_limits(kmax);
 }
 
 // ----------------------------------------------------- device utilities
-static double dev_nrm2(Ctx &c, const double *x, int n)
+template <typename T>
+static double dev_nrm2(Ctx &c, const T *x, int n)
 {
-    k_sumsq_part<<<c.nb, BS, 0, c.s>>>(x, n, c.part_sq);
+    k_sumsq_part<T><<<c.nb, BS, 0, c.s>>>(x, n, c.part_sq);
     PGB_LAUNCHED();
     k_sum_final<<<1, BS, 0, c.s>>>(c.part_sq, c.nb, c.scal);
     PGB_LAUNCHED();
@@ -271,75 +303,97 @@ static double dev_nrm2(Ctx &c, const double *x, int n)
     c.sync();
     return std::sqrt(c.hscal[0]);
 }
-static void dev_scale(Ctx &c, double *x, int n, int mode, double val)
+template <typename T>
+static void dev_scale(Ctx &c, T *x, int n, int mode, double val)
 {
     if (mode == 0 || n <= 0) return;
-    k_scale<<<c.nb, 256, 0, c.s>>>(x, n, mode, val);
+    k_scale<T><<<c.nb, 256, 0, c.s>>>(x, n, mode, val);
     PGB_LAUNCHED();
 }
 // dsafescal on the device
-static void dev_safescal(Ctx &c, double *x, int n, double alpha)
+template <typename T>
+static void dev_safescal(Ctx &c, T *x, int n, double alpha)
 {
-    if (std::fabs(alpha) >= SFMIN) dev_scale(c, x, n, 1, 1.0 / alpha);
-    else dev_scale(c, x, n, 2, alpha);
+    if (std::fabs(alpha) >= SFMIN) dev_scale<T>(c, x, n, 1, 1.0 / alpha);
+    else dev_scale<T>(c, x, n, 2, alpha);
+}
+template <typename TS, typename TD>
+static void dev_convert(Ctx &c, const TS *src, TD *dst, int n)
+{
+    k_convert<TS, TD><<<c.nb, 256, 0, c.s>>>(src, dst, n);
+    PGB_LAUNCHED();
 }
 
 // y = op(A) x on device vectors, through the device operator or the
-// caller's host APROD
-static void dev_aprod(Ctx &c, bool trans, const double *x, double *y)
+// caller's host APROD (which sees FP64 host vectors)
+template <typename T>
+static void dev_aprod(Ctx &c, bool trans, const T *x, T *y)
 {
     const int nin = trans ? c.m : c.n, nout = trans ? c.n : c.m;
     if (c.op) {
-        op_apply(*c.op, trans, x, y, c.s);
+        op_apply<T>(*c.op, trans, x, y, c.s);
         return;
     }
-    PGB_CUDA(cudaMemcpyAsync(c.hx, x, sizeof(double) * nin, cudaMemcpyDeviceToHost, c.s));
+    const double *xd = (const double *)x;
+    if (sizeof(T) != sizeof(double)) {
+        dev_convert<T, double>(c, x, c.dx, nin);
+        xd = c.dx;
+    }
+    PGB_CUDA(cudaMemcpyAsync(c.hx, xd, sizeof(double) * nin, cudaMemcpyDeviceToHost, c.s));
     c.sync();
     const char ta = trans ? 't' : 'n';
     c.aprod(&ta, &c.m, &c.n, c.hx, c.hy, c.dparm, c.iparm, 1);
-    PGB_CUDA(cudaMemcpyAsync(y, c.hy, sizeof(double) * nout, cudaMemcpyHostToDevice, c.s));
+    if (sizeof(T) != sizeof(double)) {
+        PGB_CUDA(cudaMemcpyAsync(c.dy, c.hy, sizeof(double) * nout, cudaMemcpyHostToDevice, c.s));
+        dev_convert<double, T>(c, c.dy, y, nout);
+    } else {
+        PGB_CUDA(cudaMemcpyAsync((double *)y, c.hy, sizeof(double) * nout, cudaMemcpyHostToDevice, c.s));
+    }
 }
 
 // dreorth against all of W(:,0:kk) (index = [1, kk, kk+1]), iterated CGS;
 // host-driven (resume prologue and dgetu0 only)
-static void dev_reorth_full(Ctx &c, const double *W, size_t ld, int len, int kk, double *x, double *nrm, double kappa)
+template <typename T>
+static void dev_reorth_full(Ctx &c, const T *W, size_t ld, int len, int kk, T *x, double *nrm, double kappa)
 {
     if (kk <= 0 || len <= 0) return;
     for (int itry = 0; itry < NTRY; itry++) {
         const double nrm0 = *nrm;
-        k_gemvt_part<<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, x, c.part_cols);
+        k_gemvt_part<T><<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, x, c.part_cols);
         PGB_LAUNCHED();
         k_gemvt_final<<<1, BS, 0, c.s>>>(c.part_cols, c.nb, kk, c.h);
         PGB_LAUNCHED();
-        k_gemvn_upd<<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, c.h, x);
+        k_gemvn_upd<T><<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, c.h, x);
         PGB_LAUNCHED();
         g_last.ndot += 2 * (int64_t)kk;
-        *nrm = dev_nrm2(c, x, len);
+        *nrm = dev_nrm2<T>(c, x, len);
         if (*nrm > kappa * nrm0) { g_last.nreorth++; return; }
     }
     *nrm = 0.0;
-    dev_scale(c, x, len, 3, 0.0);
+    dev_scale<T>(c, x, len, 3, 0.0);
     g_last.nreorth++;
 }
 
 // dgetu0 (double/dgetu0.F:11-89): a random vector in span(op(A)) orthogonal
 // to the first j columns of W; returns u0norm, anormest, ierr.
-static int dev_getu0(Ctx &c, bool trans, int j, int ntry, double *u0, double *u0norm, const double *W, size_t ld,
+template <typename T>
+static int dev_getu0(Ctx &c, bool trans, int j, int ntry, T *u0, double *u0norm, const T *W, size_t ld,
                      double *anormest)
 {
     const unsigned long long seed = (1ull << 36) | (3ull << 24) | (5ull << 12) | 7ull;
     const int rsize = trans ? c.m : c.n, usize = trans ? c.n : c.m;
+    T *xr = (T *)c.xr;
     for (int itry = 0; itry < ntry; itry++) {
         const int nch = (rsize + 63) / 64;
-        k_rng_pm1<<<std::max(1, std::min(c.nb, (nch + 255) / 256)), 256, 0, c.s>>>(c.xr, rsize, seed,
-                                                                                   (long long)itry * rsize);
+        k_rng_pm1<T><<<std::max(1, std::min(c.nb, (nch + 255) / 256)), 256, 0, c.s>>>(xr, rsize, seed,
+                                                                                      (long long)itry * rsize);
         PGB_LAUNCHED();
-        const double nrm = dev_nrm2(c, c.xr, rsize);
-        dev_aprod(c, trans, c.xr, u0);
+        const double nrm = dev_nrm2<T>(c, xr, rsize);
+        dev_aprod<T>(c, trans, xr, u0);
         g_last.nopx++;
-        *u0norm = dev_nrm2(c, u0, usize);
+        *u0norm = dev_nrm2<T>(c, u0, usize);
         *anormest = *u0norm / nrm;
-        if (j >= 1) dev_reorth_full(c, W, ld, usize, j, u0, u0norm, KAPPA_GETU0);
+        if (j >= 1) dev_reorth_full<T>(c, W, ld, usize, j, u0, u0norm, KAPPA_GETU0);
         if (*u0norm > 0) return 0;
     }
     return -1;
@@ -351,6 +405,7 @@ struct LbResult {
 };
 
 // Run dlanbpro (double/dlanbpro.F:1-549) from k0 to *kp on the device.
+template <typename T>
 static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption, const int *ioption, int *ierr)
 {
     const int m = c.m, n = c.n;
@@ -362,10 +417,13 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
     const int mn = std::max(m, n);
     h.m = m; h.n = n; h.k = k; h.ldu = c.ldu; h.ldv = c.ldv;
     h.icgs = ioption[0]; h.ielr = ioption[1];
-    h.epsn = (double)mn * EPS;
-    h.epsn2 = std::sqrt((double)mn) * EPS;
-    h.delta = doption[0] < 0 ? std::sqrt(EPS / k) : doption[0];
-    h.eta = doption[1] < 0 ? std::pow(EPS, 0.75) / std::sqrt((double)k) : doption[1];
+    // machine constants of the Lanczos vectors (FP32 vectors: eps = 2^-24)
+    const double eps = sizeof(T) == sizeof(double) ? EPS : 5.9604644775390625e-08;
+    h.eps_vec = eps;
+    h.epsn = (double)mn * eps;
+    h.epsn2 = std::sqrt((double)mn) * eps;
+    h.delta = doption[0] < 0 ? std::sqrt(eps / k) : doption[0];
+    h.eta = doption[1] < 0 ? std::pow(eps, 0.75) / std::sqrt((double)k) : doption[1];
     h.full_reorth = (h.delta <= h.eta || h.delta == 0.0);
     h.status = 0;
     h.elr_active = 0;
@@ -393,7 +451,7 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
     PGB_CUDA(cudaMemsetAsync(c.index, 0, sizeof(int) * (2 * (size_t)k + 4), c.s));
     double anormest = 0.0;
     if (*rnorm == 0.0) {
-        int e = dev_getu0(c, false, k0, 3, c.U + (size_t)k0 * c.ldu, rnorm, c.U, c.ldu, &anormest);
+        int e = dev_getu0<T>(c, false, k0, 3, c.Ucol<T>(k0), rnorm, (T *)c.U, c.ldu, &anormest);
         *ierr = e;
         anorm = std::max(anorm, anormest);
     }
@@ -406,8 +464,8 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
         h.force_reorth = 0;
         double s;
         int e;
-        if (n > m) e = dev_getu0(c, false, 0, 1, c.yr, &s, c.U, c.ldu, &anormest);
-        else e = dev_getu0(c, true, 0, 1, c.yr, &s, c.V, c.ldv, &anormest);
+        if (n > m) e = dev_getu0<T>(c, false, 0, 1, (T *)c.yr, &s, (T *)c.U, c.ldu, &anormest);
+        else e = dev_getu0<T>(c, true, 0, 1, (T *)c.yr, &s, (T *)c.V, c.ldv, &anormest);
         *ierr = e;
         anorm = std::max(anorm, FUDGE * anormest);
         j0 = 1;
@@ -424,13 +482,13 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
         h.force_reorth = 1;
         h.alpha = ba[k0 - 1];
         h.beta = *rnorm;
-        if (k0 < k && h.beta * h.delta < anorm * EPS) { h.full_reorth = 1; *ierr = k0; }
+        if (k0 < k && h.beta * h.delta < anorm * eps) { h.full_reorth = 1; *ierr = k0; }
         const int idx3[3] = {1, k0, k0 + 1};
         PGB_CUDA(cudaMemcpyAsync(c.index, idx3, sizeof(idx3), cudaMemcpyHostToDevice, c.s));
-        double *uk = c.U + (size_t)k0 * c.ldu;
-        dev_scale(c, uk, m, 1, *rnorm);
-        dev_reorth_full(c, c.U, c.ldu, m, k0, uk, rnorm, KAPPA);
-        dev_safescal(c, uk, m, *rnorm);
+        T *uk = c.Ucol<T>(k0);
+        dev_scale<T>(c, uk, m, 1, *rnorm);
+        dev_reorth_full<T>(c, (T *)c.U, c.ldu, m, k0, uk, rnorm, KAPPA);
+        dev_safescal<T>(c, uk, m, *rnorm);
         std::vector<double> mus(k0, h.epsn2);
         PGB_CUDA(cudaMemcpyAsync(c.mu, mus.data(), sizeof(double) * k0, cudaMemcpyHostToDevice, c.s));
         PGB_CUDA(cudaMemcpyAsync(c.nu, mus.data(), sizeof(double) * k0, cudaMemcpyHostToDevice, c.s));
@@ -478,7 +536,7 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
         LbArgs a = c.args();
         if (!host_ap) {
             for (; j <= k; j++) {
-                for (; side < 2; side++) lb_enqueue_half(a, c.op, side, j, h.ielr, c.ntry_spec, false, c.s);
+                for (; side < 2; side++) lb_enqueue_half<T>(a, c.op, side, j, h.ielr, c.ntry_spec, false, c.s);
                 side = 0;
             }
             c.get_ctl();
@@ -487,15 +545,16 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
             bool susp = false;
             for (; j <= k && !susp; j++) {
                 for (; side < 2 && !susp; side++) {
-                    double *x = side == 0 ? c.U + (size_t)(j - 1) * c.ldu : c.V + (size_t)(j - 1) * c.ldv;
-                    double *y = side == 0 ? c.V + (size_t)(j - 1) * c.ldv : c.U + (size_t)j * c.ldu;
+                    T *x = side == 0 ? c.Ucol<T>(j - 1) : c.Vcol<T>(j - 1);
+                    T *y = side == 0 ? c.Vcol<T>(j - 1) : c.Ucol<T>(j);
                     // the product must see the scaled input
-                    k_apply_pend_col<<<c.nb, 256, 0, c.s>>>(c.ctl, c.U, c.ldu, c.V, c.ldv, m, n, side == 0 ? 0 : 1);
+                    k_apply_pend_col<T><<<c.nb, 256, 0, c.s>>>(c.ctl, (T *)c.U, c.ldu, (T *)c.V, c.ldv, m, n,
+                                                               side == 0 ? 0 : 1);
                     PGB_LAUNCHED();
                     k_clear_pend<<<1, 1, 0, c.s>>>(c.ctl, side == 0 ? 0 : 1);
                     PGB_LAUNCHED();
-                    dev_aprod(c, side == 0, x, y);
-                    lb_enqueue_half(a, nullptr, side, j, h.ielr, c.ntry_spec, true, c.s);
+                    dev_aprod<T>(c, side == 0, x, y);
+                    lb_enqueue_half<T>(a, nullptr, side, j, h.ielr, c.ntry_spec, true, c.s);
                     c.get_ctl();
                     if (h.status != 0) susp = true;
                     if (susp) break;
@@ -514,7 +573,7 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
         if (h.susp_reason == 2) {
             h.status = 0;
             c.put_ctl();
-            lb_enqueue_cgs_more(c.args(), ss, sj, NTRY - c.ntry_spec, c.s);
+            lb_enqueue_cgs_more<T>(c.args(), ss, sj, NTRY - c.ntry_spec, c.s);
             c.get_ctl();
             if (h.status != 0 && h.susp_reason == 2) {
                 set_error("reorthogonalisation did not finish within NTRY passes");
@@ -539,14 +598,14 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
                 // dlanbpro.F:372-405: new random v_j orthogonal to V(:,1:j-1)
                 // (u_j may still carry its deferred scale: apply it first)
                 c.put_ctl();
-                k_apply_pend_col<<<c.nb, 256, 0, c.s>>>(c.ctl, c.U, c.ldu, c.V, c.ldv, m, n, 0);
+                k_apply_pend_col<T><<<c.nb, 256, 0, c.s>>>(c.ctl, (T *)c.U, c.ldu, (T *)c.V, c.ldv, m, n, 0);
                 PGB_LAUNCHED();
                 k_clear_pend<<<1, 1, 0, c.s>>>(c.ctl, 0);
                 PGB_LAUNCHED();
                 c.get_ctl();
                 double alpha = 0.0;
-                double *vj = c.V + (size_t)(jj - 1) * c.ldv;
-                int e = dev_getu0(c, true, jj - 1, 3, vj, &alpha, c.V, c.ldv, &anormest);
+                T *vj = c.Vcol<T>(jj - 1);
+                int e = dev_getu0<T>(c, true, jj - 1, 3, vj, &alpha, (T *)c.V, c.ldv, &anormest);
                 h.ierr = e;
                 if (alpha == 0.0) {
                     k = jj - 1;
@@ -555,7 +614,7 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
                     finished = true;
                     break;
                 }
-                dev_safescal(c, vj, n, alpha);
+                dev_safescal<T>(c, vj, n, alpha);
                 h.alpha = 0.0;
                 h.force_reorth = 1;
                 if (h.delta > 0) h.full_reorth = 0;
@@ -568,14 +627,14 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
             } else {
                 // dlanbpro.F:503-535: new random u_{j+1} orthogonal to U(:,1:j)
                 c.put_ctl();
-                k_apply_pend_col<<<c.nb, 256, 0, c.s>>>(c.ctl, c.U, c.ldu, c.V, c.ldv, m, n, 1);
+                k_apply_pend_col<T><<<c.nb, 256, 0, c.s>>>(c.ctl, (T *)c.U, c.ldu, (T *)c.V, c.ldv, m, n, 1);
                 PGB_LAUNCHED();
                 k_clear_pend<<<1, 1, 0, c.s>>>(c.ctl, 1);
                 PGB_LAUNCHED();
                 c.get_ctl();
                 double beta = 0.0;
-                double *uj1 = c.U + (size_t)jj * c.ldu;
-                int e = dev_getu0(c, false, jj, 3, uj1, &beta, c.U, c.ldu, &anormest);
+                T *uj1 = c.Ucol<T>(jj);
+                int e = dev_getu0<T>(c, false, jj, 3, uj1, &beta, (T *)c.U, c.ldu, &anormest);
                 h.ierr = e;
                 if (beta == 0.0) {
                     k = jj;
@@ -584,7 +643,7 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
                     finished = true;
                     break;
                 }
-                dev_safescal(c, uj1, m, beta);
+                dev_safescal<T>(c, uj1, m, beta);
                 h.beta = 0.0;
                 h.force_reorth = 1;
                 if (h.delta > 0) h.full_reorth = 0;
@@ -600,7 +659,7 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
         }
     }
     // apply the deferred scaling of the newest columns
-    lb_enqueue_flush(c.args(), c.s);
+    lb_enqueue_flush<T>(c.args(), c.s);
     c.get_ctl();
     *kp = k;
     *rnorm = h.rnorm;
@@ -611,14 +670,21 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
 // ------------------------------------------------------------- drivers
 static inline bool yes(const char *c) { return c && (c[0] == 'y' || c[0] == 'Y'); }
 
-static void copy_in_u1(Ctx &c, const double *U)
-{
-    PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(double) * c.m, cudaMemcpyHostToDevice, c.s));
-}
+// precision of the Lanczos vectors for this host thread: 0 = FP64 (the
+// reference's method), 1 = mixed (FP32 vectors and FP64 scalars, then a
+// short FP64 refinement)
+static thread_local int g_precision = 0;
+constexpr double EPS32 = 5.9604644775390625e-08;
+constexpr double MIXED_TOL = 1e-6;  // convergence level of the FP32 phase
 
+template <typename T>
 static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, bool du, bool dv)
 {
     if (ncols <= 0) return;
+    if (sizeof(T) != sizeof(double)) {
+        set_error("copy_out: only FP64 bases are returned");
+        throw ArgFailure();
+    }
     if (du)
         PGB_CUDA(cudaMemcpy2DAsync(U, sizeof(double) * ldu, c.U, sizeof(double) * c.ldu, sizeof(double) * c.m, ncols,
                                    cudaMemcpyDeviceToHost, c.s));
@@ -627,14 +693,16 @@ static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, 
                                    cudaMemcpyDeviceToHost, c.s));
 }
 
-// U(:,0:nc) <- U(:,0:kk) op(B)   (dgemm_ovwr_left)
-static void ovwr_left(Ctx &c, double *A, int lda, int rows, int nc, int kk, const double *B, int ldb, bool tb)
+// A(:,0:nc) <- A(:,0:kk) op(B)   (dgemm_ovwr_left)
+template <typename T>
+static void ovwr_left(Ctx &c, T *A, int lda, int rows, int nc, int kk, const double *B, int ldb, bool tb)
 {
-    gemm(rows, nc, kk, A, lda, false, B, ldb, tb, c.gout, lda, c.s);
-    copy_cols(c.gout, lda, A, lda, rows, nc, c.s);
+    gemm<T>(rows, nc, kk, A, lda, false, B, ldb, tb, (T *)c.gout, lda, c.s);
+    copy_cols<T>((T *)c.gout, lda, A, lda, rows, nc, c.s);
 }
 
 // dritzvec (double/dritzvec.F:1-199)
+template <typename T>
 static void dev_ritzvec(Ctx &c, bool small_side, bool du, bool dv, int k, int dim)
 {
     RitzArgs r;
@@ -643,10 +711,10 @@ static void dev_ritzvec(Ctx &c, bool small_side, bool du, bool dv, int k, int di
     launch_ritz_prep(r, c.s);
     const int dp1 = dim + 1;
     // X = P' Mt(1:dim, 1:dim+1)   (dim x dim+1, ld dim+1)
-    gemm(dim, dp1, dim, c.Pr, dim, true, c.Mt, dp1, false, c.X, dp1, c.s);
+    gemm<double>(dim, dp1, dim, c.Pr, dim, true, c.Mt, dp1, false, c.X, dp1, c.s);
     const int mstart = small_side ? dim - k + 1 : 1;
-    if (du) ovwr_left(c, c.U, c.ldu, c.m, k, dp1, c.X + (mstart - 1), dp1, true);
-    if (dv) ovwr_left(c, c.V, c.ldv, c.n, k, dim, c.Qt + (mstart - 1), dim, true);
+    if (du) ovwr_left<T>(c, (T *)c.U, c.ldu, c.m, k, dp1, c.X + (mstart - 1), dp1, true);
+    if (dv) ovwr_left<T>(c, (T *)c.V, c.ldv, c.n, k, dim, c.Qt + (mstart - 1), dim, true);
 }
 
 struct Timer {
@@ -671,11 +739,16 @@ struct Timer {
     }
 };
 
-static void finish_stats(Ctx &c, int64_t launches0)
+static void add_ctx_counters(Ctx &c)
 {
+    c.get_ctl();
     g_last.nopx += c.hctl->nopx;
     g_last.nreorth += c.hctl->nreorth;
     g_last.ndot += c.hctl->ndot;
+}
+
+static void finish_stats(int64_t launches0)
+{
     g_last.launches = g_launches - launches0;
     g_stat.nopx += g_last.nopx;
     g_stat.nreorth += g_last.nreorth;
@@ -710,6 +783,113 @@ static void setup_operator(Ctx &c, propack_aprod_t aprod, double *dparm, int *ip
     }
 }
 
+struct IrlIn {
+    bool small_side = false, du = true, dv = true;
+    int m = 0, n = 0, dim = 0, p = 0, neig = 0, maxiter = 0;
+    double tol = 0.0;
+    // mixed form only: form the top-neig Ritz vectors even when not all
+    // converged, and stop after this many restarts without a new converged
+    // value (0: never; the reference's behaviour)
+    bool ritz_always = false;
+    int stall_limit = 0;
+};
+struct IrlOut {
+    int nconv = 0, info = 0, dim = 0, ritz = 0;
+    std::vector<double> sigma, bnd;
+};
+
+// dlansvd_irl.F:188-418 on a context whose U(:,1) holds the start vector;
+// the Ritz vectors are left in the context.
+template <typename T>
+static void irl_loop(Ctx &c, const IrlIn &in, double *doption, const int *ioption, IrlOut &out)
+{
+    const int m = in.m, n = in.n, neig0 = in.neig;
+    int dim = in.dim;
+    const int k = dim - in.p;
+    double rnorm = dev_nrm2<T>(c, c.Ucol<T>(0), m);
+    int ierr = 0;
+    double anorm_drv = 0.0;
+    if (rnorm == 0.0) {
+        double est = 0.0;
+        ierr = dev_getu0<T>(c, false, 0, 1, c.Ucol<T>(0), &rnorm, (T *)c.U, c.ldu, &est);
+        anorm_drv = est;
+    }
+    PGB_CUDA(cudaMemcpyAsync(c.anorm_drv, &anorm_drv, sizeof(double), cudaMemcpyHostToDevice, c.s));
+    out.info = 0;
+    int iter = 0, nconv = 0, kold = 0, best = 0, since = 0;
+    while (nconv < neig0 && iter < in.maxiter) {
+        {
+            Timer t(c, g_last.lanczos_ms);
+            dev_lanbpro<T>(c, kold, &dim, &rnorm, doption, ioption, &ierr);
+        }
+        kold = k;
+        {
+            Timer t(c, g_last.bsvd_ms);
+            AnaArgs a;
+            a.balpha = c.balpha; a.bbeta = c.bbeta; a.a1 = c.a1; a.b1 = c.b1; a.bnd = c.bnd; a.w = c.w;
+            a.ctl = c.ctl; a.sigma_out = c.sig_out; a.bnd_out = c.bnd_out; a.nconv_out = c.nconv;
+            a.anorm_drv = c.anorm_drv; a.dim = dim; a.m = m; a.n = n; a.neig = neig0; a.kk = k;
+            a.irl = 1; a.small_side = in.small_side; a.tol = in.tol;
+            launch_analyse(a, c.s);
+            g_last.nbsvd++;
+            PGB_CUDA(cudaMemcpyAsync(c.hscal, c.nconv, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+            c.sync();
+            int nc = 0;
+            memcpy(&nc, c.hscal, sizeof(int));
+            nconv = nc;
+        }
+        if (ierr < 0) {
+            if (dim < k) out.info = dim;
+            break;
+        }
+        if (in.stall_limit > 0) {
+            if (nconv > best) { best = nconv; since = 0; }
+            else if (++since >= in.stall_limit) break;
+        }
+        if (nconv < neig0) {
+            {
+                Timer t(c, g_last.bsvd_ms);
+                SweepArgs sw;
+                sw.balpha = c.balpha; sw.bbeta = c.bbeta; sw.a1 = c.a1; sw.bnd = c.bnd; sw.P = c.P; sw.Q = c.Q;
+                sw.shifts = c.shifts; sw.w = c.w; sw.ctl = c.ctl; sw.dim = dim; sw.k = k; sw.neig = neig0;
+                sw.small_side = in.small_side; sw.min_relgap = doption[3];
+                launch_sweeps(sw, c.s);
+            }
+            {
+                Timer t(c, g_last.gemm_ms);
+                ovwr_left<T>(c, (T *)c.U, c.ldu, m, k + 1, dim + 1, c.P, dim + 1, false);
+                ovwr_left<T>(c, (T *)c.V, c.ldv, n, k, dim, c.Q, dim, false);
+            }
+            // rnorm = beta_k after the sweeps (written into the control block)
+            c.get_ctl();
+            rnorm = c.hctl->rnorm;
+            g_last.nrestart++;
+        }
+        iter++;
+    }
+    out.sigma.assign(std::max(nconv, 1), 0.0);
+    out.bnd.assign(std::max(nconv, 1), 0.0);
+    PGB_CUDA(cudaMemcpyAsync(out.sigma.data(), c.sig_out, sizeof(double) * std::max(nconv, 1), cudaMemcpyDeviceToHost,
+                             c.s));
+    PGB_CUDA(cudaMemcpyAsync(out.bnd.data(), c.bnd_out, sizeof(double) * std::max(nconv, 1), cudaMemcpyDeviceToHost,
+                             c.s));
+    c.sync();
+    if ((nconv >= neig0 || out.info > 0) && (in.du || in.dv)) {
+        Timer t(c, g_last.gemm_ms);
+        dev_ritzvec<T>(c, in.small_side, in.du, in.dv, nconv, dim);
+    } else if (in.ritz_always && (in.du || in.dv)) {
+        // the restart above left B and the bases at dimension k; when the
+        // loop stopped before a restart they are at dim
+        Timer t(c, g_last.gemm_ms);
+        const int kk = std::min(neig0, dim);
+        dev_ritzvec<T>(c, in.small_side, in.du, in.dv, kk, dim);
+        nconv = std::max(nconv, 0);
+        out.ritz = kk;
+    }
+    out.nconv = nconv;
+    out.dim = dim;
+}
+
 static void run_irl(const char *which, const char *jobu, const char *jobv, int m, int n, int dim, int p, int *neig,
                     int maxiter, propack_aprod_t aprod, double *U, int ldu, double *sigma, double *bnd, double *V,
                     int ldv, double tolin, double *doption, const int *ioption, int *info, double *dparm, int *iparm)
@@ -721,102 +901,105 @@ static void run_irl(const char *which, const char *jobu, const char *jobv, int m
     }
     const int64_t l0 = g_launches;
     g_last = Stats();
-    const bool small_side = which && (which[0] == 's' || which[0] == 'S');
-    dim = std::min(dim, std::min(n + 1, m + 1));
-    const int k = dim - p;
-    if (k < 1 || *neig > k) {
+    IrlIn in;
+    in.small_side = which && (which[0] == 's' || which[0] == 'S');
+    in.du = yes(jobu);
+    in.dv = yes(jobv);
+    in.m = m;
+    in.n = n;
+    in.dim = std::min(dim, std::min(n + 1, m + 1));
+    in.p = p;
+    in.neig = *neig;
+    in.maxiter = maxiter;
+    in.tol = std::min(1.0, std::max(16.0 * EPS, tolin));
+    const int k = in.dim - p;
+    if (k < 1 || in.neig > k) {
         set_error("dlansvd_irl_: need 1 <= neig <= dim - p");
         throw ArgFailure();
     }
-    const double tol = std::min(1.0, std::max(16.0 * EPS, tolin));
-    Ctx c;
-    init_ctx(c, m, n, dim);
-    setup_operator(c, aprod, dparm, iparm);
-    const int neig0 = *neig;
-    PGB_CUDA(cudaEventRecord(c.ev0, c.s));
-    copy_in_u1(c, U);
-    PGB_CUDA(cudaEventRecord(c.evs0, c.s));
-    double rnorm = dev_nrm2(c, c.U, m);
-    int ierr = 0;
-    double anorm_drv = 0.0;
-    if (rnorm == 0.0) {
-        double est = 0.0;
-        ierr = dev_getu0(c, false, 0, 1, c.U, &rnorm, c.U, c.ldu, &est);
-        anorm_drv = est;
+    IrlOut out;
+    if (g_precision == 0 || in.small_side) {
+        Ctx c;
+        init_ctx<double>(c, m, n, in.dim);
+        setup_operator(c, aprod, dparm, iparm);
+        PGB_CUDA(cudaEventRecord(c.ev0, c.s));
+        PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(double) * m, cudaMemcpyHostToDevice, c.s));
+        PGB_CUDA(cudaEventRecord(c.evs0, c.s));
+        irl_loop<double>(c, in, doption, ioption, out);
+        PGB_CUDA(cudaEventRecord(c.evs1, c.s));
+        copy_out<double>(c, U, ldu, V, ldv, out.nconv, in.du, in.dv);
+        PGB_CUDA(cudaEventRecord(c.ev1, c.s));
+        c.sync();
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+        g_last.device_ms = ms;
+        cudaEventElapsedTime(&ms, c.evs0, c.evs1);
+        g_last.solve_ms = ms;
+        add_ctx_counters(c);
+    } else {
+        // mixed form: FP32 Lanczos to MIXED_TOL, then FP64 refinement
+        Ctx c32;
+        init_ctx<float>(c32, m, n, in.dim);
+        setup_operator(c32, aprod, dparm, iparm);
+        PGB_CUDA(cudaEventRecord(c32.ev0, c32.s));
+        PGB_CUDA(cudaMemcpyAsync(c32.dx, U, sizeof(double) * m, cudaMemcpyHostToDevice, c32.s));
+        PGB_CUDA(cudaEventRecord(c32.evs0, c32.s));
+        dev_convert<double, float>(c32, c32.dx, c32.Ucol<float>(0), m);
+        double dop32[4] = {doption[0], doption[1], doption[2], doption[3]};
+        if (dop32[0] >= 0) dop32[0] = std::max(dop32[0], std::sqrt(EPS32));
+        if (dop32[1] >= 0) dop32[1] = std::max(dop32[1], std::pow(EPS32, 0.75));
+        IrlIn in32 = in;
+        in32.tol = std::max(in.tol, MIXED_TOL);
+        in32.du = true;
+        in32.dv = false;
+        in32.ritz_always = true;
+        in32.stall_limit = 8;
+        IrlOut out32;
+        irl_loop<float>(c32, in32, dop32, ioption, out32);
+        add_ctx_counters(c32);
+        const int64_t nopx32 = g_last.nopx;
+        PGB_CUDA(cudaEventRecord(c32.evs1, c32.s));
+        c32.sync();
+        float ms32 = 0;
+        cudaEventElapsedTime(&ms32, c32.evs0, c32.evs1);
+        // FP64 refinement: the FP64 IRL with the caller's dim and shifts,
+        // started from the sum of the FP32 Ritz vectors (a vector whose
+        // Krylov space holds the wanted subspace to FP32 accuracy), with the
+        // FP32 run's ||A|| estimate
+        IrlIn in64 = in;
+        Ctx c64;
+        init_ctx<double>(c64, m, n, in64.dim);
+        setup_operator(c64, aprod, dparm, iparm);
+        const int nwarm = std::min(std::max(out32.nconv, out32.ritz), in.neig);
+        if (nwarm > 0) {
+            k_sum_cols<float><<<c64.nb, 256, 0, c64.s>>>(c32.Ucol<float>(0), c32.ldu, m, nwarm, c64.Ucol<double>(0));
+            PGB_LAUNCHED();
+        } else {
+            PGB_CUDA(cudaMemcpyAsync(c64.U, U, sizeof(double) * m, cudaMemcpyHostToDevice, c64.s));
+        }
+        double dop64[4] = {doption[0], doption[1], dop32[2], doption[3]};
+        PGB_CUDA(cudaEventRecord(c64.evs0, c64.s));
+        irl_loop<double>(c64, in64, dop64, ioption, out);
+        PGB_CUDA(cudaEventRecord(c64.evs1, c64.s));
+        copy_out<double>(c64, U, ldu, V, ldv, out.nconv, in.du, in.dv);
+        PGB_CUDA(cudaEventRecord(c64.ev1, c64.s));
+        c64.sync();
+        float ms64 = 0, msall = 0;
+        cudaEventElapsedTime(&ms64, c64.evs0, c64.evs1);
+        cudaEventElapsedTime(&msall, c32.ev0, c64.ev1);
+        g_last.solve_ms = ms32 + ms64;
+        g_last.device_ms = msall;
+        g_last.low_ms = ms32;
+        add_ctx_counters(c64);
+        g_last.nopx_low = nopx32;
+        doption[2] = dop64[2];
     }
-    PGB_CUDA(cudaMemcpyAsync(c.anorm_drv, &anorm_drv, sizeof(double), cudaMemcpyHostToDevice, c.s));
-    *info = 0;
-    int iter = 0, nconv = 0, kold = 0;
-    std::vector<double> hs(dim + 2), hb(dim + 2);
-    while (nconv < neig0 && iter < maxiter) {
-        {
-            Timer t(c, g_last.lanczos_ms);
-            dev_lanbpro(c, kold, &dim, &rnorm, doption, ioption, &ierr);
-        }
-        kold = k;
-        {
-            Timer t(c, g_last.bsvd_ms);
-            AnaArgs a;
-            a.balpha = c.balpha; a.bbeta = c.bbeta; a.a1 = c.a1; a.b1 = c.b1; a.bnd = c.bnd; a.w = c.w;
-            a.ctl = c.ctl; a.sigma_out = c.sig_out; a.bnd_out = c.bnd_out; a.nconv_out = c.nconv;
-            a.anorm_drv = c.anorm_drv; a.dim = dim; a.m = m; a.n = n; a.neig = neig0; a.kk = k;
-            a.irl = 1; a.small_side = small_side; a.tol = tol;
-            launch_analyse(a, c.s);
-            g_last.nbsvd++;
-            PGB_CUDA(cudaMemcpyAsync(c.hscal, c.nconv, sizeof(int), cudaMemcpyDeviceToHost, c.s));
-            c.sync();
-            int nc = 0;
-            memcpy(&nc, c.hscal, sizeof(int));
-            nconv = nc;
-        }
-        if (ierr < 0) {
-            if (dim < k) *info = dim;
-            break;
-        }
-        if (nconv < neig0) {
-            {
-                Timer t(c, g_last.bsvd_ms);
-                SweepArgs s;
-                s.balpha = c.balpha; s.bbeta = c.bbeta; s.a1 = c.a1; s.bnd = c.bnd; s.P = c.P; s.Q = c.Q;
-                s.shifts = c.shifts; s.w = c.w; s.ctl = c.ctl; s.dim = dim; s.k = k; s.neig = neig0;
-                s.small_side = small_side; s.min_relgap = doption[3];
-                launch_sweeps(s, c.s);
-            }
-            {
-                Timer t(c, g_last.gemm_ms);
-                ovwr_left(c, c.U, c.ldu, m, k + 1, dim + 1, c.P, dim + 1, false);
-                ovwr_left(c, c.V, c.ldv, n, k, dim, c.Q, dim, false);
-            }
-            // rnorm = beta_k after the sweeps (written into the control block)
-            c.get_ctl();
-            rnorm = c.hctl->rnorm;
-            g_last.nrestart++;
-        }
-        iter++;
-    }
-    PGB_CUDA(cudaMemcpyAsync(hs.data(), c.sig_out, sizeof(double) * std::max(nconv, 1), cudaMemcpyDeviceToHost, c.s));
-    PGB_CUDA(cudaMemcpyAsync(hb.data(), c.bnd_out, sizeof(double) * std::max(nconv, 1), cudaMemcpyDeviceToHost, c.s));
-    c.sync();
-    for (int i = 0; i < nconv && i < neig0; i++) { sigma[i] = hs[i]; bnd[i] = hb[i]; }
-    const bool du = yes(jobu), dv = yes(jobv);
-    if ((nconv >= neig0 || *info > 0) && (du || dv)) {
-        Timer t(c, g_last.gemm_ms);
-        dev_ritzvec(c, small_side, du, dv, nconv, dim);
-    }
-    PGB_CUDA(cudaEventRecord(c.evs1, c.s));
-    copy_out(c, U, ldu, V, ldv, nconv, du, dv);
-    PGB_CUDA(cudaEventRecord(c.ev1, c.s));
-    c.sync();
-    float ms = 0;
-    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
-    g_last.device_ms = ms;
-    cudaEventElapsedTime(&ms, c.evs0, c.evs1);
-    g_last.solve_ms = ms;
+    for (int i = 0; i < out.nconv && i < in.neig; i++) { sigma[i] = out.sigma[i]; bnd[i] = out.bnd[i]; }
+    *info = out.info;
+    *neig = out.nconv;
+    g_last.nlandim = out.dim;
     prof_collect();
-    *neig = nconv;
-    g_last.nlandim = dim;
-    c.get_ctl();
-    finish_stats(c, l0);
+    finish_stats(l0);
 }
 
 static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp, int kmax, propack_aprod_t aprod,
@@ -834,17 +1017,17 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
     const int lanmax = std::min(std::min(n + 1, m + 1), kmax);
     const double tol = std::min(1.0, std::max(16.0 * EPS, tolin));
     Ctx c;
-    init_ctx(c, m, n, lanmax);
+    init_ctx<double>(c, m, n, lanmax);
     setup_operator(c, aprod, dparm, iparm);
     PGB_CUDA(cudaEventRecord(c.ev0, c.s));
-    copy_in_u1(c, U);
+    PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(double) * m, cudaMemcpyHostToDevice, c.s));
     PGB_CUDA(cudaEventRecord(c.evs0, c.s));
-    double rnorm = dev_nrm2(c, c.U, m);
+    double rnorm = dev_nrm2<double>(c, c.Ucol<double>(0), m);
     int ierr = 0;
     double anorm_drv = 0.0;
     if (rnorm == 0.0) {
         double est = 0.0;
-        ierr = dev_getu0(c, false, 0, 1, c.U, &rnorm, c.U, c.ldu, &est);
+        ierr = dev_getu0<double>(c, false, 0, 1, c.Ucol<double>(0), &rnorm, (double *)c.U, c.ldu, &est);
         anorm_drv = est;
     }
     PGB_CUDA(cudaMemcpyAsync(c.anorm_drv, &anorm_drv, sizeof(double), cudaMemcpyHostToDevice, c.s));
@@ -856,7 +1039,7 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
     while (neig < k) {
         {
             Timer t(c, g_last.lanczos_ms);
-            dev_lanbpro(c, jold, &j, &rnorm, doption, ioption, &ierr);
+            dev_lanbpro<double>(c, jold, &j, &rnorm, doption, ioption, &ierr);
         }
         jold = j;
         {
@@ -899,10 +1082,10 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
     const bool du = yes(jobu), dv = yes(jobv);
     if ((neig >= k || *info > 0) && (du || dv)) {
         Timer t(c, g_last.gemm_ms);
-        dev_ritzvec(c, false, du, dv, neig, jold);
+        dev_ritzvec<double>(c, false, du, dv, neig, jold);
     }
     PGB_CUDA(cudaEventRecord(c.evs1, c.s));
-    copy_out(c, U, ldu, V, ldv, neig, du, dv);
+    copy_out<double>(c, U, ldu, V, ldv, neig, du, dv);
     PGB_CUDA(cudaEventRecord(c.ev1, c.s));
     c.sync();
     float ms = 0;
@@ -910,11 +1093,11 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
     g_last.device_ms = ms;
     cudaEventElapsedTime(&ms, c.evs0, c.evs1);
     g_last.solve_ms = ms;
-    prof_collect();
     *kp = neig;
     g_last.nlandim = j;
-    c.get_ctl();
-    finish_stats(c, l0);
+    add_ctx_counters(c);
+    prof_collect();
+    finish_stats(l0);
 }
 
 }  // namespace pgb
@@ -965,6 +1148,14 @@ extern "C" void dlansvd_(const char *jobu, const char *jobv, const int *m, const
 
 extern "C" void clearstat_(void) { g_stat = Stats(); }
 
+extern "C" int propack_set_precision(int mode)
+{
+    if (mode != 0 && mode != 1) return PROPACK_ERR_ARG;
+    g_precision = mode;
+    return 0;
+}
+extern "C" int propack_get_precision(void) { return g_precision; }
+
 extern "C" void printstat_(void)
 {
     const Stats &s = g_stat;
@@ -996,4 +1187,6 @@ extern "C" void propack_get_stats(propack_stats_t *out)
     out->gemm_ms = s.gemm_ms;
     out->kernel_launches = s.launches;
     out->solve_ms = s.solve_ms;
+    out->nopx_low = s.nopx_low;
+    out->low_ms = s.low_ms;
 }

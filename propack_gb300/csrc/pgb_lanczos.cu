@@ -206,7 +206,7 @@ __device__ void v_post(Tail &t, const LbArgs &a, int j)
         c.susp_side = 0;
         c.susp_j = j;
         return;
-    } else if (j > 1 && !c.full_reorth && j < c.k && (c.delta * c.alpha < c.anorm * EPS)) {
+    } else if (j > 1 && !c.full_reorth && j < c.k && (c.delta * c.alpha < c.anorm * c.eps_vec)) {
         c.ierr = j;
     }
     a.balpha[j - 1] = c.alpha;
@@ -217,7 +217,7 @@ __device__ void v_post(Tail &t, const LbArgs &a, int j)
 __device__ void v_post_reorth(Tail &t, const LbArgs &a, int j)
 {
     if (threadIdx.x != 0) return;
-    set_mu(j - 1, a.nu, a.index, EPS);
+    set_mu(j - 1, a.nu, a.index, t.c.eps_vec);
     t.c.numax = t.c.eta;
     t.c.force_reorth = !t.c.force_reorth;
 }
@@ -287,7 +287,7 @@ __device__ void u_post(Tail &t, const LbArgs &a, int j)
         c.susp_side = 1;
         c.susp_j = j;
         return;
-    } else if (!c.full_reorth && j < c.k && (c.delta * c.beta < c.anorm * EPS)) {
+    } else if (!c.full_reorth && j < c.k && (c.delta * c.beta < c.anorm * c.eps_vec)) {
         c.ierr = j;
     }
     a.bbeta[j - 1] = c.beta;
@@ -300,7 +300,7 @@ __device__ void u_post(Tail &t, const LbArgs &a, int j)
 __device__ void u_post_reorth(Tail &t, const LbArgs &a, int j)
 {
     if (threadIdx.x != 0) return;
-    set_mu(j, a.mu, a.index, EPS);
+    set_mu(j, a.mu, a.index, t.c.eps_vec);
     t.c.mumax = t.c.eta;
     t.c.force_reorth = !t.c.force_reorth;
 }
@@ -404,8 +404,8 @@ __device__ void after_elr(Tail &t, const LbArgs &a, int j, double snrm, double d
         double &oth = SIDE == 0 ? c.beta : c.alpha;
         t.go = 0;
         if (snrm >= KAPPA * cur || c.elr_iter >= c.ielr) {
-            if (SIDE == 0) a.nu[j - 2] = EPS;
-            else a.mu[j - 1] = EPS;
+            if (SIDE == 0) a.nu[j - 2] = c.eps_vec;
+            else a.mu[j - 1] = c.eps_vec;
             cur = snrm;
             c.elr_active = 0;
             t.go = 1;
@@ -486,50 +486,61 @@ __device__ void after_cgs(Tail &t, const LbArgs &a, int j, double nrm, int last)
 }
 
 // ----------------------------------------------------------------- kernels
-template <int SIDE>
+// T is the type of the Lanczos vectors: double (the reference's FP64
+// method) or float (the mixed form: FP32 vectors, FP32 SpMV on the FP32
+// copy of the values, compensated FP32 reductions; all scalars FP64).
+template <typename T>
+__device__ __forceinline__ const T *csr_vals(const Csr &A);
+template <>
+__device__ __forceinline__ const double *csr_vals<double>(const Csr &A) { return A.val; }
+template <>
+__device__ __forceinline__ const float *csr_vals<float>(const Csr &A) { return A.valf; }
+
+template <int SIDE, typename T>
 __global__ void __launch_bounds__(BS) k_lb_spmv(LbArgs a, int j, int host_product)
 {
-    __shared__ SpmvStage<double, double> st[SPMV_WARPS];
+    __shared__ SpmvStage<T, T> st[SPMV_WARPS];
     __shared__ double sred[32];
     __shared__ Tail t;
     if (a.ctl->status != 0) return;
     const Pend pin = SIDE == 0 ? a.ctl->pend_u : a.ctl->pend_v;
     const Pend pprev = SIDE == 0 ? a.ctl->pend_v : a.ctl->pend_u;
     const bool has_prev = SIDE == 1 || j > 1;
-    const double coef = SIDE == 0 ? a.ctl->beta : a.ctl->alpha;
-    const double *x = SIDE == 0 ? a.U + (size_t)(j - 1) * a.ldu : a.V + (size_t)(j - 1) * a.ldv;
-    double *out = SIDE == 0 ? a.V + (size_t)(j - 1) * a.ldv : a.U + (size_t)j * a.ldu;
-    double *prev = SIDE == 0 ? (j > 1 ? a.V + (size_t)(j - 2) * a.ldv : nullptr) : a.U + (size_t)(j - 1) * a.ldu;
+    const T coef = (T)(SIDE == 0 ? a.ctl->beta : a.ctl->alpha);
+    const T *x = SIDE == 0 ? ucol<T>(a, j - 1) : vcol<T>(a, j - 1);
+    T *out = SIDE == 0 ? vcol<T>(a, j - 1) : ucol<T>(a, j);
+    T *prev = SIDE == 0 ? (j > 1 ? vcol<T>(a, j - 2) : nullptr) : ucol<T>(a, j - 1);
     const Csr &A = SIDE == 0 ? a.adj : a.fwd;
     const double *z = a.z;
     const int n0 = A.ncol0;
-    double sq = 0.0, dt = 0.0;
-    auto epi = [&](int r, double acc, double pv) {
-        double y = apply_pend(acc, pin);
+    Acc<T> sq, dt;
+    auto epi = [&](int r, double acc, double pvd) {
+        T y = apply_pend((T)acc, pin);
         if (has_prev) {
+            T pv = (T)pvd;
             if (pprev.mode) {
                 pv = apply_pend(pv, pprev);
                 prev[r] = pv;
             }
             y = fma(-coef, pv, y);
-            dt = fma(pv, y, dt);
+            dt.add_prod(pv, y);
         }
         out[r] = y;
-        sq = fma(y, y, sq);
+        sq.add_prod(y, y);
     };
-    auto pre = [&](int r) -> double { return has_prev ? prev[r] : 0.0; };
+    auto pre = [&](int r) -> double { return has_prev ? (double)prev[r] : 0.0; };
     if (!host_product) {
-        auto xl = [&](int c) -> double { return c < n0 ? x[c] : z[c - n0]; };
-        csr_rows<double, double>(A.ptr, A.idx, A.val, A.blk, A.nblk, xl, pre, epi, st);
+        auto xl = [&](int c) -> T { return c < n0 ? x[c] : (T)z[c - n0]; };
+        csr_rows<T, T>(A.ptr, A.idx, csr_vals<T>(A), A.blk, A.nblk, xl, pre, epi, st);
     } else {
         // the caller's APROD already wrote the product into out
-        for (int r = blockIdx.x * BS + threadIdx.x; r < A.rows; r += gridDim.x * BS) epi(r, out[r], pre(r));
+        for (int r = blockIdx.x * BS + threadIdx.x; r < A.rows; r += gridDim.x * BS) epi(r, (double)out[r], pre(r));
     }
-    sq = block_sum<BS>(sq, sred);
-    dt = block_sum<BS>(dt, sred);
+    const double sq2 = block_sum<BS>(sq.value(), sred);
+    const double dt2 = block_sum<BS>(dt.value(), sred);
     if (threadIdx.x == 0) {
-        a.part_sq[blockIdx.x] = sq;
-        a.part_dot[blockIdx.x] = dt;
+        a.part_sq[blockIdx.x] = sq2;
+        a.part_dot[blockIdx.x] = dt2;
     }
     if (last_cta(&a.ctl->ticket)) {
         tail_load(a, t);
@@ -540,29 +551,29 @@ __global__ void __launch_bounds__(BS) k_lb_spmv(LbArgs a, int j, int host_produc
     }
 }
 
-template <int SIDE>
+template <int SIDE, typename T>
 __global__ void __launch_bounds__(BS) k_lb_elr(LbArgs a, int j)
 {
     __shared__ double sred[32];
     __shared__ Tail t;
     if (a.ctl->status != 0 || !a.ctl->elr_active) return;
-    const double s = a.ctl->elr_s;
+    const T s = (T)a.ctl->elr_s;
     const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
-    double *x = SIDE == 0 ? a.V + (size_t)(j - 1) * a.ldv : a.U + (size_t)j * a.ldu;
-    const double *p = SIDE == 0 ? a.V + (size_t)(j - 2) * a.ldv : a.U + (size_t)(j - 1) * a.ldu;
-    double sq = 0.0, dt = 0.0;
+    T *x = SIDE == 0 ? vcol<T>(a, j - 1) : ucol<T>(a, j);
+    const T *p = SIDE == 0 ? vcol<T>(a, j - 2) : ucol<T>(a, j - 1);
+    Acc<T> sq, dt;
     for (int r = blockIdx.x * BS + threadIdx.x; r < len; r += gridDim.x * BS) {
-        const double pv = p[r];
-        const double y = fma(-s, pv, x[r]);
+        const T pv = p[r];
+        const T y = fma(-s, pv, x[r]);
         x[r] = y;
-        sq = fma(y, y, sq);
-        dt = fma(pv, y, dt);
+        sq.add_prod(y, y);
+        dt.add_prod(pv, y);
     }
-    sq = block_sum<BS>(sq, sred);
-    dt = block_sum<BS>(dt, sred);
+    const double sq2 = block_sum<BS>(sq.value(), sred);
+    const double dt2 = block_sum<BS>(dt.value(), sred);
     if (threadIdx.x == 0) {
-        a.part_sq[blockIdx.x] = sq;
-        a.part_dot[blockIdx.x] = dt;
+        a.part_sq[blockIdx.x] = sq2;
+        a.part_dot[blockIdx.x] = dt2;
     }
     if (last_cta(&a.ctl->ticket)) {
         tail_load(a, t);
@@ -575,7 +586,7 @@ __global__ void __launch_bounds__(BS) k_lb_elr(LbArgs a, int j)
 
 // projections W(:,sel)' x: each CTA owns a contiguous row chunk, each warp
 // a subset of the columns.
-template <int SIDE>
+template <int SIDE, typename T>
 __global__ void __launch_bounds__(BS) k_lb_cgs_dots(LbArgs a, int j)
 {
     __shared__ Tail t;
@@ -583,23 +594,23 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_dots(LbArgs a, int j)
     const int L = a.ctl->nsel;
     const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
     const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
-    const double *W = SIDE == 0 ? a.V : a.U;
-    const double *x = SIDE == 0 ? a.V + (size_t)(j - 1) * a.ldv : a.U + (size_t)j * a.ldu;
+    const T *W = (const T *)(SIDE == 0 ? a.V : a.U);
+    const T *x = SIDE == 0 ? vcol<T>(a, j - 1) : ucol<T>(a, j);
     const int chunk = (len + gridDim.x - 1) / gridDim.x;
     const int r0 = blockIdx.x * chunk, r1 = min(len, r0 + chunk);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int c = w; c < L; c += BS / 32) {
-        const double *col = W + (size_t)a.sel[c] * ld;
-        double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
+        const T *col = W + (size_t)a.sel[c] * ld;
+        Acc<T> acc0, acc1, acc2, acc3;
         int r = r0 + lane;
         for (; r + 96 < r1; r += 128) {
-            acc0 = fma(col[r], x[r], acc0);
-            acc1 = fma(col[r + 32], x[r + 32], acc1);
-            acc2 = fma(col[r + 64], x[r + 64], acc2);
-            acc3 = fma(col[r + 96], x[r + 96], acc3);
+            acc0.add_prod(col[r], x[r]);
+            acc1.add_prod(col[r + 32], x[r + 32]);
+            acc2.add_prod(col[r + 64], x[r + 64]);
+            acc3.add_prod(col[r + 96], x[r + 96]);
         }
-        for (; r < r1; r += 32) acc0 = fma(col[r], x[r], acc0);
-        double acc = (acc0 + acc1) + (acc2 + acc3);
+        for (; r < r1; r += 32) acc0.add_prod(col[r], x[r]);
+        double acc = (acc0.value() + acc1.value()) + (acc2.value() + acc3.value());
         acc = warp_sum(acc);
         if (lane == 0) a.part_cols[(size_t)c * a.nb + blockIdx.x] = acc;
     }
@@ -610,19 +621,19 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_dots(LbArgs a, int j)
     }
 }
 
-// x -= W(:,sel) h, then the projections of the new x for the next pass
-constexpr int CGS_TR = 64;
+// x -= W(:,sel) h, then the projections of the new x for the next pass.
 // CPW > 0: each warp owns columns w, w+8, ..., w+8*(CPW-1) and every lane
 // keeps one register accumulator per owned column across all of the CTA's
-// row tiles (one FP64 FMA per element, one warp reduction per column per
-// CTA).  CPW == 0: any number of columns, one warp reduction per column
-// per tile (used when the selection can exceed 8*24 columns).
-template <int SIDE, int CPW>
+// row tiles (one FMA per element, one warp reduction per column per CTA).
+// CPW == 0: any number of columns, one warp reduction per column per tile
+// (used when the selection can exceed 8*24 columns).
+constexpr int CGS_TR = 64;
+template <int SIDE, int CPW, typename T>
 __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
 {
     extern __shared__ double dyn[];  // h[L] | acc[L] | sel[L] (ints)
-    __shared__ double red4[4][CGS_TR];
-    __shared__ double xn[CGS_TR];
+    __shared__ T red4[4][CGS_TR];
+    __shared__ T xn[CGS_TR];
     __shared__ double sred[32];
     __shared__ Tail t;
     if (a.ctl->status != 0 || !a.ctl->reorth_active) return;
@@ -637,59 +648,57 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
     __syncthreads();
     const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
     const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
-    const double *W = SIDE == 0 ? a.V : a.U;
-    double *x = SIDE == 0 ? a.V + (size_t)(j - 1) * a.ldv : a.U + (size_t)j * a.ldu;
+    const T *W = (const T *)(SIDE == 0 ? a.V : a.U);
+    T *x = SIDE == 0 ? vcol<T>(a, j - 1) : ucol<T>(a, j);
     const int chunk = (len + gridDim.x - 1) / gridDim.x;
     const int r0 = blockIdx.x * chunk, r1 = min(len, r0 + chunk);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int rr = threadIdx.x % CGS_TR, g = threadIdx.x / CGS_TR;
-    double sq = 0.0;
-    double accr[CPW > 0 ? CPW : 1];
-#pragma unroll
-    for (int q = 0; q < (CPW > 0 ? CPW : 1); q++) accr[q] = 0.0;
+    Acc<T> sq;
+    Acc<T> accr[CPW > 0 ? CPW : 1];
     for (int tb = r0; tb < r1; tb += CGS_TR) {
         const int r = tb + rr;
-        double p0 = 0.0, p1 = 0.0;
+        T p0 = 0, p1 = 0;
         if (r < r1) {
             int c = g;
             for (; c + 4 < L; c += 8) {
-                p0 = fma(W[(size_t)ssel[c] * ld + r], hs[c], p0);
-                p1 = fma(W[(size_t)ssel[c + 4] * ld + r], hs[c + 4], p1);
+                p0 = fma(W[(size_t)ssel[c] * ld + r], (T)hs[c], p0);
+                p1 = fma(W[(size_t)ssel[c + 4] * ld + r], (T)hs[c + 4], p1);
             }
-            if (c < L) p0 = fma(W[(size_t)ssel[c] * ld + r], hs[c], p0);
+            if (c < L) p0 = fma(W[(size_t)ssel[c] * ld + r], (T)hs[c], p0);
         }
         red4[g][rr] = p0 + p1;
         __syncthreads();
         if (g == 0) {
-            double v = 0.0;
+            T v = 0;
             if (r < r1) {
                 v = x[r] - (((red4[0][rr] + red4[1][rr]) + red4[2][rr]) + red4[3][rr]);
                 x[r] = v;
-                sq = fma(v, v, sq);
+                sq.add_prod(v, v);
             }
             xn[rr] = v;
         }
         __syncthreads();
         const int ra = tb + lane, rb = tb + lane + 32;
-        const double xa = xn[lane], xb = xn[lane + 32];
+        const T xa = xn[lane], xb = xn[lane + 32];
         if (CPW > 0) {
 #pragma unroll
             for (int q = 0; q < (CPW > 0 ? CPW : 1); q++) {
                 const int c = w + 8 * q;
                 if (c < L) {
-                    const double *col = W + (size_t)ssel[c] * ld;
-                    if (ra < r1) accr[q] = fma(col[ra], xa, accr[q]);
-                    if (rb < r1) accr[q] = fma(col[rb], xb, accr[q]);
+                    const T *col = W + (size_t)ssel[c] * ld;
+                    if (ra < r1) accr[q].add_prod(col[ra], xa);
+                    if (rb < r1) accr[q].add_prod(col[rb], xb);
                 }
             }
         } else {
             for (int c = w; c < L; c += BS / 32) {
-                const double *col = W + (size_t)ssel[c] * ld;
-                double v = 0.0;
-                if (ra < r1) v = col[ra] * xa;
-                if (rb < r1) v = fma(col[rb], xb, v);
-                v = warp_sum(v);
-                if (lane == 0) acc[c] += v;
+                const T *col = W + (size_t)ssel[c] * ld;
+                Acc<T> v;
+                if (ra < r1) v.add_prod(col[ra], xa);
+                if (rb < r1) v.add_prod(col[rb], xb);
+                const double vv = warp_sum(v.value());
+                if (lane == 0) acc[c] += vv;
             }
         }
         __syncthreads();
@@ -698,14 +707,14 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
 #pragma unroll
         for (int q = 0; q < (CPW > 0 ? CPW : 1); q++) {
             const int c = w + 8 * q;
-            const double v = warp_sum(accr[q]);
+            const double v = warp_sum(accr[q].value());
             if (c < L && lane == 0) acc[c] = v;
         }
         __syncthreads();
     }
     for (int c = threadIdx.x; c < L; c += BS) a.part_cols[(size_t)c * a.nb + blockIdx.x] = acc[c];
-    sq = block_sum<BS>(sq, sred);
-    if (threadIdx.x == 0) a.part_sq[blockIdx.x] = sq;
+    const double sq2 = block_sum<BS>(sq.value(), sred);
+    if (threadIdx.x == 0) a.part_sq[blockIdx.x] = sq2;
     if (last_cta(&a.ctl->ticket)) {
         tail_load(a, t);
         const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
@@ -715,6 +724,7 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
 }
 
 // apply the deferred scaling of the newest u and v columns
+template <typename T>
 __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
 {
     if (a.ctl->status != 0) return;
@@ -722,9 +732,11 @@ __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
     const int cu = a.ctl->pend_u_col, cv = a.ctl->pend_v_col;
     const int m = a.fwd.rows, n = a.adj.rows;
     const int len = m > n ? m : n;
+    T *uc = cu >= 0 ? ucol<T>(a, cu) : nullptr;
+    T *vc = cv >= 0 ? vcol<T>(a, cv) : nullptr;
     for (int r = blockIdx.x * BS + threadIdx.x; r < len; r += gridDim.x * BS) {
-        if (pu.mode && cu >= 0 && r < m) a.U[(size_t)cu * a.ldu + r] = apply_pend(a.U[(size_t)cu * a.ldu + r], pu);
-        if (pv.mode && cv >= 0 && r < n) a.V[(size_t)cv * a.ldv + r] = apply_pend(a.V[(size_t)cv * a.ldv + r], pv);
+        if (pu.mode && uc && r < m) uc[r] = apply_pend(uc[r], pu);
+        if (pv.mode && vc && r < n) vc[r] = apply_pend(vc[r], pv);
     }
     if (last_cta(&a.ctl->ticket)) {
         if (threadIdx.x == 0) {
@@ -736,50 +748,51 @@ __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
 }
 
 // ------------------------------------------------------------ host side
-void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s);
-
+template <typename T>
 static size_t cgs_smem(const LbArgs &a) { return (sizeof(double) * 2 + sizeof(int)) * (size_t)(a.kmax + 1) + 16; }
 
-template <int SIDE>
+template <int SIDE, typename T>
 static void set_upd_limits(size_t need)
 {
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 0, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 4, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 8, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 16, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 24, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
 }
 void lb_set_smem_limits(int kmax)
 {
     const size_t need = (sizeof(double) * 2 + sizeof(int)) * (size_t)(kmax + 1) + 16;
     if (need > 48 * 1024) {
-        set_upd_limits<0>(need);
-        set_upd_limits<1>(need);
+        set_upd_limits<0, double>(need);
+        set_upd_limits<1, double>(need);
+        set_upd_limits<0, float>(need);
+        set_upd_limits<1, float>(need);
     }
 }
 
 // one CGS update pass; the template is chosen from an upper bound of the
 // number of selected columns (j-1 on the V side, j on the U side)
-template <int SIDE>
+template <int SIDE, typename T>
 static void launch_upd(const LbArgs &a, int j, int last, int maxcols, cudaStream_t s)
 {
-    const size_t sm = cgs_smem(a);
+    const size_t sm = cgs_smem<T>(a);
     const int cpw = (maxcols + 7) / 8;
-    if (cpw <= 4) k_lb_cgs_upd<SIDE, 4><<<a.nb, BS, sm, s>>>(a, j, last);
-    else if (cpw <= 8) k_lb_cgs_upd<SIDE, 8><<<a.nb, BS, sm, s>>>(a, j, last);
-    else if (cpw <= 16) k_lb_cgs_upd<SIDE, 16><<<a.nb, BS, sm, s>>>(a, j, last);
-    else if (cpw <= 24) k_lb_cgs_upd<SIDE, 24><<<a.nb, BS, sm, s>>>(a, j, last);
-    else k_lb_cgs_upd<SIDE, 0><<<a.nb, BS, sm, s>>>(a, j, last);
+    if (cpw <= 4) k_lb_cgs_upd<SIDE, 4, T><<<a.nb, BS, sm, s>>>(a, j, last);
+    else if (cpw <= 8) k_lb_cgs_upd<SIDE, 8, T><<<a.nb, BS, sm, s>>>(a, j, last);
+    else if (cpw <= 16) k_lb_cgs_upd<SIDE, 16, T><<<a.nb, BS, sm, s>>>(a, j, last);
+    else if (cpw <= 24) k_lb_cgs_upd<SIDE, 24, T><<<a.nb, BS, sm, s>>>(a, j, last);
+    else k_lb_cgs_upd<SIDE, 0, T><<<a.nb, BS, sm, s>>>(a, j, last);
 }
 
 // one wave of CTAs at the fused SpMV's occupancy (partials are summed over gridDim)
-template <int SIDE>
+template <int SIDE, typename T>
 static int spmv_grid(int nb)
 {
     static thread_local int g = 0;
     if (g == 0) {
         int per = 0;
-        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lb_spmv<SIDE>, BS, 0));
+        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lb_spmv<SIDE, T>, BS, 0));
         g = std::max(1, per) * device_info().sms;
     }
     return std::min(g, nb);
@@ -787,58 +800,70 @@ static int spmv_grid(int nb)
 
 // Enqueue the kernels of one half step.  host_product: the product was
 // written into the output column by a host APROD call.
+template <typename T>
 void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int ielr, int ntry_spec,
                      bool host_product, cudaStream_t s)
 {
     const int nb = a.nb;
     if (side == 0) {
         if (!host_product && op && op->r > 0)
-            PGB_PROF(PK_THIN, s, op_thin(*op, true, a.U + (size_t)(j - 1) * a.ldu, s));
-        PGB_PROF(PK_SPMV_ADJ, s, k_lb_spmv<0><<<spmv_grid<0>(nb), BS, 0, s>>>(a, j, host_product ? 1 : 0));
+            PGB_PROF(PK_THIN, s, op_thin<T>(*op, true, ucol<T>(a, j - 1), s));
+        PGB_PROF(sizeof(T) == 8 ? PK_SPMV_ADJ : PK_SPMV_ADJ32, s,
+                 k_lb_spmv<0, T><<<spmv_grid<0, T>(nb), BS, 0, s>>>(a, j, host_product ? 1 : 0));
         PGB_LAUNCHED();
         if (j > 1)
             for (int i = 0; i < ielr; i++) {
-                PGB_PROF(PK_ELR, s, k_lb_elr<0><<<nb, BS, 0, s>>>(a, j));
+                PGB_PROF(PK_ELR, s, k_lb_elr<0, T><<<nb, BS, 0, s>>>(a, j));
                 PGB_LAUNCHED();
             }
-        PGB_PROF(PK_CGS_DOTS, s, k_lb_cgs_dots<0><<<nb, BS, 0, s>>>(a, j));
+        PGB_PROF(sizeof(T) == 8 ? PK_CGS_DOTS : PK_CGS_DOTS32, s, k_lb_cgs_dots<0, T><<<nb, BS, 0, s>>>(a, j));
         PGB_LAUNCHED();
         for (int i = 0; i < ntry_spec; i++) {
-            PGB_PROF(PK_CGS_UPD, s, launch_upd<0>(a, j, i == ntry_spec - 1, j - 1, s));
+            PGB_PROF(sizeof(T) == 8 ? PK_CGS_UPD : PK_CGS_UPD32, s, (launch_upd<0, T>(a, j, i == ntry_spec - 1, j - 1, s)));
             PGB_LAUNCHED();
         }
     } else {
         if (!host_product && op && op->r > 0)
-            PGB_PROF(PK_THIN, s, op_thin(*op, false, a.V + (size_t)(j - 1) * a.ldv, s));
-        PGB_PROF(PK_SPMV_FWD, s, k_lb_spmv<1><<<spmv_grid<1>(nb), BS, 0, s>>>(a, j, host_product ? 1 : 0));
+            PGB_PROF(PK_THIN, s, op_thin<T>(*op, false, vcol<T>(a, j - 1), s));
+        PGB_PROF(sizeof(T) == 8 ? PK_SPMV_FWD : PK_SPMV_FWD32, s,
+                 k_lb_spmv<1, T><<<spmv_grid<1, T>(nb), BS, 0, s>>>(a, j, host_product ? 1 : 0));
         PGB_LAUNCHED();
         for (int i = 0; i < ielr; i++) {
-            PGB_PROF(PK_ELR, s, k_lb_elr<1><<<nb, BS, 0, s>>>(a, j));
+            PGB_PROF(PK_ELR, s, k_lb_elr<1, T><<<nb, BS, 0, s>>>(a, j));
             PGB_LAUNCHED();
         }
-        PGB_PROF(PK_CGS_DOTS, s, k_lb_cgs_dots<1><<<nb, BS, 0, s>>>(a, j));
+        PGB_PROF(sizeof(T) == 8 ? PK_CGS_DOTS : PK_CGS_DOTS32, s, k_lb_cgs_dots<1, T><<<nb, BS, 0, s>>>(a, j));
         PGB_LAUNCHED();
         for (int i = 0; i < ntry_spec; i++) {
-            PGB_PROF(PK_CGS_UPD, s, launch_upd<1>(a, j, i == ntry_spec - 1, j, s));
+            PGB_PROF(sizeof(T) == 8 ? PK_CGS_UPD : PK_CGS_UPD32, s, (launch_upd<1, T>(a, j, i == ntry_spec - 1, j, s)));
             PGB_LAUNCHED();
         }
     }
 }
 
 // more Gram-Schmidt passes after a suspension with reason 2
+template <typename T>
 void lb_enqueue_cgs_more(const LbArgs &a, int side, int j, int passes, cudaStream_t s)
 {
     for (int i = 0; i < passes; i++) {
-        if (side == 0) launch_upd<0>(a, j, i == passes - 1, j - 1, s);
-        else launch_upd<1>(a, j, i == passes - 1, j, s);
+        if (side == 0) launch_upd<0, T>(a, j, i == passes - 1, j - 1, s);
+        else launch_upd<1, T>(a, j, i == passes - 1, j, s);
         PGB_LAUNCHED();
     }
 }
 
+template <typename T>
 void lb_enqueue_flush(const LbArgs &a, cudaStream_t s)
 {
-    k_lb_flush<<<a.nb, BS, 0, s>>>(a);
+    k_lb_flush<T><<<a.nb, BS, 0, s>>>(a);
     PGB_LAUNCHED();
 }
+
+template void lb_enqueue_half<double>(const LbArgs &, const Operator *, int, int, int, int, bool, cudaStream_t);
+template void lb_enqueue_half<float>(const LbArgs &, const Operator *, int, int, int, int, bool, cudaStream_t);
+template void lb_enqueue_cgs_more<double>(const LbArgs &, int, int, int, cudaStream_t);
+template void lb_enqueue_cgs_more<float>(const LbArgs &, int, int, int, cudaStream_t);
+template void lb_enqueue_flush<double>(const LbArgs &, cudaStream_t);
+template void lb_enqueue_flush<float>(const LbArgs &, cudaStream_t);
 
 }  // namespace pgb

@@ -433,27 +433,25 @@ __global__ void k_to_float(const double *a, float *b, int64_t n)
 }
 
 // ------------------------------------------------------ application
-// z[c] = w[c] * sum(thin row c . x), split into segments of NNZ_PB.
-__global__ void __launch_bounds__(BS) k_thin(Csr T, const double *__restrict__ x, const double *w,
-                                             double *zpart, double *z, unsigned int *ticket, double xscale_dummy)
+// z[c] = w[c] * sum(thin row c . x), split into segments of NNZ_PB.  The
+// low-rank coefficients are always formed in FP64.
+template <typename T>
+__global__ void __launch_bounds__(BS) k_thin(Csr Th, const T *__restrict__ x, const double *w, double *zpart,
+                                             double *z, unsigned int *ticket)
 {
     __shared__ double sred[32];
-    (void)xscale_dummy;
-    const int nseg = T.segs;
-    double part_total = 0.0;
-    for (int t = blockIdx.x; t < T.rows * nseg; t += gridDim.x) {
+    const int nseg = Th.segs;
+    for (int t = blockIdx.x; t < Th.rows * nseg; t += gridDim.x) {
         const int c = t / nseg, sg = t % nseg;
-        const int a = T.ptr[c] + sg * NNZ_PB;
-        const int b = min(T.ptr[c + 1], a + NNZ_PB);
+        const int a = Th.ptr[c] + sg * NNZ_PB;
+        const int b = min(Th.ptr[c + 1], a + NNZ_PB);
         double acc = 0.0;
-        for (int e = a + threadIdx.x; e < b; e += BS) acc += T.val[e] * x[T.idx[e]];
+        for (int e = a + threadIdx.x; e < b; e += BS) acc += Th.val[e] * (double)x[Th.idx[e]];
         acc = block_sum<BS>(acc, sred);
         if (threadIdx.x == 0) zpart[t] = acc;
-        part_total += acc;
     }
-    (void)part_total;
     if (last_cta(ticket)) {
-        for (int c = threadIdx.x; c < T.rows; c += BS) {
+        for (int c = threadIdx.x; c < Th.rows; c += BS) {
             double s = 0.0;
             for (int sg = 0; sg < nseg; sg++) s += zpart[c * nseg + sg];
             z[c] = w[c] * s;
@@ -461,53 +459,68 @@ __global__ void __launch_bounds__(BS) k_thin(Csr T, const double *__restrict__ x
     }
 }
 
+template <typename T>
+__device__ __forceinline__ const T *plain_vals(const Csr &A);
+template <>
+__device__ __forceinline__ const double *plain_vals<double>(const Csr &A) { return A.val; }
+template <>
+__device__ __forceinline__ const float *plain_vals<float>(const Csr &A) { return A.valf; }
+
 // y = A x (A = fwd or adj) with x already carrying z for the tail columns
-__global__ void __launch_bounds__(BS) k_spmv_plain(Csr A, const double *__restrict__ x,
-                                                   const double *__restrict__ z, double *__restrict__ y)
+template <typename T>
+__global__ void __launch_bounds__(BS) k_spmv_plain(Csr A, const T *__restrict__ x, const double *__restrict__ z,
+                                                   T *__restrict__ y)
 {
-    __shared__ SpmvStage<double, double> st[SPMV_WARPS];
+    __shared__ SpmvStage<T, T> st[SPMV_WARPS];
     const int n0 = A.ncol0;
-    auto xl = [&](int c) -> double { return c < n0 ? __ldg(x + c) : z[c - n0]; };
+    auto xl = [&](int c) -> T { return c < n0 ? __ldg(x + c) : (T)z[c - n0]; };
     auto pre = [&](int r) -> double { return 0.0; };
-    auto epi = [&](int r, double acc, double) { y[r] = acc; };
-    csr_rows<double, double>(A.ptr, A.idx, A.val, A.blk, A.nblk, xl, pre, epi, st);
+    auto epi = [&](int r, double acc, double) { y[r] = (T)acc; };
+    csr_rows<T, T>(A.ptr, A.idx, plain_vals<T>(A), A.blk, A.nblk, xl, pre, epi, st);
 }
 
 // one wave of CTAs at the kernel's occupancy
+template <typename T>
 static int spmv_plain_grid()
 {
     static thread_local int g = 0;
     if (g == 0) {
         int per = 0;
-        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv_plain, BS, 0));
+        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv_plain<T>, BS, 0));
         g = std::max(1, per) * device_info().sms;
     }
     return g;
 }
 
-void op_thin(const Operator &op, bool trans, const double *x, cudaStream_t s)
+template <typename T>
+void op_thin(const Operator &op, bool trans, const T *x, cudaStream_t s)
 {
     if (op.r <= 0) return;
-    const Csr &T = trans ? op.thin_l : op.thin_r;
-    const int nt = std::max(1, T.rows * T.segs);
-    k_thin<<<std::min(nt, device_info().nb), BS, 0, s>>>(T, x, op.w, op.zpart, op.zbuf, op.zticket, 1.0);
+    const Csr &Th = trans ? op.thin_l : op.thin_r;
+    const int nt = std::max(1, Th.rows * Th.segs);
+    k_thin<T><<<std::min(nt, device_info().nb), BS, 0, s>>>(Th, x, op.w, op.zpart, op.zbuf, op.zticket);
     PGB_LAUNCHED();
 }
 
 // y = A x with a caller-supplied z (the low-rank coefficients); no scratch
 void op_spmv_plain_launch(const Csr &A, const double *x, const double *z, double *y, cudaStream_t s)
 {
-    k_spmv_plain<<<spmv_plain_grid(), BS, 0, s>>>(A, x, z, y);
+    k_spmv_plain<double><<<spmv_plain_grid<double>(), BS, 0, s>>>(A, x, z, y);
     PGB_LAUNCHED();
 }
 
-void op_apply(const Operator &op, bool trans, const double *x, double *y, cudaStream_t s)
+template <typename T>
+void op_apply(const Operator &op, bool trans, const T *x, T *y, cudaStream_t s)
 {
-    op_thin(op, trans, x, s);
+    op_thin<T>(op, trans, x, s);
     const Csr &A = trans ? op.adj : op.fwd;
-    k_spmv_plain<<<spmv_plain_grid(), BS, 0, s>>>(A, x, op.zbuf, y);
+    k_spmv_plain<T><<<spmv_plain_grid<T>(), BS, 0, s>>>(A, x, op.zbuf, y);
     PGB_LAUNCHED();
 }
+template void op_thin<double>(const Operator &, bool, const double *, cudaStream_t);
+template void op_thin<float>(const Operator &, bool, const float *, cudaStream_t);
+template void op_apply<double>(const Operator &, bool, const double *, double *, cudaStream_t);
+template void op_apply<float>(const Operator &, bool, const float *, float *, cudaStream_t);
 
 // ------------------------------------------------------- registry
 static std::mutex g_reg_mu;
@@ -706,7 +719,7 @@ extern "C" void propack_gpu_csr_aprod_(const char *transa, const int *m, const i
         PGB_CUDA(cudaMallocAsync(&dx, sizeof(double) * nin, s));
         PGB_CUDA(cudaMallocAsync(&dy, sizeof(double) * nout, s));
         PGB_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * nin, cudaMemcpyHostToDevice, s));
-        op_apply(*op, t, dx, dy, s);
+        op_apply<double>(*op, t, dx, dy, s);
         PGB_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
         PGB_CUDA(cudaFreeAsync(dx, s));
         PGB_CUDA(cudaFreeAsync(dy, s));

@@ -25,7 +25,9 @@ def golden():
 def csr_from(g, prefix):
     import scipy.sparse as sp
     shape = tuple(int(x) for x in g[prefix + "_shape"])
-    return sp.csr_array((g[prefix + "_data"], g[prefix + "_indices"], g[prefix + "_indptr"]), shape=shape)
+    # copies, so that no consumer can alter the session-wide fixture
+    return sp.csr_array((g[prefix + "_data"].copy(), g[prefix + "_indices"].copy(), g[prefix + "_indptr"].copy()),
+                        shape=shape)
 
 
 def illc1850():

@@ -189,3 +189,42 @@ def test_bad_operator_handle_is_an_error():
     op.close()
     with pytest.raises(pg.PropackError):
         pg.svdp(op, 2, rng=rng0())
+
+
+# ----------------------------------------------------- mixed form (FP32 + FP64 refinement)
+MIXED_SIG_RTOL = 1e-10   # after the FP64 refinement: the FP64 bar
+MIXED_VEC_TOL = 1e-8
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(cgs=True), dict(delta=-1.0, eta=-1.0)],
+                         ids=["default", "cgs", "propack_defaults"])
+def test_mixed_vs_golden(golden, opts):
+    S, L, R = csr_from(golden, "lr_S"), csr_from(golden, "lr_L"), csr_from(golden, "lr_R")
+    op = pg.CsrOperator(S, L, R, golden["lr_w"])
+    u, s, vt, bnd = pg.svdp(op, 10, irl_mode=True, kmax=30, tol=1e-10, rng=rng0(), precision="mixed", **opts)
+    st = pg.get_stats()
+    assert st["nopx_low"] > 0, "the FP32 phase did not run"
+    assert pg.get_precision() == "fp64"
+    np.testing.assert_allclose(s, golden["lowrank_irl_sigma"], rtol=MIXED_SIG_RTOL)
+    np.testing.assert_allclose(s, golden["lowrank_dense_sigma"][:10], rtol=MIXED_SIG_RTOL)
+    uo = golden["lowrank_irl_u"] if "lowrank_irl_u" in golden else None
+    res = max(max(np.linalg.norm(op.matvec(vt[i]) - s[i] * u[:, i]),
+                  np.linalg.norm(op.rmatvec(u[:, i]) - s[i] * vt[i])) for i in range(10))
+    assert res <= 1e-8 * s[0], res
+    if uo is not None:
+        assert subspace_err(u, uo) < MIXED_VEC_TOL
+    op.close()
+
+
+def test_mixed_plain_config0(golden):
+    A = csr_from(golden, "plain")
+    u, s, vt, bnd = pg.svdp(A, 10, irl_mode=True, kmax=40, tol=1e-12, rng=rng0(), precision="mixed")
+    np.testing.assert_allclose(s, golden["plain_dense_sigma"][:10], rtol=1e-11)
+    assert subspace_err(u, golden["plain_lansvd_u"]) < MIXED_VEC_TOL
+    assert subspace_err(vt.T, golden["plain_lansvd_vt"].T) < MIXED_VEC_TOL
+
+
+def test_mixed_host_callback(golden):
+    M = csr_from(golden, "small").toarray()
+    u, s, vt, bnd = pg.svdp(aslinearoperator(M), 3, tol=1e-8, rng=rng0(), precision="mixed")
+    np.testing.assert_allclose(s, golden["small_irl_lm_sigma"], rtol=1e-8, atol=1e-8)

@@ -110,3 +110,11 @@ def test_illc1850_vs_golden(golden):
     np.testing.assert_allclose(s, golden["illc_sigma"], rtol=1e-11)
     np.testing.assert_allclose(u.T @ u, np.eye(200), atol=1e-9)
     np.testing.assert_allclose(vt @ vt.T, np.eye(200), atol=1e-9)
+
+
+def test_operator_does_not_modify_its_inputs(golden):
+    S, L, R = csr_from(golden, "lr_S"), csr_from(golden, "lr_L"), csr_from(golden, "lr_R")
+    before = [a.copy() for a in (S.data, S.indices, S.indptr, L.data, R.data)]
+    oracle.Operator(S, L, R, golden["lr_w"])
+    after = (S.data, S.indices, S.indptr, L.data, R.data)
+    assert all(np.array_equal(x, y) for x, y in zip(before, after))
