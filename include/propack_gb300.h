@@ -163,7 +163,8 @@ int propack_get_precision(void);
  * and launch counts accumulated since propack_set_profiling(1).  Classes
  * in order: SpMV A'u (fused), SpMV Av (fused), ELR pass, CGS projection,
  * CGS update, low-rank prepass, bidiagonal analysis, IRL sweeps, GEMM,
- * then the FP32 (mixed form) SpMV A'u, SpMV Av, CGS projection, CGS update.
+ * then the FP32 (mixed form) SpMV A'u, SpMV Av, CGS projection, CGS update,
+ * then the Ritz preparation (SVD of the final bidiagonal).
  * Returns the number of classes.  No reference counterpart. */
 void propack_set_profiling(int on);
 int propack_get_profile(double *total_ms, int64_t *launches, int n);

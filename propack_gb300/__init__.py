@@ -44,7 +44,7 @@ class _Stats(C.Structure):
 
 
 PROFILE_KINDS = ("spmv_adj", "spmv_fwd", "elr", "cgs_dots", "cgs_upd", "lowrank_prepass", "analyse", "sweeps",
-                 "gemm", "spmv_adj_fp32", "spmv_fwd_fp32", "cgs_dots_fp32", "cgs_upd_fp32")
+                 "gemm", "spmv_adj_fp32", "spmv_fwd_fp32", "cgs_dots_fp32", "cgs_upd_fp32", "ritz_prep")
 
 
 _lib = None

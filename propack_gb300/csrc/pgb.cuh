@@ -29,7 +29,7 @@ extern thread_local int64_t g_launches;
 // Optional per-kernel timing with CUDA events recorded on the launching
 // stream (propack_set_profiling); off by default.
 enum ProfKind { PK_SPMV_ADJ, PK_SPMV_FWD, PK_ELR, PK_CGS_DOTS, PK_CGS_UPD, PK_THIN, PK_ANALYSE, PK_SWEEPS,
-                PK_GEMM, PK_SPMV_ADJ32, PK_SPMV_FWD32, PK_CGS_DOTS32, PK_CGS_UPD32, PK_N };
+                PK_GEMM, PK_SPMV_ADJ32, PK_SPMV_FWD32, PK_CGS_DOTS32, PK_CGS_UPD32, PK_RITZ, PK_N };
 extern thread_local int g_prof_on;
 void prof_mark(int kind, cudaStream_t s, bool begin);
 void prof_collect();
@@ -282,6 +282,7 @@ struct AnaArgs {
     int dim, m, n, neig, kk;       // kk: k = dim - p (IRL) or k (lansvd)
     int irl, small_side;
     double tol;
+    double *wz;                    // bidiag_scratch(dim) doubles (lane-parallel path)
 };
 
 struct SweepArgs {
@@ -293,6 +294,7 @@ struct SweepArgs {
     LbCtl *ctl;               // rnorm <- beta_k, nrestart counted by the host
     int dim, k, neig, small_side;
     double min_relgap;
+    double *wz;               // bidiag_scratch(dim) doubles: the sweeps' rotations
 };
 
 struct RitzArgs {
@@ -303,11 +305,23 @@ struct RitzArgs {
     double *Qt;         // dim^2 : right vectors' transpose
     double *w;          // 4*(dim+1)
     int dim, m, n;
+    double *wz;         // bidiag_scratch(dim) doubles (lane-parallel path)
+    int *flag;          // set to 1 when the lane-parallel vectors are not trusted
+    int k, mstart;      // the wanted vectors: indices mstart-1 .. mstart+k-2
 };
 
+// scratch of the lane-parallel bidiagonal kernels for dimension dim
+inline size_t bidiag_scratch(int dim) { return 8 * (size_t)(dim + 1) * (dim + 1) + 64; }
+
+// analysis: nconv_out < 0 signals that the lane-parallel path declined and
+// launch_analyse_qr must be run instead
 void launch_analyse(const AnaArgs &a, cudaStream_t s);
+void launch_analyse_qr(const AnaArgs &a, cudaStream_t s);
 void launch_sweeps(const SweepArgs &a, cudaStream_t s);
-void launch_ritz_prep(const RitzArgs &a, cudaStream_t s);
+// Ritz preparation: returns false when only the QR path applies; otherwise
+// *a.flag != 0 afterwards asks for launch_ritz_prep_qr
+bool launch_ritz_prep(const RitzArgs &a, cudaStream_t s);
+void launch_ritz_prep_qr(const RitzArgs &a, cudaStream_t s);
 template <typename T>
 void gemm(int mr, int nc, int kk, const T *A, int lda, bool ta, const double *B, int ldb, bool tb, T *C, int ldc,
           cudaStream_t s);

@@ -16,6 +16,7 @@
 // whole CTA then applies the chain to the singular-vector matrices, one row
 // (or column) per thread.
 #include "pgb.cuh"
+#include "pgb_bidiag.cuh"
 
 namespace pgb {
 
@@ -579,6 +580,304 @@ __global__ void k_ritz_prep(RitzArgs a, int use_smem)
     bdsqr_cta(dim, D, E, dim, a.Qt, dim, dim, a.P, dim, w, q);
 }
 
+// ------------------------------------------------- lane-parallel analysis
+// (the same outputs as k_analyse; see pgb_bidiag.cuh for the methods)
+
+// bidiagonal size up to which the lane-parallel kernels are used
+constexpr int PAR_DIM_MAX = 2048;
+
+// dbdqr of B into a1 (d) / b1 (e), c1 -> bnd[dim-1], c2 -> bnd[dim]
+__global__ void k_ana_qr(AnaArgs a)
+{
+    const int dim = a.dim;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) { a.a1[i] = a.balpha[i]; a.b1[i] = a.bbeta[i]; }
+    for (int i = threadIdx.x; i <= dim; i += blockDim.x) a.bnd[i] = 0.0;
+    __syncthreads();
+    const int mn = a.m < a.n ? a.m : a.n;
+    if (threadIdx.x == 0) bdqr_dev(dim == mn, dim, a.a1, a.b1, &a.bnd[dim - 1], &a.bnd[dim], nullptr, 0);
+}
+
+// sigma_t of the upper bidiagonal (d, e), one warp per t; sig[t-1]
+__global__ void __launch_bounds__(256) k_bisect(const double *d, const double *e, int n, double *sig)
+{
+    extern __shared__ double b2[];
+    const int N = 2 * n;
+    for (int j = threadIdx.x; j < N - 1; j += blockDim.x) {
+        const double b = tgk_b(d, e, j);
+        b2[j] = b * b;
+    }
+    __shared__ double gs, ps;
+    if (threadIdx.x == 0) tgk_bounds(d, e, n, gs, ps);
+    __syncthreads();
+    const int t = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5) + 1;
+    if (t > n) return;
+    const double s = warp_sigma(n, b2, t, gs, ps);
+    if ((threadIdx.x & 31) == 0) sig[t - 1] = s;
+}
+
+// bounds from the last components of the left vectors, then the same
+// bookkeeping as k_analyse (anorm, refinebounds, convergence count)
+__global__ void k_ana_finish(AnaArgs a)
+{
+    const int dim = a.dim, N = 2 * dim;
+    const double *sig = a.w;
+    __shared__ double gs, ps;
+    __shared__ int bad;
+    if (threadIdx.x == 0) { tgk_bounds(a.a1, a.b1, dim, gs, ps); bad = 0; }
+    __syncthreads();
+    const double c1 = a.bnd[dim - 1];
+    double bi = 0.0;
+    if (threadIdx.x < dim) {
+        const int i = threadIdx.x;
+        double *Dp = a.wz + (size_t)i * 2 * N, *Dm = Dp + N;
+        const double zn = tgk_twisted(a.a1, a.b1, dim, sig[i], ps, Dp, Dm, nullptr);
+        bi = c1 * (sqrt(2.0) * zn);
+        if (!(bi == bi) || !(sig[i] == sig[i])) bad = 1;
+    }
+    __syncthreads();
+    if (bad) {
+        if (threadIdx.x == 0) *a.nconv_out = -1;
+        return;
+    }
+    if (threadIdx.x < dim) {
+        a.bnd[threadIdx.x] = bi;
+        a.a1[threadIdx.x] = sig[threadIdx.x];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double *d = a.a1, *bnd = a.bnd;
+        const int mn = a.m < a.n ? a.m : a.n;
+        const double eps34 = pow(EPS, 0.75);
+        const double epsn = (double)(a.m > a.n ? a.m : a.n) * EPS / 2.0;
+        double anorm = *a.anorm_drv;
+        if (dim > 5) anorm = d[0];
+        else anorm = fmax(anorm, d[0]);
+        *a.anorm_drv = anorm;
+        const double rnorm = a.ctl->rnorm;
+        for (int i = 0; i < dim; i++) bnd[i] = fabs(rnorm * bnd[i]);
+        int nconv = 0;
+        if (a.irl) {
+            const int neig = a.neig;
+            refinebounds_dev(mn, dim < neig ? dim : neig, d, bnd, epsn * anorm, eps34);
+            int i = 1;
+            const int lim = dim < neig ? dim : neig;
+            while (i <= lim) {
+                if (bnd[i - 1] <= a.tol * d[i - 1]) {
+                    a.sigma_out[nconv] = d[i - 1];
+                    a.bnd_out[nconv] = bnd[i - 1];
+                    nconv++;
+                    i++;
+                } else {
+                    i = a.kk + 1;
+                }
+            }
+        } else {
+            refinebounds_dev(mn, dim, d, bnd, epsn * anorm, eps34);
+            const int lim = dim < a.kk ? dim : a.kk;
+            for (int i = 0; i < lim; i++) a.bnd_out[i] = bnd[i];
+            int i = 0;
+            while (i < lim) {
+                if (bnd[i] <= a.tol * d[i]) { a.sigma_out[nconv] = d[i]; nconv++; i++; }
+                else i = a.kk;
+            }
+        }
+        *a.nconv_out = nconv;
+    }
+}
+
+// ----------------------------------------------- wavefront IRL sweeps
+// The p sweeps of dlansvd_irl.F:346-363 (dbsvdstep, double/dbsvd.F:5-82)
+// with their exact shifts known in advance.  Step i of a sweep touches
+// D[i-1..i] and E[i-2..i] only, so sweep s+1 may run its step i while sweep
+// s runs step i+3: one thread per sweep, one CTA barrier per step.  Every
+// value is produced by the same operations in the same order as in the
+// sequential sweeps, so B, P and Q are identical to theirs.  The rotations
+// go to wz as [sweep][4][dim+1] (cu, su, cv, sv).
+__global__ void k_irl_chain(SweepArgs a)
+{
+    extern __shared__ double dsm[];
+    const int dim = a.dim, k = a.k, dp1 = dim + 1, nsw = dim - k;
+    double *D = dsm, *E = dsm + dp1;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) { D[i] = a.balpha[i]; E[i] = a.bbeta[i]; }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < dim - k; i++) a.shifts[i] = 0.0;
+        int nshft = 0;
+        for (int i = dim; i >= k + 1; i--) {
+            const double relgap = a.a1[k - 1] - (a.a1[i - 1] + a.bnd[i - 1]);
+            a.shifts[nshft++] = (relgap > a.min_relgap * a.a1[k - 1]) ? a.a1[i - 1] : 0.0;
+        }
+    }
+    __syncthreads();
+    const int s = threadIdx.x;  // this thread's sweep (blockDim >= nsw)
+    const int kk = dim - s;     // dbsvdstep size of sweep s
+    const bool active = s < nsw && kk > 1;
+    const double sigma = active ? a.shifts[s] : 0.0;
+    double *cu = a.wz + (size_t)s * 4 * dp1, *su = cu + dp1, *cv = cu + 2 * dp1, *sv = cu + 3 * dp1;
+    double x = 0.0, y = 0.0, c, sn, r;
+    const int gend = dim + 3 * (nsw - 1);
+    for (int g = 0; g <= gend; g++) {
+        const int i = g - 3 * s;
+        if (active && i >= 0 && i <= kk) {
+            if (i == 0) {
+                x = D[0] * D[0] - sigma * sigma;
+                y = E[0] * D[0];
+            } else if (i < kk) {
+                if (i > 1) lartg(x, y, c, sn, E[i - 2]);
+                else lartg(x, y, c, sn, r);
+                x = c * D[i - 1] + sn * E[i - 1];
+                E[i - 1] = -sn * D[i - 1] + c * E[i - 1];
+                D[i - 1] = x;
+                y = sn * D[i];
+                D[i] = c * D[i];
+                cu[i - 1] = c; su[i - 1] = sn;
+                lartg(x, y, c, sn, D[i - 1]);
+                x = c * E[i - 1] + sn * D[i];
+                D[i] = -sn * E[i - 1] + c * D[i];
+                E[i - 1] = x;
+                y = sn * E[i];
+                E[i] = c * E[i];
+                cv[i - 1] = c; sv[i - 1] = sn;
+            } else {
+                lartg(x, y, c, sn, E[kk - 2]);
+                x = c * D[kk - 1] + sn * E[kk - 1];
+                E[kk - 1] = -sn * D[kk - 1] + c * E[kk - 1];
+                D[kk - 1] = x;
+                cu[kk - 1] = c; su[kk - 1] = sn;
+            }
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) { a.balpha[i] = D[i]; a.bbeta[i] = E[i]; }
+    if (threadIdx.x == 0) a.ctl->rnorm = E[k - 1];
+}
+
+// P (dim+1)^2 and Q dim^2 from the recorded rotations: one warp per row,
+// lane l applying sweep 32w+l two columns behind sweep 32w+l-1 (a sweep's
+// rotation t reads column t+1 and finishes column t), waves of 32 sweeps.
+constexpr int APPLY_WARPS = 8;
+__global__ void __launch_bounds__(APPLY_WARPS * 32) k_irl_apply(SweepArgs a, int prow_blocks)
+{
+    extern __shared__ double rows[];
+    const int dim = a.dim, k = a.k, dp1 = dim + 1, nsw = dim - k;
+    const bool isP = blockIdx.x < prow_blocks;
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = (isP ? blockIdx.x : blockIdx.x - prow_blocks) * APPLY_WARPS + wid;
+    const int nrows = isP ? dp1 : dim, ncols = nrows;
+    if (row >= nrows) return;
+    double *rw = rows + (size_t)wid * dp1;
+    for (int t = lane; t < ncols; t += 32) rw[t] = (t == row) ? 1.0 : 0.0;
+    __syncwarp();
+    for (int w0 = 0; w0 < nsw; w0 += 32) {
+        const int s = w0 + lane;
+        const int kk = dim - s;
+        // rotations of this sweep on this matrix: P gets kk (cu, su), Q kk-1 (cv, sv)
+        const int nrot = (s < nsw && kk > 1) ? (isP ? kk : kk - 1) : -1;
+        const double *cc = a.wz + (size_t)s * 4 * dp1 + (isP ? 0 : 2 * dp1), *ss = cc + dp1;
+        const int kk0 = dim - w0;
+        const int gend = (isP ? kk0 : kk0 - 1) + 2 * 31;
+        double xc = 0.0;
+        double cn = 0.0, sn = 0.0;
+        if (nrot > 0) { cn = cc[0]; sn = ss[0]; }
+        for (int g = 0; g <= gend; g++) {
+            const int t = g - 2 * lane;
+            if (nrot > 0 && t >= 0 && t <= nrot) {
+                if (t < nrot) {
+                    const double c = cn, s_ = sn;
+                    if (t + 1 < nrot) { cn = cc[t + 1]; sn = ss[t + 1]; }
+                    if (t == 0) xc = rw[0];
+                    const double yc = rw[t + 1];
+                    rw[t] = c * xc + s_ * yc;
+                    xc = c * yc - s_ * xc;
+                } else {
+                    rw[nrot] = xc;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    double *M = isP ? a.P : a.Q;
+    for (int t = lane; t < ncols; t += 32) M[(size_t)t * nrows + row] = rw[t];
+}
+
+// ----------------------------------------------- lane-parallel Ritz prep
+// dbdqr with Q' (dritzvec.F:112-114): thread 0 runs the rotation chain on
+// R, then one thread per column of Mt replays it (the same operations as
+// bdqr_dev's Q' update, column by column).
+__global__ void k_ritz_qr(RitzArgs a)
+{
+    const int dim = a.dim, n1 = dim + 1;
+    double *cs = a.w, *sn = a.w + n1;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) { a.D[i] = a.balpha[i]; a.E[i] = a.bbeta[i]; }
+    if (threadIdx.x == 0) *a.flag = 0;
+    __syncthreads();
+    const int mn = a.m < a.n ? a.m : a.n;
+    __shared__ int nrot_s;
+    if (threadIdx.x == 0) {
+        double c, s, r;
+        double *D = a.D, *E = a.E;
+        int i;
+        for (i = 1; i <= dim - 1; i++) {
+            lartg(D[i - 1], E[i - 1], c, s, r);
+            D[i - 1] = r;
+            E[i - 1] = s * D[i];
+            D[i] = c * D[i];
+            cs[i - 1] = c; sn[i - 1] = s;
+        }
+        int nrot = dim - 1;
+        if (dim != mn) {
+            lartg(D[dim - 1], E[dim - 1], c, s, r);
+            D[dim - 1] = r;
+            E[dim - 1] = 0.0;
+            cs[dim - 1] = c; sn[dim - 1] = s;
+            nrot = dim;
+        }
+        nrot_s = nrot;
+    }
+    __syncthreads();
+    const int nrot = nrot_s;
+    // column j (0-based) of Q': created by rotation j-1 (for j >= 1), then
+    // rotated by rotations j, j+1, ..., nrot-1 on rows (i, i+1)
+    for (int j = threadIdx.x; j < n1; j += blockDim.x) {
+        double *col = a.Mt + (size_t)j * n1;
+        for (int i = 0; i < n1; i++) col[i] = 0.0;
+        if (j == 0) col[0] = 1.0;
+        else if (j - 1 < nrot) { col[j - 1] = sn[j - 1]; col[j] = cs[j - 1]; }
+        else col[j] = 1.0;
+        for (int i = (j == 0 ? 0 : j); i < nrot; i++) {
+            col[i + 1] = -sn[i] * col[i];
+            col[i] = cs[i] * col[i];
+        }
+    }
+}
+
+// The wanted singular vector pairs of R (indices mstart-1 .. mstart+k-2 of
+// the decreasing order), one lane each: P(:, i) = y_i, Qt(i, :) = x_i'.
+// Values closer than 1e-9 sigma_max to a neighbour are left to the QR path
+// (flag), since single twisted vectors are only accurate to eps/gap.
+__global__ void k_ritz_vecs(RitzArgs a)
+{
+    const int dim = a.dim, N = 2 * dim;
+    const double *sig = a.w + 2 * (dim + 1);
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.k) return;
+    const int i = a.mstart - 1 + q;
+    const double smax = sig[0];
+    const double gap = fmin(i > 0 ? sig[i - 1] - sig[i] : INFINITY, i + 1 < dim ? sig[i] - sig[i + 1] : INFINITY);
+    double gs, ps;
+    tgk_bounds(a.D, a.E, dim, gs, ps);
+    if (!(gap > 1e-9 * smax) || !(sig[i] > 1e-9 * smax)) { *a.flag = 1; return; }
+    double *Dp = a.wz + (size_t)q * 3 * N, *Dm = Dp + N, *z = Dm + N;
+    tgk_twisted(a.D, a.E, dim, sig[i], ps, Dp, Dm, z);
+    double nx = 0.0, ny = 0.0;
+    for (int t = 0; t < dim; t++) { nx += z[2 * t] * z[2 * t]; ny += z[2 * t + 1] * z[2 * t + 1]; }
+    if (!(nx > 0.0) || !(ny > 0.0) || !(nx < INFINITY) || !(ny < INFINITY)) { *a.flag = 1; return; }
+    const double ix = 1.0 / sqrt(nx), iy = 1.0 / sqrt(ny);
+    for (int t = 0; t < dim; t++) {
+        a.Qt[(size_t)t * dim + i] = z[2 * t] * ix;
+        a.P[(size_t)i * dim + t] = z[2 * t + 1] * iy;
+    }
+}
+
 // ------------------------------------------------------------------ GEMM
 // C(mr x nc) = op(A) op(B), 64 x 64 tiles, 256 threads x 4 x 4.  A and C
 // hold T (the Lanczos vector type), B is FP64 (the small restart / Ritz
@@ -652,26 +951,79 @@ static int smem_for(const void *fn, size_t bytes)
     if (bytes > 48 * 1024) PGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return 1;
 }
-void launch_analyse(const AnaArgs &a, cudaStream_t s)
+void launch_analyse_qr(const AnaArgs &a, cudaStream_t s)
 {
     const size_t bytes = sizeof(double) * (7 * (size_t)(a.dim + 1) + 2);
     const int use = smem_for((const void *)k_analyse, bytes);
     PGB_PROF(PK_ANALYSE, s, k_analyse<<<1, 32, use ? bytes : 0, s>>>(a, use));
     PGB_LAUNCHED();
 }
-void launch_sweeps(const SweepArgs &a, cudaStream_t s)
+static bool bisect_fits(int dim)
 {
-    const size_t bytes = sizeof(double) * 6 * (size_t)(a.dim + 1);
-    const int use = smem_for((const void *)k_irl_sweeps, bytes);
-    PGB_PROF(PK_SWEEPS, s, k_irl_sweeps<<<1, 256, use ? bytes : 0, s>>>(a, use));
+    return dim <= PAR_DIM_MAX && smem_for((const void *)k_bisect, sizeof(double) * 2 * (size_t)dim) != 0;
+}
+static void launch_bisect(const double *d, const double *e, int n, double *sig, cudaStream_t s)
+{
+    const int wpb = 8;
+    k_bisect<<<(n + wpb - 1) / wpb, 32 * wpb, sizeof(double) * 2 * (size_t)n, s>>>(d, e, n, sig);
     PGB_LAUNCHED();
 }
-void launch_ritz_prep(const RitzArgs &a, cudaStream_t s)
+void launch_analyse(const AnaArgs &a, cudaStream_t s)
+{
+    // the smallest triplets (which = 'S') keep the QR path: their twisted
+    // vectors on the Golub-Kahan form are not reliable near sigma = 0
+    if (a.small_side || !a.wz || a.dim > 1024 || !bisect_fits(a.dim)) {
+        launch_analyse_qr(a, s);
+        return;
+    }
+    PGB_PROF(PK_ANALYSE, s, {
+        k_ana_qr<<<1, 32, 0, s>>>(a);
+        PGB_LAUNCHED();
+        launch_bisect(a.a1, a.b1, a.dim, a.w, s);
+        k_ana_finish<<<1, ((a.dim + 31) / 32) * 32, 0, s>>>(a);
+        PGB_LAUNCHED();
+    });
+}
+void launch_sweeps(const SweepArgs &a, cudaStream_t s)
+{
+    const int nsw = a.dim - a.k;
+    const size_t chain_bytes = sizeof(double) * 2 * (size_t)(a.dim + 1);
+    const size_t apply_bytes = sizeof(double) * APPLY_WARPS * (size_t)(a.dim + 1);
+    if (a.small_side || !a.wz || nsw < 1 || nsw > 1024 || a.dim > PAR_DIM_MAX ||
+        !smem_for((const void *)k_irl_chain, chain_bytes) || !smem_for((const void *)k_irl_apply, apply_bytes)) {
+        const size_t bytes = sizeof(double) * 6 * (size_t)(a.dim + 1);
+        const int use = smem_for((const void *)k_irl_sweeps, bytes);
+        PGB_PROF(PK_SWEEPS, s, k_irl_sweeps<<<1, 256, use ? bytes : 0, s>>>(a, use));
+        PGB_LAUNCHED();
+        return;
+    }
+    const int pblocks = (a.dim + 1 + APPLY_WARPS - 1) / APPLY_WARPS;
+    const int qblocks = (a.dim + APPLY_WARPS - 1) / APPLY_WARPS;
+    PGB_PROF(PK_SWEEPS, s, {
+        k_irl_chain<<<1, ((nsw + 31) / 32) * 32, chain_bytes, s>>>(a);
+        PGB_LAUNCHED();
+        k_irl_apply<<<pblocks + qblocks, APPLY_WARPS * 32, apply_bytes, s>>>(a, pblocks);
+        PGB_LAUNCHED();
+    });
+}
+void launch_ritz_prep_qr(const RitzArgs &a, cudaStream_t s)
 {
     const size_t bytes = sizeof(double) * 6 * (size_t)(a.dim + 1);
     const int use = smem_for((const void *)k_ritz_prep, bytes);
-    k_ritz_prep<<<1, 256, use ? bytes : 0, s>>>(a, use);
+    PGB_PROF(PK_RITZ, s, k_ritz_prep<<<1, 256, use ? bytes : 0, s>>>(a, use));
     PGB_LAUNCHED();
+}
+bool launch_ritz_prep(const RitzArgs &a, cudaStream_t s)
+{
+    if (a.mstart != 1 || !a.wz || !a.flag || a.k < 1 || !bisect_fits(a.dim)) return false;
+    PGB_PROF(PK_RITZ, s, {
+        k_ritz_qr<<<1, 256, 0, s>>>(a);
+        PGB_LAUNCHED();
+        launch_bisect(a.D, a.E, a.dim, a.w + 2 * (a.dim + 1), s);
+        k_ritz_vecs<<<(a.k + 31) / 32, 32, 0, s>>>(a);
+        PGB_LAUNCHED();
+    });
+    return true;
 }
 // C = op(A) op(B) (out of place)
 template <typename T>

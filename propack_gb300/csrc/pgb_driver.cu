@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -31,6 +32,20 @@ struct Stats {
 };
 static thread_local Stats g_stat;       // cumulative (clearstat_/printstat_)
 static thread_local Stats g_last;       // last driver call (propack_get_stats)
+
+// PROPACK_GB300_TRACE=1 prints the driver's decisions (suspensions of the
+// Lanczos step sequence, restarts, phases of the mixed form) to stderr
+static bool trace_on()
+{
+    static const bool on = [] {
+        const char *e = getenv("PROPACK_GB300_TRACE");
+        return e && e[0] && e[0] != '0';
+    }();
+    return on;
+}
+
+// steps enqueued between two looks at the device status word
+constexpr int LB_WINDOW = 8;
 
 // ------------------------------------------------------------ small kernels
 #define LCG_A 33952834046453ULL
@@ -177,6 +192,8 @@ struct Ctx {
     double *shifts = nullptr, *sig_out = nullptr, *bnd_out = nullptr, *anorm_drv = nullptr;
     int *nconv = nullptr;
     double *D = nullptr, *E = nullptr, *Mt = nullptr, *Pr = nullptr, *Qt = nullptr, *X = nullptr;
+    double *wz = nullptr;                   // scratch of the lane-parallel bidiagonal kernels
+    int *dflag = nullptr;
     void *gout = nullptr;                   // GEMM output scratch (vector type)
     // operator
     const Operator *op = nullptr;
@@ -186,6 +203,8 @@ struct Ctx {
     double *hx = nullptr, *hy = nullptr;    // pinned host vectors for a host APROD
     int nb = 0;
     int ntry_spec = 2;
+    int *hstat = nullptr;                   // pinned status words of the enqueue windows
+    cudaEvent_t wev[2] = {nullptr, nullptr};
     std::vector<void *> allocs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
 
@@ -206,6 +225,9 @@ struct Ctx {
         for (void *p : allocs) cudaFree(p);
         if (hctl) cudaFreeHost(hctl);
         if (hscal) cudaFreeHost(hscal);
+        if (hstat) cudaFreeHost(hstat);
+        for (cudaEvent_t e : wev)
+            if (e) cudaEventDestroy(e);
         if (hx) cudaFreeHost(hx);
         if (hy) cudaFreeHost(hy);
         if (ev0) cudaEventDestroy(ev0);
@@ -276,9 +298,14 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
     c.dy = c.dalloc<double>(mn);
     c.scal = c.dalloc<double>(8);
     PGB_CUDA(cudaMallocHost(&c.hscal, sizeof(double) * 8));
+    PGB_CUDA(cudaMallocHost(&c.hstat, sizeof(int) * 2));
+    c.hstat[0] = c.hstat[1] = 0;
+    for (cudaEvent_t &e : c.wev) PGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     const size_t d1 = kmax + 2;
     c.a1 = c.dalloc<double>(d1); c.b1 = c.dalloc<double>(d1); c.bnd = c.dalloc<double>(d1);
     c.w = c.dalloc<double>(4 * d1);
+    c.wz = c.dalloc<double>(bidiag_scratch(kmax));
+    c.dflag = c.dalloc<int>(4);
     c.P = c.dalloc<double>(d1 * d1); c.Q = c.dalloc<double>(d1 * d1);
     c.shifts = c.dalloc<double>(d1);
     c.sig_out = c.dalloc<double>(d1); c.bnd_out = c.dalloc<double>(d1);
@@ -420,7 +447,12 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
     // machine constants of the Lanczos vectors (FP32 vectors: eps = 2^-24)
     const double eps = sizeof(T) == sizeof(double) ? EPS : 5.9604644775390625e-08;
     h.eps_vec = eps;
-    h.epsn = (double)mn * eps;
+    // the breakdown level of alpha/beta: max(m,n)*eps in FP64 (as the
+    // reference); with FP32 vectors that worst-case bound reaches ~0.2*||A||
+    // at a few million rows, so the FP32 level is the statistical
+    // sqrt(max(m,n))*eps (2^-24), which still sits far above the rounding noise
+    // of an FP32 product with compensated norms
+    h.epsn = sizeof(T) == sizeof(double) ? (double)mn * eps : std::sqrt((double)mn) * eps;
     h.epsn2 = std::sqrt((double)mn) * eps;
     h.delta = doption[0] < 0 ? std::sqrt(eps / k) : doption[0];
     h.eta = doption[1] < 0 ? std::pow(eps, 0.75) / std::sqrt((double)k) : doption[1];
@@ -535,9 +567,25 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
         }
         LbArgs a = c.args();
         if (!host_ap) {
-            for (; j <= k; j++) {
-                for (; side < 2; side++) lb_enqueue_half<T>(a, c.op, side, j, h.ielr, c.ntry_spec, false, c.s);
-                side = 0;
+            // enqueue in windows of LB_WINDOW steps; before a window goes in,
+            // the status word of the window two back is read (its copy was
+            // queued behind it), so at most two windows of launches are
+            // wasted when a step suspends, and the device never runs dry
+            int wnum = 0;
+            while (j <= k) {
+                if (wnum >= 2) {
+                    PGB_CUDA(cudaEventSynchronize(c.wev[wnum & 1]));
+                    if (c.hstat[wnum & 1] != 0) break;
+                }
+                const int jend = std::min(k, j + LB_WINDOW - 1);
+                for (; j <= jend; j++) {
+                    for (; side < 2; side++) lb_enqueue_half<T>(a, c.op, side, j, h.ielr, c.ntry_spec, false, c.s);
+                    side = 0;
+                }
+                PGB_CUDA(cudaMemcpyAsync(&c.hstat[wnum & 1], &c.ctl->status, sizeof(int), cudaMemcpyDeviceToHost,
+                                         c.s));
+                PGB_CUDA(cudaEventRecord(c.wev[wnum & 1], c.s));
+                wnum++;
             }
             c.get_ctl();
         } else {
@@ -570,6 +618,9 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
         }
         // ---- a suspension: finish the case on the host side, then resume
         const int sj = h.susp_j, ss = h.susp_side;
+        if (trace_on())
+            fprintf(stderr, "[propack_gb300] lanbpro suspension: reason %d step %d side %c alpha %.3e beta %.3e anorm %.3e\n",
+                    h.susp_reason, sj, ss == 0 ? 'v' : 'u', h.alpha, h.beta, h.anorm);
         if (h.susp_reason == 2) {
             h.status = 0;
             c.put_ctl();
@@ -701,6 +752,25 @@ static void ovwr_left(Ctx &c, T *A, int lda, int rows, int nc, int kk, const dou
     copy_cols<T>((T *)c.gout, lda, A, lda, rows, nc, c.s);
 }
 
+// the bidiagonal analysis; returns the number of converged values
+static int analyse(Ctx &c, const AnaArgs &a)
+{
+    launch_analyse(a, c.s);
+    g_last.nbsvd++;
+    int nc = 0;
+    PGB_CUDA(cudaMemcpyAsync(c.hscal, c.nconv, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+    c.sync();
+    memcpy(&nc, c.hscal, sizeof(int));
+    if (nc < 0) {
+        if (trace_on()) fprintf(stderr, "[propack_gb300] analysis: lane-parallel path declined, QR path\n");
+        launch_analyse_qr(a, c.s);
+        PGB_CUDA(cudaMemcpyAsync(c.hscal, c.nconv, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+        c.sync();
+        memcpy(&nc, c.hscal, sizeof(int));
+    }
+    return nc;
+}
+
 // dritzvec (double/dritzvec.F:1-199)
 template <typename T>
 static void dev_ritzvec(Ctx &c, bool small_side, bool du, bool dv, int k, int dim)
@@ -708,7 +778,19 @@ static void dev_ritzvec(Ctx &c, bool small_side, bool du, bool dv, int k, int di
     RitzArgs r;
     r.balpha = c.balpha; r.bbeta = c.bbeta; r.D = c.D; r.E = c.E; r.Mt = c.Mt; r.P = c.Pr; r.Qt = c.Qt;
     r.w = c.w; r.dim = dim; r.m = c.m; r.n = c.n;
-    launch_ritz_prep(r, c.s);
+    r.wz = c.wz; r.flag = c.dflag;
+    r.mstart = small_side ? dim - k + 1 : 1;
+    r.k = k;
+    bool qr = !launch_ritz_prep(r, c.s);
+    if (!qr) {
+        PGB_CUDA(cudaMemcpyAsync(c.hscal, c.dflag, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+        c.sync();
+        int f = 0;
+        memcpy(&f, c.hscal, sizeof(int));
+        qr = f != 0;
+        if (qr && trace_on()) fprintf(stderr, "[propack_gb300] Ritz vectors: clustered values, QR path\n");
+    }
+    if (qr) launch_ritz_prep_qr(r, c.s);
     const int dp1 = dim + 1;
     // X = P' Mt(1:dim, 1:dim+1)   (dim x dim+1, ld dim+1)
     gemm<double>(dim, dp1, dim, c.Pr, dim, true, c.Mt, dp1, false, c.X, dp1, c.s);
@@ -829,19 +911,16 @@ static void irl_loop(Ctx &c, const IrlIn &in, double *doption, const int *ioptio
             a.balpha = c.balpha; a.bbeta = c.bbeta; a.a1 = c.a1; a.b1 = c.b1; a.bnd = c.bnd; a.w = c.w;
             a.ctl = c.ctl; a.sigma_out = c.sig_out; a.bnd_out = c.bnd_out; a.nconv_out = c.nconv;
             a.anorm_drv = c.anorm_drv; a.dim = dim; a.m = m; a.n = n; a.neig = neig0; a.kk = k;
-            a.irl = 1; a.small_side = in.small_side; a.tol = in.tol;
-            launch_analyse(a, c.s);
-            g_last.nbsvd++;
-            PGB_CUDA(cudaMemcpyAsync(c.hscal, c.nconv, sizeof(int), cudaMemcpyDeviceToHost, c.s));
-            c.sync();
-            int nc = 0;
-            memcpy(&nc, c.hscal, sizeof(int));
-            nconv = nc;
+            a.irl = 1; a.small_side = in.small_side; a.tol = in.tol; a.wz = c.wz;
+            nconv = analyse(c, a);
         }
         if (ierr < 0) {
             if (dim < k) out.info = dim;
             break;
         }
+        if (trace_on())
+            fprintf(stderr, "[propack_gb300] irl %s iter %d: dim %d nconv %d ierr %d\n",
+                    sizeof(T) == sizeof(double) ? "fp64" : "fp32", iter, dim, nconv, ierr);
         if (in.stall_limit > 0) {
             if (nconv > best) { best = nconv; since = 0; }
             else if (++since >= in.stall_limit) break;
@@ -852,7 +931,7 @@ static void irl_loop(Ctx &c, const IrlIn &in, double *doption, const int *ioptio
                 SweepArgs sw;
                 sw.balpha = c.balpha; sw.bbeta = c.bbeta; sw.a1 = c.a1; sw.bnd = c.bnd; sw.P = c.P; sw.Q = c.Q;
                 sw.shifts = c.shifts; sw.w = c.w; sw.ctl = c.ctl; sw.dim = dim; sw.k = k; sw.neig = neig0;
-                sw.small_side = in.small_side; sw.min_relgap = doption[3];
+                sw.small_side = in.small_side; sw.min_relgap = doption[3]; sw.wz = c.wz;
                 launch_sweeps(sw, c.s);
             }
             {
@@ -1048,12 +1127,8 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
             a.balpha = c.balpha; a.bbeta = c.bbeta; a.a1 = c.a1; a.b1 = c.b1; a.bnd = c.bnd; a.w = c.w;
             a.ctl = c.ctl; a.sigma_out = c.sig_out; a.bnd_out = c.bnd_out; a.nconv_out = c.nconv;
             a.anorm_drv = c.anorm_drv; a.dim = j; a.m = m; a.n = n; a.neig = k; a.kk = k;
-            a.irl = 0; a.small_side = 0; a.tol = tol;
-            launch_analyse(a, c.s);
-            g_last.nbsvd++;
-            PGB_CUDA(cudaMemcpyAsync(c.hscal, c.nconv, sizeof(int), cudaMemcpyDeviceToHost, c.s));
-            c.sync();
-            memcpy(&neig, c.hscal, sizeof(int));
+            a.irl = 0; a.small_side = 0; a.tol = tol; a.wz = c.wz;
+            neig = analyse(c, a);
         }
         if (ierr < 0) {
             if (j < k) *info = j;
