@@ -65,7 +65,9 @@ struct Csr {
     int nblk = 0;             // row blocks
     int *blk = nullptr;       // nblk+1 row boundaries
     int segs = 0;             // thin matrices: segments per row for the split reduction
+    int short_rows = 0;       // 1: lane-per-row SpMV schedule (mean row length below SHORT_MEAN)
 };
+constexpr int SHORT_MEAN = 16;
 
 // A = S + L diag(w) R'.  fwd = [S | L] (m x (n+r)), adj = [S' | R]
 // (n x (m+r)); thin_r = R' (r x n), thin_l = L' (r x m).
@@ -107,6 +109,7 @@ struct LbCtl {
     int elr_active, elr_iter;
     double elr_s;           // ELR inner product for the coming iteration
     int reorth_active, reorth_iter, reorth_count;
+    int cgs_phase;          // 0: the next CGS kernel forms the projections, 1: it applies them
     double reorth_nrm0;
     int nsel;               // columns selected for reorthogonalisation
     int collapsed;          // the last reorthogonalisation zeroed the vector

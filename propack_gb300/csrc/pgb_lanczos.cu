@@ -7,9 +7,10 @@
 //   k_lb_spmv     fused SpMV + axpy with the previous vector + partial
 //                 sums of ||y||^2 and <prev, y>  (dlanbpro.F:288-296, :420-424)
 //   k_lb_elr      one extended-local-reorthogonalisation pass (:301-316, :429-443)
-//   k_lb_cgs_dots first classical Gram-Schmidt projection (dreorth.F:174)
-//   k_lb_cgs_upd  v -= W h fused with the projections of the updated
-//                 vector for the next pass (dreorth.F:85-95, dcgs :199)
+//   k_lb_cgs_dots projections of one classical Gram-Schmidt pass
+//                 (dreorth.F:174)
+//   k_lb_cgs_upd  v -= W h and ||v||^2 (dreorth.F:85-95, dcgs :199);
+//                 a second pass (the iterated refinement) repeats the pair
 //
 // Every kernel ends with a last-CTA tail that reduces the partial sums in a
 // fixed order and runs the scalar logic of dlanbpro on the device: the
@@ -244,6 +245,7 @@ __device__ void v_reorth_decide(Tail &t, const LbArgs &a, int j)
                 c.reorth_active = 1;
                 c.reorth_iter = 0;
                 c.reorth_nrm0 = c.alpha;
+                c.cgs_phase = 0;
                 t.go = 0;
             }
         }
@@ -327,6 +329,7 @@ __device__ void u_reorth_decide(Tail &t, const LbArgs &a, int j)
             c.reorth_active = 1;
             c.reorth_iter = 0;
             c.reorth_nrm0 = c.beta;
+            c.cgs_phase = 0;
             t.go = 0;
         }
     }
@@ -481,7 +484,7 @@ __device__ void after_cgs(Tail &t, const LbArgs &a, int j, double nrm, int last)
         if (SIDE == 0) { v_post_reorth(t, a, j); v_post(t, a, j); }
         else { u_post_reorth(t, a, j); u_post(t, a, j); }
     } else if (t.go == 2) {
-        reduce_cols(a, t.c.nsel);
+        if (threadIdx.x == 0) t.c.cgs_phase = 0;  // the next pass starts with its projections
     }
 }
 
@@ -531,7 +534,7 @@ __global__ void __launch_bounds__(BS) k_lb_spmv(LbArgs a, int j, int host_produc
     auto pre = [&](int r) -> double { return has_prev ? (double)prev[r] : 0.0; };
     if (!host_product) {
         auto xl = [&](int c) -> T { return c < n0 ? x[c] : (T)z[c - n0]; };
-        csr_rows<T, T>(A.ptr, A.idx, csr_vals<T>(A), A.blk, A.nblk, xl, pre, epi, st);
+        csr_spmv<T, T>(A, csr_vals<T>(A), xl, pre, epi, st);
     } else {
         // the caller's APROD already wrote the product into out
         for (int r = blockIdx.x * BS + threadIdx.x; r < A.rows; r += gridDim.x * BS) epi(r, (double)out[r], pre(r));
@@ -584,65 +587,129 @@ __global__ void __launch_bounds__(BS) k_lb_elr(LbArgs a, int j)
     }
 }
 
-// projections W(:,sel)' x: each CTA owns a contiguous row chunk, each warp
-// a subset of the columns.
+// 16-byte vectors of the Lanczos type: 4 floats or 2 doubles
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using V = float4;
+    static constexpr int W = 4;
+    __device__ static __forceinline__ float get(const V &v, int i)
+    {
+        return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+    }
+    __device__ static __forceinline__ void fms(V &x, const V &w, float h)
+    {
+        x.x = fmaf(-w.x, h, x.x);
+        x.y = fmaf(-w.y, h, x.y);
+        x.z = fmaf(-w.z, h, x.z);
+        x.w = fmaf(-w.w, h, x.w);
+    }
+};
+template <>
+struct Vec16<double> {
+    using V = double2;
+    static constexpr int W = 2;
+    __device__ static __forceinline__ double get(const V &v, int i) { return i == 0 ? v.x : v.y; }
+    __device__ static __forceinline__ void fms(V &x, const V &w, double h)
+    {
+        x.x = fma(-w.x, h, x.x);
+        x.y = fma(-w.y, h, x.y);
+    }
+};
+
+// projections h = W(:,sel)' x (dreorth.F:174, the dgemv('T') of dcgs):
+// each CTA owns a contiguous chunk of 16-byte row vectors; each warp takes
+// four columns at a time and streams the chunk once for them, so every x
+// vector it loads serves four columns (ten 16-byte loads in flight per
+// lane).  The last CTA also takes the rows past the last whole vector.
+constexpr int DOT_COLS = 4;
 template <int SIDE, typename T>
 __global__ void __launch_bounds__(BS) k_lb_cgs_dots(LbArgs a, int j)
 {
+    using VT = Vec16<T>;
+    using V = typename VT::V;
     __shared__ Tail t;
-    if (a.ctl->status != 0 || !a.ctl->reorth_active) return;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 0) return;
     const int L = a.ctl->nsel;
     const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
     const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
     const T *W = (const T *)(SIDE == 0 ? a.V : a.U);
     const T *x = SIDE == 0 ? vcol<T>(a, j - 1) : ucol<T>(a, j);
-    const int chunk = (len + gridDim.x - 1) / gridDim.x;
-    const int r0 = blockIdx.x * chunk, r1 = min(len, r0 + chunk);
+    const int nvec = len / VT::W;
+    const int chunk = (nvec + gridDim.x - 1) / gridDim.x;
+    const int v0 = blockIdx.x * chunk, v1 = min(nvec, v0 + chunk);
+    const bool tail_rows = blockIdx.x == gridDim.x - 1;
+    const V *xv = reinterpret_cast<const V *>(x);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int c = w; c < L; c += BS / 32) {
-        const T *col = W + (size_t)a.sel[c] * ld;
-        Acc<T> acc0, acc1, acc2, acc3;
-        int r = r0 + lane;
-        for (; r + 96 < r1; r += 128) {
-            acc0.add_prod(col[r], x[r]);
-            acc1.add_prod(col[r + 32], x[r + 32]);
-            acc2.add_prod(col[r + 64], x[r + 64]);
-            acc3.add_prod(col[r + 96], x[r + 96]);
+    for (int c0 = w * DOT_COLS; c0 < L; c0 += (BS / 32) * DOT_COLS) {
+        const int nc = min(DOT_COLS, L - c0);
+        const T *col[DOT_COLS];
+#pragma unroll
+        for (int u = 0; u < DOT_COLS; u++) col[u] = W + (size_t)a.sel[c0 + (u < nc ? u : 0)] * ld;
+        Acc<T> acc[DOT_COLS][2];
+        int v = v0 + lane;
+        for (; v + 32 < v1; v += 64) {
+            const V x0 = xv[v], x1 = xv[v + 32];
+            V w0[DOT_COLS], w1[DOT_COLS];
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) {
+                w0[u] = reinterpret_cast<const V *>(col[u])[v];
+                w1[u] = reinterpret_cast<const V *>(col[u])[v + 32];
+            }
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++)
+#pragma unroll
+                for (int q = 0; q < VT::W; q++) {
+                    acc[u][0].add_prod(VT::get(w0[u], q), VT::get(x0, q));
+                    acc[u][1].add_prod(VT::get(w1[u], q), VT::get(x1, q));
+                }
         }
-        for (; r < r1; r += 32) acc0.add_prod(col[r], x[r]);
-        double acc = (acc0.value() + acc1.value()) + (acc2.value() + acc3.value());
-        acc = warp_sum(acc);
-        if (lane == 0) a.part_cols[(size_t)c * a.nb + blockIdx.x] = acc;
+        if (v < v1) {
+            const V x0 = xv[v];
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) {
+                const V w0 = reinterpret_cast<const V *>(col[u])[v];
+#pragma unroll
+                for (int q = 0; q < VT::W; q++) acc[u][0].add_prod(VT::get(w0, q), VT::get(x0, q));
+            }
+        }
+        if (tail_rows)
+            for (int r = nvec * VT::W + lane; r < len; r += 32)
+#pragma unroll
+                for (int u = 0; u < DOT_COLS; u++) acc[u][1].add_prod(col[u][r], x[r]);
+#pragma unroll
+        for (int u = 0; u < DOT_COLS; u++) {
+            const double sum = warp_sum(acc[u][0].value() + acc[u][1].value());
+            if (lane == 0 && u < nc) a.part_cols[(size_t)(c0 + u) * a.nb + blockIdx.x] = sum;
+        }
     }
     if (last_cta(&a.ctl->ticket)) {
         tail_load(a, t);
         reduce_cols(a, L);
+        if (threadIdx.x == 0) t.c.cgs_phase = 1;
         tail_store(a, t);
     }
 }
 
-// x -= W(:,sel) h, then the projections of the new x for the next pass.
-// CPW > 0: each warp owns columns w, w+8, ..., w+8*(CPW-1) and every lane
-// keeps one register accumulator per owned column across all of the CTA's
-// row tiles (one FMA per element, one warp reduction per column per CTA).
-// CPW == 0: any number of columns, one warp reduction per column per tile
-// (used when the selection can exceed 8*24 columns).
-constexpr int CGS_TR = 64;
-template <int SIDE, int CPW, typename T>
+// x -= W(:,sel) h (dreorth.F:85-95, the dgemv('N') of dcgs) and ||x||^2:
+// one 16-byte row vector per thread and step, the selected columns streamed
+// with CGS_UNROLL loads in flight; h and the selection sit in shared memory.
+constexpr int CGS_UNROLL = 8;
+template <int SIDE, typename T>
 __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
 {
-    extern __shared__ double dyn[];  // h[L] | acc[L] | sel[L] (ints)
-    __shared__ T red4[4][CGS_TR];
-    __shared__ T xn[CGS_TR];
+    using VT = Vec16<T>;
+    using V = typename VT::V;
+    extern __shared__ double dyn[];  // h[L] (as T, one double slot each) | sel[L]
     __shared__ double sred[32];
     __shared__ Tail t;
-    if (a.ctl->status != 0 || !a.ctl->reorth_active) return;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 1) return;
     const int L = a.ctl->nsel;
-    double *hs = dyn, *acc = dyn + L;
-    int *ssel = reinterpret_cast<int *>(dyn + 2 * L);
+    T *hs = reinterpret_cast<T *>(dyn);
+    int *ssel = reinterpret_cast<int *>(dyn + L);
     for (int c = threadIdx.x; c < L; c += BS) {
-        hs[c] = a.h[c];
-        acc[c] = 0.0;
+        hs[c] = (T)a.h[c];
         ssel[c] = a.sel[c];
     }
     __syncthreads();
@@ -650,69 +717,32 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
     const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
     const T *W = (const T *)(SIDE == 0 ? a.V : a.U);
     T *x = SIDE == 0 ? vcol<T>(a, j - 1) : ucol<T>(a, j);
-    const int chunk = (len + gridDim.x - 1) / gridDim.x;
-    const int r0 = blockIdx.x * chunk, r1 = min(len, r0 + chunk);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int rr = threadIdx.x % CGS_TR, g = threadIdx.x / CGS_TR;
+    V *xv = reinterpret_cast<V *>(x);
+    const int nvec = len / VT::W;
     Acc<T> sq;
-    Acc<T> accr[CPW > 0 ? CPW : 1];
-    for (int tb = r0; tb < r1; tb += CGS_TR) {
-        const int r = tb + rr;
-        T p0 = 0, p1 = 0;
-        if (r < r1) {
-            int c = g;
-            for (; c + 4 < L; c += 8) {
-                p0 = fma(W[(size_t)ssel[c] * ld + r], (T)hs[c], p0);
-                p1 = fma(W[(size_t)ssel[c + 4] * ld + r], (T)hs[c + 4], p1);
-            }
-            if (c < L) p0 = fma(W[(size_t)ssel[c] * ld + r], (T)hs[c], p0);
-        }
-        red4[g][rr] = p0 + p1;
-        __syncthreads();
-        if (g == 0) {
-            T v = 0;
-            if (r < r1) {
-                v = x[r] - (((red4[0][rr] + red4[1][rr]) + red4[2][rr]) + red4[3][rr]);
-                x[r] = v;
-                sq.add_prod(v, v);
-            }
-            xn[rr] = v;
-        }
-        __syncthreads();
-        const int ra = tb + lane, rb = tb + lane + 32;
-        const T xa = xn[lane], xb = xn[lane + 32];
-        if (CPW > 0) {
+    for (int v = blockIdx.x * BS + threadIdx.x; v < nvec; v += gridDim.x * BS) {
+        V acc = xv[v];
+        int c = 0;
+        for (; c + CGS_UNROLL <= L; c += CGS_UNROLL) {
+            V wv[CGS_UNROLL];
 #pragma unroll
-            for (int q = 0; q < (CPW > 0 ? CPW : 1); q++) {
-                const int c = w + 8 * q;
-                if (c < L) {
-                    const T *col = W + (size_t)ssel[c] * ld;
-                    if (ra < r1) accr[q].add_prod(col[ra], xa);
-                    if (rb < r1) accr[q].add_prod(col[rb], xb);
-                }
-            }
-        } else {
-            for (int c = w; c < L; c += BS / 32) {
-                const T *col = W + (size_t)ssel[c] * ld;
-                Acc<T> v;
-                if (ra < r1) v.add_prod(col[ra], xa);
-                if (rb < r1) v.add_prod(col[rb], xb);
-                const double vv = warp_sum(v.value());
-                if (lane == 0) acc[c] += vv;
-            }
-        }
-        __syncthreads();
-    }
-    if (CPW > 0) {
+            for (int u = 0; u < CGS_UNROLL; u++) wv[u] = reinterpret_cast<const V *>(W + (size_t)ssel[c + u] * ld)[v];
 #pragma unroll
-        for (int q = 0; q < (CPW > 0 ? CPW : 1); q++) {
-            const int c = w + 8 * q;
-            const double v = warp_sum(accr[q].value());
-            if (c < L && lane == 0) acc[c] = v;
+            for (int u = 0; u < CGS_UNROLL; u++) VT::fms(acc, wv[u], hs[c + u]);
         }
-        __syncthreads();
+        for (; c < L; c++) VT::fms(acc, reinterpret_cast<const V *>(W + (size_t)ssel[c] * ld)[v], hs[c]);
+        xv[v] = acc;
+#pragma unroll
+        for (int q = 0; q < VT::W; q++) sq.add_prod(VT::get(acc, q), VT::get(acc, q));
     }
-    for (int c = threadIdx.x; c < L; c += BS) a.part_cols[(size_t)c * a.nb + blockIdx.x] = acc[c];
+    if (blockIdx.x == gridDim.x - 1) {
+        for (int r = nvec * VT::W + threadIdx.x; r < len; r += BS) {
+            T y = x[r];
+            for (int c = 0; c < L; c++) y = fma(-W[(size_t)ssel[c] * ld + r], hs[c], y);
+            x[r] = y;
+            sq.add_prod(y, y);
+        }
+    }
     const double sq2 = block_sum<BS>(sq.value(), sred);
     if (threadIdx.x == 0) a.part_sq[blockIdx.x] = sq2;
     if (last_cta(&a.ctl->ticket)) {
@@ -749,20 +779,16 @@ __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
 
 // ------------------------------------------------------------ host side
 template <typename T>
-static size_t cgs_smem(const LbArgs &a) { return (sizeof(double) * 2 + sizeof(int)) * (size_t)(a.kmax + 1) + 16; }
+static size_t cgs_smem(const LbArgs &a) { return (sizeof(double) + sizeof(int)) * (size_t)(a.kmax + 1) + 16; }
 
 template <int SIDE, typename T>
 static void set_upd_limits(size_t need)
 {
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 0, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 4, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 8, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 16, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, 24, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd<SIDE, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
 }
 void lb_set_smem_limits(int kmax)
 {
-    const size_t need = (sizeof(double) * 2 + sizeof(int)) * (size_t)(kmax + 1) + 16;
+    const size_t need = (sizeof(double) + sizeof(int)) * (size_t)(kmax + 1) + 16;
     if (need > 48 * 1024) {
         set_upd_limits<0, double>(need);
         set_upd_limits<1, double>(need);
@@ -771,18 +797,16 @@ void lb_set_smem_limits(int kmax)
     }
 }
 
-// one CGS update pass; the template is chosen from an upper bound of the
-// number of selected columns (j-1 on the V side, j on the U side)
+// one CGS pass: the projections, then the update (each kernel returns at
+// once when the control block says that its half of the pass is not due)
 template <int SIDE, typename T>
-static void launch_upd(const LbArgs &a, int j, int last, int maxcols, cudaStream_t s)
+static void launch_cgs_pass(const LbArgs &a, int j, int last, cudaStream_t s)
 {
-    const size_t sm = cgs_smem<T>(a);
-    const int cpw = (maxcols + 7) / 8;
-    if (cpw <= 4) k_lb_cgs_upd<SIDE, 4, T><<<a.nb, BS, sm, s>>>(a, j, last);
-    else if (cpw <= 8) k_lb_cgs_upd<SIDE, 8, T><<<a.nb, BS, sm, s>>>(a, j, last);
-    else if (cpw <= 16) k_lb_cgs_upd<SIDE, 16, T><<<a.nb, BS, sm, s>>>(a, j, last);
-    else if (cpw <= 24) k_lb_cgs_upd<SIDE, 24, T><<<a.nb, BS, sm, s>>>(a, j, last);
-    else k_lb_cgs_upd<SIDE, 0, T><<<a.nb, BS, sm, s>>>(a, j, last);
+    PGB_PROF(sizeof(T) == 8 ? PK_CGS_DOTS : PK_CGS_DOTS32, s, k_lb_cgs_dots<SIDE, T><<<a.nb, BS, 0, s>>>(a, j));
+    PGB_LAUNCHED();
+    PGB_PROF(sizeof(T) == 8 ? PK_CGS_UPD : PK_CGS_UPD32, s,
+             k_lb_cgs_upd<SIDE, T><<<a.nb, BS, cgs_smem<T>(a), s>>>(a, j, last));
+    PGB_LAUNCHED();
 }
 
 // one wave of CTAs at the fused SpMV's occupancy (partials are summed over gridDim)
@@ -816,12 +840,7 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
                 PGB_PROF(PK_ELR, s, k_lb_elr<0, T><<<nb, BS, 0, s>>>(a, j));
                 PGB_LAUNCHED();
             }
-        PGB_PROF(sizeof(T) == 8 ? PK_CGS_DOTS : PK_CGS_DOTS32, s, k_lb_cgs_dots<0, T><<<nb, BS, 0, s>>>(a, j));
-        PGB_LAUNCHED();
-        for (int i = 0; i < ntry_spec; i++) {
-            PGB_PROF(sizeof(T) == 8 ? PK_CGS_UPD : PK_CGS_UPD32, s, (launch_upd<0, T>(a, j, i == ntry_spec - 1, j - 1, s)));
-            PGB_LAUNCHED();
-        }
+        for (int i = 0; i < ntry_spec; i++) launch_cgs_pass<0, T>(a, j, i == ntry_spec - 1, s);
     } else {
         if (!host_product && op && op->r > 0)
             PGB_PROF(PK_THIN, s, op_thin<T>(*op, false, vcol<T>(a, j - 1), s));
@@ -832,12 +851,7 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
             PGB_PROF(PK_ELR, s, k_lb_elr<1, T><<<nb, BS, 0, s>>>(a, j));
             PGB_LAUNCHED();
         }
-        PGB_PROF(sizeof(T) == 8 ? PK_CGS_DOTS : PK_CGS_DOTS32, s, k_lb_cgs_dots<1, T><<<nb, BS, 0, s>>>(a, j));
-        PGB_LAUNCHED();
-        for (int i = 0; i < ntry_spec; i++) {
-            PGB_PROF(sizeof(T) == 8 ? PK_CGS_UPD : PK_CGS_UPD32, s, (launch_upd<1, T>(a, j, i == ntry_spec - 1, j, s)));
-            PGB_LAUNCHED();
-        }
+        for (int i = 0; i < ntry_spec; i++) launch_cgs_pass<1, T>(a, j, i == ntry_spec - 1, s);
     }
 }
 
@@ -846,9 +860,8 @@ template <typename T>
 void lb_enqueue_cgs_more(const LbArgs &a, int side, int j, int passes, cudaStream_t s)
 {
     for (int i = 0; i < passes; i++) {
-        if (side == 0) launch_upd<0, T>(a, j, i == passes - 1, j - 1, s);
-        else launch_upd<1, T>(a, j, i == passes - 1, j, s);
-        PGB_LAUNCHED();
+        if (side == 0) launch_cgs_pass<0, T>(a, j, i == passes - 1, s);
+        else launch_cgs_pass<1, T>(a, j, i == passes - 1, s);
     }
 }
 

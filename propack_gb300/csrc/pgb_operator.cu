@@ -210,6 +210,7 @@ static void build_blocks(Csr &A, cudaStream_t s)
 {
     int *flag = nullptr, *pos = nullptr;
     const int rows = A.rows;
+    A.short_rows = rows > 0 && A.nnz < (int64_t)SHORT_MEAN * rows;
     PGB_CUDA(cudaMallocAsync(&flag, sizeof(int) * (rows + 1), s));
     PGB_CUDA(cudaMallocAsync(&pos, sizeof(int) * (rows + 1), s));
     const int g = std::min(4096, std::max(1, (rows + 255) / 256));
@@ -476,7 +477,7 @@ __global__ void __launch_bounds__(BS) k_spmv_plain(Csr A, const T *__restrict__ 
     auto xl = [&](int c) -> T { return c < n0 ? __ldg(x + c) : (T)z[c - n0]; };
     auto pre = [&](int r) -> double { return 0.0; };
     auto epi = [&](int r, double acc, double) { y[r] = (T)acc; };
-    csr_rows<T, T>(A.ptr, A.idx, plain_vals<T>(A), A.blk, A.nblk, xl, pre, epi, st);
+    csr_spmv<T, T>(A, plain_vals<T>(A), xl, pre, epi, st);
 }
 
 // one wave of CTAs at the kernel's occupancy

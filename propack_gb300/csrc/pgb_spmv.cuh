@@ -1,25 +1,33 @@
-// pgb_spmv.cuh -- the CSR-stream sparse matrix-vector core shared by the
-// plain operator application and the fused Lanczos steps.
+// pgb_spmv.cuh -- the CSR sparse matrix-vector cores shared by the plain
+// operator application and the fused Lanczos steps.  Two row schedules,
+// chosen per matrix when the operator is built (Csr::short_rows):
 //
-// Row blocks (built once per matrix) hold at most ROWS_W rows and NNZ_W
-// nonzeros, or one long row.  Each warp owns whole blocks and works without
-// CTA barriers: every lane issues all of its (index, value) loads for the
-// block, then all of its gathers x[index] (one HBM and one L2 round trip
-// per block, many requests in flight), and parks value and gathered input
-// in its warp's slice of shared memory.  g lanes per row (g = 32 / rows in
-// the block, a power of two) then form the row sums from shared memory; with
-// ~20-nonzero rows g is 1 or 2, so the FP64 pipe issues about one FMA per
-// nonzero and almost no shuffle adds.  A long row is streamed by the whole
-// warp straight from global memory.  Summation order depends only on the
-// matrix, never on timing, so results are bit-reproducible.
+// staged (rows of ~16 and more nonzeros): row blocks of at most ROWS_W rows
+//   and NNZ_W nonzeros, or one long row.  Each warp owns whole blocks and
+//   works without CTA barriers: every lane issues all of its (index, value)
+//   loads for the block, then all of its gathers x[index], and parks value
+//   and gathered input in its warp's slice of shared memory.  g lanes per
+//   row (g = 32 / rows in the block, a power of two) then form the row sums
+//   from shared memory.  A long row is streamed by the whole warp.
+//
+// short (most rows shorter than ~16): a warp takes 32 consecutive rows, one
+//   lane per row; each lane walks its row in order with four (index, value)
+//   pairs and four gathers in flight, so an instruction per nonzero and
+//   lane is all the row costs.  Rows longer than SHORT_MAX are skipped by
+//   their lane and streamed afterwards by the whole warp.
+//
+// Summation order depends only on the matrix, never on timing, so results
+// are bit-reproducible.
 #pragma once
 #include "pgb.cuh"
 
 namespace pgb {
 
 constexpr int SPMV_WARPS = BS / 32;  // warps per CTA
+constexpr int SHORT_MAX = 48;        // longest row a lane sums alone (short schedule)
 
-// One warp's shared-memory stage: the block's values and gathered inputs.
+// One warp's shared-memory stage of the staged schedule: the block's
+// values and gathered inputs.
 template <typename VT, typename AT>
 struct SpmvStage {
     VT val[NNZ_W];
@@ -29,18 +37,12 @@ struct SpmvStage {
 constexpr int SPMV_PER_LANE = NNZ_W / 32;  // staged nonzeros per lane
 
 // Visit every row; epi(row, sum, pre) is called by exactly one lane per row,
-// where pre = pre_load(row) was issued early (with the block's own loads) so
+// where pre = pre_load(row) was issued early (with the row's own loads) so
 // that per-row epilogue inputs never add a round trip.  xload(col) returns
 // the gathered input for a column.  AT is the accumulation type (double for
 // the FP64 path, float for FP32).
-//
-// Per block each lane issues, all at once, its (index, value) loads, the
-// row pointer and the pre_load of "its" row (lane l owns row r0+l), and the
-// bounds of the warp's next block; then all of its gathers.  So a block
-// costs one HBM and one L2 round trip; the row sums read shared memory and
-// row bounds / pre values arrive by warp shuffles.
 template <typename VT, typename AT, typename XF, typename PF, typename EPI>
-__device__ __forceinline__ void csr_rows(const int *__restrict__ ptr, const int *__restrict__ idx,
+__device__ __forceinline__ void csr_rows_staged(const int *__restrict__ ptr, const int *__restrict__ idx,
                                          const VT *__restrict__ val, const int *__restrict__ blk,
                                          int nblk, XF xload, PF pre_load, EPI epi, SpmvStage<VT, AT> *stages)
 {
@@ -127,6 +129,89 @@ __device__ __forceinline__ void csr_rows(const int *__restrict__ ptr, const int 
             e0 = ptr[r0]; e1 = ptr[r1];
         }
     }
+}
+
+
+// the short-row schedule (see the top of the file).  Each round a lane
+// loads up to SHORT_UNROLL (index, value) pairs of its row at once, then
+// all their gathers; the warp repeats rounds while any short row has
+// entries left.  The next tile's row bounds are loaded with the current one.
+constexpr int SHORT_UNROLL = 4;
+template <typename VT, typename AT, typename XF, typename PF, typename EPI>
+__device__ __forceinline__ void csr_rows_short(const int *__restrict__ ptr, const int *__restrict__ idx,
+                                               const VT *__restrict__ val, int nrows, XF xload, PF pre_load,
+                                               EPI epi)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * SPMV_WARPS;
+    const int ntiles = (nrows + 31) / 32;
+    int tile = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
+    if (tile >= ntiles) return;
+    int r = tile * 32 + lane;
+    int e0 = r < nrows ? ptr[r] : 0;
+    int e1 = r < nrows ? ptr[r + 1] : 0;
+    while (true) {
+        const bool valid = r < nrows;
+        const double pre = valid ? pre_load(r) : 0.0;
+        // bounds of the next tile, in flight with this one
+        const int ntile = tile + nwarps;
+        const int nr = ntile * 32 + lane;
+        int n0 = 0, n1 = 0;
+        if (ntile < ntiles && nr < nrows) { n0 = ptr[nr]; n1 = ptr[nr + 1]; }
+        const bool lng = e1 - e0 > SHORT_MAX;
+        const int lim = lng ? e0 : e1;
+        AT acc = 0;
+        for (int e = e0; __any_sync(FULL, e < lim); e += SHORT_UNROLL) {
+            int c[SHORT_UNROLL];
+            VT v[SHORT_UNROLL];
+#pragma unroll
+            for (int u = 0; u < SHORT_UNROLL; u++) {
+                c[u] = 0;
+                v[u] = 0;
+                if (e + u < lim) { c[u] = idx[e + u]; v[u] = val[e + u]; }
+            }
+            AT x[SHORT_UNROLL];
+#pragma unroll
+            for (int u = 0; u < SHORT_UNROLL; u++) x[u] = (e + u < lim) ? (AT)xload(c[u]) : (AT)0;
+#pragma unroll
+            for (int u = 0; u < SHORT_UNROLL; u++)
+                if (e + u < lim) acc = fma((AT)v[u], x[u], acc);
+        }
+        unsigned todo = __ballot_sync(FULL, lng);
+        while (todo) {
+            const int l = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int f0 = __shfl_sync(FULL, e0, l), f1 = __shfl_sync(FULL, e1, l);
+            AT s = 0;
+            int e = f0 + lane;
+            for (; e + 96 < f1; e += 128) {
+                const int c0 = idx[e], c1 = idx[e + 32], c2 = idx[e + 64], c3 = idx[e + 96];
+                const VT v0 = val[e], v1 = val[e + 32], v2 = val[e + 64], v3 = val[e + 96];
+                const AT x0 = (AT)xload(c0), x1 = (AT)xload(c1), x2 = (AT)xload(c2), x3 = (AT)xload(c3);
+                s = fma((AT)v0, x0, s);
+                s = fma((AT)v1, x1, s);
+                s = fma((AT)v2, x2, s);
+                s = fma((AT)v3, x3, s);
+            }
+            for (; e < f1; e += 32) s = fma((AT)val[e], (AT)xload(idx[e]), s);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+            if (lane == l) acc = s;
+        }
+        if (valid) epi(r, (double)acc, pre);
+        tile = ntile;
+        if (tile >= ntiles) break;
+        r = nr; e0 = n0; e1 = n1;
+    }
+}
+
+// the schedule chosen for the matrix
+template <typename VT, typename AT, typename XF, typename PF, typename EPI>
+__device__ __forceinline__ void csr_spmv(const Csr &A, const VT *__restrict__ val, XF xload, PF pre_load, EPI epi,
+                                         SpmvStage<VT, AT> *stages)
+{
+    if (A.short_rows) csr_rows_short<VT, AT>(A.ptr, A.idx, val, A.rows, xload, pre_load, epi);
+    else csr_rows_staged<VT, AT>(A.ptr, A.idx, val, A.blk, A.nblk, xload, pre_load, epi, stages);
 }
 
 }  // namespace pgb
