@@ -328,6 +328,10 @@ void launch_ritz_prep_qr(const RitzArgs &a, cudaStream_t s);
 template <typename T>
 void gemm(int mr, int nc, int kk, const T *A, int lda, bool ta, const double *B, int ldb, bool tb, T *C, int ldc,
           cudaStream_t s);
+// FP64 C = A op(B) on the BF16 tensor cores (error-free digit split); false
+// when the shape is outside its range (then the caller uses the FP64 kernel)
+bool gemm_f64_tc(int mr, int nc, int kk, const double *A, int lda, const double *B, int ldb, bool tb, double *C,
+                 int ldc, cudaStream_t s);
 template <typename T>
 void copy_cols(const T *src, int lds, T *dst, int ldd, int rows, int cols, cudaStream_t s);
 

@@ -1031,6 +1031,9 @@ void gemm(int mr, int nc, int kk, const T *A, int lda, bool ta, const double *B,
           cudaStream_t s)
 {
     if (mr <= 0 || nc <= 0) return;
+    if (sizeof(T) == sizeof(double) && !ta &&
+        gemm_f64_tc(mr, nc, kk, (const double *)A, lda, B, ldb, tb, (double *)C, ldc, s))
+        return;
     dim3 grid((mr + 63) / 64, (nc + 63) / 64);
     PGB_PROF(PK_GEMM, s, k_gemm<T><<<grid, 256, 0, s>>>(mr, nc, kk, A, lda, ta ? 1 : 0, B, ldb, tb ? 1 : 0, C, ldc));
     PGB_LAUNCHED();

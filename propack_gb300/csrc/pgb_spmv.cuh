@@ -132,11 +132,7 @@ __device__ __forceinline__ void csr_rows_staged(const int *__restrict__ ptr, con
 }
 
 
-// the short-row schedule (see the top of the file).  Each round a lane
-// loads up to SHORT_UNROLL (index, value) pairs of its row at once, then
-// all their gathers; the warp repeats rounds while any short row has
-// entries left.  The next tile's row bounds are loaded with the current one.
-constexpr int SHORT_UNROLL = 4;
+// the short-row schedule (see the top of the file)
 template <typename VT, typename AT, typename XF, typename PF, typename EPI>
 __device__ __forceinline__ void csr_rows_short(const int *__restrict__ ptr, const int *__restrict__ idx,
                                                const VT *__restrict__ val, int nrows, XF xload, PF pre_load,
@@ -146,37 +142,26 @@ __device__ __forceinline__ void csr_rows_short(const int *__restrict__ ptr, cons
     const int lane = threadIdx.x & 31;
     const int nwarps = gridDim.x * SPMV_WARPS;
     const int ntiles = (nrows + 31) / 32;
-    int tile = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
-    if (tile >= ntiles) return;
-    int r = tile * 32 + lane;
-    int e0 = r < nrows ? ptr[r] : 0;
-    int e1 = r < nrows ? ptr[r + 1] : 0;
-    while (true) {
+    for (int tile = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5); tile < ntiles; tile += nwarps) {
+        const int r = tile * 32 + lane;
         const bool valid = r < nrows;
+        const int e0 = valid ? ptr[r] : 0;
+        const int e1 = valid ? ptr[r + 1] : 0;
         const double pre = valid ? pre_load(r) : 0.0;
-        // bounds of the next tile, in flight with this one
-        const int ntile = tile + nwarps;
-        const int nr = ntile * 32 + lane;
-        int n0 = 0, n1 = 0;
-        if (ntile < ntiles && nr < nrows) { n0 = ptr[nr]; n1 = ptr[nr + 1]; }
         const bool lng = e1 - e0 > SHORT_MAX;
-        const int lim = lng ? e0 : e1;
         AT acc = 0;
-        for (int e = e0; __any_sync(FULL, e < lim); e += SHORT_UNROLL) {
-            int c[SHORT_UNROLL];
-            VT v[SHORT_UNROLL];
-#pragma unroll
-            for (int u = 0; u < SHORT_UNROLL; u++) {
-                c[u] = 0;
-                v[u] = 0;
-                if (e + u < lim) { c[u] = idx[e + u]; v[u] = val[e + u]; }
+        if (!lng) {
+            int e = e0;
+            for (; e + 3 < e1; e += 4) {
+                const int c0 = idx[e], c1 = idx[e + 1], c2 = idx[e + 2], c3 = idx[e + 3];
+                const VT v0 = val[e], v1 = val[e + 1], v2 = val[e + 2], v3 = val[e + 3];
+                const AT x0 = (AT)xload(c0), x1 = (AT)xload(c1), x2 = (AT)xload(c2), x3 = (AT)xload(c3);
+                acc = fma((AT)v0, x0, acc);
+                acc = fma((AT)v1, x1, acc);
+                acc = fma((AT)v2, x2, acc);
+                acc = fma((AT)v3, x3, acc);
             }
-            AT x[SHORT_UNROLL];
-#pragma unroll
-            for (int u = 0; u < SHORT_UNROLL; u++) x[u] = (e + u < lim) ? (AT)xload(c[u]) : (AT)0;
-#pragma unroll
-            for (int u = 0; u < SHORT_UNROLL; u++)
-                if (e + u < lim) acc = fma((AT)v[u], x[u], acc);
+            for (; e < e1; e++) acc = fma((AT)val[e], (AT)xload(idx[e]), acc);
         }
         unsigned todo = __ballot_sync(FULL, lng);
         while (todo) {
@@ -199,9 +184,6 @@ __device__ __forceinline__ void csr_rows_short(const int *__restrict__ ptr, cons
             if (lane == l) acc = s;
         }
         if (valid) epi(r, (double)acc, pre);
-        tile = ntile;
-        if (tile >= ntiles) break;
-        r = nr; e0 = n0; e1 = n1;
     }
 }
 

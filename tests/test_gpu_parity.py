@@ -151,6 +151,25 @@ def test_vs_oracle_same_trajectory(golden, opts, irl):
     op.close()
 
 
+@pytest.mark.parametrize("irl", [True, False])
+def test_tall_bases_vs_oracle(irl):
+    """m, n >= 4096: the restart and Ritz products run on the tensor cores
+    (the FP64 digit-split GEMM); results stay within the FP64 tolerances."""
+    S, L, R, w = workloads.lowrank_irl(seed=11, m=9000, n=5000, nnz_row=6, rank=8, udens=0.02, vdens=0.05)
+    op = pg.CsrOperator(S, L, R, w)
+    oop = oracle.Operator(S, L, R, w)
+    kw = dict(irl_mode=irl, kmax=40 if irl else 90, tol=1e-10)
+    u, s, vt, bnd = pg.svdp(op, 12, rng=rng0(), **kw)
+    uo, so, vto, bo, info, kc = oracle.svdp(None, 12, rng=rng0(), op=oop, **kw)
+    assert info == 0 and kc == 12
+    np.testing.assert_allclose(s, so, rtol=SIG_RTOL)
+    assert subspace_err(u, uo) < VEC_TOL
+    assert subspace_err(vt.T, vto.T) < VEC_TOL
+    res = max(np.linalg.norm(op.matvec(vt[i]) - s[i] * u[:, i]) for i in range(12))
+    assert res < 1e-9 * s[0]
+    op.close()
+
+
 def test_zero_start_vector_uses_dlarnv(golden):
     """v0 = 0 makes the driver draw PROPACK's own dlarnv start vector (dgetu0)."""
     A = csr_from(golden, "plain")
