@@ -169,6 +169,36 @@ int propack_get_precision(void);
 void propack_set_profiling(int on);
 int propack_get_profile(double *total_ms, int64_t *launches, int n);
 
+/* ---- Learned start vector (no reference counterpart) ----------------
+ * A row-wise MLP (18 -> 256 -> 256 -> 1, ReLU; BF16 weights, FP32
+ * accumulation) that proposes the start vector U(:,1) in place of dgetu0's
+ * random one (double/dgetu0.F:11-89) for a family of related matrices.
+ * Features of row i: log1p(nnz)/4, ||y_i||/rho and 2 y_i/rho for the
+ * 16-column Gaussian sketch y = A*Omega (Omega drawn from `seed` by a
+ * counter-based generator; rho = RMS of ||y_i||).  Training minimises
+ * -(1/k) sum_j log(c_j^2 + 1e-4 ||u0||^2/k) + log ||u0||^2, c = U'u0, for
+ * the leading k left singular vectors U of a training matrix (column-major,
+ * ldu >= m).  The operator is a propack_csr_create handle.  All functions
+ * return 0 or a negative PROPACK_ERR_*; the model runs on the device that
+ * was current at creation. */
+int propack_mlp_create(uint64_t seed, int64_t *handle);
+int propack_mlp_destroy(int64_t handle);
+/* number of parameters; flat FP32 order W1[256][18], b1[256], W2[256][256]
+ * ([out][in]), b2[256], w3[256], b3[1] */
+int propack_mlp_nparams(void);
+/* copy the parameters out (get) and/or in (set); either may be NULL */
+int propack_mlp_params(int64_t handle, float *get, const float *set);
+/* the m x 18 feature matrix of the operator's rows (row-major), host */
+int propack_mlp_features(int64_t handle, int64_t op_handle, uint64_t seed, float *F);
+/* the proposed start vector (m entries, host; not normalised) */
+int propack_mlp_start(int64_t handle, int64_t op_handle, uint64_t seed, double *u0);
+/* loss and its gradient (nparams floats, host) for (operator, U); no update */
+int propack_mlp_grad(int64_t handle, int64_t op_handle, uint64_t seed, const double *U, int ldu, int k,
+                     float *grad, double *loss);
+/* one Adam step (beta 0.9 / 0.999) with learning rate lr on (operator, U) */
+int propack_mlp_train_step(int64_t handle, int64_t op_handle, uint64_t seed, const double *U, int ldu, int k,
+                           double lr, double *loss);
+
 /* Last error message for the calling thread ("" if none). */
 const char *propack_last_error(void);
 

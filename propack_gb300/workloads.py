@@ -83,6 +83,41 @@ def zipf_mixed(seed=2, m=4_000_000, alpha=2.0, lo=4, hi=2000):
     return sp.csr_array((data.astype(np.float64), indices, indptr), shape=(m, m))
 
 
+def lowrank_family(seed=4, m=200_000, n=50_000, rank=32, theta=0.05, sigma0=50.0, decay=0.85, nnz_row=10,
+                   noise=0.1):
+    """A_t = L_t + E_t, t = 0, 1, ...: L_t = X_t diag(sigma0 decay^i) Y_t'
+    with orthonormal X_t (m x rank), Y_t (n x rank) that a random Givens
+    sweep of angle +-theta over adjacent column pairs rotates at every step;
+    E_t sparse noise with nnz_row uniform columns per row, N(0, noise^2).
+    Yields (S, L, R, w) for CsrOperator(S, L, R, w) with L = X_t, R = Y_t
+    as dense-as-CSR factors and w the singular weights."""
+    rng = np.random.default_rng(seed)
+    X, _ = np.linalg.qr(rng.standard_normal((m, rank)))
+    Y, _ = np.linalg.qr(rng.standard_normal((n, rank)))
+    w = sigma0 * decay ** np.arange(rank)
+
+    def sweep(M):
+        for j in range(rank - 1):
+            a = theta * (1.0 if rng.random() < 0.5 else -1.0)
+            c, s = np.cos(a), np.sin(a)
+            x, y = M[:, j].copy(), M[:, j + 1].copy()
+            M[:, j] = c * x - s * y
+            M[:, j + 1] = s * x + c * y
+        return M
+
+    t = 0
+    while True:
+        er = np.random.default_rng((seed, t))
+        indptr = np.arange(m + 1, dtype=np.int64) * nnz_row
+        E = sp.csr_array((er.standard_normal(m * nnz_row) * noise, er.integers(0, n, size=m * nnz_row,
+                                                                                dtype=np.int32), indptr),
+                         shape=(m, n))
+        yield E, sp.csr_array(X), sp.csr_array(Y), w.copy()
+        X = sweep(X)
+        Y = sweep(Y)
+        t += 1
+
+
 def dense_of(S, L=None, R=None, w=None):
     A = S.toarray()
     if L is not None:

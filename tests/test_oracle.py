@@ -118,3 +118,32 @@ def test_operator_does_not_modify_its_inputs(golden):
     oracle.Operator(S, L, R, golden["lr_w"])
     after = (S.data, S.indices, S.indptr, L.data, R.data)
     assert all(np.array_equal(x, y) for x, y in zip(before, after))
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The CPU oracle of the learned start model: its backward pass (in FP64)
+    against central differences of its own loss."""
+    import oracle.mlp_oracle as mo
+    rng = np.random.default_rng(0)
+    F = rng.standard_normal((300, 18))
+    U, _ = np.linalg.qr(rng.standard_normal((300, 5)))
+    p = mo.init_params(1)
+    p[mo.OB1:mo.OW2] = 0.1
+    p[mo.OB2:mo.OW3] = 0.1
+    _, g = mo.loss_and_grad(p, F, U, bf=False)
+    h = 1e-6
+    for i in list(rng.integers(0, mo.NP, 24)) + [mo.OB3, mo.OW3, mo.OB1, mo.OB2]:
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (mo.loss_and_grad(pp, F, U, bf=False)[0] - mo.loss_and_grad(pm, F, U, bf=False)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-5 * (abs(g[i]) + 1e-3)
+
+
+def test_bf16_rounding_of_the_mlp_oracle():
+    import oracle.mlp_oracle as mo
+    x = np.array([1.0, 1.00390625, 1.005859375, -3.14159, 0.0], dtype=np.float32)
+    r = mo.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0  # tie to even
+    assert r[2] == np.float32(1.0078125)
+    assert abs(r[3] - (-3.140625)) < 1e-7 and r[4] == 0.0
