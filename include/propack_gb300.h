@@ -199,6 +199,41 @@ int propack_mlp_grad(int64_t handle, int64_t op_handle, uint64_t seed, const dou
 int propack_mlp_train_step(int64_t handle, int64_t op_handle, uint64_t seed, const double *U, int ldu, int k,
                            double lr, double *loss);
 
+/* ---- Batched solver (no reference counterpart) -----------------------
+ * nprob independent CSR matrices with FP32 values, solved by dlansvd_irl
+ * (double/dlansvd_irl.F) with full reorthogonalisation (iterated classical
+ * Gram-Schmidt on every step), FP64 vectors, p = dim - neig exact shifts,
+ * one persistent kernel (a CTA per problem, work queue by decreasing size)
+ * whose restart cycles are replayed as a CUDA graph.
+ * Problem p: m[p] x n[p]; its m[p]+1 row pointers (0-based, its own
+ * nonzeros) follow those of problem p-1 in `rowptr`; its column indices
+ * and values are colidx/val[nnz_off[p] .. nnz_off[p+1]).  Total nonzeros
+ * below 2^31. */
+int propack_batch_create(int nprob, const int *m, const int *n, const int *rowptr, const int64_t *nnz_off,
+                         const int *colidx, const float *val, int64_t *handle);
+int propack_batch_destroy(int64_t handle);
+/* u0: the start vectors (U(:,1) of every problem, concatenated, sum(m)
+ * entries).  sigma, bnd: nprob x neig (row p = problem p).  info[p]: 0
+ * converged, -1 not converged within maxiter (dlansvd_irl's INFO=-1), 1
+ * the problem met an invariant subspace or clustered Ritz values that the
+ * batched kernel leaves to the single-problem driver.  U, V (optional):
+ * the neig left / right singular vectors of every converged problem,
+ * concatenated (m[p] x neig, n[p] x neig, column-major each).
+ * Requires 1 <= neig < dim <= min(64, m[p], n[p]). */
+int propack_batch_solve(int64_t handle, int dim, int neig, int maxiter, double tol, const double *u0,
+                        double *sigma, double *bnd, int *info, double *U, double *V);
+typedef struct {
+    int64_t nopx;            /* matvecs of all problems */
+    int64_t nreorth;         /* Gram-Schmidt reorthogonalisations */
+    int64_t converged;       /* problems with info 0 */
+    int64_t fallback;        /* problems with info 1 */
+    double device_ms;        /* device time of the solve (start vectors to results) */
+    int64_t cycles;          /* CUDA-graph replays of the restart cycle */
+    int64_t grid;            /* CTAs of the persistent kernel */
+    int64_t kernel_launches;
+} propack_batch_stats_t;
+int propack_batch_get_stats(propack_batch_stats_t *out);
+
 /* Last error message for the calling thread ("" if none). */
 const char *propack_last_error(void);
 

@@ -16,7 +16,7 @@ OBJ_DIR = os.path.join(HERE, "_lib", "obj")
 LIB = os.path.join(OUT_DIR, "libpropack_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["pgb_operator.cu", "pgb_lanczos.cu", "pgb_dense.cu", "pgb_driver.cu", "pgb_noalloc.cu", "pgb_gemm_tc.cu", "pgb_mlp.cu"]
+SOURCES = ["pgb_operator.cu", "pgb_lanczos.cu", "pgb_dense.cu", "pgb_driver.cu", "pgb_noalloc.cu", "pgb_gemm_tc.cu", "pgb_mlp.cu", "pgb_batch.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=default"]
 

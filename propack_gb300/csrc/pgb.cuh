@@ -357,6 +357,9 @@ struct Dev {
 };
 const Dev &device_info();
 
+// exclusive scan of n ints into out[0..n] (out[n] = total, also returned)
+int scan_excl(const int *in, int *out, int n, cudaStream_t s);
+
 // operator application on device vectors (no Lanczos fusion)
 template <typename T>
 void op_apply(const Operator &op, bool trans, const T *x, T *y, cudaStream_t s);

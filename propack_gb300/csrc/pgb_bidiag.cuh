@@ -51,7 +51,7 @@ __device__ __forceinline__ int tgk_negcount(int N, const double *b2, double lam,
 
 // sigma_t (t = 1: largest) of R by warp multisection; all lanes return it.
 // hi0: an upper bound of sigma_max (Gershgorin of TGK).
-__device__ double warp_sigma(int n, const double *b2, int t, double hi0, double pivmin)
+__device__ inline double warp_sigma(int n, const double *b2, int t, double hi0, double pivmin)
 {
     const int lane = threadIdx.x & 31, N = 2 * n;
     double lo = 0.0, hi = hi0;
@@ -74,7 +74,7 @@ __device__ double warp_sigma(int n, const double *b2, int t, double hi0, double 
 
 // Twisted factorization of TGK - lam I.  Dp/Dm: N scratch each.  When z is
 // given it receives the unit eigenvector; returns |z_N| of the unit vector.
-__device__ double tgk_twisted(const double *d, const double *e, int n, double lam, double pivmin, double *Dp,
+__device__ inline double tgk_twisted(const double *d, const double *e, int n, double lam, double pivmin, double *Dp,
                               double *Dm, double *z)
 {
     const int N = 2 * n;

@@ -167,7 +167,7 @@ __global__ void k_scan_final(const int *in, int n, const int *boff, int *out)
     }
 }
 // out has n+1 entries; returns the total on the host.
-static int scan_excl(const int *in, int *out, int n, cudaStream_t s)
+int scan_excl(const int *in, int *out, int n, cudaStream_t s)
 {
     const int nblk = std::max(1, (n + 4095) / 4096);
     int *bsum = nullptr;
