@@ -11,11 +11,18 @@ Workloads (seeded synthetic data, numpy default_rng):
   rank-64 term sum_i 100*0.9^i u_i v_i' (sparse unit-norm u_i, v_i; kept
   factored); k = 50, dimension 150, tol = 1e-10.
 
+* batched: independent CSR problems (m ~ U[500, 20000], n ~ U[200, 8000],
+  density 1%, FP32 values), top-8, kmax 40, tol 1e-8, all in one persistent
+  kernel; --scale sets the fraction of the 4096 problems (default 1).
+* learned: the learned start vector on a matrix family (200000 x 50000,
+  rank-32 rotating factors + sparse noise), k = 32, kmax 64, tol 1e-8.
+
 A step is one complete DLANSVD_IRL solve (start vector -> k converged Ritz
 triplets), run in each form of --forms (the first is the chosen form):
+* fp64: the reference's FP64 method (the default chosen form: on GB300 it is
+  the faster of the two for these workloads);
 * mixed: FP32 Lanczos vectors / SpMV / Gram-Schmidt with compensated
-  reductions, FP64 scalars, then a short FP64 refinement to tol;
-* fp64: the reference's FP64 method.
+  reductions, FP64 scalars, then an FP64 refinement to tol.
 
 * value    chosen form, device ms per solve with the operator already in
            HBM (CUDA events the library records on its own stream, start
@@ -61,7 +68,18 @@ WORKLOADS = {
         desc="4000000x4000000 CSR, nnz/row Zipf(2) clipped to [4,2000], uniform columns, "
              "N(0,1)*(1+i mod 1000)^-0.7 values (FP32-representable), DLANSVD_IRL k=50 dim=150 p=100 tol=1e-8",
         k=50, kmax=150, tol=1e-8,
-        matvecs_full=None,
+        matvecs_full=301,
+    ),
+    "batched": dict(
+        desc="independent CSR problems, m~U[500,20000], n~U[200,8000], density 1%, N(0,1) FP32 values; "
+             "top-8 triplets each, kmax=40, tol=1e-8, one persistent kernel + CUDA-graph restart cycles",
+        k=8, kmax=40, tol=1e-8, nprob=4096, matvecs_full=None,
+    ),
+    "learned": dict(
+        desc="matrix family A_t = L_t + E_t, 200000x50000, rank-32 factors rotated by a Givens sweep of 0.05 rad "
+             "per t, sigma=50*0.85^i, E_t 10 nnz/row N(0,0.1^2); k=32, kmax=64, tol=1e-8; MLP start vector "
+             "trained on the first solves vs the random start",
+        k=32, kmax=64, tol=1e-8, matvecs_full=None,
     ),
 }
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the fused SpMV
@@ -76,7 +94,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="zipf_mixed", choices=sorted(WORKLOADS))
-    ap.add_argument("--forms", default="mixed,fp64",
+    ap.add_argument("--forms", default="fp64,mixed",
                     help="comma list; the first is the chosen form reported as value")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -387,10 +405,12 @@ def run_ours(args, wl):
     forms_out = {f: {"ms": per[f], "matvecs": results[f]["matvecs"], "matvecs_fp32": results[f]["matvecs_fp32"],
                      "restarts": results[f]["restarts"], "max_rel_residual": results[f]["rel_resid"],
                      "wall_ms_per_step": results[f]["wall_ms"] / args.steps} for f in forms}
-    sig_err = None
-    if "fp64" in results and chosen != "fp64":
-        s1, s2 = results["fp64"]["sigma"], results[chosen]["sigma"]
-        sig_err = float(np.max(np.abs(s1 - s2) / s1))
+    sig_err = {}
+    if "fp64" in results:
+        for f in forms:
+            if f != "fp64":
+                s1, s2 = results["fp64"]["sigma"], results[f]["sigma"]
+                sig_err[f] = float(np.max(np.abs(s1 - s2) / s1))
     line = {"metric": "ms & matvecs to k=50 triplets at resid<=1e-8*||A||: chosen form vs plain FP64, 1 GB300",
             "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -399,7 +419,7 @@ def run_ours(args, wl):
             "config": {"workload": args.workload, "desc": wl["desc"], "chosen_form": chosen, "scale": args.scale,
                        "l2": "inputs larger than L2 (operator and Lanczos basis are GBs); no flush"},
             "matvecs": results[chosen]["matvecs"], "forms": forms_out,
-            "speedup_vs_plain_fp64": (per["fp64"] / per[chosen]) if "fp64" in per and chosen != "fp64" else None,
+            "speedup_vs_plain_fp64": {f: per["fp64"] / per[f] for f in forms} if "fp64" in per else None,
             "max_rel_sigma_diff_vs_fp64": sig_err,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(sum(results[f]["launches"] for f in forms)), "roofline": roof,
@@ -408,9 +428,170 @@ def run_ours(args, wl):
     return 0
 
 
+def run_batched(args, wl):
+    """Config: many independent problems in one call.  value = device ms of
+    the whole batch per step (start vectors in HBM -> every problem's
+    triplets); e2e = the same through propack_batch_create + solve from host
+    arrays (upload, device transposition, solve, results back)."""
+    import numpy as np
+    from propack_gb300 import batch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    nprob = max(1, int(round(wl["nprob"] * args.scale)))
+    mats = batch.random_batch(nprob, seed=3)
+    nnz = sum(A.nnz for A in mats)
+    mtot = sum(A.shape[0] for A in mats)
+    ntot = sum(A.shape[1] for A in mats)
+    rng = np.random.default_rng(0)
+    u0 = [rng.uniform(size=A.shape[0]) for A in mats]
+    k, kmax, tol = wl["k"], wl["kmax"], wl["tol"]
+    if args.impl == "reference":
+        return run_batched_reference(args, wl, mats, u0, nprob)
+    B = batch.Batch(mats)
+    for _ in range(args.warmup):
+        B.solve(k, kmax=kmax, tol=tol, maxiter=100, u0=u0, vectors=False)
+    sampler = ClockSampler(0)
+    sampler.start()
+    dev, stats_l, info = [], [], None
+    for _ in range(args.steps):
+        sig, bnd, info, U, V = B.solve(k, kmax=kmax, tol=tol, maxiter=100, u0=u0, vectors=False)
+        dev.append(B.stats["device_ms"])
+        stats_l.append(B.stats)
+    clocks = sampler.stop()
+    B.close()
+    value = statistics.mean(dev)
+    st = stats_l[-1]
+    # e2e: host CSR arrays -> batch -> sigma/U/V back
+    t0 = time.perf_counter()
+    B2 = batch.Batch(mats)
+    sig, bnd, info2, U, V = B2.solve(k, kmax=kmax, tol=tol, maxiter=100, u0=u0, vectors=True)
+    B2.close()
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    conv = int(np.sum(info == 0))
+    # algorithmic bytes: every matvec reads its matrix (FP32 value + int32
+    # index per nonzero, row pointers) and its FP64 in/out vectors
+    avg_mv_bytes = (nnz * 8 + (mtot + ntot) * 4 + 2 * (mtot + ntot) * 8) / nprob
+    achieved = st["nopx"] * avg_mv_bytes / (value * 1e-3) / 1e9
+    peak, kind = peaks()
+    cpu = None
+    if not args.no_cpu:
+        cpu = batched_cpu_sample(mats, u0, wl)
+    line = {"metric": "ms per batch to top-8 triplets of every problem at tol=1e-8 (problems/s alongside), 1 GB300",
+            "value": value, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 vectors, f32 matrix values", "data": "synthetic (seeded numpy default_rng)",
+            "config": {"workload": "batched", "desc": wl["desc"], "nprob": nprob, "nnz": int(nnz),
+                       "fraction_of_4096": nprob / 4096, "l2": "batch data (GBs) larger than L2; no flush"},
+            "problems_per_s": nprob / (value * 1e-3), "converged": conv, "matvecs": st["nopx"],
+            "cycles": st["cycles"], "persistent_grid": st["grid"],
+            "e2e": {"value": e2e_ms, "unit": "ms",
+                    "h2d_bytes_per_step": int(nnz * 8 + (mtot + nprob) * 4 + mtot * 8),
+                    "d2h_bytes_per_step": int(nprob * k * 16 + (mtot + ntot) * k * 8)},
+            "gpu_launches": int(sum(s["kernel_launches"] for s in stats_l)),
+            "roofline": {"bound": "hbm", "kernel": "k_batch_cycle (SpMV share of its traffic)", "achieved": achieved,
+                         "peak": peak, "peak_source": kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None},
+            "cpu_baseline": cpu, "clocks": clocks}
+    print(json.dumps(line))
+    return 0
+
+
+def batched_cpu_sample(mats, u0, wl, budget_s=20.0):
+    """The oracle on the host cores over a prefix of the problems (about
+    budget_s seconds of work; OpenMP inside each solve), scaled to all."""
+    import numpy as np
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.lib().oracle_set_threads(cores)
+    t0 = time.perf_counter()
+    done = 0
+    for A, u in zip(mats, u0):
+        oracle.svdp(A, wl["k"], kmax=wl["kmax"], tol=wl["tol"], v0=u, cgs=True, delta=0.0, eta=0.0,
+                    rng=np.random.default_rng(0), compute_u=False, compute_v=False)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = (time.perf_counter() - t0) * 1e3
+    return {"value": dt * len(mats) / done, "unit": "ms", "cores": cores, "kind": "port",
+            "sample": f"oracle (FP64, full reorthogonalisation, OpenMP) on the first {done} of {len(mats)} problems "
+                      f"({dt:.0f} ms), scaled by problem count"}
+
+
+def run_batched_reference(args, wl, mats, u0, nprob):
+    vals, info = [], None
+    for it in range(args.warmup + args.steps):
+        c = batched_cpu_sample(mats, u0, wl, budget_s=10.0)
+        if it >= args.warmup:
+            vals.append(c["value"])
+            info = c
+    value = statistics.mean(vals)
+    print(json.dumps({"impl": "reference", "metric": "ms per batch to top-8 triplets of every problem at tol=1e-8",
+                      "value": value, "unit": "ms", "higher_is_better": False, "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                      "config": {"workload": "batched", "nprob": nprob},
+                      "cpu_baseline": {"value": value, "unit": "ms", "cores": info["cores"], "kind": "port",
+                                       "sample": info["sample"]},
+                      "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+    return 0
+
+
+def run_learned(args, wl):
+    """Config: learned start vector on a matrix family.  value = mean device
+    ms per solve from the learned start on held-out members (training not
+    counted); the random start is timed on the same members."""
+    import numpy as np
+    import propack_gb300 as pg
+    from propack_gb300 import learned, workloads
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    m, n = int(200_000 * args.scale), int(50_000 * args.scale)
+    ntrain, ntest = 24, 8
+    fam = workloads.lowrank_family(seed=4, m=m, n=n, rank=32)
+    ops = [pg.CsrOperator(*next(fam)) for _ in range(ntrain + ntest)]
+    k, kmax, tol = wl["k"], wl["kmax"], wl["tol"]
+    model = learned.StartModel(seed=0)
+    t0 = time.perf_counter()
+    Us = [learned.solve(op, k, None, tol=tol, kmax=kmax)[0] for op in ops[:ntrain]]
+    losses = []
+    for epoch in range(30):
+        losses.append(float(np.mean([model.train_step(op, U, lr=1e-3) for op, U in zip(ops[:ntrain], Us)])))
+    train_s = time.perf_counter() - t0
+    res = {"random": [], "learned": []}
+    for it in range(args.warmup + args.steps):
+        for op in ops[ntrain:]:
+            for mode in ("random", "learned"):
+                u, s, vt, bnd, info = learned.solve(op, k, model if mode == "learned" else None, tol=tol, kmax=kmax)
+                if it >= args.warmup:
+                    res[mode].append((info["nopx"], pg.get_stats()["solve_ms"], info["start"]))
+    for op in ops:
+        op.close()
+    model.close()
+    mv = {kk: float(np.mean([r[0] for r in v])) for kk, v in res.items()}
+    ms = {kk: float(np.mean([r[1] for r in v])) for kk, v in res.items()}
+    fallbacks = sum(r[2] != "learned" for r in res["learned"])
+    print(json.dumps({"metric": "matvecs & ms per solve, learned start vs random start (k=32, tol=1e-8), 1 GB300",
+                      "value": ms["learned"], "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": ms["learned"], "higher_is_better": False, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f64 solve, bf16 MLP", "data": "synthetic (seeded)",
+                      "config": {"workload": "learned", "desc": wl["desc"], "m": m, "n": n, "train": ntrain,
+                                 "held_out": ntest, "epochs": 30},
+                      "matvecs": mv, "ms": ms, "fallbacks_to_random": fallbacks, "train_s": train_s,
+                      "loss_first_last": [losses[0], losses[-1]], "speedup_vs_random_start": ms["random"] / ms["learned"],
+                      "e2e": None, "gpu_launches": None, "roofline": None, "cpu_baseline": None}))
+    return 0
+
+
 def main():
     args = parse()
     wl = WORKLOADS[args.workload]
+    if args.workload == "batched":
+        return run_batched(args, wl)
+    if args.workload == "learned":
+        return run_learned(args, wl)
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_ours(args, wl)

@@ -8,7 +8,7 @@
 //
 // Execution: one CTA owns one problem at a time.  A persistent grid pulls
 // problems from a work queue ordered by decreasing cost (an atomic ticket)
-// and runs ONE restart cycle of each active problem:
+// and runs up to BATCH_CYCLES_PER_LAUNCH restart cycles of each active problem:
 //   Lanczos extension k0 -> dim (both SpMVs, ELR, CGS) ... dlanbpro.F
 //   bidiagonal analysis (lane-parallel bisection + twisted bounds,
 //   drefinebounds, convergence count) ..................... dlansvd_irl.F:218-290
@@ -36,6 +36,12 @@ namespace pgb {
 constexpr int BT = 256;  // threads per CTA
 constexpr int BW = BT / 32;
 constexpr int BDIM_MAX = 64;
+// restart cycles a CTA runs on one problem per graph replay.  The cycle is
+// FP64-pipe bound on its SM, and every replay ends at the slowest CTA, so
+// problems run (nearly) to completion inside one replay: the makespan is then
+// the largest problem's solve or the total work over the grid, whichever is
+// longer; further replays only serve problems that need more cycles
+constexpr int BATCH_CYCLES_PER_LAUNCH = 64;
 
 enum { BS_ACTIVE = 0, BS_CONVERGED = 1, BS_MAXITER = 2, BS_FALLBACK = 3 };
 
@@ -118,15 +124,26 @@ __device__ void cta_safescal(int n, double a, double *x)
     }
     __syncthreads();
 }
-// y = A x (A: rows x *, CSR with FP32 values), one warp per row
+// y = A x (A: rows x *, CSR with FP32 values), one thread per row: every
+// thread keeps a row in flight (rows of ~1% density are tens of nonzeros),
+// four (index, value) pairs and four gathers at a time
 __device__ void cta_spmv(const int *ptr, const int *idx, const float *val, int rows, const double *x, double *y)
 {
-    const int lane = threadIdx.x & 31;
-    for (int r = threadIdx.x >> 5; r < rows; r += BW) {
+    for (int r = threadIdx.x; r < rows; r += BT) {
+        const int e1 = ptr[r + 1];
+        int e = ptr[r];
         double s = 0.0;
-        for (int e = ptr[r] + lane; e < ptr[r + 1]; e += 32) s = fma((double)val[e], x[idx[e]], s);
-        s = warp_sum(s);
-        if (lane == 0) y[r] = s;
+        for (; e + 3 < e1; e += 4) {
+            const int c0 = idx[e], c1 = idx[e + 1], c2 = idx[e + 2], c3 = idx[e + 3];
+            const float v0 = val[e], v1 = val[e + 1], v2 = val[e + 2], v3 = val[e + 3];
+            const double x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+            s = fma((double)v0, x0, s);
+            s = fma((double)v1, x1, s);
+            s = fma((double)v2, x2, s);
+            s = fma((double)v3, x3, s);
+        }
+        for (; e < e1; e++) s = fma((double)val[e], x[idx[e]], s);
+        y[r] = s;
     }
     __syncthreads();
 }
@@ -149,7 +166,16 @@ __device__ void cta_reorth(const double *W, int ld, int ncols, double *x, int le
         double a = 0.0;
         for (int i = threadIdx.x; i < len; i += BT) {
             double v = x[i];
-            for (int c = 0; c < ncols; c++) v = fma(-W[(size_t)c * ld + i], S.h[c], v);
+            int c = 0;
+            for (; c + 3 < ncols; c += 4) {
+                const double w0 = W[(size_t)c * ld + i], w1 = W[(size_t)(c + 1) * ld + i];
+                const double w2 = W[(size_t)(c + 2) * ld + i], w3 = W[(size_t)(c + 3) * ld + i];
+                v = fma(-w0, S.h[c], v);
+                v = fma(-w1, S.h[c + 1], v);
+                v = fma(-w2, S.h[c + 2], v);
+                v = fma(-w3, S.h[c + 3], v);
+            }
+            for (; c < ncols; c++) v = fma(-W[(size_t)c * ld + i], S.h[c], v);
             x[i] = v;
             a = fma(v, v, a);
         }
@@ -573,7 +599,8 @@ __device__ bool b_ritz(BProb &P, const BCfg &c, BShared &S, double *scr, const B
 
 // ------------------------------------------------------- the cycle kernel
 __global__ void __launch_bounds__(BT) k_batch_cycle(BProb *probs, const int *order, int nprob, BCfg c,
-                                                    double *scratch, size_t scr_stride, int *ticket, int *active)
+                                                    double *scratch, size_t scr_stride, int *ticket, int *active,
+                                                    int cycles_per_launch)
 {
     __shared__ BShared S;
     __shared__ int pidx;
@@ -585,34 +612,34 @@ __global__ void __launch_bounds__(BT) k_batch_cycle(BProb *probs, const int *ord
         const int qi = pidx;
         if (qi >= nprob) break;
         BProb &P = probs[order[qi]];
-        if (P.status != BS_ACTIVE) {
-            __syncthreads();
-            continue;
-        }
-        bool ok = b_lanbpro(P, c, S);
-        int nconv = ok ? b_analyse(P, c, S, scr, L) : -1;
-        if (nconv < 0) {
-            if (threadIdx.x == 0) P.status = BS_FALLBACK;
-        } else if (nconv >= c.neig) {
-            // the bounds of the converged values are the ones reported
-            for (int q = threadIdx.x; q < c.neig; q += BT) P.bnd[q] = S.bnd[q];
-            if (!b_ritz(P, c, S, scr, L)) {
+        // up to cycles_per_launch restart cycles of this problem, then it is
+        // handed back to the queue of the next replay
+        for (int rep = 0; rep < cycles_per_launch && P.status == BS_ACTIVE; rep++) {
+            bool ok = b_lanbpro(P, c, S);
+            int nconv = ok ? b_analyse(P, c, S, scr, L) : -1;
+            if (nconv < 0) {
                 if (threadIdx.x == 0) P.status = BS_FALLBACK;
-            } else if (threadIdx.x == 0) {
-                P.status = BS_CONVERGED;
-            }
-        } else {
-            b_restart(P, c, S, scr, L);
-            if (threadIdx.x == 0) {
-                P.iter++;
-                if (P.iter >= c.maxiter) {
-                    P.status = BS_MAXITER;
-                    for (int q = 0; q < c.neig; q++) { P.sig[q] = S.sig[q]; P.bnd[q] = S.bnd[q]; }
-                } else {
-                    atomicAdd(active, 1);
+            } else if (nconv >= c.neig) {
+                // the bounds of the converged values are the ones reported
+                for (int q = threadIdx.x; q < c.neig; q += BT) P.bnd[q] = S.bnd[q];
+                if (!b_ritz(P, c, S, scr, L)) {
+                    if (threadIdx.x == 0) P.status = BS_FALLBACK;
+                } else if (threadIdx.x == 0) {
+                    P.status = BS_CONVERGED;
+                }
+            } else {
+                b_restart(P, c, S, scr, L);
+                if (threadIdx.x == 0) {
+                    P.iter++;
+                    if (P.iter >= c.maxiter) {
+                        P.status = BS_MAXITER;
+                        for (int q = 0; q < c.neig; q++) { P.sig[q] = S.sig[q]; P.bnd[q] = S.bnd[q]; }
+                    }
                 }
             }
+            __syncthreads();
         }
+        if (threadIdx.x == 0 && P.status == BS_ACTIVE) atomicAdd(active, 1);
         __syncthreads();
     }
 }
@@ -927,12 +954,13 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
         PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         PGB_CUDA(cudaMemsetAsync(dticket, 0, sizeof(int), s));
         PGB_CUDA(cudaMemsetAsync(dactive, 0, sizeof(int), s));
-        k_batch_cycle<<<grid, BT, 0, s>>>(dprob, dorder, np, cfg, scratch, stride, dticket, dactive);
+        k_batch_cycle<<<grid, BT, 0, s>>>(dprob, dorder, np, cfg, scratch, stride, dticket, dactive,
+                                          BATCH_CYCLES_PER_LAUNCH);
         PGB_CUDA(cudaMemcpyAsync(hactive, dactive, sizeof(int), cudaMemcpyDeviceToHost, s));
         PGB_CUDA(cudaStreamEndCapture(s, &graph));
         PGB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
         int cycles = 0;
-        while (cycles < maxiter) {
+        while (cycles * BATCH_CYCLES_PER_LAUNCH < maxiter) {
             PGB_CUDA(cudaGraphLaunch(exec, s));
             PGB_LAUNCHED();
             PGB_CUDA(cudaStreamSynchronize(s));
