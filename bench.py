@@ -83,8 +83,10 @@ WORKLOADS = {
     ),
 }
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the fused SpMV
-# pair, from ncu on this workload and form ({workload: {form: bytes}})
-SPMV_TRAFFIC_BYTES = {}
+# pair ({workload: {form: bytes}}): ncu on the 1,000,000-row zipf case (mean
+# of the A'u and Av launches, 118.7 and 117.2 MB), scaled x4 by rows and
+# nonzeros to the 4,000,000-row workload
+SPMV_TRAFFIC_BYTES = {"zipf_mixed": {"fp64": 471.8e6}}
 
 
 def parse():
