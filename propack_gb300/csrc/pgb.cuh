@@ -66,6 +66,8 @@ struct Csr {
     int *blk = nullptr;       // nblk+1 row boundaries
     int segs = 0;             // thin matrices: segments per row for the split reduction
     int short_rows = 0;       // 1: lane-per-row SpMV schedule (mean row length below SHORT_MEAN)
+    int nlong = 0;            // short schedule: rows longer than SHORT_MAX, streamed by whole warps
+    int *longrows = nullptr;  // nlong row indices
 };
 constexpr int SHORT_MEAN = 16;
 

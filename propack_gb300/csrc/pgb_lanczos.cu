@@ -499,10 +499,13 @@ __device__ __forceinline__ const double *csr_vals<double>(const Csr &A) { return
 template <>
 __device__ __forceinline__ const float *csr_vals<float>(const Csr &A) { return A.valf; }
 
-template <int SIDE, typename T>
-__global__ void __launch_bounds__(BS) k_lb_spmv(LbArgs a, int j, int host_product)
+// SHORT: the matrix of this side uses the lane-per-row schedule (compiled
+// separately so that it carries neither the staged schedule's shared memory
+// nor its registers, and fits more CTAs per SM)
+template <int SIDE, typename T, int SHORT>
+__global__ void __launch_bounds__(BS, SHORT ? 5 : 3) k_lb_spmv(LbArgs a, int j, int host_product)
 {
-    __shared__ SpmvStage<T, T> st[SPMV_WARPS];
+    __shared__ SpmvStage<T, T> st[SHORT ? 1 : SPMV_WARPS];
     __shared__ double sred[32];
     __shared__ Tail t;
     if (a.ctl->status != 0) return;
@@ -534,7 +537,8 @@ __global__ void __launch_bounds__(BS) k_lb_spmv(LbArgs a, int j, int host_produc
     auto pre = [&](int r) -> double { return has_prev ? (double)prev[r] : 0.0; };
     if (!host_product) {
         auto xl = [&](int c) -> T { return c < n0 ? x[c] : (T)z[c - n0]; };
-        csr_spmv<T, T>(A, csr_vals<T>(A), xl, pre, epi, st);
+        if (SHORT) csr_rows_short<T, T>(A.ptr, A.idx, csr_vals<T>(A), A.rows, A.longrows, A.nlong, xl, pre, epi);
+        else csr_rows_staged<T, T>(A.ptr, A.idx, csr_vals<T>(A), A.blk, A.nblk, xl, pre, epi, st);
     } else {
         // the caller's APROD already wrote the product into out
         for (int r = blockIdx.x * BS + threadIdx.x; r < A.rows; r += gridDim.x * BS) epi(r, (double)out[r], pre(r));
@@ -810,16 +814,24 @@ static void launch_cgs_pass(const LbArgs &a, int j, int last, cudaStream_t s)
 }
 
 // one wave of CTAs at the fused SpMV's occupancy (partials are summed over gridDim)
-template <int SIDE, typename T>
+template <int SIDE, typename T, int SHORT>
 static int spmv_grid(int nb)
 {
     static thread_local int g = 0;
     if (g == 0) {
         int per = 0;
-        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lb_spmv<SIDE, T>, BS, 0));
+        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lb_spmv<SIDE, T, SHORT>, BS, 0));
         g = std::max(1, per) * device_info().sms;
     }
     return std::min(g, nb);
+}
+template <int SIDE, typename T>
+static void launch_spmv(const LbArgs &a, const Csr &A, int j, bool host_product, cudaStream_t s)
+{
+    if (host_product || A.short_rows)
+        k_lb_spmv<SIDE, T, 1><<<spmv_grid<SIDE, T, 1>(a.nb), BS, 0, s>>>(a, j, host_product ? 1 : 0);
+    else
+        k_lb_spmv<SIDE, T, 0><<<spmv_grid<SIDE, T, 0>(a.nb), BS, 0, s>>>(a, j, host_product ? 1 : 0);
 }
 
 // Enqueue the kernels of one half step.  host_product: the product was
@@ -833,7 +845,7 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
         if (!host_product && op && op->r > 0)
             PGB_PROF(PK_THIN, s, op_thin<T>(*op, true, ucol<T>(a, j - 1), s));
         PGB_PROF(sizeof(T) == 8 ? PK_SPMV_ADJ : PK_SPMV_ADJ32, s,
-                 k_lb_spmv<0, T><<<spmv_grid<0, T>(nb), BS, 0, s>>>(a, j, host_product ? 1 : 0));
+                 launch_spmv<0, T>(a, a.adj, j, host_product, s));
         PGB_LAUNCHED();
         if (j > 1)
             for (int i = 0; i < ielr; i++) {
@@ -845,7 +857,7 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
         if (!host_product && op && op->r > 0)
             PGB_PROF(PK_THIN, s, op_thin<T>(*op, false, vcol<T>(a, j - 1), s));
         PGB_PROF(sizeof(T) == 8 ? PK_SPMV_FWD : PK_SPMV_FWD32, s,
-                 k_lb_spmv<1, T><<<spmv_grid<1, T>(nb), BS, 0, s>>>(a, j, host_product ? 1 : 0));
+                 launch_spmv<1, T>(a, a.fwd, j, host_product, s));
         PGB_LAUNCHED();
         for (int i = 0; i < ielr; i++) {
             PGB_PROF(PK_ELR, s, k_lb_elr<1, T><<<nb, BS, 0, s>>>(a, j));

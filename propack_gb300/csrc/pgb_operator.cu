@@ -206,6 +206,16 @@ __global__ void k_blk_emit(const int *flag, const int *pos, int rows, int *blk)
         if (flag[r]) blk[pos[r]] = r;
     if (blockIdx.x == 0 && threadIdx.x == 0) blk[pos[rows]] = rows;
 }
+__global__ void k_long_flags(const int *ptr, int rows, int *flag)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+        flag[r] = (ptr[r + 1] - ptr[r]) > SHORT_MAX;
+}
+__global__ void k_long_emit(const int *flag, const int *pos, int rows, int *list)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+        if (flag[r]) list[pos[r]] = r;
+}
 static void build_blocks(Csr &A, cudaStream_t s)
 {
     int *flag = nullptr, *pos = nullptr;
@@ -222,6 +232,15 @@ static void build_blocks(Csr &A, cudaStream_t s)
     PGB_CUDA(cudaMalloc(&A.blk, sizeof(int) * (A.nblk + 1)));
     k_blk_emit<<<g, 256, 0, s>>>(flag, pos, rows, A.blk);
     PGB_LAUNCHED();
+    if (A.short_rows && rows > 0) {
+        // the rows the lane-per-row schedule leaves to whole warps
+        k_long_flags<<<g, 256, 0, s>>>(A.ptr, rows, flag);
+        PGB_LAUNCHED();
+        A.nlong = scan_excl(flag, pos, rows, s);
+        PGB_CUDA(cudaMalloc(&A.longrows, sizeof(int) * std::max(A.nlong, 1)));
+        k_long_emit<<<g, 256, 0, s>>>(flag, pos, rows, A.longrows);
+        PGB_LAUNCHED();
+    }
     PGB_CUDA(cudaFreeAsync(flag, s));
     PGB_CUDA(cudaFreeAsync(pos, s));
 }
@@ -537,7 +556,7 @@ Operator *lookup_operator(int64_t handle)
 
 static void free_csr(Csr &A)
 {
-    cudaFree(A.ptr); cudaFree(A.idx); cudaFree(A.val); cudaFree(A.valf); cudaFree(A.blk);
+    cudaFree(A.ptr); cudaFree(A.idx); cudaFree(A.val); cudaFree(A.valf); cudaFree(A.blk); cudaFree(A.longrows);
     A = Csr();
 }
 

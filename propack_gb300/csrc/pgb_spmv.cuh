@@ -14,7 +14,7 @@
 //   lane per row; each lane walks its row in order with four (index, value)
 //   pairs and four gathers in flight, so an instruction per nonzero and
 //   lane is all the row costs.  Rows longer than SHORT_MAX are skipped by
-//   their lane and streamed afterwards by the whole warp.
+//   the tiles and streamed afterwards, a whole warp per row, from a list.
 //
 // Summation order depends only on the matrix, never on timing, so results
 // are bit-reproducible.
@@ -132,58 +132,72 @@ __device__ __forceinline__ void csr_rows_staged(const int *__restrict__ ptr, con
 }
 
 
-// the short-row schedule (see the top of the file)
+// the short-row schedule (see the top of the file).  Rows longer than
+// SHORT_MAX are skipped by the tiles and streamed afterwards, one whole warp
+// per row, from the matrix's list of long rows; the bounds of a warp's next
+// tile are loaded with the current tile's first pairs.
 template <typename VT, typename AT, typename XF, typename PF, typename EPI>
 __device__ __forceinline__ void csr_rows_short(const int *__restrict__ ptr, const int *__restrict__ idx,
-                                               const VT *__restrict__ val, int nrows, XF xload, PF pre_load,
-                                               EPI epi)
+                                               const VT *__restrict__ val, int nrows, const int *__restrict__ longrows,
+                                               int nlong, XF xload, PF pre_load, EPI epi)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int nwarps = gridDim.x * SPMV_WARPS;
+    const int gw = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
     const int ntiles = (nrows + 31) / 32;
-    for (int tile = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5); tile < ntiles; tile += nwarps) {
-        const int r = tile * 32 + lane;
-        const bool valid = r < nrows;
-        const int e0 = valid ? ptr[r] : 0;
-        const int e1 = valid ? ptr[r + 1] : 0;
-        const double pre = valid ? pre_load(r) : 0.0;
-        const bool lng = e1 - e0 > SHORT_MAX;
-        AT acc = 0;
-        if (!lng) {
-            int e = e0;
-            for (; e + 3 < e1; e += 4) {
-                const int c0 = idx[e], c1 = idx[e + 1], c2 = idx[e + 2], c3 = idx[e + 3];
-                const VT v0 = val[e], v1 = val[e + 1], v2 = val[e + 2], v3 = val[e + 3];
-                const AT x0 = (AT)xload(c0), x1 = (AT)xload(c1), x2 = (AT)xload(c2), x3 = (AT)xload(c3);
-                acc = fma((AT)v0, x0, acc);
-                acc = fma((AT)v1, x1, acc);
-                acc = fma((AT)v2, x2, acc);
-                acc = fma((AT)v3, x3, acc);
+    int tile = gw;
+    if (tile < ntiles) {
+        int r = tile * 32 + lane;
+        int e0 = r < nrows ? ptr[r] : 0;
+        int e1 = r < nrows ? ptr[r + 1] : 0;
+        while (true) {
+            const bool own = r < nrows && e1 - e0 <= SHORT_MAX;
+            const double pre = own ? pre_load(r) : 0.0;
+            const int ntile = tile + nwarps;
+            const int rn = ntile * 32 + lane;
+            int n0 = 0, n1 = 0;
+            if (ntile < ntiles && rn < nrows) { n0 = ptr[rn]; n1 = ptr[rn + 1]; }
+            if (own) {
+                AT acc = 0;
+                int e = e0;
+                for (; e + 3 < e1; e += 4) {
+                    const int c0 = idx[e], c1 = idx[e + 1], c2 = idx[e + 2], c3 = idx[e + 3];
+                    const VT v0 = val[e], v1 = val[e + 1], v2 = val[e + 2], v3 = val[e + 3];
+                    const AT x0 = (AT)xload(c0), x1 = (AT)xload(c1), x2 = (AT)xload(c2), x3 = (AT)xload(c3);
+                    acc = fma((AT)v0, x0, acc);
+                    acc = fma((AT)v1, x1, acc);
+                    acc = fma((AT)v2, x2, acc);
+                    acc = fma((AT)v3, x3, acc);
+                }
+                for (; e < e1; e++) acc = fma((AT)val[e], (AT)xload(idx[e]), acc);
+                epi(r, (double)acc, pre);
             }
-            for (; e < e1; e++) acc = fma((AT)val[e], (AT)xload(idx[e]), acc);
+            tile = ntile;
+            if (tile >= ntiles) break;
+            r = rn;
+            e0 = n0;
+            e1 = n1;
         }
-        unsigned todo = __ballot_sync(FULL, lng);
-        while (todo) {
-            const int l = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const int f0 = __shfl_sync(FULL, e0, l), f1 = __shfl_sync(FULL, e1, l);
-            AT s = 0;
-            int e = f0 + lane;
-            for (; e + 96 < f1; e += 128) {
-                const int c0 = idx[e], c1 = idx[e + 32], c2 = idx[e + 64], c3 = idx[e + 96];
-                const VT v0 = val[e], v1 = val[e + 32], v2 = val[e + 64], v3 = val[e + 96];
-                const AT x0 = (AT)xload(c0), x1 = (AT)xload(c1), x2 = (AT)xload(c2), x3 = (AT)xload(c3);
-                s = fma((AT)v0, x0, s);
-                s = fma((AT)v1, x1, s);
-                s = fma((AT)v2, x2, s);
-                s = fma((AT)v3, x3, s);
-            }
-            for (; e < f1; e += 32) s = fma((AT)val[e], (AT)xload(idx[e]), s);
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
-            if (lane == l) acc = s;
+    }
+    for (int li = gw; li < nlong; li += nwarps) {
+        const int r = longrows[li];
+        const int f0 = ptr[r], f1 = ptr[r + 1];
+        const double pre = lane == 0 ? pre_load(r) : 0.0;
+        AT s = 0;
+        int e = f0 + lane;
+        for (; e + 96 < f1; e += 128) {
+            const int c0 = idx[e], c1 = idx[e + 32], c2 = idx[e + 64], c3 = idx[e + 96];
+            const VT v0 = val[e], v1 = val[e + 32], v2 = val[e + 64], v3 = val[e + 96];
+            const AT x0 = (AT)xload(c0), x1 = (AT)xload(c1), x2 = (AT)xload(c2), x3 = (AT)xload(c3);
+            s = fma((AT)v0, x0, s);
+            s = fma((AT)v1, x1, s);
+            s = fma((AT)v2, x2, s);
+            s = fma((AT)v3, x3, s);
         }
-        if (valid) epi(r, (double)acc, pre);
+        for (; e < f1; e += 32) s = fma((AT)val[e], (AT)xload(idx[e]), s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+        if (lane == 0) epi(r, (double)s, pre);
     }
 }
 
@@ -192,7 +206,7 @@ template <typename VT, typename AT, typename XF, typename PF, typename EPI>
 __device__ __forceinline__ void csr_spmv(const Csr &A, const VT *__restrict__ val, XF xload, PF pre_load, EPI epi,
                                          SpmvStage<VT, AT> *stages)
 {
-    if (A.short_rows) csr_rows_short<VT, AT>(A.ptr, A.idx, val, A.rows, xload, pre_load, epi);
+    if (A.short_rows) csr_rows_short<VT, AT>(A.ptr, A.idx, val, A.rows, A.longrows, A.nlong, xload, pre_load, epi);
     else csr_rows_staged<VT, AT>(A.ptr, A.idx, val, A.blk, A.nblk, xload, pre_load, epi, stages);
 }
 
