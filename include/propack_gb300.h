@@ -151,7 +151,9 @@ void propack_get_stats(propack_stats_t *out);
  * max(tol, 1e-6) (or after 8 restarts without a new converged value) and
  * an FP64 run with the same dim and p, started from the sum of the top
  * neig FP32 Ritz vectors, refines the triplets to the requested tol.
- * which = 'S' always runs in FP64.
+ * which = 'S' always runs in FP64.  Mode 2 is the FP32 form alone (no FP64
+ * refinement; tol no finer than 16 * 2^-24), the form of slansvd_ and
+ * slansvd_irl_.
  * Returns 0, or PROPACK_ERR_ARG for another mode.  No reference
  * counterpart. */
 int propack_set_precision(int mode);
@@ -168,6 +170,38 @@ int propack_get_precision(void);
  * Returns the number of classes.  No reference counterpart. */
 void propack_set_profiling(int on);
 int propack_get_profile(double *total_ms, int64_t *launches, int n);
+
+/* ---- Single-precision drivers ------------------------------------------
+ * SLANSVD / SLANSVD_IRL: the argument lists of single/slansvd.F:1-3 and
+ * single/slansvd_irl.F:1-3 (REAL arrays, REAL tolin/doption/dparm, a REAL
+ * APROD).  They run the FP32 form: FP32 Lanczos vectors, SpMV on the FP32
+ * copy of the values and Gram-Schmidt with compensated reductions, FP64
+ * scalars, tol no finer than 16 * 2^-24.  which = 'S' runs in FP64.  A user
+ * APROD receives REAL host vectors; propack_gpu_csr_saprod_ is recognised by
+ * address like the double version. */
+typedef void (*propack_saprod_t)(const char *transa, const int *m, const int *n,
+                                 const float *x, float *y, float *dparm,
+                                 int *iparm, size_t transa_len);
+void slansvd_(const char *jobu, const char *jobv, const int *m, const int *n,
+              int *k, const int *kmax, propack_saprod_t aprod,
+              float *U, const int *ldu, float *sigma, float *bnd,
+              float *V, const int *ldv, const float *tolin,
+              float *work, const int *lwork, int *iwork, const int *liwork,
+              float *doption, const int *ioption, int *info,
+              float *dparm, int *iparm, size_t jobu_len, size_t jobv_len);
+void slansvd_irl_(const char *which, const char *jobu, const char *jobv,
+                  const int *m, const int *n, const int *dim, const int *p,
+                  int *neig, const int *maxiter, propack_saprod_t aprod,
+                  float *U, const int *ldu, float *sigma, float *bnd,
+                  float *V, const int *ldv, const float *tolin,
+                  float *work, const int *lwork, int *iwork, const int *liwork,
+                  float *doption, const int *ioption, int *info,
+                  float *dparm, int *iparm,
+                  size_t which_len, size_t jobu_len, size_t jobv_len);
+/* The device operator as a REAL APROD (host REAL vectors in and out). */
+void propack_gpu_csr_saprod_(const char *transa, const int *m, const int *n,
+                             const float *x, float *y, float *dparm, int *iparm,
+                             size_t transa_len);
 
 /* ---- Learned start vector (no reference counterpart) ----------------
  * A row-wise MLP (18 -> 256 -> 256 -> 1, ReLU; BF16 weights, FP32

@@ -237,7 +237,7 @@ def lansvd(jobu, jobv, m, n, k, kmax, aprod, U, sigma, bnd, V, tol, doption, iop
 _which_converter = {"LM": b"L", "SM": b"S"}
 
 
-PRECISIONS = {"fp64": 0, "mixed": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1, "fp32": 2}
 
 
 def set_precision(precision):
@@ -261,8 +261,10 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
     Argument semantics, defaults, validation and return values follow
     scipy.sparse.linalg._svdp._svdp (scipy/sparse/linalg/_svdp.py); the
     Fortran-level call follows double/dlansvd_irl.F:1-3 / dlansvd.F:1-3.
-    precision: 'fp64' (default; the reference's method) or 'mixed' (FP32
-    Lanczos vectors, FP64 scalars, FP64 refinement to the requested tol).
+    precision: 'fp64' (default; the reference's method), 'mixed' (FP32
+    Lanczos vectors, FP64 scalars, FP64 refinement to the requested tol) or
+    'fp32' (the FP32 form alone, tol no finer than 16 * 2^-24: the form of
+    the single-precision drivers slansvd_ / slansvd_irl_).
     Returns (u, sigma, vt, bnd) like scipy's _svdp."""
     from scipy.linalg import LinAlgError
     if rng is None:

@@ -733,8 +733,20 @@ static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, 
 {
     if (ncols <= 0) return;
     if (sizeof(T) != sizeof(double)) {
-        set_error("copy_out: only FP64 bases are returned");
-        throw ArgFailure();
+        // FP32 bases: widen column by column through the FP64 scratch
+        for (int side = 0; side < 2; side++) {
+            if (side == 0 ? !du : !dv) continue;
+            const int rows = side == 0 ? c.m : c.n;
+            double *H = side == 0 ? U : V;
+            const int ldh = side == 0 ? ldu : ldv;
+            for (int col = 0; col < ncols; col++) {
+                const T *src = side == 0 ? c.Ucol<T>(col) : c.Vcol<T>(col);
+                dev_convert<T, double>(c, src, c.dx, rows);
+                PGB_CUDA(cudaMemcpyAsync(H + (size_t)col * ldh, c.dx, sizeof(double) * rows, cudaMemcpyDeviceToHost,
+                                         c.s));
+            }
+        }
+        return;
     }
     if (du)
         PGB_CUDA(cudaMemcpy2DAsync(U, sizeof(double) * ldu, c.U, sizeof(double) * c.ldu, sizeof(double) * c.m, ncols,
@@ -997,7 +1009,36 @@ static void run_irl(const char *which, const char *jobu, const char *jobv, int m
         throw ArgFailure();
     }
     IrlOut out;
-    if (g_precision == 0 || in.small_side) {
+    if (g_precision == 2 && !in.small_side) {
+        // FP32 only (the single-precision drivers): FP32 vectors, SpMV and
+        // Gram-Schmidt, FP64 scalars; tol no finer than 16 * 2^-24
+        Ctx c;
+        init_ctx<float>(c, m, n, in.dim);
+        setup_operator(c, aprod, dparm, iparm);
+        PGB_CUDA(cudaEventRecord(c.ev0, c.s));
+        PGB_CUDA(cudaMemcpyAsync(c.dx, U, sizeof(double) * m, cudaMemcpyHostToDevice, c.s));
+        PGB_CUDA(cudaEventRecord(c.evs0, c.s));
+        dev_convert<double, float>(c, c.dx, c.Ucol<float>(0), m);
+        double dop32[4] = {doption[0], doption[1], doption[2], doption[3]};
+        if (dop32[0] >= 0) dop32[0] = std::max(dop32[0], std::sqrt(EPS32));
+        if (dop32[1] >= 0) dop32[1] = std::max(dop32[1], std::pow(EPS32, 0.75));
+        IrlIn in32 = in;
+        in32.tol = std::min(1.0, std::max(16.0 * EPS32, tolin));
+        irl_loop<float>(c, in32, dop32, ioption, out);
+        PGB_CUDA(cudaEventRecord(c.evs1, c.s));
+        copy_out<float>(c, U, ldu, V, ldv, out.nconv, in.du, in.dv);
+        PGB_CUDA(cudaEventRecord(c.ev1, c.s));
+        c.sync();
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+        g_last.device_ms = ms;
+        cudaEventElapsedTime(&ms, c.evs0, c.evs1);
+        g_last.solve_ms = ms;
+        g_last.low_ms = ms;
+        add_ctx_counters(c);
+        g_last.nopx_low = g_last.nopx;
+        doption[2] = dop32[2];
+    } else if (g_precision == 0 || in.small_side) {
         Ctx c;
         init_ctx<double>(c, m, n, in.dim);
         setup_operator(c, aprod, dparm, iparm);
@@ -1081,7 +1122,8 @@ static void run_irl(const char *which, const char *jobu, const char *jobv, int m
     finish_stats(l0);
 }
 
-static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp, int kmax, propack_aprod_t aprod,
+template <typename T>
+static void run_lansvd_t(const char *jobu, const char *jobv, int m, int n, int *kp, int kmax, propack_aprod_t aprod,
                        double *U, int ldu, double *sigma, double *bnd, double *V, int ldv, double tolin,
                        double *doption, const int *ioption, int *info, double *dparm, int *iparm)
 {
@@ -1094,19 +1136,25 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
     const int64_t l0 = g_launches;
     g_last = Stats();
     const int lanmax = std::min(std::min(n + 1, m + 1), kmax);
-    const double tol = std::min(1.0, std::max(16.0 * EPS, tolin));
+    const bool f32 = sizeof(T) != sizeof(double);
+    const double tol = std::min(1.0, std::max(16.0 * (f32 ? EPS32 : EPS), tolin));
+    // the FP32 vectors keep orthogonality at the FP32 levels sqrt(eps), eps^(3/4)
+    double dop[4] = {doption[0], doption[1], doption[2], 0.0};
+    if (f32 && dop[0] >= 0) dop[0] = std::max(dop[0], std::sqrt(EPS32));
+    if (f32 && dop[1] >= 0) dop[1] = std::max(dop[1], std::pow(EPS32, 0.75));
     Ctx c;
-    init_ctx<double>(c, m, n, lanmax);
+    init_ctx<T>(c, m, n, lanmax);
     setup_operator(c, aprod, dparm, iparm);
     PGB_CUDA(cudaEventRecord(c.ev0, c.s));
-    PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(double) * m, cudaMemcpyHostToDevice, c.s));
+    PGB_CUDA(cudaMemcpyAsync(c.dx, U, sizeof(double) * m, cudaMemcpyHostToDevice, c.s));
     PGB_CUDA(cudaEventRecord(c.evs0, c.s));
-    double rnorm = dev_nrm2<double>(c, c.Ucol<double>(0), m);
+    dev_convert<double, T>(c, c.dx, c.Ucol<T>(0), m);
+    double rnorm = dev_nrm2<T>(c, c.Ucol<T>(0), m);
     int ierr = 0;
     double anorm_drv = 0.0;
     if (rnorm == 0.0) {
         double est = 0.0;
-        ierr = dev_getu0<double>(c, false, 0, 1, c.Ucol<double>(0), &rnorm, (double *)c.U, c.ldu, &est);
+        ierr = dev_getu0<T>(c, false, 0, 1, c.Ucol<T>(0), &rnorm, (T *)c.U, c.ldu, &est);
         anorm_drv = est;
     }
     PGB_CUDA(cudaMemcpyAsync(c.anorm_drv, &anorm_drv, sizeof(double), cudaMemcpyHostToDevice, c.s));
@@ -1118,7 +1166,7 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
     while (neig < k) {
         {
             Timer t(c, g_last.lanczos_ms);
-            dev_lanbpro<double>(c, jold, &j, &rnorm, doption, ioption, &ierr);
+            dev_lanbpro<T>(c, jold, &j, &rnorm, dop, ioption, &ierr);
         }
         jold = j;
         {
@@ -1157,10 +1205,11 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
     const bool du = yes(jobu), dv = yes(jobv);
     if ((neig >= k || *info > 0) && (du || dv)) {
         Timer t(c, g_last.gemm_ms);
-        dev_ritzvec<double>(c, false, du, dv, neig, jold);
+        dev_ritzvec<T>(c, false, du, dv, neig, jold);
     }
     PGB_CUDA(cudaEventRecord(c.evs1, c.s));
-    copy_out<double>(c, U, ldu, V, ldv, neig, du, dv);
+    copy_out<T>(c, U, ldu, V, ldv, neig, du, dv);
+    doption[2] = dop[2];
     PGB_CUDA(cudaEventRecord(c.ev1, c.s));
     c.sync();
     float ms = 0;
@@ -1173,6 +1222,19 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
     add_ctx_counters(c);
     prof_collect();
     finish_stats(l0);
+}
+
+// dlansvd (double/dlansvd.F:131-291); FP32 vectors when the precision is 2
+static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp, int kmax, propack_aprod_t aprod,
+                       double *U, int ldu, double *sigma, double *bnd, double *V, int ldv, double tolin,
+                       double *doption, const int *ioption, int *info, double *dparm, int *iparm)
+{
+    if (g_precision == 2)
+        run_lansvd_t<float>(jobu, jobv, m, n, kp, kmax, aprod, U, ldu, sigma, bnd, V, ldv, tolin, doption, ioption,
+                            info, dparm, iparm);
+    else
+        run_lansvd_t<double>(jobu, jobv, m, n, kp, kmax, aprod, U, ldu, sigma, bnd, V, ldv, tolin, doption,
+                             ioption, info, dparm, iparm);
 }
 
 }  // namespace pgb
@@ -1221,11 +1283,147 @@ extern "C" void dlansvd_(const char *jobu, const char *jobv, const int *m, const
     }
 }
 
+// ---------------------------------------------- single-precision drivers
+// SLANSVD / SLANSVD_IRL (single/slansvd.F:1-3, single/slansvd_irl.F:1-3):
+// the same argument lists with REAL arrays and a REAL APROD.  They run the
+// FP32 form (FP32 vectors, SpMV and Gram-Schmidt, FP64 scalars) and widen /
+// narrow at the boundary.  A user APROD is reached through a trampoline that
+// narrows the FP64 vectors of the host path to the caller's REAL arrays.
+struct SAprod {
+    propack_saprod_t f = nullptr;
+    float *sparm = nullptr;
+    std::vector<float> xf, yf;
+};
+static thread_local SAprod g_saprod;
+
+static void saprod_trampoline(const char *transa, const int *m, const int *n, const double *x, double *y,
+                              double *dparm, int *iparm, size_t transa_len)
+{
+    (void)dparm;
+    const bool t = transa[0] == 't' || transa[0] == 'T';
+    const int nin = t ? *m : *n, nout = t ? *n : *m;
+    g_saprod.xf.resize(std::max(nin, 1));
+    g_saprod.yf.resize(std::max(nout, 1));
+    for (int i = 0; i < nin; i++) g_saprod.xf[i] = (float)x[i];
+    g_saprod.f(transa, m, n, g_saprod.xf.data(), g_saprod.yf.data(), g_saprod.sparm, iparm, transa_len);
+    for (int i = 0; i < nout; i++) y[i] = g_saprod.yf[i];
+}
+
+// widened copies of the caller's REAL arrays for the FP64-interfaced drivers
+struct SArgs {
+    std::vector<double> U, V, sig, bnd, opt;
+    propack_aprod_t ap = nullptr;
+};
+static void s_prepare(SArgs &w, propack_saprod_t aprod, int m, int n, int ncols_u, int ncols_v, int ldu, int ldv,
+                      const float *U, int nsig, const float *soption, int nopt, float *sparm)
+{
+    w.U.assign((size_t)m * ncols_u, 0.0);
+    for (int i = 0; i < m; i++) w.U[i] = U[i];  // U(:,1), the start vector
+    w.V.assign((size_t)n * ncols_v, 0.0);
+    w.sig.assign(std::max(nsig, 1), 0.0);
+    w.bnd.assign(std::max(nsig, 1), 0.0);
+    w.opt.assign(4, 0.0);
+    for (int i = 0; i < nopt; i++) w.opt[i] = soption[i];
+    (void)ldu; (void)ldv;
+    if (aprod == propack_gpu_csr_saprod_) {
+        w.ap = propack_gpu_csr_aprod_;
+    } else {
+        g_saprod.f = aprod;
+        g_saprod.sparm = sparm;
+        w.ap = saprod_trampoline;
+    }
+}
+static void s_finish(const SArgs &w, int m, int n, int ncols, bool du, bool dv, float *U, int ldu, float *V, int ldv,
+                     float *sigma, float *bnd, int nsig, float *soption, int nopt)
+{
+    for (int c = 0; c < ncols; c++) {
+        if (du)
+            for (int i = 0; i < m; i++) U[(size_t)c * ldu + i] = (float)w.U[(size_t)c * m + i];
+        if (dv)
+            for (int i = 0; i < n; i++) V[(size_t)c * ldv + i] = (float)w.V[(size_t)c * n + i];
+    }
+    for (int i = 0; i < nsig; i++) { sigma[i] = (float)w.sig[i]; bnd[i] = (float)w.bnd[i]; }
+    for (int i = 0; i < nopt; i++) soption[i] = (float)w.opt[i];
+}
+
+extern "C" void slansvd_irl_(const char *which, const char *jobu, const char *jobv, const int *m, const int *n,
+                             const int *dim, const int *p, int *neig, const int *maxiter, propack_saprod_t aprod,
+                             float *U, const int *ldu, float *sigma, float *bnd, float *V, const int *ldv,
+                             const float *tolin, float *work, const int *lwork, int *iwork, const int *liwork,
+                             float *soption, const int *ioption, int *info, float *sparm, int *iparm,
+                             size_t which_len, size_t jobu_len, size_t jobv_len)
+{
+    (void)work; (void)lwork; (void)iwork; (void)liwork; (void)which_len; (void)jobu_len; (void)jobv_len;
+    set_error("");
+    const int saved = g_precision;
+    try {
+        if (!m || !n || !dim || !neig || !U || !V || !sigma || !bnd || !soption || !ioption || !info || !aprod ||
+            *m <= 0 || *n <= 0 || *dim <= 0 || *ldu < *m || *ldv < *n) {
+            set_error("slansvd_irl_: invalid argument");
+            throw ArgFailure();
+        }
+        SArgs w;
+        const int k0 = *neig;
+        s_prepare(w, aprod, *m, *n, *dim + 1, *dim, *ldu, *ldv, U, k0, soption, 4, sparm);
+        g_precision = 2;
+        run_irl(which, jobu, jobv, *m, *n, *dim, *p, neig, *maxiter, w.ap, w.U.data(), *m, w.sig.data(),
+                w.bnd.data(), w.V.data(), *n, (double)*tolin, w.opt.data(), ioption, info, nullptr, iparm);
+        g_precision = saved;
+        s_finish(w, *m, *n, std::min(*neig, k0), yes(jobu), yes(jobv), U, *ldu, V, *ldv, sigma, bnd,
+                 std::min(*neig, k0), soption, 4);
+    } catch (const CudaFailure &) {
+        g_precision = saved;
+        *info = PROPACK_ERR_CUDA;
+    } catch (const ArgFailure &) {
+        g_precision = saved;
+        *info = PROPACK_ERR_ARG;
+    } catch (const WaitFailure &) {
+        g_precision = saved;
+        *info = PROPACK_ERR_WAIT;
+    }
+}
+
+extern "C" void slansvd_(const char *jobu, const char *jobv, const int *m, const int *n, int *k, const int *kmax,
+                         propack_saprod_t aprod, float *U, const int *ldu, float *sigma, float *bnd, float *V,
+                         const int *ldv, const float *tolin, float *work, const int *lwork, int *iwork,
+                         const int *liwork, float *soption, const int *ioption, int *info, float *sparm, int *iparm,
+                         size_t jobu_len, size_t jobv_len)
+{
+    (void)work; (void)lwork; (void)iwork; (void)liwork; (void)jobu_len; (void)jobv_len;
+    set_error("");
+    const int saved = g_precision;
+    try {
+        if (!m || !n || !k || !kmax || !U || !V || !sigma || !bnd || !soption || !ioption || !info || !aprod ||
+            *m <= 0 || *n <= 0 || *kmax <= 0 || *k <= 0 || *ldu < *m || *ldv < *n) {
+            set_error("slansvd_: invalid argument");
+            throw ArgFailure();
+        }
+        SArgs w;
+        const int k0 = *k;
+        s_prepare(w, aprod, *m, *n, *kmax + 1, *kmax, *ldu, *ldv, U, k0, soption, 3, sparm);
+        g_precision = 2;
+        run_lansvd(jobu, jobv, *m, *n, k, *kmax, w.ap, w.U.data(), *m, w.sig.data(), w.bnd.data(), w.V.data(), *n,
+                   (double)*tolin, w.opt.data(), ioption, info, nullptr, iparm);
+        g_precision = saved;
+        // dlansvd returns bounds for the first k values even when fewer converged
+        s_finish(w, *m, *n, std::min(*k, k0), yes(jobu), yes(jobv), U, *ldu, V, *ldv, sigma, bnd, k0, soption, 3);
+    } catch (const CudaFailure &) {
+        g_precision = saved;
+        *info = PROPACK_ERR_CUDA;
+    } catch (const ArgFailure &) {
+        g_precision = saved;
+        *info = PROPACK_ERR_ARG;
+    } catch (const WaitFailure &) {
+        g_precision = saved;
+        *info = PROPACK_ERR_WAIT;
+    }
+}
+
 extern "C" void clearstat_(void) { g_stat = Stats(); }
 
 extern "C" int propack_set_precision(int mode)
 {
-    if (mode != 0 && mode != 1) return PROPACK_ERR_ARG;
+    if (mode != 0 && mode != 1 && mode != 2) return PROPACK_ERR_ARG;
     g_precision = mode;
     return 0;
 }

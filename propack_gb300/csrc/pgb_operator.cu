@@ -724,6 +724,18 @@ extern "C" void propack_handle_to_iparm(int64_t handle, int *iparm)
     iparm[1] = (int)(uint32_t)((uint64_t)handle >> 32);
 }
 
+extern "C" void propack_gpu_csr_saprod_(const char *transa, const int *m, const int *n, const float *x, float *y,
+                                        float *dparm, int *iparm, size_t transa_len)
+{
+    (void)dparm;
+    const bool t = (transa[0] == 't' || transa[0] == 'T');
+    const int nin = t ? *m : *n, nout = t ? *n : *m;
+    std::vector<double> xd(std::max(nin, 1)), yd(std::max(nout, 1));
+    for (int i = 0; i < nin; i++) xd[i] = x[i];
+    propack_gpu_csr_aprod_(transa, m, n, xd.data(), yd.data(), nullptr, iparm, transa_len);
+    for (int i = 0; i < nout; i++) y[i] = (float)yd[i];
+}
+
 extern "C" void propack_gpu_csr_aprod_(const char *transa, const int *m, const int *n, const double *x, double *y,
                                        double *dparm, int *iparm, size_t transa_len)
 {
