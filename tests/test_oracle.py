@@ -147,3 +147,32 @@ def test_bf16_rounding_of_the_mlp_oracle():
     assert r[0] == 1.0 and r[1] == 1.0  # tie to even
     assert r[2] == np.float32(1.0078125)
     assert abs(r[3] - (-3.140625)) < 1e-7 and r[4] == 0.0
+
+
+def test_matrix_file_formats_round_trip(tmp_path):
+    """propack_gb300.io reads the example programs' formats back exactly."""
+    import scipy.io as sio
+    import scipy.sparse as sp
+    from propack_gb300 import io as pio
+    rng = np.random.default_rng(3)
+    A = sp.random_array((40, 25), density=0.2, format="csr", random_state=rng)
+    A = sp.csr_array(A)
+    p = tmp_path / "a.mtx"
+    sio.mmwrite(str(p), A)
+    assert np.array_equal(pio.read(str(p)).toarray(), A.toarray())
+    p = tmp_path / "a.rua"
+    sio.hb_write(str(p), sp.csc_array(A))
+    np.testing.assert_allclose(pio.read(str(p)).toarray(), A.toarray(), rtol=1e-15, atol=0)
+    C = A.tocoo()
+    p = tmp_path / "a.coord"
+    with open(p, "w") as f:
+        f.write(f"{A.shape[0]} {A.shape[1]} {C.nnz}\n")
+        for i, j, v in zip(C.row, C.col, C.data):
+            f.write(f"{i + 1} {j + 1} {float(v)!r}\n")
+    assert np.array_equal(pio.read(str(p)).toarray(), A.toarray())
+    D = A.toarray()
+    p = tmp_path / "a.dense"
+    with open(p, "w") as f:
+        f.write(f"{D.shape[0]} {D.shape[1]}\n")
+        f.write("\n".join(repr(float(x)) for x in D.ravel(order="F")))
+    assert np.array_equal(pio.read(str(p)).toarray(), D)
