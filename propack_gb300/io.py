@@ -63,7 +63,8 @@ def _read_coord(path):
 
 
 def _read_dense(path):
-    v = np.loadtxt(path, dtype=np.float64).ravel()
+    with open(path) as f:
+        v = np.array(f.read().split(), dtype=np.float64)
     m, n = int(v[0]), int(v[1])
     return v[2:2 + m * n].reshape((m, n), order="F")
 
