@@ -89,6 +89,19 @@ int propack_csr_create(int m, int n, const int64_t *s_rowptr,
                        const int32_t *r_colidx, const double *r_val,
                        const double *w, int64_t *handle);
 int propack_csr_destroy(int64_t handle);
+/* SpMV schedule of the operators built after the call (per host process):
+ * 0 (default) a timed choice per direction -- propack_csr_create builds
+ * the run-interleaved copy of any matrix with fewer than 64 nonzeros per
+ * row on average, times the chunked and the staged schedule on the device
+ * and keeps the faster (the row-length rule, chunked below 16 per row, is
+ * kept unless the other is more than 5 % faster); 1 always chunked;
+ * 2 always staged.  Both schedules give results that depend only on the
+ * matrix.  Returns 0 or PROPACK_ERR_ARG. */
+int propack_set_spmv_schedule(int mode);
+/* The schedules chosen for A (sched[0]) and A' (sched[1]): 1 chunked,
+ * 0 staged; tuned_ms (optional, 4 floats): the timed chunked / staged ms
+ * per product of A, then of A' (0 where not timed). */
+int propack_csr_schedule(int64_t handle, int *sched, float *tuned_ms);
 /* Store a handle in iparm[0..1] (helper for C callers). */
 void propack_handle_to_iparm(int64_t handle, int *iparm);
 
@@ -139,6 +152,8 @@ typedef struct {
                           to the Ritz vectors in HBM (no host copies) */
     int64_t nopx_low;  /* mixed form: matvecs of the FP32 phase        */
     double low_ms;     /* mixed form: device ms of the FP32 phase      */
+    int64_t cgs_cols_u; /* basis columns (length m) read by Gram-Schmidt passes */
+    int64_t cgs_cols_v; /* basis columns (length n) read by Gram-Schmidt passes */
 } propack_stats_t;
 void propack_get_stats(propack_stats_t *out);
 
@@ -267,6 +282,18 @@ typedef struct {
     int64_t kernel_launches;
 } propack_batch_stats_t;
 int propack_batch_get_stats(propack_batch_stats_t *out);
+
+/* ---- FP64 product on the tensor cores --------------------------------
+ * C (mr x nc, column-major ldc) = A (mr x kk, column-major lda) op(B), with
+ * op(B)(l, j) = B[j * ldb + l] (tb = 0) or B[l * ldb + j] (tb = 1); all
+ * pointers are device memory.  This is the restart / Ritz product of
+ * dlansvd_irl.F:371-398 and dritzvec.F:130-198 (dgemm_ovwr.F:56-87) as the
+ * drivers run it: an error-free split of both operands into seven BF16
+ * digits, exact FP32 level sums, int64 recombination.  impl 1 is the
+ * tcgen05 kernel the drivers use, impl 0 the mma.sync kernel; both give the
+ * same bits.  Requires mr >= 1, 1 <= kk <= 256, lda, ldc >= mr. */
+int propack_gemm_f64_tc(int impl, int mr, int nc, int kk, const double *A, int lda, const double *B, int ldb,
+                        int tb, double *C, int ldc);
 
 /* Last error message for the calling thread ("" if none). */
 const char *propack_last_error(void);

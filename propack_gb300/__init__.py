@@ -40,7 +40,7 @@ class _Stats(C.Structure):
                 ("nbsvd", C.c_int64), ("nlandim", C.c_int64), ("device_ms", C.c_double),
                 ("lanczos_ms", C.c_double), ("bsvd_ms", C.c_double), ("gemm_ms", C.c_double),
                 ("kernel_launches", C.c_int64), ("solve_ms", C.c_double), ("nopx_low", C.c_int64),
-                ("low_ms", C.c_double)]
+                ("low_ms", C.c_double), ("cgs_cols_u", C.c_int64), ("cgs_cols_v", C.c_int64)]
 
 
 PROFILE_KINDS = ("spmv_adj", "spmv_fwd", "elr", "cgs_dots", "cgs_upd", "lowrank_prepass", "analyse", "sweeps",
@@ -97,6 +97,14 @@ def get_profile():
     cnt = (C.c_int64 * n)()
     L.propack_get_profile(ms, cnt, n)
     return {k: (int(cnt[i]), float(ms[i])) for i, k in enumerate(PROFILE_KINDS)}
+
+
+def set_spmv_schedule(mode):
+    """SpMV schedule of operators built afterwards: "tuned" (default),
+    "chunked" or "staged" (propack_set_spmv_schedule)."""
+    m = {"tuned": 0, "chunked": 1, "staged": 2}[mode]
+    if load().propack_set_spmv_schedule(m) != 0:
+        raise PropackError("propack_set_spmv_schedule failed")
 
 
 def printstat():
@@ -156,6 +164,20 @@ class CsrOperator:
         self.iparm = np.array([h.value & 0xFFFFFFFF, (h.value >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
         self.aprod = C.cast(lib.propack_gpu_csr_aprod_, APROD)
         self.r = r
+
+    @property
+    def schedule(self):
+        """({'fwd': ..., 'adj': ...} with 'chunked' / 'staged', timed ms per
+        product {(direction, schedule): ms} where the choice was timed)."""
+        sched = (C.c_int * 2)()
+        ms = (C.c_float * 4)()
+        rc = load().propack_csr_schedule(C.c_int64(self.handle), sched, ms)
+        if rc != 0:
+            raise PropackError(f"propack_csr_schedule failed ({rc})")
+        names = {1: "chunked", 0: "staged"}
+        timed = {(d, s_): ms[2 * i + j] for i, d in enumerate(("fwd", "adj"))
+                 for j, s_ in enumerate(("chunked", "staged")) if ms[2 * i + j] > 0}
+        return {"fwd": names[sched[0]], "adj": names[sched[1]]}, timed
 
     def close(self):
         if getattr(self, "handle", 0):

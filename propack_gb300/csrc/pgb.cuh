@@ -65,9 +65,14 @@ struct Csr {
     int nblk = 0;             // row blocks
     int *blk = nullptr;       // nblk+1 row boundaries
     int segs = 0;             // thin matrices: segments per row for the split reduction
-    int short_rows = 0;       // 1: lane-per-row SpMV schedule (mean row length below SHORT_MEAN)
-    int nlong = 0;            // short schedule: rows longer than SHORT_MAX, streamed by whole warps
-    int *longrows = nullptr;  // nlong row indices
+    int short_rows = 0;       // 1: the chunked schedule, 0: the staged one
+    float tuned_ms[2] = {0.f, 0.f};  // timed choice: chunked, staged ms per product (0: not timed)
+    // chunked schedule: the entries of each 32-row tile re-laid so that lane
+    // l's run of C consecutive entries is read with coalesced loads
+    int *tbase = nullptr;     // tiles+1: first 32-entry unit of each tile
+    int *cidx = nullptr;      // 32 * tbase[tiles] (padding: column 0, value 0)
+    double *cval = nullptr;
+    float *cvalf = nullptr;
 };
 constexpr int SHORT_MEAN = 16;
 
@@ -125,6 +130,7 @@ struct LbCtl {
     int susp_j;
     // statistics (double/stat.h)
     long long nopx, nreorth, ndot;
+    long long cgs_cols_u, cgs_cols_v;  // basis columns streamed by Gram-Schmidt passes, per side
     // last-CTA tickets
     unsigned int ticket;
 };

@@ -29,6 +29,7 @@ struct Stats {
     double solve_ms = 0;
     int64_t nopx_low = 0;   // matvecs of the FP32 phase (mixed form)
     double low_ms = 0;      // device ms of the FP32 phase (mixed form)
+    int64_t cgs_cols_u = 0, cgs_cols_v = 0;  // basis columns streamed by Gram-Schmidt
 };
 static thread_local Stats g_stat;       // cumulative (clearstat_/printstat_)
 static thread_local Stats g_last;       // last driver call (propack_get_stats)
@@ -839,6 +840,8 @@ static void add_ctx_counters(Ctx &c)
     g_last.nopx += c.hctl->nopx;
     g_last.nreorth += c.hctl->nreorth;
     g_last.ndot += c.hctl->ndot;
+    g_last.cgs_cols_u += c.hctl->cgs_cols_u;
+    g_last.cgs_cols_v += c.hctl->cgs_cols_v;
 }
 
 static void finish_stats(int64_t launches0)
@@ -1462,4 +1465,6 @@ extern "C" void propack_get_stats(propack_stats_t *out)
     out->solve_ms = s.solve_ms;
     out->nopx_low = s.nopx_low;
     out->low_ms = s.low_ms;
+    out->cgs_cols_u = s.cgs_cols_u;
+    out->cgs_cols_v = s.cgs_cols_v;
 }

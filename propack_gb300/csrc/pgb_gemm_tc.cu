@@ -22,6 +22,9 @@
 // The digits of A are produced in registers from the FP64 bits with integer
 // operations, straight into mma.sync fragments (m16n8k16, row.col); the
 // digits of B come from a small pre-pass and are staged in shared memory.
+#include <algorithm>
+
+#include "../../include/propack_gb300.h"
 #include "pgb.cuh"
 
 namespace pgb {
@@ -259,36 +262,365 @@ __global__ void __launch_bounds__(OZ_WARPS * 32) k_oz_gemm(int mr, int nc, int k
         }
 }
 
+// ===========================================================================
+// The same product on the 5th-generation tensor cores: tcgen05.mma with the
+// seven level sums T_g accumulated in tensor memory.
+//
+// One CTA (256 threads, one per SM: its shared memory and 512 TMEM columns
+// admit no second) owns 128 rows x UM_BN columns.  K runs in stages of
+// UM_KC = 32 (two K = 16 MMA steps), double-buffered: while the tensor core
+// works on stage c, the threads load the FP64 values of stage c + 1, split
+// them into digits and write the digit planes of A into the other buffer;
+// the digit planes of B for the stage arrive by one bulk copy (cp.async.bulk
+// into shared memory, completion on an mbarrier).  Per stage, thread 0
+// issues 2 x 28 MMAs (M = 128, N = UM_BN, K = 16, BF16 x BF16 -> FP32): the
+// digit pair (p, q) of K step s accumulates into the TMEM columns of level
+// p + q.  tcgen05.commit arrives on the stage's mbarrier when those MMAs are
+// done, which frees the stage's buffers.  After the last stage every warp
+// reads its 32 TMEM lanes (rows) with tcgen05.ld and combines the levels
+// in int64 as above.
+//
+// Operand layout in shared memory (no swizzle, K-major): a (digit, K step)
+// tile of R rows x 16 K is R/8 x 2 core matrices of 8 rows x 16 bytes; row
+// group g, K half h sits at g * 256 + h * 128 bytes (descriptor leading
+// byte offset 128 = next core matrix along K, stride byte offset 256 = next
+// 8-row group).  Every wait is bounded; a wait that runs out sets *err and
+// the CTA skips the rest of its work.
+constexpr int UM_BM = 128;
+constexpr int UM_BN = 64;
+constexpr int UM_KC = 32;
+constexpr int UM_THREADS = 256;
+constexpr int UM_ATILE = UM_BM * 16 * 2;        // 4096 bytes
+constexpr int UM_BTILE = UM_BN * 16 * 2;        // 2048 bytes
+constexpr int UM_ASTAGE = OZ_S * 2 * UM_ATILE;  // 57344 bytes
+constexpr int UM_BSTAGE = OZ_S * 2 * UM_BTILE;  // 28672 bytes
+constexpr int UM_SMEM = 2 * (UM_ASTAGE + UM_BSTAGE) + 2048;
+constexpr unsigned UM_TMEM_COLS = 512;          // OZ_S * UM_BN = 448 FP32 columns, rounded up to a power of two
+// instruction descriptor (kind::f16): FP32 accumulator, BF16 A and B, both
+// K-major, N / 8, M / 16
+constexpr uint32_t UM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(UM_BN >> 3) << 17) |
+                              ((uint32_t)(UM_BM >> 4) << 24);
+constexpr long UM_WAIT_LIMIT = 1L << 22;
+static_assert(OZ_S * UM_BN <= (int)UM_TMEM_COLS, "levels must fit in TMEM");
+static_assert(UM_SMEM <= 227 * 1024, "shared memory");
+
+__device__ __forceinline__ uint32_t um_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared memory matrix descriptor: start address, LBO 128 B, SBO 256 B,
+// the fixed 0b001 at bits 46-48, no swizzle
+__device__ __forceinline__ uint64_t um_desc(uint32_t saddr)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+           (1ull << 46);
+}
+__device__ __forceinline__ void um_bar_init(uint32_t bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool um_bar_try(uint32_t bar, unsigned parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool um_bar_wait(uint32_t bar, unsigned parity)
+{
+    for (long it = 0; it < UM_WAIT_LIMIT; it++)
+        if (um_bar_try(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void um_st16(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d)
+{
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+__device__ __forceinline__ void um_mma(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t acc)
+{
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
+        "l"(ad), "l"(bd), "r"(UM_IDESC), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void um_ld16(uint32_t taddr, uint32_t (&v)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr)
+        : "memory");
+}
+
+template <int P>
+__device__ __forceinline__ void um_plane(uint32_t arow, const unsigned long long (&Mb)[16], const unsigned (&ng)[16])
+{
+    uint32_t w[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        w[j] = oz_digit_bf16<P>(Mb[2 * j], ng[2 * j]) | (oz_digit_bf16<P>(Mb[2 * j + 1], ng[2 * j + 1]) << 16);
+    const uint32_t a = arow + P * 2 * UM_ATILE;
+    um_st16(a, w[0], w[1], w[2], w[3]);        // K 0..7 of the step
+    um_st16(a + 128, w[4], w[5], w[6], w[7]);  // K 8..15
+}
+
+// digit planes of op(B) in the shared-memory image of every (column tile,
+// stage): [tile][stage][q][K step][UM_BTILE], and the column exponents
+__global__ void k_oz_bimg(int kk, int nc, const double *B, int ldb, int tb, int ntc, int nstage,
+                          unsigned short *img, int *Fe)
+{
+    const int jg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (jg >= ntc * UM_BN) return;
+    auto bval = [&](int l) -> double { return tb ? B[(size_t)l * ldb + jg] : B[(size_t)jg * ldb + l]; };
+    int E = -2000;
+    if (jg < nc)
+        for (int l = 0; l < kk; l++) E = max(E, oz_exp_of(bval(l)));
+    if (E == -2000) E = 0;
+    Fe[jg] = E;
+    const int ct = jg / UM_BN, j = jg % UM_BN;
+    for (int l = 0; l < nstage * UM_KC; l++) {
+        int d[OZ_S];
+        if (jg < nc && l < kk) oz_digits(bval(l), E, d);
+        else
+#pragma unroll
+            for (int p = 0; p < OZ_S; p++) d[p] = 0;
+        const int c = l / UM_KC, st = (l % UM_KC) / 16, k = l % 16;
+        const size_t base = ((size_t)ct * nstage + c) * UM_BSTAGE + (size_t)((j >> 3) * 256 + (k >> 3) * 128 +
+                                                                             (j & 7) * 16 + (k & 7) * 2);
+#pragma unroll
+        for (int q = 0; q < OZ_S; q++) img[(base + (size_t)(q * 2 + st) * UM_BTILE) / 2] = (unsigned short)oz_bf16(d[q]);
+    }
+}
+
+__global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int kk, const double *__restrict__ A, int lda,
+                                                          const unsigned short *__restrict__ Bimg,
+                                                          const int *__restrict__ Fe, int nstage,
+                                                          double *__restrict__ C, int ldc, int *err)
+{
+    extern __shared__ __align__(1024) unsigned char um_sm[];
+    unsigned char *As = um_sm;
+    unsigned char *Bs = um_sm + 2 * UM_ASTAGE;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(Bs + 2 * UM_BSTAGE);  // [0..1] B copies, [2..3] MMAs
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 4);
+    int *sbad = reinterpret_cast<int *>(tslot + 1);
+    int *Ep = reinterpret_cast<int *>(tslot + 4);  // [2][UM_BM]
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int ntc = (nc + UM_BN - 1) / UM_BN;
+    const int row0 = (blockIdx.x / ntc) * UM_BM, ct = blockIdx.x % ntc, col0 = ct * UM_BN;
+    const uint32_t a_s = um_smem(As), b_s = um_smem(Bs), bar_s = um_smem(bar);
+    if (tid == 0) {
+        for (int i = 0; i < 4; i++) um_bar_init(bar_s + 8 * i, 1);
+        *sbad = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (w == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(um_smem(tslot)),
+                     "r"(UM_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // row exponents: thread (r, h) scans the K columns h, h + 2, ... of row r,
+    // sixteen loads in flight (the scan is latency bound otherwise)
+    const int r = tid & (UM_BM - 1), h = tid >> 7, row = row0 + r;
+    int E = -2000;
+    if (row < mr) {
+        for (int l0 = h; l0 < kk; l0 += 32) {
+            double t[16];
+#pragma unroll
+            for (int u = 0; u < 16; u++) t[u] = (l0 + 2 * u < kk) ? A[(size_t)(l0 + 2 * u) * lda + row] : 0.0;
+#pragma unroll
+            for (int u = 0; u < 16; u++) E = max(E, oz_exp_of(t[u]));
+        }
+    }
+    Ep[h * UM_BM + r] = E;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    E = max(Ep[r], Ep[UM_BM + r]);
+    if (E == -2000) E = 0;
+
+    // thread (r, h) owns K step h of row r in every stage
+    double xv[16];
+    auto load_stage = [&](int c) {
+        const int k0 = c * UM_KC + h * 16;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int l = k0 + i;
+            xv[i] = (row < mr && l < kk) ? A[(size_t)l * lda + row] : 0.0;
+        }
+    };
+    load_stage(0);
+    const uint32_t arow_off = (uint32_t)(h * UM_ATILE + (r >> 3) * 256 + (r & 7) * 16);
+    for (int c = 0; c < nstage; c++) {
+        const int b = c & 1;
+        bool ok = true;
+        if (c >= 2) ok = um_bar_wait(bar_s + 8 * (2 + b), ((c - 2) >> 1) & 1);  // MMAs of stage c - 2 done
+        if (__syncthreads_or(!ok || *sbad)) {
+            if (tid == 0) atomicExch(err, 1);
+            break;
+        }
+        if (tid == 0) {
+            const uint32_t tb_ = bar_s + 8 * b;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tb_), "r"(UM_BSTAGE)
+                         : "memory");
+            const unsigned short *src = Bimg + ((size_t)ct * nstage + c) * (UM_BSTAGE / 2);
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    b_s + b * UM_BSTAGE),
+                "l"(src), "r"(UM_BSTAGE), "r"(tb_)
+                : "memory");
+        }
+        unsigned long long Mb[16];
+        unsigned ng[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) Mb[i] = oz_fixed(xv[i], E, ng[i]);
+        if (c + 1 < nstage) load_stage(c + 1);
+        const uint32_t arow = a_s + b * UM_ASTAGE + arow_off;
+        um_plane<0>(arow, Mb, ng);
+        um_plane<1>(arow, Mb, ng);
+        um_plane<2>(arow, Mb, ng);
+        um_plane<3>(arow, Mb, ng);
+        um_plane<4>(arow, Mb, ng);
+        um_plane<5>(arow, Mb, ng);
+        um_plane<6>(arow, Mb, ng);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            if (!um_bar_wait(bar_s + 8 * b, (c >> 1) & 1)) {
+                *sbad = 1;
+            } else {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+                for (int st = 0; st < 2; st++)
+#pragma unroll
+                    for (int p = 0; p < OZ_S; p++)
+#pragma unroll
+                        for (int q = 0; p + q < OZ_S; q++) {
+                            const uint64_t ad = um_desc(a_s + b * UM_ASTAGE + (p * 2 + st) * UM_ATILE);
+                            const uint64_t bd = um_desc(b_s + b * UM_BSTAGE + (q * 2 + st) * UM_BTILE);
+                            um_mma(tmem + (uint32_t)((p + q) * UM_BN), ad, bd, (c == 0 && st == 0 && p == 0) ? 0u : 1u);
+                        }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 bar_s + 8 * (2 + b))
+                             : "memory");
+            }
+        }
+    }
+    // the last stage's commit covers every MMA of this CTA
+    const int cl = nstage - 1;
+    bool ok = !*sbad && um_bar_wait(bar_s + 8 * (2 + (cl & 1)), (cl >> 1) & 1);
+    const bool bad = __syncthreads_or(!ok);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (bad) {
+        if (tid == 0) atomicExch(err, 1);
+    } else {
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows), columns
+        // 32 (w / 4) .. + 31 in two halves of 16
+        const int L = 32 * (w & 3), hc = w >> 2;
+        const int orow = row0 + L + lane;  // == row
+#pragma unroll
+        for (int ph = 0; ph < 2; ph++) {
+            const int cb = hc * 32 + ph * 16;
+            uint32_t v[OZ_S][16];
+#pragma unroll
+            for (int g = 0; g < OZ_S; g++) um_ld16(tmem + ((uint32_t)L << 16) + (uint32_t)(g * UM_BN + cb), v[g]);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int jj = 0; jj < 16; jj++) {
+                const int col = col0 + cb + jj;
+                long long V = 0;
+#pragma unroll
+                for (int g = 0; g < OZ_S; g++) V = V * 128 + (long long)__float2int_rn(__uint_as_float(v[g][jj]));
+                if (orow < mr && col < nc) C[(size_t)col * ldc + orow] = ldexp((double)V, E + Fe[col] - 14 - 7 * (OZ_S - 1));
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (w == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
+}
+
 // scratch for the digits of B (grown on demand, per host thread)
 struct OzScratch {
     unsigned short *bd = nullptr;
     int *fe = nullptr;
-    size_t cap = 0;
+    int *err = nullptr;
+    int *herr = nullptr;
+    size_t cap = 0, fecap = 0;
     int dev = -1;
     ~OzScratch()
     {
         if (bd) cudaFree(bd);
         if (fe) cudaFree(fe);
+        if (err) cudaFree(err);
+        if (herr) cudaFreeHost(herr);
     }
 };
 
-bool gemm_f64_tc(int mr, int nc, int kk, const double *A, int lda, const double *B, int ldb, bool tb, double *C,
-                 int ldc, cudaStream_t s)
+// need: digit elements of B; nfe: column exponents
+static void oz_scratch(OzScratch &sc, size_t need, int nfe)
 {
-    if (mr < 4096 || nc <= 0 || kk <= 0 || kk > OZ_KMAX) return false;
-    const int Kp = (kk + 15) / 16 * 16;
-    const int ncp = (nc + OZ_BN - 1) / OZ_BN * OZ_BN;
-    static thread_local OzScratch sc;
     int dev = 0;
     PGB_CUDA(cudaGetDevice(&dev));
-    const size_t need = (size_t)OZ_S * ncp * Kp;
-    if (sc.cap < need || sc.dev != dev) {
-        if (sc.bd) { PGB_CUDA(cudaStreamSynchronize(s)); cudaFree(sc.bd); cudaFree(sc.fe); }
-        PGB_CUDA(cudaMalloc(&sc.bd, sizeof(unsigned short) * need));
-        PGB_CUDA(cudaMalloc(&sc.fe, sizeof(int) * (size_t)ncp));
-        sc.cap = need;
+    if (sc.cap < need || sc.fecap < (size_t)nfe || sc.dev != dev) {
+        if (sc.bd) {
+            PGB_CUDA(cudaDeviceSynchronize());
+            cudaFree(sc.bd);
+            cudaFree(sc.fe);
+            sc.bd = nullptr;
+            sc.fe = nullptr;
+        }
+        sc.cap = std::max(sc.cap, need);
+        sc.fecap = std::max(sc.fecap, (size_t)nfe);
+        PGB_CUDA(cudaMalloc(&sc.bd, sizeof(unsigned short) * sc.cap));
+        PGB_CUDA(cudaMalloc(&sc.fe, sizeof(int) * sc.fecap));
         sc.dev = dev;
     }
+    if (!sc.err) {
+        PGB_CUDA(cudaMalloc(&sc.err, sizeof(int)));
+        PGB_CUDA(cudaMallocHost(&sc.herr, sizeof(int)));
+    }
+}
+
+// impl 0: mma.sync kernel; impl 1: tcgen05 kernel
+static void oz_gemm_launch(int impl, int mr, int nc, int kk, const double *A, int lda, const double *B, int ldb,
+                           bool tb, double *C, int ldc, cudaStream_t s)
+{
+    static thread_local OzScratch sc;
+    if (impl == 1) {
+        const int ntc = (nc + UM_BN - 1) / UM_BN;
+        const int nstage = (kk + UM_KC - 1) / UM_KC;
+        oz_scratch(sc, (size_t)ntc * nstage * UM_BSTAGE / 2, ntc * UM_BN);
+        static thread_local bool attr = false;
+        if (!attr) {
+            PGB_CUDA(cudaFuncSetAttribute(k_oz_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
+            attr = true;
+        }
+        PGB_CUDA(cudaMemsetAsync(sc.err, 0, sizeof(int), s));
+        PGB_PROF(PK_GEMM, s, {
+            k_oz_bimg<<<(ntc * UM_BN + 127) / 128, 128, 0, s>>>(kk, nc, B, ldb, tb ? 1 : 0, ntc, nstage, sc.bd, sc.fe);
+            PGB_LAUNCHED();
+            const int grid = (mr + UM_BM - 1) / UM_BM * ntc;
+            k_oz_umma<<<grid, UM_THREADS, UM_SMEM, s>>>(mr, nc, kk, A, lda, sc.bd, sc.fe, nstage, C, ldc, sc.err);
+            PGB_LAUNCHED();
+        });
+        PGB_CUDA(cudaMemcpyAsync(sc.herr, sc.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PGB_CUDA(cudaStreamSynchronize(s));
+        if (*sc.herr) {
+            set_error("tensor-core GEMM: an mbarrier wait ran out");
+            throw WaitFailure();
+        }
+        return;
+    }
+    const int Kp = (kk + 15) / 16 * 16;
+    const int ncp = (nc + OZ_BN - 1) / OZ_BN * OZ_BN;
+    oz_scratch(sc, (size_t)OZ_S * ncp * Kp, ncp);
     const size_t smem = sizeof(unsigned short) * OZ_S * OZ_BN * (size_t)(Kp + 8);
     static thread_local size_t smem_set = 0;
     if (smem > 48 * 1024 && smem_set < smem) {
@@ -302,7 +634,35 @@ bool gemm_f64_tc(int mr, int nc, int kk, const double *A, int lda, const double 
         k_oz_gemm<<<grid, OZ_WARPS * 32, smem, s>>>(mr, nc, kk, A, lda, sc.bd, sc.fe, Kp, ncp, C, ldc);
         PGB_LAUNCHED();
     });
+}
+
+bool gemm_f64_tc(int mr, int nc, int kk, const double *A, int lda, const double *B, int ldb, bool tb, double *C,
+                 int ldc, cudaStream_t s)
+{
+    if (mr < 4096 || nc <= 0 || kk <= 0 || kk > OZ_KMAX) return false;
+    oz_gemm_launch(1, mr, nc, kk, A, lda, B, ldb, tb, C, ldc, s);
     return true;
 }
 
 }  // namespace pgb
+
+// C = A op(B) with device operands through one of the two tensor-core
+// kernels (0: mma.sync, 1: tcgen05); both give the same bits.  Used by the
+// tests to hold the kernels against each other and against FP64 products.
+extern "C" int propack_gemm_f64_tc(int impl, int mr, int nc, int kk, const double *A, int lda, const double *B,
+                                   int ldb, int tb, double *C, int ldc)
+{
+    using namespace pgb;
+    set_error("");
+    if (mr <= 0 || nc <= 0 || kk <= 0 || kk > OZ_KMAX || (impl != 0 && impl != 1) || lda < mr || ldc < mr)
+        return PROPACK_ERR_ARG;
+    try {
+        oz_gemm_launch(impl, mr, nc, kk, A, lda, B, ldb, tb != 0, C, ldc, 0);
+        PGB_CUDA(cudaStreamSynchronize(0));
+    } catch (const CudaFailure &) {
+        return PROPACK_ERR_CUDA;
+    } catch (const WaitFailure &) {
+        return PROPACK_ERR_WAIT;
+    }
+    return 0;
+}

@@ -451,6 +451,7 @@ __device__ void after_cgs(Tail &t, const LbArgs &a, int j, double nrm, int last)
         LbCtl &c = t.c;
         double &cur = SIDE == 0 ? c.alpha : c.beta;
         c.ndot += c.ndot_iter;
+        (SIDE == 1 ? c.cgs_cols_u : c.cgs_cols_v) += c.nsel;
         t.go = 0;
         if (nrm > KAPPA * c.reorth_nrm0) {
             cur = nrm;
@@ -499,13 +500,14 @@ __device__ __forceinline__ const double *csr_vals<double>(const Csr &A) { return
 template <>
 __device__ __forceinline__ const float *csr_vals<float>(const Csr &A) { return A.valf; }
 
-// SHORT: the matrix of this side uses the lane-per-row schedule (compiled
+// SHORT: the matrix of this side uses the chunked schedule (compiled
 // separately so that it carries neither the staged schedule's shared memory
 // nor its registers, and fits more CTAs per SM)
 template <int SIDE, typename T, int SHORT>
-__global__ void __launch_bounds__(BS, SHORT ? 5 : 3) k_lb_spmv(LbArgs a, int j, int host_product)
+__global__ void __launch_bounds__(BS, SHORT ? 4 : 3) k_lb_spmv(LbArgs a, int j, int host_product)
 {
     __shared__ SpmvStage<T, T> st[SHORT ? 1 : SPMV_WARPS];
+    __shared__ ChunkStage<T> cst[SHORT ? SPMV_WARPS : 1];
     __shared__ double sred[32];
     __shared__ Tail t;
     if (a.ctl->status != 0) return;
@@ -537,7 +539,7 @@ __global__ void __launch_bounds__(BS, SHORT ? 5 : 3) k_lb_spmv(LbArgs a, int j, 
     auto pre = [&](int r) -> double { return has_prev ? (double)prev[r] : 0.0; };
     if (!host_product) {
         auto xl = [&](int c) -> T { return c < n0 ? x[c] : (T)z[c - n0]; };
-        if (SHORT) csr_rows_short<T, T>(A.ptr, A.idx, csr_vals<T>(A), A.rows, A.longrows, A.nlong, xl, pre, epi);
+        if (SHORT) csr_rows_chunked<T, T>(A.ptr, A.tbase, A.cidx, chunk_vals<T>(A), A.rows, xl, pre, epi, cst);
         else csr_rows_staged<T, T>(A.ptr, A.idx, csr_vals<T>(A), A.blk, A.nblk, xl, pre, epi, st);
     } else {
         // the caller's APROD already wrote the product into out

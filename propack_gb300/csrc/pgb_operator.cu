@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -206,16 +207,65 @@ __global__ void k_blk_emit(const int *flag, const int *pos, int rows, int *blk)
         if (flag[r]) blk[pos[r]] = r;
     if (blockIdx.x == 0 && threadIdx.x == 0) blk[pos[rows]] = rows;
 }
-__global__ void k_long_flags(const int *ptr, int rows, int *flag)
+// chunked schedule: C = max(1, ceil(E / 32)) units of 32 entries per tile
+__global__ void k_chunk_count(const int *ptr, int rows, int *cnt)
 {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
-        flag[r] = (ptr[r + 1] - ptr[r]) > SHORT_MAX;
+    const int ntiles = (rows + 31) / 32;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+        const int e = ptr[min(32 * t + 32, rows)] - ptr[32 * t];
+        cnt[t] = max(1, (e + 31) / 32);
+    }
 }
-__global__ void k_long_emit(const int *flag, const int *pos, int rows, int *list)
+// entry p of tile t goes to unit tbase[t] + p % C, lane p / C
+__global__ void k_chunk_scatter(const int *ptr, const int *idx, const double *val, const float *valf, int rows,
+                                const int *tbase, int *cidx, double *cval, float *cvalf)
 {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
-        if (flag[r]) list[pos[r]] = r;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        const int t = r >> 5, eb = ptr[32 * t], t0 = tbase[t], C = tbase[t + 1] - t0;
+        for (int e = ptr[r]; e < ptr[r + 1]; e++) {
+            const int p = e - eb;
+            const size_t pos = ((size_t)t0 + p % C) * 32 + p / C;
+            cidx[pos] = idx[e];
+            cval[pos] = val[e];
+            cvalf[pos] = valf[e];
+        }
+    }
 }
+
+// the run-interleaved copy of the matrix for the chunked schedule (after
+// its FP32 values)
+static void build_chunks(Csr &A, cudaStream_t s)
+{
+    if (A.rows == 0 || A.cidx) return;
+    const int ntiles = (A.rows + 31) / 32;
+    int *cnt = nullptr;
+    PGB_CUDA(cudaMallocAsync(&cnt, sizeof(int) * (ntiles + 1), s));
+    PGB_CUDA(cudaMalloc(&A.tbase, sizeof(int) * (ntiles + 1)));
+    const int g = std::min(4096, std::max(1, (ntiles + 255) / 256));
+    k_chunk_count<<<g, 256, 0, s>>>(A.ptr, A.rows, cnt);
+    PGB_LAUNCHED();
+    const size_t units = (size_t)scan_excl(cnt, A.tbase, ntiles, s);
+    PGB_CUDA(cudaFreeAsync(cnt, s));
+    const size_t len = units * 32;
+    PGB_CUDA(cudaMalloc(&A.cidx, sizeof(int) * len));
+    PGB_CUDA(cudaMalloc(&A.cval, sizeof(double) * len));
+    PGB_CUDA(cudaMalloc(&A.cvalf, sizeof(float) * len));
+    PGB_CUDA(cudaMemsetAsync(A.cidx, 0, sizeof(int) * len, s));
+    PGB_CUDA(cudaMemsetAsync(A.cval, 0, sizeof(double) * len, s));
+    PGB_CUDA(cudaMemsetAsync(A.cvalf, 0, sizeof(float) * len, s));
+    const int gr = std::min(4096, std::max(1, (A.rows + 255) / 256));
+    k_chunk_scatter<<<gr, 256, 0, s>>>(A.ptr, A.idx, A.val, A.valf, A.rows, A.tbase, A.cidx, A.cval, A.cvalf);
+    PGB_LAUNCHED();
+}
+
+static void free_chunks(Csr &A)
+{
+    cudaFree(A.tbase); cudaFree(A.cidx); cudaFree(A.cval); cudaFree(A.cvalf);
+    A.tbase = A.cidx = nullptr;
+    A.cval = nullptr;
+    A.cvalf = nullptr;
+}
+
 static void build_blocks(Csr &A, cudaStream_t s)
 {
     int *flag = nullptr, *pos = nullptr;
@@ -232,15 +282,6 @@ static void build_blocks(Csr &A, cudaStream_t s)
     PGB_CUDA(cudaMalloc(&A.blk, sizeof(int) * (A.nblk + 1)));
     k_blk_emit<<<g, 256, 0, s>>>(flag, pos, rows, A.blk);
     PGB_LAUNCHED();
-    if (A.short_rows && rows > 0) {
-        // the rows the lane-per-row schedule leaves to whole warps
-        k_long_flags<<<g, 256, 0, s>>>(A.ptr, rows, flag);
-        PGB_LAUNCHED();
-        A.nlong = scan_excl(flag, pos, rows, s);
-        PGB_CUDA(cudaMalloc(&A.longrows, sizeof(int) * std::max(A.nlong, 1)));
-        k_long_emit<<<g, 256, 0, s>>>(flag, pos, rows, A.longrows);
-        PGB_LAUNCHED();
-    }
     PGB_CUDA(cudaFreeAsync(flag, s));
     PGB_CUDA(cudaFreeAsync(pos, s));
 }
@@ -492,11 +533,12 @@ __global__ void __launch_bounds__(BS) k_spmv_plain(Csr A, const T *__restrict__ 
                                                    T *__restrict__ y)
 {
     __shared__ SpmvStage<T, T> st[SPMV_WARPS];
+    __shared__ ChunkStage<T> cst[SPMV_WARPS];
     const int n0 = A.ncol0;
     auto xl = [&](int c) -> T { return c < n0 ? __ldg(x + c) : (T)z[c - n0]; };
     auto pre = [&](int r) -> double { return 0.0; };
     auto epi = [&](int r, double acc, double) { y[r] = (T)acc; };
-    csr_spmv<T, T>(A, plain_vals<T>(A), xl, pre, epi, st);
+    csr_spmv<T, T>(A, plain_vals<T>(A), xl, pre, epi, st, cst);
 }
 
 // one wave of CTAs at the kernel's occupancy
@@ -529,6 +571,68 @@ void op_spmv_plain_launch(const Csr &A, const double *x, const double *z, double
     PGB_LAUNCHED();
 }
 
+// ------------------------------------------------- schedule selection
+// propack_set_spmv_schedule: 0 timed choice (default), 1 chunked, 2 staged
+static std::atomic<int> g_sched{0};
+constexpr int CHUNK_MEAN_MAX = 64;  // the timed choice tries the chunked schedule below this mean row length
+
+// mean device ms of one plain product with the matrix's current schedule
+static float time_spmv(const Csr &A, const double *x, const double *z, double *y, cudaStream_t s)
+{
+    cudaEvent_t e0, e1;
+    PGB_CUDA(cudaEventCreate(&e0));
+    PGB_CUDA(cudaEventCreate(&e1));
+    op_spmv_plain_launch(A, x, z, y, s);
+    PGB_CUDA(cudaEventRecord(e0, s));
+    for (int i = 0; i < 3; i++) op_spmv_plain_launch(A, x, z, y, s);
+    PGB_CUDA(cudaEventRecord(e1, s));
+    PGB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    PGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / 3.f;
+}
+
+// Sets A.short_rows (1: chunked, 0: staged).  The timed choice builds the
+// chunked copy, runs both schedules on the device and keeps the chunked one
+// when it wins (the staged one needs no extra memory).  The rule it starts
+// from (chunked below a mean of SHORT_MEAN nonzeros per row) is kept unless
+// the other schedule is more than 5 % faster, so that near-ties do not
+// flip between builds.
+static void choose_schedule(Csr &A, const double *z, cudaStream_t s)
+{
+    const int mode = g_sched.load();
+    const bool rule = A.rows > 0 && A.nnz < (int64_t)SHORT_MEAN * A.rows;
+    A.short_rows = 0;
+    if (A.rows == 0 || mode == 2) return;
+    if (mode == 1) {
+        build_chunks(A, s);
+        A.short_rows = 1;
+        return;
+    }
+    if (A.nnz >= (int64_t)CHUNK_MEAN_MAX * A.rows) return;
+    build_chunks(A, s);
+    double *x = nullptr, *y = nullptr;
+    PGB_CUDA(cudaMallocAsync(&x, sizeof(double) * std::max(A.ncol0, 1), s));
+    PGB_CUDA(cudaMallocAsync(&y, sizeof(double) * A.rows, s));
+    PGB_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * std::max(A.ncol0, 1), s));
+    A.short_rows = 1;
+    const float tc = time_spmv(A, x, z, y, s);
+    A.short_rows = 0;
+    const float ts = time_spmv(A, x, z, y, s);
+    PGB_CUDA(cudaFreeAsync(x, s));
+    PGB_CUDA(cudaFreeAsync(y, s));
+    const bool chunked = rule ? !(ts < 0.95f * tc) : (tc < 0.95f * ts);
+    A.short_rows = chunked ? 1 : 0;
+    A.tuned_ms[0] = tc;
+    A.tuned_ms[1] = ts;
+    if (!chunked) {
+        PGB_CUDA(cudaStreamSynchronize(s));
+        free_chunks(A);
+    }
+}
+
 template <typename T>
 void op_apply(const Operator &op, bool trans, const T *x, T *y, cudaStream_t s)
 {
@@ -556,7 +660,8 @@ Operator *lookup_operator(int64_t handle)
 
 static void free_csr(Csr &A)
 {
-    cudaFree(A.ptr); cudaFree(A.idx); cudaFree(A.val); cudaFree(A.valf); cudaFree(A.blk); cudaFree(A.longrows);
+    cudaFree(A.ptr); cudaFree(A.idx); cudaFree(A.val); cudaFree(A.valf); cudaFree(A.blk);
+    free_chunks(A);
     A = Csr();
 }
 
@@ -658,6 +763,7 @@ static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, c
         PGB_CUDA(cudaMalloc(&A->valf, sizeof(float) * std::max<int64_t>(A->nnz, 1)));
         k_to_float<<<g, 256, 0, s>>>(A->val, A->valf, A->nnz);
         PGB_LAUNCHED();
+        choose_schedule(*A, op->zbuf, s);
     }
     PGB_CUDA(cudaStreamSynchronize(s));
     cudaFree(dsp); cudaFree(dsi); cudaFree(dsv);
@@ -717,6 +823,28 @@ extern "C" int propack_csr_create(int m, int n, const int64_t *s_rowptr, const i
 }
 
 extern "C" int propack_csr_destroy(int64_t handle) { return destroy_operator(handle); }
+
+extern "C" int propack_set_spmv_schedule(int mode)
+{
+    if (mode < 0 || mode > 2) return PROPACK_ERR_ARG;
+    g_sched.store(mode);
+    return 0;
+}
+
+extern "C" int propack_csr_schedule(int64_t handle, int *sched, float *tuned_ms)
+{
+    Operator *op = lookup_operator(handle);
+    if (!op) return PROPACK_ERR_HANDLE;
+    const Csr *M[2] = {&op->fwd, &op->adj};
+    for (int i = 0; i < 2; i++) {
+        if (sched) sched[i] = M[i]->short_rows;
+        if (tuned_ms) {
+            tuned_ms[2 * i] = M[i]->tuned_ms[0];
+            tuned_ms[2 * i + 1] = M[i]->tuned_ms[1];
+        }
+    }
+    return 0;
+}
 
 extern "C" void propack_handle_to_iparm(int64_t handle, int *iparm)
 {

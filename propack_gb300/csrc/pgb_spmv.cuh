@@ -10,21 +10,29 @@
 //   row (g = 32 / rows in the block, a power of two) then form the row sums
 //   from shared memory.  A long row is streamed by the whole warp.
 //
-// short (most rows shorter than ~16): a warp takes 32 consecutive rows, one
-//   lane per row; each lane walks its row in order with four (index, value)
-//   pairs and four gathers in flight, so an instruction per nonzero and
-//   lane is all the row costs.  Rows longer than SHORT_MAX are skipped by
-//   the tiles and streamed afterwards, a whole warp per row, from a list.
+// chunked (rows shorter than ~16 on average): a warp takes 32 consecutive
+//   rows (a tile; each warp a contiguous range of tiles holding an equal
+//   share of the entries) and splits the tile's E entries, in CSR order, into 32
+//   runs of C = ceil(E / 32) entries, one run per lane, whatever the row
+//   lengths.  The operator build stores the tile's entries run-interleaved
+//   (entry p at unit p % C, lane p / C), so every (index, value) load of
+//   the warp is one coalesced 128/256-byte access, and every lane issues
+//   the same C FP64 FMAs: a tile's FMA count is E / 32 instead of the
+//   length of its longest row, which matters on a GPU whose FP64 pipe
+//   retires two lanes per clock.  A row that ends inside a run is summed
+//   by that lane alone, in CSR order; a row spread over several runs adds
+//   the runs' partial sums in lane order.
 //
 // Summation order depends only on the matrix, never on timing, so results
 // are bit-reproducible.
 #pragma once
+#include <climits>
+
 #include "pgb.cuh"
 
 namespace pgb {
 
 constexpr int SPMV_WARPS = BS / 32;  // warps per CTA
-constexpr int SHORT_MAX = 48;        // longest row a lane sums alone (short schedule)
 
 // One warp's shared-memory stage of the staged schedule: the block's
 // values and gathered inputs.
@@ -132,81 +140,133 @@ __device__ __forceinline__ void csr_rows_staged(const int *__restrict__ ptr, con
 }
 
 
-// the short-row schedule (see the top of the file).  Rows longer than
-// SHORT_MAX are skipped by the tiles and streamed afterwards, one whole warp
-// per row, from the matrix's list of long rows; the bounds of a warp's next
-// tile are loaded with the current tile's first pairs.
-template <typename VT, typename AT, typename XF, typename PF, typename EPI>
-__device__ __forceinline__ void csr_rows_short(const int *__restrict__ ptr, const int *__restrict__ idx,
-                                               const VT *__restrict__ val, int nrows, const int *__restrict__ longrows,
-                                               int nlong, XF xload, PF pre_load, EPI epi)
+template <typename VT>
+__device__ __forceinline__ const VT *chunk_vals(const Csr &A);
+template <>
+__device__ __forceinline__ const double *chunk_vals<double>(const Csr &A) { return A.cval; }
+template <>
+__device__ __forceinline__ const float *chunk_vals<float>(const Csr &A) { return A.cvalf; }
+
+template <typename AT>
+struct ChunkStage {
+    AT part[32];  // row q: the sum of its entries in the run where it ends
+    AT tail[32];  // lane l: the sum of the row still open at the end of its run
+    int bnd[33];  // row bounds of the tile, relative to its first entry
+};
+
+// first i in [0, n) with t[i] >= key (t non-decreasing, t[n-1] >= key), by
+// a 32-way search of the whole warp
+__device__ __forceinline__ int warp_lower_bound(const int *__restrict__ t, int n, int key)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int nwarps = gridDim.x * SPMV_WARPS;
-    const int gw = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
-    const int ntiles = (nrows + 31) / 32;
-    int tile = gw;
-    if (tile < ntiles) {
-        int r = tile * 32 + lane;
-        int e0 = r < nrows ? ptr[r] : 0;
-        int e1 = r < nrows ? ptr[r + 1] : 0;
-        while (true) {
-            const bool own = r < nrows && e1 - e0 <= SHORT_MAX;
-            const double pre = own ? pre_load(r) : 0.0;
-            const int ntile = tile + nwarps;
-            const int rn = ntile * 32 + lane;
-            int n0 = 0, n1 = 0;
-            if (ntile < ntiles && rn < nrows) { n0 = ptr[rn]; n1 = ptr[rn + 1]; }
-            if (own) {
-                AT acc = 0;
-                int e = e0;
-                for (; e + 3 < e1; e += 4) {
-                    const int c0 = idx[e], c1 = idx[e + 1], c2 = idx[e + 2], c3 = idx[e + 3];
-                    const VT v0 = val[e], v1 = val[e + 1], v2 = val[e + 2], v3 = val[e + 3];
-                    const AT x0 = (AT)xload(c0), x1 = (AT)xload(c1), x2 = (AT)xload(c2), x3 = (AT)xload(c3);
-                    acc = fma((AT)v0, x0, acc);
-                    acc = fma((AT)v1, x1, acc);
-                    acc = fma((AT)v2, x2, acc);
-                    acc = fma((AT)v3, x3, acc);
-                }
-                for (; e < e1; e++) acc = fma((AT)val[e], (AT)xload(idx[e]), acc);
-                epi(r, (double)acc, pre);
-            }
-            tile = ntile;
-            if (tile >= ntiles) break;
-            r = rn;
-            e0 = n0;
-            e1 = n1;
+    int lo = 0, hi = n;  // the answer lies in [lo, hi]
+    while (hi - lo > 32) {
+        const int step = (hi - lo + 31) / 32;
+        const unsigned m = __ballot_sync(FULL, t[min(lo + lane * step, hi - 1)] >= key);
+        if (m == 0) {
+            lo = min(lo + 31 * step + 1, hi);
+        } else {
+            const int f = __ffs(m) - 1;
+            const int nhi = min(lo + f * step, hi);
+            lo = f > 0 ? lo + (f - 1) * step + 1 : lo;
+            hi = nhi;
         }
     }
-    for (int li = gw; li < nlong; li += nwarps) {
-        const int r = longrows[li];
-        const int f0 = ptr[r], f1 = ptr[r + 1];
-        const double pre = lane == 0 ? pre_load(r) : 0.0;
-        AT s = 0;
-        int e = f0 + lane;
-        for (; e + 96 < f1; e += 128) {
-            const int c0 = idx[e], c1 = idx[e + 32], c2 = idx[e + 64], c3 = idx[e + 96];
-            const VT v0 = val[e], v1 = val[e + 32], v2 = val[e + 64], v3 = val[e + 96];
-            const AT x0 = (AT)xload(c0), x1 = (AT)xload(c1), x2 = (AT)xload(c2), x3 = (AT)xload(c3);
-            s = fma((AT)v0, x0, s);
-            s = fma((AT)v1, x1, s);
-            s = fma((AT)v2, x2, s);
-            s = fma((AT)v3, x3, s);
+    const unsigned m = __ballot_sync(FULL, lo + lane < hi ? t[lo + lane] >= key : true);
+    return lo + __ffs(m) - 1;
+}
+
+template <typename VT, typename AT, typename XF, typename PF, typename EPI>
+__device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, const int *__restrict__ tbase,
+                                                 const int *__restrict__ cidx, const VT *__restrict__ cval,
+                                                 int nrows, XF xload, PF pre_load, EPI epi, ChunkStage<AT> *stages)
+{
+    const int lane = threadIdx.x & 31;
+    ChunkStage<AT> &cs = stages[threadIdx.x >> 5];
+    const int nwarps = gridDim.x * SPMV_WARPS;
+    const int ntiles = (nrows + 31) / 32;
+    // each warp takes the contiguous tiles whose first unit falls in its
+    // equal share of all units: equal work per warp, so that no warp of a
+    // CTA waits long for the others at the closing reductions
+    const long long gw = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
+    const int units = tbase[ntiles];
+    const int tb0 = warp_lower_bound(tbase, ntiles + 1, (int)(units * gw / nwarps));
+    const int tb1 = warp_lower_bound(tbase, ntiles + 1, (int)(units * (gw + 1) / nwarps));
+    for (int tile = tb0; tile < tb1; tile++) {
+        const int r = tile * 32 + lane;
+        const int eb = ptr[tile * 32];
+        const int lo = ptr[min(r, nrows)] - eb;      // rows past the end are empty
+        const int hi = ptr[min(r + 1, nrows)] - eb;
+        const int t0 = tbase[tile], C = tbase[tile + 1] - t0;  // C >= 1
+        const double pre = r < nrows ? pre_load(r) : 0.0;
+        cs.bnd[lane] = lo;
+        if (lane == 31) cs.bnd[32] = hi;
+        cs.part[lane] = (AT)0;
+        __syncwarp();
+        // the row holding the run's first entry p0: the last q with
+        // bnd[q] <= p0 (a non-empty row), or 32 when p0 is past the entries
+        const int p0 = lane * C;
+        int q = 0;
+#pragma unroll
+        for (int st = 16; st > 0; st >>= 1)
+            if (cs.bnd[q + st] <= p0) q += st;
+        if (cs.bnd[32] <= p0) q = 32;
+        int nend = q < 32 ? cs.bnd[q + 1] : INT_MAX;
+        int p = p0;
+        AT acc = (AT)0;
+        const size_t off = (size_t)t0 * 32 + lane;
+        const int *ci = cidx + off;
+        const VT *cv = cval + off;
+        // one entry of the run; closes row q when it ends at this entry
+        auto step = [&](VT v, AT xv) {
+            acc = fma((AT)v, xv, acc);
+            if (++p == nend) {
+                cs.part[q] = acc;
+                acc = (AT)0;
+                do { ++q; } while (q < 32 && cs.bnd[q + 1] == p);
+                nend = q < 32 ? cs.bnd[q + 1] : INT_MAX;
+            }
+        };
+        int i = 0;
+        for (; i + 3 < C; i += 4) {
+            int c[4];
+            VT v[4];
+            AT xv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) { c[u] = ci[32 * (i + u)]; v[u] = cv[32 * (i + u)]; }
+#pragma unroll
+            for (int u = 0; u < 4; u++) xv[u] = (AT)xload(c[u]);
+#pragma unroll
+            for (int u = 0; u < 4; u++) step(v[u], xv[u]);
         }
-        for (; e < f1; e += 32) s = fma((AT)val[e], (AT)xload(idx[e]), s);
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
-        if (lane == 0) epi(r, (double)s, pre);
+        for (; i < C; i++) step(cv[32 * i], (AT)xload(ci[32 * i]));
+        cs.tail[lane] = acc;
+        __syncwarp();
+        // row `lane`: its runs ls .. le, added in lane order
+        AT tot = (AT)0;
+        if (lo < hi) {
+            const int ls = lo / C, le = (hi - 1) / C;
+            if (ls == le) {
+                tot = cs.part[lane];
+            } else {
+                tot = cs.tail[ls];
+                for (int l2 = ls + 1; l2 < le; l2++) tot += cs.tail[l2];
+                tot += cs.part[lane];
+            }
+        }
+        if (r < nrows) epi(r, (double)tot, pre);
+        __syncwarp();
     }
 }
 
 // the schedule chosen for the matrix
 template <typename VT, typename AT, typename XF, typename PF, typename EPI>
 __device__ __forceinline__ void csr_spmv(const Csr &A, const VT *__restrict__ val, XF xload, PF pre_load, EPI epi,
-                                         SpmvStage<VT, AT> *stages)
+                                         SpmvStage<VT, AT> *stages, ChunkStage<AT> *cstages)
 {
-    if (A.short_rows) csr_rows_short<VT, AT>(A.ptr, A.idx, val, A.rows, A.longrows, A.nlong, xload, pre_load, epi);
+    if (A.short_rows)
+        csr_rows_chunked<VT, AT>(A.ptr, A.tbase, A.cidx, chunk_vals<VT>(A), A.rows, xload, pre_load, epi, cstages);
     else csr_rows_staged<VT, AT>(A.ptr, A.idx, val, A.blk, A.nblk, xload, pre_load, epi, stages);
 }
 

@@ -9,7 +9,12 @@ schedule).
 * coordinate ASCII (``.coord``): one ``i j a`` triple per line, 1-based,
   optionally preceded by an ``m n nnz`` line;
 * dense ASCII (``.dense``): ``m n`` then the m*n values, column by column
-  (Fortran order, as the reference's programs store arrays).
+  (Fortran order, as the reference's programs store arrays);
+* diagonal ASCII (``.diag``): ``m n ndiag``, then per stored diagonal its
+  offset d (entries A(i, i+d)) followed by its min(m, n-d) - max(0, -d)
+  values in order of increasing row.  The reference's example reader for
+  this format is not in its source tree (README:113-118 names it), so this
+  is the plain DIA layout its name describes.
 Symmetric Harwell-Boeing / Matrix Market input is expanded to both
 triangles by the scipy readers.
 """
@@ -34,6 +39,8 @@ def read(path, fmt=None):
         A = _read_coord(path)
     elif fmt == "dense":
         A = _read_dense(path)
+    elif fmt == "diag":
+        A = _read_diag(path)
     else:
         raise ValueError(f"unknown matrix format {fmt!r}")
     A = sp.csr_array(A, dtype=np.float64)
@@ -67,6 +74,25 @@ def _read_dense(path):
         v = np.array(f.read().split(), dtype=np.float64)
     m, n = int(v[0]), int(v[1])
     return v[2:2 + m * n].reshape((m, n), order="F")
+
+
+def _read_diag(path):
+    with open(path) as f:
+        v = f.read().split()
+    m, n, nd = int(v[0]), int(v[1]), int(v[2])
+    pos, rows, cols, vals = 3, [], [], []
+    for _ in range(nd):
+        d = int(float(v[pos]))
+        pos += 1
+        i0, i1 = max(0, -d), min(m, n - d)
+        cnt = max(0, i1 - i0)
+        i = np.arange(i0, i0 + cnt)
+        rows.append(i)
+        cols.append(i + d)
+        vals.append(np.array(v[pos:pos + cnt], dtype=np.float64))
+        pos += cnt
+    cat = lambda a, t: np.concatenate(a).astype(t) if a else np.zeros(0, t)
+    return sp.coo_array((cat(vals, np.float64), (cat(rows, np.int64), cat(cols, np.int64))), shape=(m, n))
 
 
 def load(path, fmt=None):

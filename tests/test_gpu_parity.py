@@ -25,7 +25,7 @@ def rng0():
 
 
 # ------------------------------------------------------------ operator
-@pytest.mark.parametrize("kind", ["plain", "lowrank", "zipf", "longcols"])
+@pytest.mark.parametrize("kind", ["plain", "lowrank", "zipf", "longcols", "ragged"])
 def test_operator_products(kind):
     rng = np.random.default_rng(3)
     if kind == "plain":
@@ -39,6 +39,18 @@ def test_operator_products(kind):
         S = workloads.zipf_mixed(seed=4, m=20000, hi=5000)
         L = R = w = None
         Ad = None
+    elif kind == "ragged":
+        # short-row schedule edge cases: empty rows, single entries, rows
+        # spread over many lanes' runs, a row count that is not a multiple of 32
+        m, n = 5003, 4000
+        lens = rng.integers(0, 8, m)
+        lens[rng.random(m) < 0.2] = 0
+        lens[rng.choice(m, 12, replace=False)] = rng.integers(100, 3500, 12)
+        ptr = np.concatenate([[0], np.cumsum(lens)])
+        idx = np.concatenate([np.sort(rng.choice(n, k, replace=False)) for k in lens]).astype(np.int32)
+        S = sp.csr_array((rng.standard_normal(ptr[-1]), idx, ptr), shape=(m, n))
+        L = R = w = None
+        Ad = S.toarray()
     else:
         # dense columns and long rows: exercises the long-segment transpose and single-row blocks
         m, n = 3000, 50
@@ -60,6 +72,27 @@ def test_operator_products(kind):
     np.testing.assert_allclose(got_t, ref_t, rtol=1e-12, atol=1e-12 * np.abs(ref_t).max())
     # bit-reproducible: same inputs give the same bits
     assert np.array_equal(op.rmatvec(y), got_t)
+    op.close()
+
+
+@pytest.mark.parametrize("mode", ["chunked", "staged", "tuned"])
+def test_spmv_schedules(mode):
+    # every schedule gives the product; the timed choice picks one of them
+    rng = np.random.default_rng(11)
+    S = workloads.zipf_mixed(seed=6, m=30000, hi=3000)
+    pg.set_spmv_schedule(mode)
+    try:
+        op = pg.CsrOperator(S)
+    finally:
+        pg.set_spmv_schedule("tuned")
+    sched, timed = op.schedule
+    if mode != "tuned":
+        assert sched == {"fwd": mode, "adj": mode} and not timed
+    else:
+        assert set(timed) == {("fwd", "chunked"), ("fwd", "staged"), ("adj", "chunked"), ("adj", "staged")}
+    x, y = rng.standard_normal(S.shape[1]), rng.standard_normal(S.shape[0])
+    for got, ref in ((op.matvec(x), S @ x), (op.rmatvec(y), S.T @ y)):
+        np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
     op.close()
 
 

@@ -176,3 +176,15 @@ def test_matrix_file_formats_round_trip(tmp_path):
         f.write(f"{D.shape[0]} {D.shape[1]}\n")
         f.write("\n".join(repr(float(x)) for x in D.ravel(order="F")))
     assert np.array_equal(pio.read(str(p)).toarray(), D)
+    # banded matrix in the diagonal format (offsets -2, 0, 3; a wide shape)
+    m, n = 12, 17
+    B = np.zeros((m, n))
+    p = tmp_path / "a.diag"
+    with open(p, "w") as f:
+        f.write(f"{m} {n} 3\n")
+        for d in (-2, 0, 3):
+            i = np.arange(max(0, -d), min(m, n - d))
+            vals = rng.standard_normal(i.size)
+            B[i, i + d] = vals
+            f.write(f"{d} " + " ".join(repr(float(x)) for x in vals) + "\n")
+    assert np.array_equal(pio.read(str(p)).toarray(), B)
