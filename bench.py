@@ -30,9 +30,12 @@ triplets), run in each form of --forms (the first is the chosen form):
 * e2e      chosen form through the public C ABI with HOST inputs: upload of
            the CSR arrays from pinned memory + device transpose + solve +
            copy of sigma, U(:,1:k), V(:,1:k) back to pinned memory.
-* roofline the fused SpMV pair of the chosen form (the HBM-bound kernel):
-           algorithmic bytes per launch / mean launch time, from events
-           around every launch in one profiled solve.
+* roofline the kernel pair with the most device time (`rooflines` has
+           both): the fused SpMV pair (algorithmic bytes per launch / mean
+           launch time, from events around every launch in one profiled
+           solve) or the Gram-Schmidt projection + update pair (2 x basis
+           columns streamed x length x 8 bytes / their total time; FP64 FMA
+           rate against the FP64 pipe's nominal 2 lanes/clock/SM beside it).
 * cpu_baseline / --impl reference: the oracle (the C restatement of
            PROPACK, FP64, OpenMP) on the host cores, timing one complete IRL
            cycle (maxiter=1) of the same workload and scaling it by matvecs
@@ -110,6 +113,32 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def shard_problems(costs, rank, world):
+    """Indices of the batched problems that rank `rank` of `world` solves:
+    longest-processing-time greedy on the costs (nonzeros), ties broken by
+    index, so that every rank computes the same partition without talking."""
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0] * world
+    owner = [0] * len(costs)
+    for i in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[i] = r
+        load[r] += costs[i]
+    return [i for i in range(len(costs)) if owner[i] == rank]
+
+
+def reduce_ranks(vals, op, world):
+    """Elementwise max (op "max") or sum (op "sum") of a list of floats over
+    the ranks of the default process group (identity for one rank)."""
+    if world == 1:
+        return [float(v) for v in vals]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return t.tolist()
 
 
 def make_workload(name, scale=1.0):
@@ -402,12 +431,23 @@ def run_ours(args, wl):
     kd, ku = ("cgs_dots_fp32", "cgs_upd_fp32") if chosen == "mixed" else ("cgs_dots", "cgs_upd")
     cgs_ms = prof[kd][1] + prof[ku][1]
     if cgs_ms > 0:
-        cgs_bytes = 2.0 * vb * (st_prof["cgs_cols_u"] * m + st_prof["cgs_cols_v"] * n)
+        elems = st_prof["cgs_cols_u"] * m + st_prof["cgs_cols_v"] * n
+        cgs_bytes = 2.0 * vb * elems
         a_cgs = cgs_bytes / (cgs_ms * 1e-3) / 1e9
         roof_cgs = {"bound": "hbm", "kernel": "Gram-Schmidt projection + update pair", "achieved": a_cgs, "peak": peak,
                     "peak_source": peak_kind, "unit": "GB/s", "frac": a_cgs / peak,
                     "columns_streamed": {"u": int(st_prof["cgs_cols_u"]), "v": int(st_prof["cgs_cols_v"])},
                     "algorithmic_bytes": cgs_bytes, "ms": cgs_ms}
+        if vb == 8 and clocks and clocks.get("sm_mhz"):
+            # one FP64 FMA per element in each of the two kernels; the FP64
+            # pipe retires 2 lanes per clock per SM (152 SMs)
+            rate = 2.0 * elems / (cgs_ms * 1e-3)
+            nominal = 2.0 * 152 * clocks["sm_mhz"] * 1e6
+            roof_cgs["fp64_fma_per_s"] = rate
+            roof_cgs["fp64_pipe_frac_of_nominal"] = rate / nominal
+    roof["ms"] = t_fwd + t_adj
+    # the headline roofline is the kernel pair that takes the most device time
+    dominant = roof_cgs if roof_cgs and roof_cgs["ms"] > roof["ms"] else roof
     cpu = None
     if not args.no_cpu:
         cores = os.cpu_count() or 1
@@ -438,8 +478,8 @@ def run_ours(args, wl):
             "speedup_vs_plain_fp64": {f: per["fp64"] / per[f] for f in forms} if "fp64" in per else None,
             "max_rel_sigma_diff_vs_fp64": sig_err,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": int(sum(results[f]["launches"] for f in forms)), "roofline": roof,
-            "roofline_reorth": roof_cgs,
+            "gpu_launches": int(sum(results[f]["launches"] for f in forms)), "roofline": dominant,
+            "rooflines": {"spmv_pair": roof, "gram_schmidt": roof_cgs},
             "cpu_baseline": cpu, "clocks": clocks, "kernel_breakdown": breakdown}
     print(json.dumps(line))
     return 0
@@ -453,18 +493,27 @@ def run_batched(args, wl):
     import numpy as np
     from propack_gb300 import batch
     rank, world, local = dist_env()
-    if rank != 0:
+    if args.impl == "reference" and rank != 0:
         return 0
     nprob = max(1, int(round(wl["nprob"] * args.scale)))
     mats = batch.random_batch(nprob, seed=3)
-    nnz = sum(A.nnz for A in mats)
-    mtot = sum(A.shape[0] for A in mats)
-    ntot = sum(A.shape[1] for A in mats)
     rng = np.random.default_rng(0)
     u0 = [rng.uniform(size=A.shape[0]) for A in mats]
     k, kmax, tol = wl["k"], wl["kmax"], wl["tol"]
     if args.impl == "reference":
         return run_batched_reference(args, wl, mats, u0, nprob)
+    all_mats, all_u0 = mats, u0
+    if world > 1:
+        # independent problems: each rank solves its share, no collective on
+        # the data path (gloo only for the closing max / sums)
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        mine = shard_problems([A.nnz for A in mats], rank, world)
+        mats, u0 = [mats[i] for i in mine], [u0[i] for i in mine]
+    nnz = sum(A.nnz for A in all_mats)
+    mtot = sum(A.shape[0] for A in all_mats)
+    ntot = sum(A.shape[1] for A in all_mats)
     B = batch.Batch(mats)
     for _ in range(args.warmup):
         B.solve(k, kmax=kmax, tol=tol, maxiter=100, u0=u0, vectors=False)
@@ -486,6 +535,14 @@ def run_batched(args, wl):
     B2.close()
     e2e_ms = (time.perf_counter() - t0) * 1e3
     conv = int(np.sum(info == 0))
+    launches = int(sum(s_["kernel_launches"] for s_ in stats_l))
+    # whole job: the slowest rank's times, every rank's counts
+    value, e2e_ms = reduce_ranks([value, e2e_ms], "max", world)
+    conv, nopx, launches = (int(v) for v in reduce_ranks([conv, st["nopx"], launches], "sum", world))
+    st = dict(st, nopx=nopx)
+    if rank != 0:
+        return 0
+    mats, u0 = all_mats, all_u0
     # algorithmic bytes: every matvec reads its matrix (FP32 value + int32
     # index per nonzero, row pointers) and its FP64 in/out vectors
     avg_mv_bytes = (nnz * 8 + (mtot + ntot) * 4 + 2 * (mtot + ntot) * 8) / nprob
@@ -495,8 +552,9 @@ def run_batched(args, wl):
     if not args.no_cpu:
         cpu = batched_cpu_sample(mats, u0, wl)
     line = {"metric": "ms per batch to top-8 triplets of every problem at tol=1e-8 (problems/s alongside), 1 GB300",
-            "value": value, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": value, "higher_is_better": False, "scaling": "strong" if world > 1 else "weak",
+            "vs_baseline": None,
             "dtype": "f64 vectors, f32 matrix values", "data": "synthetic (seeded numpy default_rng)",
             "config": {"workload": "batched", "desc": wl["desc"], "nprob": nprob, "nnz": int(nnz),
                        "fraction_of_4096": nprob / 4096, "l2": "batch data (GBs) larger than L2; no flush"},
@@ -505,7 +563,7 @@ def run_batched(args, wl):
             "e2e": {"value": e2e_ms, "unit": "ms",
                     "h2d_bytes_per_step": int(nnz * 8 + (mtot + nprob) * 4 + mtot * 8),
                     "d2h_bytes_per_step": int(nprob * k * 16 + (mtot + ntot) * k * 8)},
-            "gpu_launches": int(sum(s["kernel_launches"] for s in stats_l)),
+            "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": "k_batch_cycle (SpMV share of its traffic)", "achieved": achieved,
                          "peak": peak, "peak_source": kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None},
