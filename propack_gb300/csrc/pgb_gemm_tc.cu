@@ -16,8 +16,9 @@
 // and each T_g (g < OZ_S; the dropped levels sit below 2^-56 of the row and
 // column scales) is an integer below 2^24 in magnitude, so the FP32
 // accumulation of the tensor core is exact.  The levels are combined in
-// int64 and converted to FP64 once per output: the FP64 pipe (two lanes per
-// clock per SM) does ~3 operations per output instead of K FMAs.
+// int64 and the FP64 result is assembled from its bits with integer
+// operations (oz_levels), so the FP64 pipe (two lanes per clock per SM)
+// does no work per output at all.
 //
 // The digits of A are produced in registers from the FP64 bits with integer
 // operations, straight into mma.sync fragments (m16n8k16, row.col); the
@@ -149,6 +150,49 @@ __device__ __forceinline__ void oz_frag(unsigned (&af)[OZ_S][4], const unsigned 
     af[P][3] = oz_digit_bf16<P>(Mb[6], ng[6]) | (oz_digit_bf16<P>(Mb[7], ng[7]) << 16);
 }
 
+// V 2^sc as an FP64 value, rounded to nearest even: the bits are assembled
+// with integer operations (the same value as ldexp((double)V, sc) whenever
+// the result is a normal number; otherwise that general path runs).  This
+// keeps the epilogue off the FP64 pipe, which retires two lanes per clock.
+__device__ __forceinline__ double oz_compose(long long V, int sc)
+{
+    if (V == 0) return 0.0;
+    const unsigned long long sgn = V < 0 ? (1ull << 63) : 0ull;
+    const unsigned long long a = V < 0 ? 0ull - (unsigned long long)V : (unsigned long long)V;
+    const int nb = 64 - __clzll((long long)a);  // significant bits of |V|
+    int ex = nb - 1 + sc;                       // unbiased exponent of the result
+    unsigned long long m;                       // significand with its leading bit
+    if (nb <= 53) {
+        m = a << (53 - nb);
+    } else {
+        const int sh = nb - 53;
+        m = a >> sh;
+        const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (m & 1ull))) m++;
+        if (m >> 53) {
+            m >>= 1;
+            ex++;
+        }
+    }
+    if (ex < -1022 || ex > 1023) return ldexp((double)V, sc);
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)(ex + 1023) << 52) | (m & ((1ull << 52) - 1))));
+}
+
+// The levels T_0 .. T_6 (exact integers) of one output, scaled by 2^sc:
+// sum_g T_g 128^(6-g) 2^sc.  The low levels fit an int64 (|lo| < 2^59); the
+// whole sum does while |T_0| < 2^19, which holds unless nearly every
+// product of a row and a column has the same sign and the largest size --
+// there the two parts are rounded separately.
+__device__ __forceinline__ double oz_levels(const int (&T)[OZ_S], int sc)
+{
+    long long lo = 0;
+#pragma unroll
+    for (int g = 1; g < OZ_S; g++) lo = lo * 128 + T[g];
+    const long long hi = T[0];
+    if (hi > -(1ll << 19) && hi < (1ll << 19)) return oz_compose(hi * (1ll << (7 * (OZ_S - 1))) + lo, sc);
+    return ldexp((double)hi, sc + 7 * (OZ_S - 1)) + ldexp((double)lo, sc);
+}
+
 // C(mr x nc) = A(mr x kk, column-major lda) op(B); one warp per 16 rows and
 // OZ_BN columns.  Row fragment positions (m16n8k16): rows gid, gid+8; K
 // columns 2 tig + {0, 1, 8, 9}; C columns 2 tig + {0, 1} of each n8 tile.
@@ -252,12 +296,12 @@ __global__ void __launch_bounds__(OZ_WARPS * 32) k_oz_gemm(int mr, int nc, int k
         for (int r = 0; r < 4; r++) {
             const int row = (r < 2) ? ra : rb;
             const int col = col0 + 8 * t + 2 * tig + (r & 1);
-            long long V = 0;
+            int T[OZ_S];
 #pragma unroll
-            for (int g = 0; g < OZ_S; g++) V = V * 128 + (long long)__float2int_rn(acc[g][t][r]);
+            for (int g = 0; g < OZ_S; g++) T[g] = __float2int_rn(acc[g][t][r]);
             if (row < mr && col < nc) {
                 const int sc = ((r < 2) ? Ea : Eb) + Fe[col] - 14 - 7 * (OZ_S - 1);
-                C[(size_t)col * ldc + row] = ldexp((double)V, sc);
+                C[(size_t)col * ldc + row] = oz_levels(T, sc);
             }
         }
 }
@@ -396,6 +440,11 @@ __global__ void k_oz_bimg(int kk, int nc, const double *B, int ldb, int tb, int 
     }
 }
 
+// Persistent: CTA b takes the tiles b, b + grid, ... (tile = row block x
+// column tile, column tiles fastest).  While a tile's stages run, every
+// thread also loads sixteen values of its row of the CTA's next tile per
+// stage and keeps their largest exponent, so the next tile's row scales
+// are ready when it starts (and its values sit in L2).
 __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int kk, const double *__restrict__ A, int lda,
                                                           const unsigned short *__restrict__ Bimg,
                                                           const int *__restrict__ Fe, int nstage,
@@ -410,7 +459,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
     int *Ep = reinterpret_cast<int *>(tslot + 4);  // [2][UM_BM]
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const int ntc = (nc + UM_BN - 1) / UM_BN;
-    const int row0 = (blockIdx.x / ntc) * UM_BM, ct = blockIdx.x % ntc, col0 = ct * UM_BN;
+    const int ntiles = (mr + UM_BM - 1) / UM_BM * ntc;
     const uint32_t a_s = um_smem(As), b_s = um_smem(Bs), bar_s = um_smem(bar);
     if (tid == 0) {
         for (int i = 0; i < 4; i++) um_bar_init(bar_s + 8 * i, 1);
@@ -423,122 +472,168 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    // row exponents: thread (r, h) scans the K columns h, h + 2, ... of row r,
-    // sixteen loads in flight (the scan is latency bound otherwise)
-    const int r = tid & (UM_BM - 1), h = tid >> 7, row = row0 + r;
-    int E = -2000;
-    if (row < mr) {
-        for (int l0 = h; l0 < kk; l0 += 32) {
-            double t[16];
+    // thread (r, h): row r of the tile; K step h of every stage; K columns
+    // h, h + 2, ... of the exponent scans
+    const int r = tid & (UM_BM - 1), h = tid >> 7;
+    auto tile_row = [&](int t) { return (t / ntc) * UM_BM + r; };
+    // the sixteen scan values of stage c of tile t (columns h + 2 (16 c + u))
+    auto scan_load = [&](int t, int c, double (&sv)[16]) {
+        const int row = tile_row(t);
 #pragma unroll
-            for (int u = 0; u < 16; u++) t[u] = (l0 + 2 * u < kk) ? A[(size_t)(l0 + 2 * u) * lda + row] : 0.0;
-#pragma unroll
-            for (int u = 0; u < 16; u++) E = max(E, oz_exp_of(t[u]));
+        for (int u = 0; u < 16; u++) {
+            const int l = h + 2 * (16 * c + u);
+            sv[u] = (t < ntiles && row < mr && l < kk) ? A[(size_t)l * lda + row] : 0.0;
         }
+    };
+    auto scan_fold = [&](int &Eacc, const double (&sv)[16]) {
+#pragma unroll
+        for (int u = 0; u < 16; u++) Eacc = max(Eacc, oz_exp_of(sv[u]));
+    };
+    // the sixteen stage values of stage c of tile t (this thread's K step)
+    double xv[16];
+    auto load_stage = [&](int t, int c) {
+        const int row = tile_row(t), k0 = c * UM_KC + h * 16;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int l = k0 + i;
+            xv[i] = (t < ntiles && row < mr && l < kk) ? A[(size_t)l * lda + row] : 0.0;
+        }
+    };
+    // row scales of the CTA's first tile: a plain scan
+    int t = blockIdx.x;
+    int E = -2000;
+    for (int c = 0; c < nstage; c++) {
+        double sv[16];
+        scan_load(t, c, sv);
+        scan_fold(E, sv);
     }
     Ep[h * UM_BM + r] = E;
+    load_stage(t, 0);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
     E = max(Ep[r], Ep[UM_BM + r]);
     if (E == -2000) E = 0;
+    __syncthreads();  // Ep is written again at the end of the first tile
 
-    // thread (r, h) owns K step h of row r in every stage
-    double xv[16];
-    auto load_stage = [&](int c) {
-        const int k0 = c * UM_KC + h * 16;
-#pragma unroll
-        for (int i = 0; i < 16; i++) {
-            const int l = k0 + i;
-            xv[i] = (row < mr && l < kk) ? A[(size_t)l * lda + row] : 0.0;
-        }
-    };
-    load_stage(0);
     const uint32_t arow_off = (uint32_t)(h * UM_ATILE + (r >> 3) * 256 + (r & 7) * 16);
-    for (int c = 0; c < nstage; c++) {
-        const int b = c & 1;
-        bool ok = true;
-        if (c >= 2) ok = um_bar_wait(bar_s + 8 * (2 + b), ((c - 2) >> 1) & 1);  // MMAs of stage c - 2 done
-        if (__syncthreads_or(!ok || *sbad)) {
-            if (tid == 0) atomicExch(err, 1);
+    int g = 0;  // stages issued so far by this CTA (mbarrier phases)
+    bool bad = false;
+    for (; t < ntiles && !bad; t += gridDim.x) {
+        const int tn = t + gridDim.x;
+        const int ct = t % ntc, col0 = ct * UM_BN, row0 = (t / ntc) * UM_BM;
+        int En = -2000;
+        double sv[16];
+        for (int c = 0; c < nstage; c++, g++) {
+            const int b = g & 1;
+            bool ok = true;
+            if (g >= 2) ok = um_bar_wait(bar_s + 8 * (2 + b), ((g - 2) >> 1) & 1);  // MMAs of stage g - 2 done
+            if (__syncthreads_or(!ok || *sbad)) {
+                bad = true;
+                break;
+            }
+            if (c > 0) scan_fold(En, sv);
+            if (tid == 0) {
+                const uint32_t tb_ = bar_s + 8 * b;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tb_), "r"(UM_BSTAGE)
+                             : "memory");
+                const unsigned short *src = Bimg + ((size_t)ct * nstage + c) * (UM_BSTAGE / 2);
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        b_s + b * UM_BSTAGE),
+                    "l"(src), "r"(UM_BSTAGE), "r"(tb_)
+                    : "memory");
+            }
+            unsigned long long Mb[16];
+            unsigned ng[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) Mb[i] = oz_fixed(xv[i], E, ng[i]);
+            // the next stage's values (this tile's, or the next tile's first)
+            if (c + 1 < nstage) load_stage(t, c + 1);
+            else load_stage(tn, 0);
+            scan_load(tn, c, sv);
+            const uint32_t arow = a_s + b * UM_ASTAGE + arow_off;
+            um_plane<0>(arow, Mb, ng);
+            um_plane<1>(arow, Mb, ng);
+            um_plane<2>(arow, Mb, ng);
+            um_plane<3>(arow, Mb, ng);
+            um_plane<4>(arow, Mb, ng);
+            um_plane<5>(arow, Mb, ng);
+            um_plane<6>(arow, Mb, ng);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (tid == 0) {
+                if (!um_bar_wait(bar_s + 8 * b, (g >> 1) & 1)) {
+                    *sbad = 1;
+                } else {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+                    for (int st = 0; st < 2; st++)
+#pragma unroll
+                        for (int p = 0; p < OZ_S; p++)
+#pragma unroll
+                            for (int q = 0; p + q < OZ_S; q++) {
+                                const uint64_t ad = um_desc(a_s + b * UM_ASTAGE + (p * 2 + st) * UM_ATILE);
+                                const uint64_t bd = um_desc(b_s + b * UM_BSTAGE + (q * 2 + st) * UM_BTILE);
+                                um_mma(tmem + (uint32_t)((p + q) * UM_BN), ad, bd,
+                                       (c == 0 && st == 0 && p == 0) ? 0u : 1u);
+                            }
+                    asm volatile(
+                        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                            bar_s + 8 * (2 + b))
+                        : "memory");
+                }
+            }
+        }
+        if (bad) break;
+        // every MMA of the tile is covered by its last stage's commit
+        const int gl = g - 1;
+        const bool ok = !*sbad && um_bar_wait(bar_s + 8 * (2 + (gl & 1)), (gl >> 1) & 1);
+        if (__syncthreads_or(!ok)) {
+            bad = true;
             break;
         }
-        if (tid == 0) {
-            const uint32_t tb_ = bar_s + 8 * b;
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tb_), "r"(UM_BSTAGE)
-                         : "memory");
-            const unsigned short *src = Bimg + ((size_t)ct * nstage + c) * (UM_BSTAGE / 2);
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                    b_s + b * UM_BSTAGE),
-                "l"(src), "r"(UM_BSTAGE), "r"(tb_)
-                : "memory");
-        }
-        unsigned long long Mb[16];
-        unsigned ng[16];
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        scan_fold(En, sv);
+        Ep[h * UM_BM + r] = En;
+        {
+            // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows), columns
+            // 32 (w / 4) .. + 31 in two halves of 16
+            const int L = 32 * (w & 3), hc = w >> 2;
+            const int orow = row0 + L + lane;  // this thread's row r
 #pragma unroll
-        for (int i = 0; i < 16; i++) Mb[i] = oz_fixed(xv[i], E, ng[i]);
-        if (c + 1 < nstage) load_stage(c + 1);
-        const uint32_t arow = a_s + b * UM_ASTAGE + arow_off;
-        um_plane<0>(arow, Mb, ng);
-        um_plane<1>(arow, Mb, ng);
-        um_plane<2>(arow, Mb, ng);
-        um_plane<3>(arow, Mb, ng);
-        um_plane<4>(arow, Mb, ng);
-        um_plane<5>(arow, Mb, ng);
-        um_plane<6>(arow, Mb, ng);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            for (int ph = 0; ph < 2; ph++) {
+                const int cb = hc * 32 + ph * 16;
+                uint32_t v[OZ_S][16];
+#pragma unroll
+                for (int gg = 0; gg < OZ_S; gg++)
+                    um_ld16(tmem + ((uint32_t)L << 16) + (uint32_t)(gg * UM_BN + cb), v[gg]);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int jj = 0; jj < 16; jj++) {
+                    const int col = col0 + cb + jj;
+                    int T[OZ_S];
+#pragma unroll
+                    for (int gg = 0; gg < OZ_S; gg++) T[gg] = __float2int_rn(__uint_as_float(v[gg][jj]));
+                    if (orow < mr && col < nc)
+                        C[(size_t)col * ldc + orow] = oz_levels(T, E + Fe[col] - 14 - 7 * (OZ_S - 1));
+                }
+            }
+        }
+        // the TMEM reads and the exponent halves are done before the next
+        // tile's first MMAs overwrite the levels
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
-        if (tid == 0) {
-            if (!um_bar_wait(bar_s + 8 * b, (c >> 1) & 1)) {
-                *sbad = 1;
-            } else {
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-                for (int st = 0; st < 2; st++)
-#pragma unroll
-                    for (int p = 0; p < OZ_S; p++)
-#pragma unroll
-                        for (int q = 0; p + q < OZ_S; q++) {
-                            const uint64_t ad = um_desc(a_s + b * UM_ASTAGE + (p * 2 + st) * UM_ATILE);
-                            const uint64_t bd = um_desc(b_s + b * UM_BSTAGE + (q * 2 + st) * UM_BTILE);
-                            um_mma(tmem + (uint32_t)((p + q) * UM_BN), ad, bd, (c == 0 && st == 0 && p == 0) ? 0u : 1u);
-                        }
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 bar_s + 8 * (2 + b))
-                             : "memory");
-            }
-        }
+        E = max(Ep[r], Ep[UM_BM + r]);
+        if (E == -2000) E = 0;
+        __syncthreads();
     }
-    // the last stage's commit covers every MMA of this CTA
-    const int cl = nstage - 1;
-    bool ok = !*sbad && um_bar_wait(bar_s + 8 * (2 + (cl & 1)), (cl >> 1) & 1);
-    const bool bad = __syncthreads_or(!ok);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (bad) {
-        if (tid == 0) atomicExch(err, 1);
-    } else {
-        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows), columns
-        // 32 (w / 4) .. + 31 in two halves of 16
-        const int L = 32 * (w & 3), hc = w >> 2;
-        const int orow = row0 + L + lane;  // == row
-#pragma unroll
-        for (int ph = 0; ph < 2; ph++) {
-            const int cb = hc * 32 + ph * 16;
-            uint32_t v[OZ_S][16];
-#pragma unroll
-            for (int g = 0; g < OZ_S; g++) um_ld16(tmem + ((uint32_t)L << 16) + (uint32_t)(g * UM_BN + cb), v[g]);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int jj = 0; jj < 16; jj++) {
-                const int col = col0 + cb + jj;
-                long long V = 0;
-#pragma unroll
-                for (int g = 0; g < OZ_S; g++) V = V * 128 + (long long)__float2int_rn(__uint_as_float(v[g][jj]));
-                if (orow < mr && col < nc) C[(size_t)col * ldc + orow] = ldexp((double)V, E + Fe[col] - 14 - 7 * (OZ_S - 1));
-            }
-        }
+    if (bad && tid == 0) atomicExch(err, 1);
+    if (bad && g > 0) {
+        // let the MMAs in flight finish (bounded) before the columns are freed
+        const int gl = g - 1;
+        um_bar_wait(bar_s + 8 * (2 + (gl & 1)), (gl >> 1) & 1);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -606,7 +701,8 @@ static void oz_gemm_launch(int impl, int mr, int nc, int kk, const double *A, in
         PGB_PROF(PK_GEMM, s, {
             k_oz_bimg<<<(ntc * UM_BN + 127) / 128, 128, 0, s>>>(kk, nc, B, ldb, tb ? 1 : 0, ntc, nstage, sc.bd, sc.fe);
             PGB_LAUNCHED();
-            const int grid = (mr + UM_BM - 1) / UM_BM * ntc;
+            const int ntiles = (mr + UM_BM - 1) / UM_BM * ntc;
+            const int grid = std::min(ntiles, device_info().sms);  // persistent: one CTA per SM
             k_oz_umma<<<grid, UM_THREADS, UM_SMEM, s>>>(mr, nc, kk, A, lda, sc.bd, sc.fe, nstage, C, ldc, sc.err);
             PGB_LAUNCHED();
         });

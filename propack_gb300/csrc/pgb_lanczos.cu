@@ -503,8 +503,9 @@ __device__ __forceinline__ const float *csr_vals<float>(const Csr &A) { return A
 // SHORT: the matrix of this side uses the chunked schedule (compiled
 // separately so that it carries neither the staged schedule's shared memory
 // nor its registers, and fits more CTAs per SM)
+constexpr int SPMV_SHORT_MINB = 4;  // CTAs per SM the chunked instance is compiled for
 template <int SIDE, typename T, int SHORT>
-__global__ void __launch_bounds__(BS, SHORT ? 4 : 3) k_lb_spmv(LbArgs a, int j, int host_product)
+__global__ void __launch_bounds__(BS, SHORT ? SPMV_SHORT_MINB : 3) k_lb_spmv(LbArgs a, int j, int host_product)
 {
     __shared__ SpmvStage<T, T> st[SHORT ? 1 : SPMV_WARPS];
     __shared__ ChunkStage<T> cst[SHORT ? SPMV_WARPS : 1];

@@ -33,6 +33,8 @@
 namespace pgb {
 
 constexpr int SPMV_WARPS = BS / 32;  // warps per CTA
+constexpr int CHUNK_UNROLL = 4;      // chunked schedule: (index, value) pairs and gathers in flight per lane
+constexpr int CHUNK_TILE_COST = 4;   // chunked schedule: fixed cost of a tile, in units of 32 entries
 
 // One warp's shared-memory stage of the staged schedule: the block's
 // values and gathered inputs.
@@ -154,16 +156,17 @@ struct ChunkStage {
     int bnd[33];  // row bounds of the tile, relative to its first entry
 };
 
-// first i in [0, n) with t[i] >= key (t non-decreasing, t[n-1] >= key), by
-// a 32-way search of the whole warp
-__device__ __forceinline__ int warp_lower_bound(const int *__restrict__ t, int n, int key)
+// first i in [0, n) with t[i] + kappa i >= key (non-decreasing in i, and
+// >= key at n-1), by a 32-way search of the whole warp
+__device__ __forceinline__ int warp_lower_bound(const int *__restrict__ t, int n, long long key, int kappa)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    auto ge = [&](int i) { return (long long)t[i] + (long long)kappa * i >= key; };
     int lo = 0, hi = n;  // the answer lies in [lo, hi]
     while (hi - lo > 32) {
         const int step = (hi - lo + 31) / 32;
-        const unsigned m = __ballot_sync(FULL, t[min(lo + lane * step, hi - 1)] >= key);
+        const unsigned m = __ballot_sync(FULL, ge(min(lo + lane * step, hi - 1)));
         if (m == 0) {
             lo = min(lo + 31 * step + 1, hi);
         } else {
@@ -173,8 +176,9 @@ __device__ __forceinline__ int warp_lower_bound(const int *__restrict__ t, int n
             hi = nhi;
         }
     }
-    const unsigned m = __ballot_sync(FULL, lo + lane < hi ? t[lo + lane] >= key : true);
-    return lo + __ffs(m) - 1;
+    // a window of exactly 32 may hold its answer at hi (no lane probes it)
+    const unsigned m = __ballot_sync(FULL, lo + lane < hi ? ge(lo + lane) : true);
+    return m ? lo + __ffs(m) - 1 : hi;
 }
 
 template <typename VT, typename AT, typename XF, typename PF, typename EPI>
@@ -186,13 +190,14 @@ __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, co
     ChunkStage<AT> &cs = stages[threadIdx.x >> 5];
     const int nwarps = gridDim.x * SPMV_WARPS;
     const int ntiles = (nrows + 31) / 32;
-    // each warp takes the contiguous tiles whose first unit falls in its
-    // equal share of all units: equal work per warp, so that no warp of a
-    // CTA waits long for the others at the closing reductions
+    // each warp takes a contiguous range of tiles holding an equal share of
+    // the work, counted as the tiles' units plus CHUNK_TILE_COST per tile
+    // (bounds, combine, epilogue), so that no warp of a CTA waits long for
+    // the others at the closing reductions
     const long long gw = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
-    const int units = tbase[ntiles];
-    const int tb0 = warp_lower_bound(tbase, ntiles + 1, (int)(units * gw / nwarps));
-    const int tb1 = warp_lower_bound(tbase, ntiles + 1, (int)(units * (gw + 1) / nwarps));
+    const long long work = (long long)tbase[ntiles] + (long long)CHUNK_TILE_COST * ntiles;
+    const int tb0 = warp_lower_bound(tbase, ntiles + 1, work * gw / nwarps, CHUNK_TILE_COST);
+    const int tb1 = warp_lower_bound(tbase, ntiles + 1, work * (gw + 1) / nwarps, CHUNK_TILE_COST);
     for (int tile = tb0; tile < tb1; tile++) {
         const int r = tile * 32 + lane;
         const int eb = ptr[tile * 32];
@@ -229,16 +234,16 @@ __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, co
             }
         };
         int i = 0;
-        for (; i + 3 < C; i += 4) {
-            int c[4];
-            VT v[4];
-            AT xv[4];
+        for (; i + CHUNK_UNROLL - 1 < C; i += CHUNK_UNROLL) {
+            int c[CHUNK_UNROLL];
+            VT v[CHUNK_UNROLL];
+            AT xv[CHUNK_UNROLL];
 #pragma unroll
-            for (int u = 0; u < 4; u++) { c[u] = ci[32 * (i + u)]; v[u] = cv[32 * (i + u)]; }
+            for (int u = 0; u < CHUNK_UNROLL; u++) { c[u] = ci[32 * (i + u)]; v[u] = cv[32 * (i + u)]; }
 #pragma unroll
-            for (int u = 0; u < 4; u++) xv[u] = (AT)xload(c[u]);
+            for (int u = 0; u < CHUNK_UNROLL; u++) xv[u] = (AT)xload(c[u]);
 #pragma unroll
-            for (int u = 0; u < 4; u++) step(v[u], xv[u]);
+            for (int u = 0; u < CHUNK_UNROLL; u++) step(v[u], xv[u]);
         }
         for (; i < C; i++) step(cv[32 * i], (AT)xload(ci[32 * i]));
         cs.tail[lane] = acc;

@@ -60,3 +60,17 @@ def test_tcgen05_matches_mma_sync_and_fp64(mr, kk, nc, tb):
     ref = A @ Bop
     bound = kk * 2.0 ** -45 * np.outer(np.abs(A).max(axis=1), np.abs(Bop).max(axis=0)) + 1e-300
     assert np.all(np.abs(outs[1] - ref) <= bound)
+
+
+def test_aligned_signs_take_the_wide_path():
+    # every product of a row and a column equal: the top level reaches
+    # K * 64 * 64 > 2^19 and the levels are combined in two parts
+    torch = pytest.importorskip("torch")
+    mr, kk, nc = 4100, 151, 3
+    dev = torch.device("cuda:0")
+    A_t = torch.ones((kk, mr), dtype=torch.float64, device=dev)
+    B_t = torch.ones((nc, kk), dtype=torch.float64, device=dev)
+    for impl in (0, 1):
+        C_t = torch.zeros((nc, mr), dtype=torch.float64, device=dev)
+        _call(impl, A_t, mr, B_t, kk, 0, C_t, mr, mr, nc, kk)
+        assert torch.all(C_t == float(kk))
