@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(OZ_WARPS * 32) k_oz_gemm(int mr, int nc, int k
 // The same product on the 5th-generation tensor cores: tcgen05.mma with the
 // seven level sums T_g accumulated in tensor memory.
 //
-// One CTA (256 threads, one per SM: its shared memory and 512 TMEM columns
+// One CTA (512 threads, one per SM: its shared memory and 512 TMEM columns
 // admit no second) owns 128 rows x UM_BN columns.  K runs in stages of
 // UM_KC = 32 (two K = 16 MMA steps), double-buffered: while the tensor core
 // works on stage c, the threads load the FP64 values of stage c + 1, split
@@ -333,12 +333,12 @@ __global__ void __launch_bounds__(OZ_WARPS * 32) k_oz_gemm(int mr, int nc, int k
 constexpr int UM_BM = 128;
 constexpr int UM_BN = 64;
 constexpr int UM_KC = 32;
-constexpr int UM_THREADS = 256;
+constexpr int UM_THREADS = 512;  // four threads per row: 8 K values of a stage each
 constexpr int UM_ATILE = UM_BM * 16 * 2;        // 4096 bytes
 constexpr int UM_BTILE = UM_BN * 16 * 2;        // 2048 bytes
 constexpr int UM_ASTAGE = OZ_S * 2 * UM_ATILE;  // 57344 bytes
 constexpr int UM_BSTAGE = OZ_S * 2 * UM_BTILE;  // 28672 bytes
-constexpr int UM_SMEM = 2 * (UM_ASTAGE + UM_BSTAGE) + 2048;
+constexpr int UM_SMEM = 2 * (UM_ASTAGE + UM_BSTAGE) + 4096;
 constexpr unsigned UM_TMEM_COLS = 512;          // OZ_S * UM_BN = 448 FP32 columns, rounded up to a power of two
 // instruction descriptor (kind::f16): FP32 accumulator, BF16 A and B, both
 // K-major, N / 8, M / 16
@@ -389,27 +389,36 @@ __device__ __forceinline__ void um_mma(uint32_t dt, uint64_t ad, uint64_t bd, ui
         "l"(ad), "l"(bd), "r"(UM_IDESC), "r"(acc)
         : "memory");
 }
-__device__ __forceinline__ void um_ld16(uint32_t taddr, uint32_t (&v)[16])
+__device__ __forceinline__ void um_ld8(uint32_t taddr, uint32_t (&v)[8])
 {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15}, [%16];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-        : "r"(taddr)
-        : "memory");
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                 : "r"(taddr)
+                 : "memory");
 }
 
+// digit P of a value in the biased fixed-point form of oz_fixed, as FP32
+// bits (exact: |digit| <= 128): the 7-bit field OR'd into the mantissa of
+// 2^23, then one FMA removes 2^23 (and the bias 64 below the top digit)
+// and applies the sign sg = +-1
 template <int P>
-__device__ __forceinline__ void um_plane(uint32_t arow, const unsigned long long (&Mb)[16], const unsigned (&ng)[16])
+__device__ __forceinline__ uint32_t um_digit(unsigned long long Mb, float sg)
 {
-    uint32_t w[8];
+    const unsigned field = P == 0 ? (unsigned)(Mb >> (7 * (OZ_S - 1)))
+                                  : ((unsigned)(Mb >> (7 * (OZ_S - 1 - P))) & 127u);
+    const float off = P == 0 ? -8388608.0f : -8388672.0f;
+    return __float_as_uint(fmaf(sg, __uint_as_float(field | 0x4B000000u), sg * off));
+}
+
+// the eight digits P of this thread's K values -> one 16-byte core-matrix row
+template <int P>
+__device__ __forceinline__ void um_plane(uint32_t arow, const unsigned long long (&Mb)[8], const float (&sg)[8])
+{
+    uint32_t w[4];
 #pragma unroll
-    for (int j = 0; j < 8; j++)
-        w[j] = oz_digit_bf16<P>(Mb[2 * j], ng[2 * j]) | (oz_digit_bf16<P>(Mb[2 * j + 1], ng[2 * j + 1]) << 16);
-    const uint32_t a = arow + P * 2 * UM_ATILE;
-    um_st16(a, w[0], w[1], w[2], w[3]);        // K 0..7 of the step
-    um_st16(a + 128, w[4], w[5], w[6], w[7]);  // K 8..15
+    for (int j = 0; j < 4; j++)
+        w[j] = __byte_perm(um_digit<P>(Mb[2 * j], sg[2 * j]), um_digit<P>(Mb[2 * j + 1], sg[2 * j + 1]), 0x7632);
+    um_st16(arow + P * 2 * UM_ATILE, w[0], w[1], w[2], w[3]);
 }
 
 // digit planes of op(B) in the shared-memory image of every (column tile,
@@ -456,7 +465,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
     uint64_t *bar = reinterpret_cast<uint64_t *>(Bs + 2 * UM_BSTAGE);  // [0..1] B copies, [2..3] MMAs
     uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 4);
     int *sbad = reinterpret_cast<int *>(tslot + 1);
-    int *Ep = reinterpret_cast<int *>(tslot + 4);  // [2][UM_BM]
+    int *Ep = reinterpret_cast<int *>(tslot + 4);  // [4][UM_BM]
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const int ntc = (nc + UM_BN - 1) / UM_BN;
     const int ntiles = (mr + UM_BM - 1) / UM_BM * ntc;
@@ -472,29 +481,30 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    // thread (r, h): row r of the tile; K step h of every stage; K columns
-    // h, h + 2, ... of the exponent scans
+    // thread (r, h): row r of the tile; K values 8 h .. 8 h + 7 of every
+    // stage (K step h / 2, its half h % 2); K columns h, h + 4, ... of the
+    // exponent scans
     const int r = tid & (UM_BM - 1), h = tid >> 7;
     auto tile_row = [&](int t) { return (t / ntc) * UM_BM + r; };
-    // the sixteen scan values of stage c of tile t (columns h + 2 (16 c + u))
-    auto scan_load = [&](int t, int c, double (&sv)[16]) {
+    // the eight scan values of stage c of tile t (columns h + 4 (8 c + u))
+    auto scan_load = [&](int t, int c, double (&sv)[8]) {
         const int row = tile_row(t);
 #pragma unroll
-        for (int u = 0; u < 16; u++) {
-            const int l = h + 2 * (16 * c + u);
+        for (int u = 0; u < 8; u++) {
+            const int l = h + 4 * (8 * c + u);
             sv[u] = (t < ntiles && row < mr && l < kk) ? A[(size_t)l * lda + row] : 0.0;
         }
     };
-    auto scan_fold = [&](int &Eacc, const double (&sv)[16]) {
+    auto scan_fold = [&](int &Eacc, const double (&sv)[8]) {
 #pragma unroll
-        for (int u = 0; u < 16; u++) Eacc = max(Eacc, oz_exp_of(sv[u]));
+        for (int u = 0; u < 8; u++) Eacc = max(Eacc, oz_exp_of(sv[u]));
     };
-    // the sixteen stage values of stage c of tile t (this thread's K step)
-    double xv[16];
+    // the eight stage values of stage c of tile t
+    double xv[8];
     auto load_stage = [&](int t, int c) {
-        const int row = tile_row(t), k0 = c * UM_KC + h * 16;
+        const int row = tile_row(t), k0 = c * UM_KC + h * 8;
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
+        for (int i = 0; i < 8; i++) {
             const int l = k0 + i;
             xv[i] = (t < ntiles && row < mr && l < kk) ? A[(size_t)l * lda + row] : 0.0;
         }
@@ -503,7 +513,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
     int t = blockIdx.x;
     int E = -2000;
     for (int c = 0; c < nstage; c++) {
-        double sv[16];
+        double sv[8];
         scan_load(t, c, sv);
         scan_fold(E, sv);
     }
@@ -513,18 +523,18 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
-    E = max(Ep[r], Ep[UM_BM + r]);
+    E = max(max(Ep[r], Ep[UM_BM + r]), max(Ep[2 * UM_BM + r], Ep[3 * UM_BM + r]));
     if (E == -2000) E = 0;
     __syncthreads();  // Ep is written again at the end of the first tile
 
-    const uint32_t arow_off = (uint32_t)(h * UM_ATILE + (r >> 3) * 256 + (r & 7) * 16);
+    const uint32_t arow_off = (uint32_t)((h >> 1) * UM_ATILE + (r >> 3) * 256 + (h & 1) * 128 + (r & 7) * 16);
     int g = 0;  // stages issued so far by this CTA (mbarrier phases)
     bool bad = false;
     for (; t < ntiles && !bad; t += gridDim.x) {
         const int tn = t + gridDim.x;
         const int ct = t % ntc, col0 = ct * UM_BN, row0 = (t / ntc) * UM_BM;
         int En = -2000;
-        double sv[16];
+        double sv[8];
         for (int c = 0; c < nstage; c++, g++) {
             const int b = g & 1;
             bool ok = true;
@@ -545,22 +555,26 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
                     "l"(src), "r"(UM_BSTAGE), "r"(tb_)
                     : "memory");
             }
-            unsigned long long Mb[16];
-            unsigned ng[16];
+            unsigned long long Mb[8];
+            float sg[8];
 #pragma unroll
-            for (int i = 0; i < 16; i++) Mb[i] = oz_fixed(xv[i], E, ng[i]);
+            for (int i = 0; i < 8; i++) {
+                unsigned ng;
+                Mb[i] = oz_fixed(xv[i], E, ng);
+                sg[i] = ng ? -1.0f : 1.0f;
+            }
             // the next stage's values (this tile's, or the next tile's first)
             if (c + 1 < nstage) load_stage(t, c + 1);
             else load_stage(tn, 0);
             scan_load(tn, c, sv);
             const uint32_t arow = a_s + b * UM_ASTAGE + arow_off;
-            um_plane<0>(arow, Mb, ng);
-            um_plane<1>(arow, Mb, ng);
-            um_plane<2>(arow, Mb, ng);
-            um_plane<3>(arow, Mb, ng);
-            um_plane<4>(arow, Mb, ng);
-            um_plane<5>(arow, Mb, ng);
-            um_plane<6>(arow, Mb, ng);
+            um_plane<0>(arow, Mb, sg);
+            um_plane<1>(arow, Mb, sg);
+            um_plane<2>(arow, Mb, sg);
+            um_plane<3>(arow, Mb, sg);
+            um_plane<4>(arow, Mb, sg);
+            um_plane<5>(arow, Mb, sg);
+            um_plane<6>(arow, Mb, sg);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
             if (tid == 0) {
@@ -568,17 +582,18 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
                     *sbad = 1;
                 } else {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    // descriptors differ only in the start address field (the
+                    // low 14 bits, which no tile offset here carries out of)
+                    const uint64_t ad0 = um_desc(a_s + b * UM_ASTAGE), bd0 = um_desc(b_s + b * UM_BSTAGE);
 #pragma unroll
                     for (int st = 0; st < 2; st++)
 #pragma unroll
                         for (int p = 0; p < OZ_S; p++)
 #pragma unroll
-                            for (int q = 0; p + q < OZ_S; q++) {
-                                const uint64_t ad = um_desc(a_s + b * UM_ASTAGE + (p * 2 + st) * UM_ATILE);
-                                const uint64_t bd = um_desc(b_s + b * UM_BSTAGE + (q * 2 + st) * UM_BTILE);
-                                um_mma(tmem + (uint32_t)((p + q) * UM_BN), ad, bd,
+                            for (int q = 0; p + q < OZ_S; q++)
+                                um_mma(tmem + (uint32_t)((p + q) * UM_BN), ad0 + (uint64_t)(((p * 2 + st) * UM_ATILE) >> 4),
+                                       bd0 + (uint64_t)(((q * 2 + st) * UM_BTILE) >> 4),
                                        (c == 0 && st == 0 && p == 0) ? 0u : 1u);
-                            }
                     asm volatile(
                         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                             bar_s + 8 * (2 + b))
@@ -599,19 +614,19 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
         Ep[h * UM_BM + r] = En;
         {
             // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows), columns
-            // 32 (w / 4) .. + 31 in two halves of 16
+            // 16 (w / 4) .. + 15 in two halves of 8
             const int L = 32 * (w & 3), hc = w >> 2;
             const int orow = row0 + L + lane;  // this thread's row r
 #pragma unroll
             for (int ph = 0; ph < 2; ph++) {
-                const int cb = hc * 32 + ph * 16;
-                uint32_t v[OZ_S][16];
+                const int cb = hc * 16 + ph * 8;
+                uint32_t v[OZ_S][8];
 #pragma unroll
                 for (int gg = 0; gg < OZ_S; gg++)
-                    um_ld16(tmem + ((uint32_t)L << 16) + (uint32_t)(gg * UM_BN + cb), v[gg]);
+                    um_ld8(tmem + ((uint32_t)L << 16) + (uint32_t)(gg * UM_BN + cb), v[gg]);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                for (int jj = 0; jj < 16; jj++) {
+                for (int jj = 0; jj < 8; jj++) {
                     const int col = col0 + cb + jj;
                     int T[OZ_S];
 #pragma unroll
@@ -625,7 +640,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
         // tile's first MMAs overwrite the levels
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
-        E = max(Ep[r], Ep[UM_BM + r]);
+        E = max(max(Ep[r], Ep[UM_BM + r]), max(Ep[2 * UM_BM + r], Ep[3 * UM_BM + r]));
         if (E == -2000) E = 0;
         __syncthreads();
     }
