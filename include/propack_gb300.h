@@ -186,6 +186,14 @@ int propack_get_precision(void);
 void propack_set_profiling(int on);
 int propack_get_profile(double *total_ms, int64_t *launches, int n);
 
+/* Arithmetic of the FP64 form's Gram-Schmidt passes for the calling host
+ * thread: 0 FP64 FMAs (dgemv as in dreorth.F:85-95, :174); 1 each FP64
+ * value split exactly into three FP32 pieces and the products summed at
+ * three levels on the FP32 pipe (error ~2^-53 of sum |w x|, like an FP64
+ * dot product's own rounding), then one FP64 FMA per row.  Returns 0 or
+ * PROPACK_ERR_ARG. */
+int propack_set_cgs_arith(int mode);
+
 /* ---- Single-precision drivers ------------------------------------------
  * SLANSVD / SLANSVD_IRL: the argument lists of single/slansvd.F:1-3 and
  * single/slansvd_irl.F:1-3 (REAL arrays, REAL tolin/doption/dparm, a REAL

@@ -270,6 +270,15 @@ def set_precision(precision):
         raise PropackError(f"propack_set_precision failed ({rc})")
 
 
+def set_cgs_arith(arith):
+    """Gram-Schmidt arithmetic of the FP64 form for this host thread:
+    "fp64" (FP64 FMAs) or "f3" (exact three-way FP32 splits summed on the
+    FP32 pipe; propack_set_cgs_arith)."""
+    rc = load().propack_set_cgs_arith({"fp64": 0, "f3": 1}[arith])
+    if rc != 0:
+        raise PropackError(f"propack_set_cgs_arith failed ({rc})")
+
+
 def get_precision():
     mode = load().propack_get_precision()
     return {v: k for k, v in PRECISIONS.items()}[mode]

@@ -345,6 +345,7 @@ void copy_cols(const T *src, int lds, T *dst, int ldd, int rows, int cols, cudaS
 
 // ------------------------------------------------ Lanczos step enqueue
 void lb_set_smem_limits(int kmax);
+extern thread_local int g_cgs_f3;  // Gram-Schmidt of the FP64 form on the FP32 pipe (pgb_f3.cuh)
 template <typename T>
 void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int ielr, int ntry_spec,
                      bool host_product, cudaStream_t s);

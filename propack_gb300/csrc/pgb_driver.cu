@@ -1432,6 +1432,13 @@ extern "C" int propack_set_precision(int mode)
 }
 extern "C" int propack_get_precision(void) { return g_precision; }
 
+extern "C" int propack_set_cgs_arith(int mode)
+{
+    if (mode != 0 && mode != 1) return PROPACK_ERR_ARG;
+    g_cgs_f3 = mode;
+    return 0;
+}
+
 extern "C" void printstat_(void)
 {
     const Stats &s = g_stat;

@@ -29,6 +29,7 @@
 // instead (A(v/a) = (Av)/a), and the next same-side SpMV, which reads it
 // row by row, writes the scaled value back.
 #include "pgb.cuh"
+#include "pgb_f3.cuh"
 #include "pgb_spmv.cuh"
 
 namespace pgb {
@@ -760,6 +761,155 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd(LbArgs a, int j, int last)
     }
 }
 
+// The FP64 form's projections on the FP32 pipe (pgb_f3.cuh): same layout
+// of work and partial sums as k_lb_cgs_dots; each thread scales its own x
+// values by a power of two (its largest exponent) and its partial sums
+// back before the warp sum.
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_cgs_dots_f3(LbArgs a, int j)
+{
+    using V = double2;
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 0) return;
+    const int L = a.ctl->nsel;
+    const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
+    const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
+    const double *W = (const double *)(SIDE == 0 ? a.V : a.U);
+    const double *x = SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j);
+    const int nvec = len / 2;
+    const int chunk = (nvec + gridDim.x - 1) / gridDim.x;
+    const int v0 = blockIdx.x * chunk, v1 = min(nvec, v0 + chunk);
+    const bool tail_rows = blockIdx.x == gridDim.x - 1;
+    const V *xv = reinterpret_cast<const V *>(x);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    // this thread's scale: |x 2^-xs| < 2
+    int xe = 0;
+    for (int v = v0 + lane; v < v1; v += 32) {
+        const V xx = xv[v];
+        xe = max(xe, max(f3_expo(xx.x), f3_expo(xx.y)));
+    }
+    if (tail_rows)
+        for (int r = nvec * 2 + lane; r < len; r += 32) xe = max(xe, f3_expo(x[r]));
+    const int xs = xe == 0 ? 0 : xe - 1023;
+    const double back = f3_pow2(xs);
+    for (int c0 = w * DOT_COLS; c0 < L; c0 += (BS / 32) * DOT_COLS) {
+        const int nc = min(DOT_COLS, L - c0);
+        const double *col[DOT_COLS];
+#pragma unroll
+        for (int u = 0; u < DOT_COLS; u++) col[u] = W + (size_t)a.sel[c0 + (u < nc ? u : 0)] * ld;
+        F3Acc acc[DOT_COLS];
+        for (int v = v0 + lane; v < v1; v += 32) {
+            const V xx = xv[v];
+            V wv[DOT_COLS];
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) wv[u] = reinterpret_cast<const V *>(col[u])[v];
+            const F3 x0 = f3_split(xx.x, xs), x1 = f3_split(xx.y, xs);
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) {
+                acc[u].add(f3_split(wv[u].x, 0), x0);
+                acc[u].add(f3_split(wv[u].y, 0), x1);
+            }
+        }
+        if (tail_rows)
+            for (int r = nvec * 2 + lane; r < len; r += 32) {
+                const F3 xr = f3_split(x[r], xs);
+#pragma unroll
+                for (int u = 0; u < DOT_COLS; u++) acc[u].add(f3_split(col[u][r], 0), xr);
+            }
+#pragma unroll
+        for (int u = 0; u < DOT_COLS; u++) {
+            const double sum = warp_sum(acc[u].value() * back);
+            if (lane == 0 && u < nc) a.part_cols[(size_t)(c0 + u) * a.nb + blockIdx.x] = sum;
+        }
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        reduce_cols(a, L);
+        if (threadIdx.x == 0) t.c.cgs_phase = 1;
+        tail_store(a, t);
+    }
+}
+
+// The FP64 form's update on the FP32 pipe: sum_c W(i, c) h_c at three
+// levels per row (h scaled by the power of two of its largest entry),
+// then one FP64 FMA per row applies it to x.
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_cgs_upd_f3(LbArgs a, int j, int last)
+{
+    using V = double2;
+    extern __shared__ double dyn[];  // h[L] as F3 (one double2 slot each) | sel[L]
+    __shared__ double sred[32];
+    __shared__ int hsh;
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 1) return;
+    const int L = a.ctl->nsel;
+    F3 *h3 = reinterpret_cast<F3 *>(dyn);
+    int *ssel = reinterpret_cast<int *>(dyn + 2 * (size_t)L);
+    if (threadIdx.x == 0) hsh = 0;
+    __syncthreads();
+    int he = 0;
+    for (int c = threadIdx.x; c < L; c += BS) he = max(he, f3_expo(a.h[c]));
+    if (he) atomicMax(&hsh, he);
+    __syncthreads();
+    const int hs = hsh == 0 ? 0 : hsh - 1023;  // |h 2^-hs| < 2
+    for (int c = threadIdx.x; c < L; c += BS) {
+        h3[c] = f3_split(a.h[c], hs);
+        ssel[c] = a.sel[c];
+    }
+    __syncthreads();
+    const double back = f3_pow2(hs);
+    const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
+    const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
+    const double *W = (const double *)(SIDE == 0 ? a.V : a.U);
+    double *x = SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j);
+    V *xv = reinterpret_cast<V *>(x);
+    const int nvec = len / 2;
+    Acc<double> sq;
+    for (int v = blockIdx.x * BS + threadIdx.x; v < nvec; v += gridDim.x * BS) {
+        F3Acc s0, s1;
+        int c = 0;
+        for (; c + CGS_UNROLL <= L; c += CGS_UNROLL) {
+            V wv[CGS_UNROLL];
+#pragma unroll
+            for (int u = 0; u < CGS_UNROLL; u++) wv[u] = reinterpret_cast<const V *>(W + (size_t)ssel[c + u] * ld)[v];
+#pragma unroll
+            for (int u = 0; u < CGS_UNROLL; u++) {
+                const F3 hc = h3[c + u];
+                s0.add(f3_split(wv[u].x, 0), hc);
+                s1.add(f3_split(wv[u].y, 0), hc);
+            }
+        }
+        for (; c < L; c++) {
+            const V wc = reinterpret_cast<const V *>(W + (size_t)ssel[c] * ld)[v];
+            s0.add(f3_split(wc.x, 0), h3[c]);
+            s1.add(f3_split(wc.y, 0), h3[c]);
+        }
+        V acc = xv[v];
+        acc.x = fma(-s0.value(), back, acc.x);
+        acc.y = fma(-s1.value(), back, acc.y);
+        xv[v] = acc;
+        sq.add_prod(acc.x, acc.x);
+        sq.add_prod(acc.y, acc.y);
+    }
+    if (blockIdx.x == gridDim.x - 1) {
+        for (int r = nvec * 2 + threadIdx.x; r < len; r += BS) {
+            F3Acc sr;
+            for (int c = 0; c < L; c++) sr.add(f3_split(W[(size_t)ssel[c] * ld + r], 0), h3[c]);
+            const double y = fma(-sr.value(), back, x[r]);
+            x[r] = y;
+            sq.add_prod(y, y);
+        }
+    }
+    const double sq2 = block_sum<BS>(sq.value(), sred);
+    if (threadIdx.x == 0) a.part_sq[blockIdx.x] = sq2;
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
+        after_cgs<SIDE>(t, a, j, sqrt(s2), last);
+        tail_store(a, t);
+    }
+}
+
 // apply the deferred scaling of the newest u and v columns
 template <typename T>
 __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
@@ -787,6 +937,11 @@ __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
 // ------------------------------------------------------------ host side
 template <typename T>
 static size_t cgs_smem(const LbArgs &a) { return (sizeof(double) + sizeof(int)) * (size_t)(a.kmax + 1) + 16; }
+static size_t cgs_smem_f3(const LbArgs &a) { return (2 * sizeof(double) + sizeof(int)) * (size_t)(a.kmax + 1) + 16; }
+
+// Gram-Schmidt arithmetic of the FP64 form (propack_set_cgs_arith): 1 the
+// FP32-pipe kernels of pgb_f3.cuh, 0 FP64 FMAs
+thread_local int g_cgs_f3 = 0;
 
 template <int SIDE, typename T>
 static void set_upd_limits(size_t need)
@@ -795,6 +950,11 @@ static void set_upd_limits(size_t need)
 }
 void lb_set_smem_limits(int kmax)
 {
+    const size_t need3 = (2 * sizeof(double) + sizeof(int)) * (size_t)(kmax + 1) + 16;
+    if (need3 > 48 * 1024) {
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd_f3<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd_f3<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
+    }
     const size_t need = (sizeof(double) + sizeof(int)) * (size_t)(kmax + 1) + 16;
     if (need > 48 * 1024) {
         set_upd_limits<0, double>(need);
@@ -809,6 +969,13 @@ void lb_set_smem_limits(int kmax)
 template <int SIDE, typename T>
 static void launch_cgs_pass(const LbArgs &a, int j, int last, cudaStream_t s)
 {
+    if (sizeof(T) == 8 && g_cgs_f3) {
+        PGB_PROF(PK_CGS_DOTS, s, k_lb_cgs_dots_f3<SIDE><<<a.nb, BS, 0, s>>>(a, j));
+        PGB_LAUNCHED();
+        PGB_PROF(PK_CGS_UPD, s, k_lb_cgs_upd_f3<SIDE><<<a.nb, BS, cgs_smem_f3(a), s>>>(a, j, last));
+        PGB_LAUNCHED();
+        return;
+    }
     PGB_PROF(sizeof(T) == 8 ? PK_CGS_DOTS : PK_CGS_DOTS32, s, k_lb_cgs_dots<SIDE, T><<<a.nb, BS, 0, s>>>(a, j));
     PGB_LAUNCHED();
     PGB_PROF(sizeof(T) == 8 ? PK_CGS_UPD : PK_CGS_UPD32, s,

@@ -198,12 +198,31 @@ __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, co
     const long long work = (long long)tbase[ntiles] + (long long)CHUNK_TILE_COST * ntiles;
     const int tb0 = warp_lower_bound(tbase, ntiles + 1, work * gw / nwarps, CHUNK_TILE_COST);
     const int tb1 = warp_lower_bound(tbase, ntiles + 1, work * (gw + 1) / nwarps, CHUNK_TILE_COST);
+    // a tile's bounds: lane l's row start (rows past the end are empty),
+    // lane 31 also the tile's end, and the tile's units; those of the next
+    // tile are loaded while the current one runs
+    int lo_c = 0, end_c = 0, t0_c = 0, t1_c = 0;
+    auto fetch = [&](int tile, int &lo_raw, int &end31, int &u0, int &u1) {
+        const int rr = tile * 32 + lane;
+        lo_raw = ptr[min(rr, nrows)];
+        end31 = lane == 31 ? ptr[min(rr + 1, nrows)] : 0;
+        u0 = tbase[tile];
+        u1 = tbase[tile + 1];
+    };
+    if (tb0 < tb1) fetch(tb0, lo_c, end_c, t0_c, t1_c);
     for (int tile = tb0; tile < tb1; tile++) {
         const int r = tile * 32 + lane;
-        const int eb = ptr[tile * 32];
-        const int lo = ptr[min(r, nrows)] - eb;      // rows past the end are empty
-        const int hi = ptr[min(r + 1, nrows)] - eb;
-        const int t0 = tbase[tile], C = tbase[tile + 1] - t0;  // C >= 1
+        int lo_n = 0, end_n = 0, t0_n = 0, t1_n = 0;
+        if (tile + 1 < tb1) fetch(tile + 1, lo_n, end_n, t0_n, t1_n);
+        const int eb = __shfl_sync(0xffffffffu, lo_c, 0);
+        const int hi_raw = __shfl_down_sync(0xffffffffu, lo_c, 1);
+        const int lo = lo_c - eb;
+        const int hi = (lane == 31 ? end_c : hi_raw) - eb;
+        const int t0 = t0_c, C = t1_c - t0_c;  // C >= 1
+        lo_c = lo_n;
+        end_c = end_n;
+        t0_c = t0_n;
+        t1_c = t1_n;
         const double pre = r < nrows ? pre_load(r) : 0.0;
         cs.bnd[lane] = lo;
         if (lane == 31) cs.bnd[32] = hi;
