@@ -303,6 +303,13 @@ int propack_batch_get_stats(propack_batch_stats_t *out);
 int propack_gemm_f64_tc(int impl, int mr, int nc, int kk, const double *A, int lda, const double *B, int ldb,
                         int tb, double *C, int ldc);
 
+/* Device memory of the library's operators and solves comes from its own
+ * stream-ordered pool, which keeps freed memory for the next call instead
+ * of returning it to the driver (repeated solves skip the mapping of GBs
+ * of device memory).  This returns all of it that is not in use.
+ * Returns 0 or PROPACK_ERR_CUDA. */
+int propack_release_memory(void);
+
 /* Last error message for the calling thread ("" if none). */
 const char *propack_last_error(void);
 

@@ -270,6 +270,12 @@ def set_precision(precision):
         raise PropackError(f"propack_set_precision failed ({rc})")
 
 
+def release_memory():
+    """Return the device memory the library's pool keeps for reuse."""
+    if load().propack_release_memory() != 0:
+        raise PropackError(f"propack_release_memory failed: {last_error()}")
+
+
 def set_cgs_arith(arith):
     """Gram-Schmidt arithmetic of the FP64 form for this host thread:
     "fp64" (FP64 FMAs) or "f3" (exact three-way FP32 splits summed on the

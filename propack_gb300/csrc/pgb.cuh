@@ -366,6 +366,18 @@ struct Dev {
 };
 const Dev &device_info();
 
+// The library's own stream-ordered device memory pool (one per device).  It
+// keeps memory that is freed for the next allocation instead of returning
+// it to the driver, so that repeated solves and operator builds do not pay
+// for mapping GBs of device memory each time; propack_release_memory()
+// gives it back.
+cudaMemPool_t lib_pool();
+void *pool_alloc(size_t bytes, cudaStream_t s);  // zero bytes allowed; never returns null
+inline void pool_free(void *p, cudaStream_t s)
+{
+    if (p) cudaFreeAsync(p, s);
+}
+
 // exclusive scan of n ints into out[0..n] (out[n] = total, also returned)
 int scan_excl(const int *in, int *out, int n, cudaStream_t s);
 

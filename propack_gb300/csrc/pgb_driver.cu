@@ -211,9 +211,8 @@ struct Ctx {
 
     void *dbytes(size_t bytes)
     {
-        void *p = nullptr;
         bytes = std::max<size_t>(bytes, 16);
-        PGB_CUDA(cudaMalloc(&p, bytes));
+        void *p = pool_alloc(bytes, s);
         PGB_CUDA(cudaMemsetAsync(p, 0, bytes, s));
         allocs.push_back(p);
         return p;
@@ -222,8 +221,10 @@ struct Ctx {
     T *dalloc(size_t count) { return (T *)dbytes(sizeof(T) * count); }
     ~Ctx()
     {
-        if (s) cudaStreamSynchronize(s);
-        for (void *p : allocs) cudaFree(p);
+        if (s) {
+            for (void *p : allocs) pool_free(p, s);
+            cudaStreamSynchronize(s);
+        }
         if (hctl) cudaFreeHost(hctl);
         if (hscal) cudaFreeHost(hscal);
         if (hstat) cudaFreeHost(hstat);

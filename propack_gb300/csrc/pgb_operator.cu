@@ -98,6 +98,37 @@ const Dev &device_info()
     return d;
 }
 
+// ------------------------------------------------------ memory pool
+cudaMemPool_t lib_pool()
+{
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    int dev = 0;
+    PGB_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = pools.find(dev);
+    if (it != pools.end()) return it->second;
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool;
+    PGB_CUDA(cudaMemPoolCreate(&pool, &props));
+    uint64_t keep = UINT64_MAX;
+    PGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    pools[dev] = pool;
+    return pool;
+}
+
+void *pool_alloc(size_t bytes, cudaStream_t s)
+{
+    void *p = nullptr;
+    PGB_CUDA(cudaMallocFromPoolAsync(&p, std::max<size_t>(bytes, 16), lib_pool(), s));
+    return p;
+}
+
 // ------------------------------------------------------------ scans
 // Exclusive prefix sum of n int counts into out[0..n] (out[n] = total).
 __global__ void k_scan_blocks(const int *in, int n, int *bsum)
@@ -240,16 +271,16 @@ static void build_chunks(Csr &A, cudaStream_t s)
     const int ntiles = (A.rows + 31) / 32;
     int *cnt = nullptr;
     PGB_CUDA(cudaMallocAsync(&cnt, sizeof(int) * (ntiles + 1), s));
-    PGB_CUDA(cudaMalloc(&A.tbase, sizeof(int) * (ntiles + 1)));
+    A.tbase = (int *)pool_alloc(sizeof(int) * (ntiles + 1), s);
     const int g = std::min(4096, std::max(1, (ntiles + 255) / 256));
     k_chunk_count<<<g, 256, 0, s>>>(A.ptr, A.rows, cnt);
     PGB_LAUNCHED();
     const size_t units = (size_t)scan_excl(cnt, A.tbase, ntiles, s);
     PGB_CUDA(cudaFreeAsync(cnt, s));
     const size_t len = units * 32;
-    PGB_CUDA(cudaMalloc(&A.cidx, sizeof(int) * len));
-    PGB_CUDA(cudaMalloc(&A.cval, sizeof(double) * len));
-    PGB_CUDA(cudaMalloc(&A.cvalf, sizeof(float) * len));
+    A.cidx = (int *)pool_alloc(sizeof(int) * len, s);
+    A.cval = (double *)pool_alloc(sizeof(double) * len, s);
+    A.cvalf = (float *)pool_alloc(sizeof(float) * len, s);
     PGB_CUDA(cudaMemsetAsync(A.cidx, 0, sizeof(int) * len, s));
     PGB_CUDA(cudaMemsetAsync(A.cval, 0, sizeof(double) * len, s));
     PGB_CUDA(cudaMemsetAsync(A.cvalf, 0, sizeof(float) * len, s));
@@ -260,7 +291,7 @@ static void build_chunks(Csr &A, cudaStream_t s)
 
 static void free_chunks(Csr &A)
 {
-    cudaFree(A.tbase); cudaFree(A.cidx); cudaFree(A.cval); cudaFree(A.cvalf);
+    pool_free(A.tbase, 0); pool_free(A.cidx, 0); pool_free(A.cval, 0); pool_free(A.cvalf, 0);
     A.tbase = A.cidx = nullptr;
     A.cval = nullptr;
     A.cvalf = nullptr;
@@ -279,7 +310,7 @@ static void build_blocks(Csr &A, cudaStream_t s)
         PGB_LAUNCHED();
     }
     A.nblk = scan_excl(flag, pos, rows, s);
-    PGB_CUDA(cudaMalloc(&A.blk, sizeof(int) * (A.nblk + 1)));
+    A.blk = (int *)pool_alloc(sizeof(int) * (A.nblk + 1), s);
     k_blk_emit<<<g, 256, 0, s>>>(flag, pos, rows, A.blk);
     PGB_LAUNCHED();
     PGB_CUDA(cudaFreeAsync(flag, s));
@@ -416,11 +447,11 @@ static void transpose_into(Csr &T, const int *ptr, const int *idx, const double 
     T.rows = cols;
     T.cols = rows + xcols;
     T.ncol0 = rows;
-    PGB_CUDA(cudaMalloc(&T.ptr, sizeof(int) * (cols + 1)));
+    T.ptr = (int *)pool_alloc(sizeof(int) * (cols + 1), s);
     const int total = scan_excl(tot, T.ptr, cols, s);
     T.nnz = total;
-    PGB_CUDA(cudaMalloc(&T.idx, sizeof(int) * std::max(total, 1)));
-    PGB_CUDA(cudaMalloc(&T.val, sizeof(double) * std::max(total, 1)));
+    T.idx = (int *)pool_alloc(sizeof(int) * std::max(total, 1), s);
+    T.val = (double *)pool_alloc(sizeof(double) * std::max(total, 1), s);
     // the sort keys live at the output positions of row c of A', whose
     // offsets T.ptr include the appended X entries: size them by `total`,
     // not by nnz(A)
@@ -660,28 +691,50 @@ Operator *lookup_operator(int64_t handle)
 
 static void free_csr(Csr &A)
 {
-    cudaFree(A.ptr); cudaFree(A.idx); cudaFree(A.val); cudaFree(A.valf); cudaFree(A.blk);
+    pool_free(A.ptr, 0); pool_free(A.idx, 0); pool_free(A.val, 0); pool_free(A.valf, 0); pool_free(A.blk, 0);
     free_chunks(A);
     A = Csr();
 }
 
-static int *upload_ptr(const int64_t *p, int rows, cudaStream_t s)
+// row pointers: int64 on the host, int32 on the device; flag |= 1 unless
+// 0 = p[0] <= p[1] <= ... <= p[rows] = nnz
+__global__ void k_ptr_narrow(const int64_t *p, int rows, int64_t nnz, int *out, int *flag)
 {
-    std::vector<int> h(rows + 1);
-    for (int i = 0; i <= rows; i++) h[i] = (int)p[i];
-    int *d = nullptr;
-    PGB_CUDA(cudaMalloc(&d, sizeof(int) * (rows + 1)));
-    PGB_CUDA(cudaMemcpyAsync(d, h.data(), sizeof(int) * (rows + 1), cudaMemcpyHostToDevice, s));
-    PGB_CUDA(cudaStreamSynchronize(s));
-    return d;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= rows; i += gridDim.x * blockDim.x) {
+        const int64_t v = p[i];
+        out[i] = (int)v;
+        const bool bad = (i == 0 && v != 0) || (i == rows && v != nnz) || (i < rows && p[i + 1] < v);
+        if (bad) atomicOr(flag, 1);
+    }
 }
+// flag |= 2 when a column index lies outside [0, limit)
+__global__ void k_check_idx(const int *idx, int64_t nnz, int limit, int *flag)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
+        if ((unsigned)idx[e] >= (unsigned)limit) atomicOr(flag, 2);
+}
+
 template <typename T>
 static T *upload(const T *p, int64_t n, cudaStream_t s)
 {
-    T *d = nullptr;
-    PGB_CUDA(cudaMalloc(&d, sizeof(T) * std::max<int64_t>(n, 1)));
+    T *d = (T *)pool_alloc(sizeof(T) * std::max<int64_t>(n, 1), s);
     if (n > 0) PGB_CUDA(cudaMemcpyAsync(d, p, sizeof(T) * n, cudaMemcpyHostToDevice, s));
     return d;
+}
+static int *upload_ptr(const int64_t *p, int rows, int64_t nnz, int *flag, cudaStream_t s)
+{
+    int64_t *d64 = upload<int64_t>(p, rows + 1, s);
+    int *d = (int *)pool_alloc(sizeof(int) * (rows + 1), s);
+    k_ptr_narrow<<<std::min(4096, rows / 256 + 1), 256, 0, s>>>(d64, rows, nnz, d, flag);
+    PGB_LAUNCHED();
+    pool_free(d64, s);
+    return d;
+}
+static void check_idx(const int *idx, int64_t nnz, int limit, int *flag, cudaStream_t s)
+{
+    if (nnz <= 0) return;
+    k_check_idx<<<(int)std::min<int64_t>(4096, nnz / 256 + 1), 256, 0, s>>>(idx, nnz, limit, flag);
+    PGB_LAUNCHED();
 }
 
 static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, const double *sv, int r,
@@ -696,29 +749,43 @@ static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, c
         throw ArgFailure();
     }
     if (r > 0 && (!lp || !li || !lv || !rp || !ri || !rv || !w)) throw ArgFailure();
-    // column indices must be in range (checked on the host, once)
-    for (int64_t e = 0; e < snnz; e++)
-        if (si[e] < 0 || si[e] >= n) { set_error("S column index out of range"); throw ArgFailure(); }
-    for (int64_t e = 0; e < lnnz; e++)
-        if (li[e] < 0 || li[e] >= r) { set_error("L column index out of range"); throw ArgFailure(); }
-    for (int64_t e = 0; e < rnnz; e++)
-        if (ri[e] < 0 || ri[e] >= r) { set_error("R column index out of range"); throw ArgFailure(); }
     device_info();
     cudaStream_t s;
     PGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    Operator *op = new Operator();
-    op->m = m; op->n = n; op->r = r;
-    PGB_CUDA(cudaGetDevice(&op->device));
-    int *dsp = upload_ptr(sp, m, s);
+    // the arrays are checked on the device before any kernel indexes by
+    // them: monotone row pointers ending at nnz, column indices in range
+    int *dflag = (int *)pool_alloc(sizeof(int), s);
+    PGB_CUDA(cudaMemsetAsync(dflag, 0, sizeof(int), s));
+    int *dsp = upload_ptr(sp, m, snnz, dflag, s);
     int *dsi = upload<int>(si, snnz, s);
     double *dsv = upload<double>(sv, snnz, s);
+    check_idx(dsi, snnz, n, dflag, s);
     int *dlp = nullptr, *dli = nullptr, *drp = nullptr, *dri = nullptr;
-    double *dlv = nullptr, *drv = nullptr;
+    double *dlv = nullptr, *drv = nullptr, *dw = nullptr;
     if (r > 0) {
-        dlp = upload_ptr(lp, m, s); dli = upload<int>(li, lnnz, s); dlv = upload<double>(lv, lnnz, s);
-        drp = upload_ptr(rp, n, s); dri = upload<int>(ri, rnnz, s); drv = upload<double>(rv, rnnz, s);
-        op->w = upload<double>(w, r, s);
+        dlp = upload_ptr(lp, m, lnnz, dflag, s); dli = upload<int>(li, lnnz, s); dlv = upload<double>(lv, lnnz, s);
+        drp = upload_ptr(rp, n, rnnz, dflag, s); dri = upload<int>(ri, rnnz, s); drv = upload<double>(rv, rnnz, s);
+        dw = upload<double>(w, r, s);
+        check_idx(dli, lnnz, r, dflag, s);
+        check_idx(dri, rnnz, r, dflag, s);
     }
+    int hflag = 0;
+    PGB_CUDA(cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PGB_CUDA(cudaStreamSynchronize(s));
+    pool_free(dflag, s);
+    if (hflag) {
+        for (void *p : {(void *)dsp, (void *)dsi, (void *)dsv, (void *)dlp, (void *)dli, (void *)dlv, (void *)drp,
+                        (void *)dri, (void *)drv, (void *)dw})
+            pool_free(p, s);
+        PGB_CUDA(cudaStreamSynchronize(s));
+        cudaStreamDestroy(s);
+        set_error(hflag & 1 ? "row pointers are not monotone from 0 to nnz" : "column index out of range");
+        throw ArgFailure();
+    }
+    Operator *op = new Operator();
+    op->m = m; op->n = n; op->r = r;
+    op->w = dw;
+    PGB_CUDA(cudaGetDevice(&op->device));
     const int g = 4096;
     // fwd = [S | L]
     {
@@ -728,10 +795,10 @@ static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, c
         PGB_CUDA(cudaMallocAsync(&tot, sizeof(int) * (m + 1), s));
         k_count_merge<<<g, 256, 0, s>>>(dsp, dlp, m, tot);
         PGB_LAUNCHED();
-        PGB_CUDA(cudaMalloc(&A.ptr, sizeof(int) * (m + 1)));
+        A.ptr = (int *)pool_alloc(sizeof(int) * (m + 1), s);
         A.nnz = scan_excl(tot, A.ptr, m, s);
-        PGB_CUDA(cudaMalloc(&A.idx, sizeof(int) * std::max<int64_t>(A.nnz, 1)));
-        PGB_CUDA(cudaMalloc(&A.val, sizeof(double) * std::max<int64_t>(A.nnz, 1)));
+        A.idx = (int *)pool_alloc(sizeof(int) * std::max<int64_t>(A.nnz, 1), s);
+        A.val = (double *)pool_alloc(sizeof(double) * std::max<int64_t>(A.nnz, 1), s);
         k_merge_rows<<<g, 256, 0, s>>>(dsp, dsi, dsv, dlp, dli, dlv, m, n, A.ptr, A.idx, A.val);
         PGB_LAUNCHED();
         PGB_CUDA(cudaFreeAsync(tot, s));
@@ -760,14 +827,16 @@ static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, c
     PGB_CUDA(cudaMemset(op->zticket, 0, sizeof(unsigned int)));
     // FP32 copies of the values for the mixed-precision path
     for (Csr *A : {&op->fwd, &op->adj}) {
-        PGB_CUDA(cudaMalloc(&A->valf, sizeof(float) * std::max<int64_t>(A->nnz, 1)));
+        A->valf = (float *)pool_alloc(sizeof(float) * std::max<int64_t>(A->nnz, 1), s);
         k_to_float<<<g, 256, 0, s>>>(A->val, A->valf, A->nnz);
         PGB_LAUNCHED();
         choose_schedule(*A, op->zbuf, s);
     }
     PGB_CUDA(cudaStreamSynchronize(s));
-    cudaFree(dsp); cudaFree(dsi); cudaFree(dsv);
-    if (r > 0) { cudaFree(dlp); cudaFree(dli); cudaFree(dlv); cudaFree(drp); cudaFree(dri); cudaFree(drv); }
+    for (void *p : {(void *)dsp, (void *)dsi, (void *)dsv, (void *)dlp, (void *)dli, (void *)dlv, (void *)drp,
+                    (void *)dri, (void *)drv})
+        pool_free(p, s);
+    PGB_CUDA(cudaStreamSynchronize(s));
     PGB_CUDA(cudaStreamDestroy(s));
     {
         std::lock_guard<std::mutex> lk(g_reg_mu);
@@ -790,7 +859,8 @@ static int destroy_operator(int64_t handle)
     }
     cudaDeviceSynchronize();
     free_csr(op->fwd); free_csr(op->adj); free_csr(op->thin_r); free_csr(op->thin_l);
-    cudaFree(op->w); cudaFree(op->zbuf); cudaFree(op->zpart); cudaFree(op->zticket);
+    pool_free(op->w, 0);
+    cudaFree(op->zbuf); cudaFree(op->zpart); cudaFree(op->zticket);
     delete op;
     return 0;
 }
@@ -823,6 +893,17 @@ extern "C" int propack_csr_create(int m, int n, const int64_t *s_rowptr, const i
 }
 
 extern "C" int propack_csr_destroy(int64_t handle) { return destroy_operator(handle); }
+
+extern "C" int propack_release_memory(void)
+{
+    try {
+        PGB_CUDA(cudaDeviceSynchronize());
+        PGB_CUDA(cudaMemPoolTrimTo(lib_pool(), 0));
+    } catch (const CudaFailure &) {
+        return PROPACK_ERR_CUDA;
+    }
+    return 0;
+}
 
 extern "C" int propack_set_spmv_schedule(int mode)
 {

@@ -261,6 +261,40 @@ def test_invariant_subspace_rank_deficient():
         assert res["gpu"] == res["oracle"]
 
 
+def test_invalid_csr_is_rejected_on_the_device():
+    # the row pointers and column indices are checked on the device before
+    # any kernel indexes by them
+    import ctypes as C
+    L = pg.load()
+    m, n = 40, 30
+    nul64, nul32, nuld = C.POINTER(C.c_int64)(), C.POINTER(C.c_int)(), C.POINTER(C.c_double)()
+
+    def create(ptr, idx):
+        val = np.ones(idx.size)
+        h = C.c_int64(0)
+        rc = L.propack_csr_create(m, n, pg._i64p(ptr), pg._ip(idx), pg._dp(val), 0, nul64, nul32, nuld, nul64,
+                                  nul32, nuld, nuld, C.byref(h))
+        if rc == 0:
+            L.propack_csr_destroy(h.value)
+        return rc, pg.last_error()
+
+    ptr = np.arange(0, 2 * m + 1, 2, dtype=np.int64)
+    idx = np.tile(np.array([0, 5], dtype=np.int32), m)
+    assert create(ptr, idx)[0] == 0
+    bad = idx.copy()
+    bad[7] = n
+    rc, msg = create(ptr, bad)
+    assert rc == pg.ERR_ARG and "column index" in msg
+    bad = idx.copy()
+    bad[3] = -1
+    assert create(ptr, bad)[0] == pg.ERR_ARG
+    badp = ptr.copy()
+    badp[10] = badp[11] + 1
+    rc, msg = create(badp, idx)
+    assert rc == pg.ERR_ARG and "monotone" in msg
+    assert create(ptr, idx)[0] == 0  # the library is still usable
+
+
 def test_bad_operator_handle_is_an_error():
     A = np.ones((5, 4))
     op = pg.CsrOperator(A)
