@@ -370,8 +370,10 @@ def run_ours(args, wl):
     import ctypes as C
     nul64, nul32, nuld = C.POINTER(C.c_int64)(), C.POINTER(C.c_int)(), C.POINTER(C.c_double)()
     barrier()
+    phases = {"create": 0.0, "solve_call": 0.0, "solve_device": 0.0, "destroy": 0.0}
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ta = time.perf_counter()
         h = C.c_int64(0)
         sp_, si, sv = h_parts["S"]
         if r:
@@ -382,6 +384,7 @@ def run_ours(args, wl):
             rc = lib.propack_csr_create(m, n, pg._i64p(sp_), pg._ip(si), pg._dp(sv), 0, nul64, nul32, nuld, nul64,
                                         nul32, nuld, nuld, C.byref(h))
         assert rc == 0, pg.last_error()
+        tb = time.perf_counter()
         iparm = np.array([h.value & 0xFFFFFFFF, (h.value >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
         aprod = C.cast(lib.propack_gpu_csr_aprod_, pg.APROD)
         u_pin[:, 0] = u0
@@ -390,10 +393,17 @@ def run_ours(args, wl):
         iop = np.array([0, 1], dtype=np.int32)
         kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, aprod, u_pin, sig, bnd, v_pin,
                                  tol, dop, iop, iparm=iparm)
+        tc = time.perf_counter()
         if args.scale == 1.0:
             assert info == 0 and kc == k
+        phases["solve_device"] += pg.get_stats()["solve_ms"]
         lib.propack_csr_destroy(h.value)
+        td = time.perf_counter()
+        phases["create"] += (tb - ta) * 1e3
+        phases["solve_call"] += (tc - tb) * 1e3
+        phases["destroy"] += (td - tc) * 1e3
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    phases = {kk: v / e2e_steps for kk, v in phases.items()}
     barrier()
     pg.set_precision("fp64")
     h2d = sum(a.nbytes for t in h_parts.values() for a in t) + (h_w.nbytes if h_w is not None else 0) + m * 8
@@ -477,7 +487,8 @@ def run_ours(args, wl):
             "matvecs": results[chosen]["matvecs"], "forms": forms_out,
             "speedup_vs_plain_fp64": {f: per["fp64"] / per[f] for f in forms} if "fp64" in per else None,
             "max_rel_sigma_diff_vs_fp64": sig_err,
-            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "phases_ms": phases},
             "gpu_launches": int(sum(results[f]["launches"] for f in forms)), "roofline": dominant,
             "rooflines": {"spmv_pair": roof, "gram_schmidt": roof_cgs},
             "cpu_baseline": cpu, "clocks": clocks, "kernel_breakdown": breakdown}
