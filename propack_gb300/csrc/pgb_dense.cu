@@ -512,23 +512,36 @@ __global__ void __launch_bounds__(256) k_bisect(const double *d, const double *e
     if ((threadIdx.x & 31) == 0) sig[t - 1] = s;
 }
 
-// bounds from the last components of the left vectors, then the same
-// bookkeeping as k_analyse (anorm, refinebounds, convergence count)
-__global__ void k_ana_finish(AnaArgs a)
+// bounds from the last components of the left vectors: one thread per
+// singular value, one warp per CTA (each twisted factorisation divides at
+// every step, and the FP64 pipe is the SM's); into w[dim + 1 + i]
+__global__ void k_ana_twisted(AnaArgs a)
 {
     const int dim = a.dim, N = 2 * dim;
     const double *sig = a.w;
     __shared__ double gs, ps;
-    __shared__ int bad;
-    if (threadIdx.x == 0) { tgk_bounds(a.a1, a.b1, dim, gs, ps); bad = 0; }
+    if (threadIdx.x == 0) tgk_bounds(a.a1, a.b1, dim, gs, ps);
     __syncthreads();
-    const double c1 = a.bnd[dim - 1];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= dim) return;
+    double *Dp = a.wz + (size_t)i * 2 * N, *Dm = Dp + N;
+    const double zn = tgk_twisted(a.a1, a.b1, dim, sig[i], ps, Dp, Dm, nullptr);
+    a.w[dim + 1 + i] = a.bnd[dim - 1] * (sqrt(2.0) * zn);
+}
+
+// the same bookkeeping as k_analyse (anorm, refinebounds, convergence
+// count) on the bounds of k_ana_twisted
+__global__ void k_ana_finish(AnaArgs a)
+{
+    const int dim = a.dim;
+    const double *sig = a.w;
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
     double bi = 0.0;
     if (threadIdx.x < dim) {
         const int i = threadIdx.x;
-        double *Dp = a.wz + (size_t)i * 2 * N, *Dm = Dp + N;
-        const double zn = tgk_twisted(a.a1, a.b1, dim, sig[i], ps, Dp, Dm, nullptr);
-        bi = c1 * (sqrt(2.0) * zn);
+        bi = a.w[dim + 1 + i];
         if (!(bi == bi) || !(sig[i] == sig[i])) bad = 1;
     }
     __syncthreads();
@@ -861,7 +874,9 @@ static bool bisect_fits(int dim)
 }
 static void launch_bisect(const double *d, const double *e, int n, double *sig, cudaStream_t s)
 {
-    const int wpb = 8;
+    // one warp per CTA, so that each singular value's Sturm sequences (an
+    // FP64 division per step) have an SM's FP64 pipe to themselves
+    const int wpb = 1;
     k_bisect<<<(n + wpb - 1) / wpb, 32 * wpb, sizeof(double) * 2 * (size_t)n, s>>>(d, e, n, sig);
     PGB_LAUNCHED();
 }
@@ -877,6 +892,8 @@ void launch_analyse(const AnaArgs &a, cudaStream_t s)
         k_ana_qr<<<1, 32, 0, s>>>(a);
         PGB_LAUNCHED();
         launch_bisect(a.a1, a.b1, a.dim, a.w, s);
+        k_ana_twisted<<<(a.dim + 31) / 32, 32, 0, s>>>(a);
+        PGB_LAUNCHED();
         k_ana_finish<<<1, ((a.dim + 31) / 32) * 32, 0, s>>>(a);
         PGB_LAUNCHED();
     });
