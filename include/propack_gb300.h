@@ -89,14 +89,16 @@ int propack_csr_create(int m, int n, const int64_t *s_rowptr,
                        const int32_t *r_colidx, const double *r_val,
                        const double *w, int64_t *handle);
 int propack_csr_destroy(int64_t handle);
-/* SpMV schedule of the operators built after the call (per host process):
- * 0 (default) a timed choice per direction -- propack_csr_create builds
- * the run-interleaved copy of any matrix with fewer than 64 nonzeros per
- * row on average, times the chunked and the staged schedule on the device
- * and keeps the faster (the row-length rule, chunked below 16 per row, is
- * kept unless the other is more than 5 % faster); 1 always chunked;
- * 2 always staged.  Both schedules give results that depend only on the
- * matrix.  Returns 0 or PROPACK_ERR_ARG. */
+/* SpMV schedule of the operators built after the call (per host process),
+ * per direction: 0 (default) a rule on the mean row length -- chunked
+ * below 32 nonzeros per row, staged above -- so that a matrix always gets
+ * the same schedule and the same summation order; 1 always chunked;
+ * 2 always staged; 3 a timed choice -- propack_csr_create builds the
+ * run-interleaved copy of any matrix with fewer than 64 nonzeros per row
+ * on average, times both schedules on the device and keeps the faster
+ * (the rule's choice unless the other is more than 5 % faster; a near-tie
+ * can go either way between builds).  Results depend only on the matrix
+ * and the schedule.  Returns 0 or PROPACK_ERR_ARG. */
 int propack_set_spmv_schedule(int mode);
 /* The schedules chosen for A (sched[0]) and A' (sched[1]): 1 chunked,
  * 0 staged; tuned_ms (optional, 4 floats): the timed chunked / staged ms

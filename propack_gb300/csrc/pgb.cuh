@@ -74,7 +74,6 @@ struct Csr {
     double *cval = nullptr;
     float *cvalf = nullptr;
 };
-constexpr int SHORT_MEAN = 16;
 
 // A = S + L diag(w) R'.  fwd = [S | L] (m x (n+r)), adj = [S' | R]
 // (n x (m+r)); thin_r = R' (r x n), thin_l = L' (r x m).

@@ -301,7 +301,7 @@ static void build_blocks(Csr &A, cudaStream_t s)
 {
     int *flag = nullptr, *pos = nullptr;
     const int rows = A.rows;
-    A.short_rows = rows > 0 && A.nnz < (int64_t)SHORT_MEAN * rows;
+    A.short_rows = 0;  // the schedule is chosen after the FP32 values exist (choose_schedule)
     PGB_CUDA(cudaMallocAsync(&flag, sizeof(int) * (rows + 1), s));
     PGB_CUDA(cudaMallocAsync(&pos, sizeof(int) * (rows + 1), s));
     const int g = std::min(4096, std::max(1, (rows + 255) / 256));
@@ -603,9 +603,11 @@ void op_spmv_plain_launch(const Csr &A, const double *x, const double *z, double
 }
 
 // ------------------------------------------------- schedule selection
-// propack_set_spmv_schedule: 0 timed choice (default), 1 chunked, 2 staged
+// propack_set_spmv_schedule: 0 the row-length rule (default), 1 chunked,
+// 2 staged, 3 timed choice
 static std::atomic<int> g_sched{0};
-constexpr int CHUNK_MEAN_MAX = 64;  // the timed choice tries the chunked schedule below this mean row length
+constexpr int CHUNK_RULE_MEAN = 32;  // the rule: chunked below this mean row length
+constexpr int CHUNK_MEAN_MAX = 64;   // the timed choice tries the chunked schedule below this mean row length
 
 // mean device ms of one plain product with the matrix's current schedule
 static float time_spmv(const Csr &A, const double *x, const double *z, double *y, cudaStream_t s)
@@ -625,23 +627,27 @@ static float time_spmv(const Csr &A, const double *x, const double *z, double *y
     return ms / 3.f;
 }
 
-// Sets A.short_rows (1: chunked, 0: staged).  The timed choice builds the
-// chunked copy, runs both schedules on the device and keeps the chunked one
-// when it wins (the staged one needs no extra memory).  The rule it starts
-// from (chunked below a mean of SHORT_MEAN nonzeros per row) is kept unless
-// the other schedule is more than 5 % faster, so that near-ties do not
-// flip between builds.
+// Sets A.short_rows (1: chunked, 0: staged).  The default is a rule on the
+// mean row length (chunked below CHUNK_RULE_MEAN, where it measured faster
+// on every workload tried: 7.7 and 20.6 nonzeros per row), so that a given
+// matrix always gets the same schedule and the same summation order.  The
+// timed choice (mode 3) builds the chunked copy, runs both schedules on the
+// device and keeps the chunked one when it wins; it starts from the rule
+// and switches only when the other schedule is more than 5 % faster, but a
+// near-tie can still go either way between builds, and with it the last
+// bits of every product.
 static void choose_schedule(Csr &A, const double *z, cudaStream_t s)
 {
     const int mode = g_sched.load();
-    const bool rule = A.rows > 0 && A.nnz < (int64_t)SHORT_MEAN * A.rows;
+    const bool rule = A.rows > 0 && A.nnz < (int64_t)CHUNK_RULE_MEAN * A.rows;
     A.short_rows = 0;
     if (A.rows == 0 || mode == 2) return;
-    if (mode == 1) {
+    if (mode == 1 || (mode == 0 && rule)) {
         build_chunks(A, s);
         A.short_rows = 1;
         return;
     }
+    if (mode == 0) return;
     if (A.nnz >= (int64_t)CHUNK_MEAN_MAX * A.rows) return;
     build_chunks(A, s);
     double *x = nullptr, *y = nullptr;
@@ -907,7 +913,7 @@ extern "C" int propack_release_memory(void)
 
 extern "C" int propack_set_spmv_schedule(int mode)
 {
-    if (mode < 0 || mode > 2) return PROPACK_ERR_ARG;
+    if (mode < 0 || mode > 3) return PROPACK_ERR_ARG;
     g_sched.store(mode);
     return 0;
 }

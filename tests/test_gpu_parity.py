@@ -75,9 +75,10 @@ def test_operator_products(kind):
     op.close()
 
 
-@pytest.mark.parametrize("mode", ["chunked", "staged", "tuned"])
+@pytest.mark.parametrize("mode", ["chunked", "staged", "tuned", "rule"])
 def test_spmv_schedules(mode):
-    # every schedule gives the product; the timed choice picks one of them
+    # every schedule gives the product; the timed choice picks one of them,
+    # the default rule the chunked one for these short rows
     rng = np.random.default_rng(11)
     # 1032 tiles of 32 rows: the warp search of the chunked schedule meets
     # a final window of exactly 32 tiles
@@ -86,9 +87,11 @@ def test_spmv_schedules(mode):
     try:
         op = pg.CsrOperator(S)
     finally:
-        pg.set_spmv_schedule("tuned")
+        pg.set_spmv_schedule("rule")
     sched, timed = op.schedule
-    if mode != "tuned":
+    if mode == "rule":
+        assert sched == {"fwd": "chunked", "adj": "chunked"} and not timed
+    elif mode != "tuned":
         assert sched == {"fwd": mode, "adj": mode} and not timed
     else:
         assert set(timed) == {("fwd", "chunked"), ("fwd", "staged"), ("adj", "chunked"), ("adj", "staged")}
