@@ -232,6 +232,27 @@ def test_tall_bases_vs_oracle(irl):
     op.close()
 
 
+def test_fp32_valued_matrix_vs_oracle():
+    """A matrix whose values are all FP32 numbers: the FP64 SpMV streams the
+    FP32 copy of the values and widens them exactly (the same products as
+    the FP64 values); the solve matches the oracle on the same trajectory."""
+    S = workloads.zipf_mixed(seed=4, m=20000, hi=3000)
+    assert np.array_equal(S.data.astype(np.float32).astype(np.float64), S.data)
+    op = pg.CsrOperator(S)
+    oop = oracle.Operator(S, None, None, None)
+    kw = dict(irl_mode=True, kmax=40, tol=1e-10)
+    u, s, vt, bnd = pg.svdp(op, 10, rng=rng0(), **kw)
+    st = pg.get_stats()
+    oracle.clearstat()
+    uo, so, vto, bo, info, kc = oracle.svdp(None, 10, rng=rng0(), op=oop, **kw)
+    sto = oracle.getstat()
+    assert info == 0 and kc == 10
+    np.testing.assert_allclose(s, so, rtol=SIG_RTOL)
+    assert subspace_err(u, uo) < VEC_TOL and subspace_err(vt.T, vto.T) < VEC_TOL
+    assert abs(st["nopx"] - sto["nopx"]) <= 0.05 * sto["nopx"] + 2 * 30 + 4
+    op.close()
+
+
 def test_zero_start_vector_uses_dlarnv(golden):
     """v0 = 0 makes the driver draw PROPACK's own dlarnv start vector (dgetu0)."""
     A = csr_from(golden, "plain")
