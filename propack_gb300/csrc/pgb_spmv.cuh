@@ -156,7 +156,8 @@ __device__ __forceinline__ double widen<double, float>(float v)
 {
     const unsigned b = __float_as_uint(v);
     const unsigned mag = b & 0x7fffffffu;
-    const unsigned long long bits = mag == 0u ? 0ull : ((unsigned long long)(mag + (896u << 23)) << 29);
+    // exponent rebias 127 -> 1023 (+896 in the field), significand moved up 29 bits
+    const unsigned long long bits = mag == 0u ? 0ull : (((unsigned long long)mag << 29) + (896ull << 52));
     return __longlong_as_double((long long)(bits | ((unsigned long long)(b & 0x80000000u) << 32)));
 }
 
