@@ -212,16 +212,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def spmv_bytes(m, n, r, nnz_s, nnz_l, nnz_r, vb=8, valb=(None, None)):
-    """Algorithmic bytes of one fused SpMV launch with vb-byte vectors (8:
-    FP64 form, 4: mixed form), valb-byte values per direction (default vb;
-    4 where the FP64 form streams an all-FP32 matrix's FP32 copy) and int32
-    indices: values+indices, row pointers, gathered input, written output,
-    previous Lanczos vector read for the axpy and written back once scaled."""
-    vf = valb[0] or vb
-    va = valb[1] or vb
-    fwd = (nnz_s + nnz_l) * (vf + 4) + (m + 1) * 4 + (n + r) * vb + 3 * m * vb
-    adj = (nnz_s + nnz_r) * (va + 4) + (n + 1) * 4 + (m + r) * vb + 3 * n * vb
+def spmv_bytes(m, n, r, nnz_s, nnz_l, nnz_r, vb=8):
+    """Algorithmic bytes of one fused SpMV launch with vb-byte values and
+    vectors (8: FP64 form, 4: mixed form) and int32 indices: values+indices,
+    row pointers, gathered input, written output, previous Lanczos vector
+    read for the axpy and written back once scaled."""
+    fwd = (nnz_s + nnz_l) * (vb + 4) + (m + 1) * 4 + (n + r) * vb + 3 * m * vb
+    adj = (nnz_s + nnz_r) * (vb + 4) + (n + 1) * 4 + (m + r) * vb + 3 * n * vb
     return fwd, adj
 
 
@@ -313,11 +310,6 @@ def run_ours(args, wl):
         return kc, info, sig, u, v
 
     op = pg.CsrOperator(S, L, R, w)
-    # value bytes the FP64 chunked SpMV streams per direction: 4 when every
-    # value is an FP32 number (the library then reads the FP32 copy)
-    f32 = lambda M: M is None or bool(np.array_equal(M.data.astype(np.float32).astype(np.float64), M.data))
-    sched = op.schedule[0]
-    valb = tuple(4 if (sched[d] == "chunked" and f32(S) and f32(X)) else 8 for d, X in (("fwd", L), ("adj", R)))
     results = {}
     sampler = ClockSampler(0) if rank == 0 else None
     if sampler:
@@ -432,7 +424,7 @@ def run_ours(args, wl):
         return 0
     vb = 4 if chosen == "mixed" else 8
     kadj, kfwd = ("spmv_adj_fp32", "spmv_fwd_fp32") if chosen == "mixed" else ("spmv_adj", "spmv_fwd")
-    fwd_b, adj_b = spmv_bytes(m, n, r, S.nnz, nnz_l, nnz_r, vb, valb if vb == 8 else (None, None))
+    fwd_b, adj_b = spmv_bytes(m, n, r, S.nnz, nnz_l, nnz_r, vb)
     n_adj, t_adj = prof[kadj]
     n_fwd, t_fwd = prof[kfwd]
     achieved = (fwd_b * n_fwd + adj_b * n_adj) / max((t_fwd + t_adj) * 1e-3, 1e-12) / 1e9
@@ -441,7 +433,6 @@ def run_ours(args, wl):
             "achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
             "traffic": SPMV_TRAFFIC_BYTES.get(args.workload, {}).get(chosen) if SPMV_TRAFFIC_BYTES else None,
             "algorithmic_bytes_per_launch": {"fwd": fwd_b, "adj": adj_b},
-            "value_bytes": {"fwd": valb[0], "adj": valb[1]} if vb == 8 else 4,
             "mean_launch_ms": {"fwd": t_fwd / max(n_fwd, 1), "adj": t_adj / max(n_adj, 1)}}
     # Gram-Schmidt: a pass over l basis columns of length len reads them in
     # the projection and again in the update (2*l*len*vb bytes; the x reads

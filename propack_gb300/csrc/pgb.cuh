@@ -66,8 +66,6 @@ struct Csr {
     int *blk = nullptr;       // nblk+1 row boundaries
     int segs = 0;             // thin matrices: segments per row for the split reduction
     int short_rows = 0;       // 1: the chunked schedule, 0: the staged one
-    int f32vals = 0;          // every value is a normal FP32 number (or zero): the FP64 chunked
-                              // SpMV streams the FP32 copy and widens it exactly
     float tuned_ms[2] = {0.f, 0.f};  // timed choice: chunked, staged ms per product (0: not timed)
     // chunked schedule: the entries of each 32-row tile re-laid so that lane
     // l's run of C consecutive entries is read with coalesced loads

@@ -541,9 +541,7 @@ __global__ void __launch_bounds__(BS, SHORT ? SPMV_SHORT_MINB : 3) k_lb_spmv(LbA
     auto pre = [&](int r) -> double { return has_prev ? (double)prev[r] : 0.0; };
     if (!host_product) {
         auto xl = [&](int c) -> T { return c < n0 ? x[c] : (T)z[c - n0]; };
-        if (SHORT && sizeof(T) == 8 && A.f32vals)
-            csr_rows_chunked<float, T>(A.ptr, A.tbase, A.cidx, A.cvalf, A.rows, xl, pre, epi, cst);
-        else if (SHORT) csr_rows_chunked<T, T>(A.ptr, A.tbase, A.cidx, chunk_vals<T>(A), A.rows, xl, pre, epi, cst);
+        if (SHORT) csr_rows_chunked<T, T>(A.ptr, A.tbase, A.cidx, chunk_vals<T>(A), A.rows, xl, pre, epi, cst);
         else csr_rows_staged<T, T>(A.ptr, A.idx, csr_vals<T>(A), A.blk, A.nblk, xl, pre, epi, st);
     } else {
         // the caller's APROD already wrote the product into out

@@ -518,16 +518,10 @@ __global__ void k_merge_rows(const int *sp, const int *si, const double *sv, con
             for (int e = lp[i]; e < lp[i + 1]; e++, p++) { oi[p] = loff + li[e]; ov[p] = lv[e]; }
     }
 }
-// FP32 copy of the values; *inexact = 1 unless every value is an FP32
-// number (then the FP64 SpMV may stream the FP32 copy: same products)
-__global__ void k_to_float(const double *a, float *b, int64_t n, int *inexact)
+__global__ void k_to_float(const double *a, float *b, int64_t n)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float f = (float)a[i];
-        b[i] = f;
-        const float af = fabsf(f);
-        if (!((double)f == a[i]) || (f != 0.f && !(af >= 1.17549435e-38f && af <= 3.40282347e38f))) *inexact = 1;
-    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
 }
 
 // ------------------------------------------------------ application
@@ -838,24 +832,12 @@ static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, c
     PGB_CUDA(cudaMalloc(&op->zticket, sizeof(unsigned int)));
     PGB_CUDA(cudaMemset(op->zticket, 0, sizeof(unsigned int)));
     // FP32 copies of the values for the mixed-precision path
-    int *dinexact = (int *)pool_alloc(2 * sizeof(int), s);
-    PGB_CUDA(cudaMemsetAsync(dinexact, 0, 2 * sizeof(int), s));
-    int hinexact[2] = {1, 1};
-    {
-        int side = 0;
-        for (Csr *A : {&op->fwd, &op->adj}) {
-            A->valf = (float *)pool_alloc(sizeof(float) * std::max<int64_t>(A->nnz, 1), s);
-            k_to_float<<<g, 256, 0, s>>>(A->val, A->valf, A->nnz, dinexact + side);
-            PGB_LAUNCHED();
-            choose_schedule(*A, op->zbuf, s);
-            side++;
-        }
+    for (Csr *A : {&op->fwd, &op->adj}) {
+        A->valf = (float *)pool_alloc(sizeof(float) * std::max<int64_t>(A->nnz, 1), s);
+        k_to_float<<<g, 256, 0, s>>>(A->val, A->valf, A->nnz);
+        PGB_LAUNCHED();
+        choose_schedule(*A, op->zbuf, s);
     }
-    PGB_CUDA(cudaMemcpyAsync(hinexact, dinexact, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
-    PGB_CUDA(cudaStreamSynchronize(s));
-    pool_free(dinexact, s);
-    op->fwd.f32vals = !hinexact[0];
-    op->adj.f32vals = !hinexact[1];
     PGB_CUDA(cudaStreamSynchronize(s));
     for (void *p : {(void *)dsp, (void *)dsi, (void *)dsv, (void *)dlp, (void *)dli, (void *)dlv, (void *)drp,
                     (void *)dri, (void *)drv})

@@ -142,25 +142,6 @@ __device__ __forceinline__ void csr_rows_staged(const int *__restrict__ ptr, con
 }
 
 
-// The value of a matrix entry in the accumulation type.  FP32 -> FP64 is
-// done with integer operations (exact for normal numbers and zero, the only
-// values a matrix streamed this way holds), keeping the FP64 pipe for the
-// products.
-template <typename AT, typename VT>
-__device__ __forceinline__ AT widen(VT v)
-{
-    return (AT)v;
-}
-template <>
-__device__ __forceinline__ double widen<double, float>(float v)
-{
-    const unsigned b = __float_as_uint(v);
-    const unsigned mag = b & 0x7fffffffu;
-    // exponent rebias 127 -> 1023 (+896 in the field), significand moved up 29 bits
-    const unsigned long long bits = mag == 0u ? 0ull : (((unsigned long long)mag << 29) + (896ull << 52));
-    return __longlong_as_double((long long)(bits | ((unsigned long long)(b & 0x80000000u) << 32)));
-}
-
 template <typename VT>
 __device__ __forceinline__ const VT *chunk_vals(const Csr &A);
 template <>
@@ -263,7 +244,7 @@ __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, co
         const VT *cv = cval + off;
         // one entry of the run; closes row q when it ends at this entry
         auto step = [&](VT v, AT xv) {
-            acc = fma(widen<AT>(v), xv, acc);
+            acc = fma((AT)v, xv, acc);
             if (++p == nend) {
                 cs.part[q] = acc;
                 acc = (AT)0;

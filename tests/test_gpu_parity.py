@@ -233,9 +233,8 @@ def test_tall_bases_vs_oracle(irl):
 
 
 def test_fp32_valued_matrix_vs_oracle():
-    """A matrix whose values are all FP32 numbers: the FP64 SpMV streams the
-    FP32 copy of the values and widens them exactly (the same products as
-    the FP64 values); the solve matches the oracle on the same trajectory."""
+    """A matrix whose values are all FP32 numbers (the zipf workload's kind):
+    the solve matches the oracle on the same trajectory."""
     S = workloads.zipf_mixed(seed=4, m=20000, hi=3000)
     assert np.array_equal(S.data.astype(np.float32).astype(np.float64), S.data)
     op = pg.CsrOperator(S)
