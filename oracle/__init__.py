@@ -18,6 +18,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(_HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle_propack.so")
 SRC = os.path.join(_HERE, "propack_oracle.c")
+SRC_Z = os.path.join(_HERE, "propack_oracle_z.inc")
 
 APROD = C.CFUNCTYPE(None, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                     C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -30,7 +31,7 @@ def build(force=False):
     """Compile the oracle with gcc + OpenMP into oracle/_build/."""
     os.makedirs(BUILD_DIR, exist_ok=True)
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC)):
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(SRC), os.path.getmtime(SRC_Z))):
         return LIB_PATH
     cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", LIB_PATH, SRC, "-lm"]
     subprocess.check_call(cmd)
@@ -215,7 +216,10 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
     u[:, 0] = rng.uniform(size=m).  Returns (u, sigma, vt, bnd, info, k_conv)."""
     L = lib()
     if op is None and not callable(getattr(A, "matvec", None)):
-        op = Operator(A)
+        op = ZOperator(A) if np.iscomplexobj(A.data if hasattr(A, "data") else A) else Operator(A)
+    if isinstance(op, ZOperator):
+        return _zsvdp(op, k, which, irl_mode, kmax, compute_u, compute_v, v0, tol, delta, eta, anorm, cgs, elr,
+                      min_relgap, shifts, maxiter, rng)
     m, n = (op.shape if op is not None else A.shape)
     if kmax is None:
         kmax = 10 * k
@@ -253,3 +257,95 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
         kc, info = call_lansvd(L.oracle_dlansvd, jobu, jobv, m, n, k, kmax, aprod, u, sigma, bnd, v,
                                tol, doption, ioption, iparm=iparm)
     return u[:, :k], sigma, v[:, :k].T, bnd, info, kc
+
+
+# ------------------------------------------------------------------ complex
+ZAPROD = C.CFUNCTYPE(None, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_void_p,
+                     C.c_void_p, C.POINTER(C.c_int), C.c_size_t)
+
+
+def _vp(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+class ZOperator:
+    """Complex A (m x n, scipy CSR) held by the oracle with A^H built once;
+    its APROD serves TRANSA 'n' (A x) and 'c' (A^H x), as
+    complex16/zlanbpro.F calls it."""
+
+    def __init__(self, A):
+        import scipy.sparse as sp
+        A = sp.csr_array(A, dtype=np.complex128, copy=True)
+        A.sort_indices()
+        self.shape = A.shape
+        self._keep = [np.ascontiguousarray(A.indptr, dtype=np.int64), np.ascontiguousarray(A.indices, dtype=np.int32),
+                      np.ascontiguousarray(A.data, dtype=np.complex128)]
+        L = lib()
+        L.oracle_zop_create.restype = C.c_void_p
+        L.oracle_zop_create.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_zop_destroy.argtypes = [C.c_void_p]
+        self.handle = L.oracle_zop_create(A.shape[0], A.shape[1], *(_vp(a) for a in self._keep))
+        h = int(self.handle)
+        self.iparm = np.array([h & 0xFFFFFFFF, (h >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
+        self.aprod = C.cast(L.oracle_zop_aprod, ZAPROD)
+
+    def __del__(self):
+        try:
+            lib().oracle_zop_destroy(C.c_void_p(self.handle))
+        except Exception:
+            pass
+
+
+def _zsvdp(op, k, which, irl_mode, kmax, compute_u, compute_v, v0, tol, delta, eta, anorm, cgs, elr,
+           min_relgap, shifts, maxiter, rng):
+    """The complex path of svdp: scipy's _svdp conventions for complex input
+    (start vector uniform + 1j*uniform, zlansvd / zlansvd_irl)."""
+    L = lib()
+    m, n = op.shape
+    if kmax is None:
+        kmax = 10 * k
+    if maxiter is None:
+        maxiter = 1000
+    kmax = min(m + 1, n + 1, kmax)
+    u = np.zeros((m, kmax + 1), order='F', dtype=np.complex128)
+    v = np.zeros((n, kmax), order='F', dtype=np.complex128)
+    sigma = np.zeros(k)
+    bnd = np.zeros(k)
+    if v0 is None:
+        u[:, 0] = rng.uniform(size=m)
+        u[:, 0] += 1j * rng.uniform(size=m)
+    else:
+        u[:, 0] = v0
+    if delta is None:
+        delta = np.sqrt(np.finfo(np.float64).eps)
+    if eta is None:
+        eta = np.finfo(np.float64).eps ** 0.75
+    ioption = np.array([int(bool(cgs)), int(bool(elr))], dtype=np.int32)
+    jobu = b'y' if compute_u else b'n'
+    jobv = b'y' if compute_v else b'n'
+    ci = lambda x: C.byref(C.c_int(x))
+    lwork = m + n + 10 * kmax + 5 * kmax ** 2 + 4 + max(3 * kmax ** 2 + 4 * kmax + 4, 32 * max(m, n))
+    work = np.zeros(lwork)
+    zwork = np.zeros(m + n + kmax, dtype=np.complex128)
+    iwork = np.zeros(8 * kmax + 8, dtype=np.int32)
+    zparm = np.zeros(1, dtype=np.complex128)
+    info = C.c_int(0)
+    tolc = C.c_double(tol)
+    if irl_mode:
+        doption = np.array([delta, eta, anorm, min_relgap], dtype=np.float64)
+        if shifts is None:
+            shifts = kmax - k
+        ne = C.c_int(k)
+        L.oracle_zlansvd_irl(b'L' if which == 'LM' else b'S', jobu, jobv, ci(m), ci(n), ci(kmax), ci(shifts),
+                             C.byref(ne), ci(maxiter), op.aprod, _vp(u), ci(m), _dp(sigma), _dp(bnd), _vp(v), ci(n),
+                             C.byref(tolc), _dp(work), ci(lwork), _vp(zwork), ci(zwork.size), _ip(iwork),
+                             ci(iwork.size), _dp(doption), _ip(ioption), C.byref(info), _vp(zparm), _ip(op.iparm),
+                             C.c_size_t(1), C.c_size_t(1), C.c_size_t(1))
+    else:
+        doption = np.array([delta, eta, anorm], dtype=np.float64)
+        ne = C.c_int(k)
+        L.oracle_zlansvd(jobu, jobv, ci(m), ci(n), C.byref(ne), ci(kmax), op.aprod, _vp(u), ci(m), _dp(sigma),
+                         _dp(bnd), _vp(v), ci(n), C.byref(tolc), _dp(work), ci(lwork), _vp(zwork), ci(zwork.size),
+                         _ip(iwork), ci(iwork.size), _dp(doption), _ip(ioption), C.byref(info), _vp(zparm),
+                         _ip(op.iparm), C.c_size_t(1), C.c_size_t(1))
+    return u[:, :k], sigma, v[:, :k].conj().T, bnd, info.value, ne.value

@@ -1338,3 +1338,6 @@ int oracle_lanbpro_sample(int m, int n, int nsteps, aprod_t aprod, double *U, in
     free(ba); free(bb);
     return k;
 }
+
+/* The complex*16 drivers share the real routines above. */
+#include "propack_oracle_z.inc"

@@ -1,6 +1,8 @@
 """The oracle (CPU restatement of PROPACK) pinned against the reference's
 outputs: scipy's packaging of PROPACK (golden fixtures), dense LAPACK, and
 the generator table of LAPACK's dlaruv."""
+import os
+
 import numpy as np
 import pytest
 
@@ -188,3 +190,74 @@ def test_matrix_file_formats_round_trip(tmp_path):
             B[i, i + d] = vals
             f.write(f"{d} " + " ".join(repr(float(x)) for x in vals) + "\n")
     assert np.array_equal(pio.read(str(p)).toarray(), B)
+
+
+# ------------------------------------------------------------------ complex
+GOLDEN_Z = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden_complex.npz")
+
+
+def _zgolden():
+    with np.load(GOLDEN_Z, allow_pickle=False) as d:
+        return {k: d[k] for k in d.files}
+
+
+def _zcsr(g, prefix):
+    import scipy.sparse as sp
+    shape = tuple(int(x) for x in g[prefix + "_shape"])
+    return sp.csr_array((g[prefix + "_data"].copy(), g[prefix + "_indices"].copy(), g[prefix + "_indptr"].copy()),
+                        shape=shape)
+
+
+@pytest.mark.parametrize("case,mat,k,kw", [("z1_lansvd", "z1", 5, dict(kmax=80)),
+                                           ("z1_lansvd_cgs", "z1", 5, dict(kmax=80, cgs=True)),
+                                           ("z2_lansvd", "z2", 6, dict(kmax=120))])
+def test_complex_oracle_matches_scipy_zlansvd(case, mat, k, kw):
+    """The complex*16 restatement (zlanbpro, zreorth, zlansvd) against
+    scipy's packaging of PROPACK's zlansvd on the same inputs: singular
+    values, bounds and vectors."""
+    import oracle
+    g = _zgolden()
+    A = _zcsr(g, mat)
+    u, s, vh, bnd, info, kc = oracle.svdp(A, k, irl_mode=False, tol=1e-12, rng=np.random.default_rng(0), **kw)
+    assert info == 0 and kc == k
+    np.testing.assert_allclose(s, g[case + "_sigma"], rtol=1e-12)
+    np.testing.assert_allclose(s, g[mat + "_dense_sigma"][:k], rtol=1e-12)
+    # the bounds follow the same Lanczos trajectory (tiny ones are rounding noise)
+    np.testing.assert_allclose(bnd, g[case + "_bnd"], rtol=1e-6, atol=1e-14 * s[0])
+    assert np.max(np.abs(np.abs(np.sum(u.conj() * g[case + "_u"], axis=0)) - 1)) < 1e-10
+    assert np.max(np.abs(np.abs(np.sum(vh.conj() * g[case + "_vh"], axis=1)) - 1)) < 1e-10
+
+
+@pytest.mark.parametrize("kmax,cgs", [(12, False), (30, False), (30, True)])
+def test_complex_oracle_irl_matches_dense(kmax, cgs):
+    """zlansvd_irl restated: restarts with the real shifts and rotations of B
+    applied to the complex bases.  Pinned to the dense SVD (scipy's
+    complex IRL returns wrong values on this input, see make_golden_complex)."""
+    import oracle
+    g = _zgolden()
+    A = _zcsr(g, "z1")
+    oracle.clearstat()
+    u, s, vh, bnd, info, kc = oracle.svdp(A, 5, irl_mode=True, kmax=kmax, tol=1e-12, cgs=cgs,
+                                          rng=np.random.default_rng(0))
+    stt = oracle.getstat()
+    assert info == 0 and kc == 5
+    if kmax == 12:
+        assert stt["nrestart"] > 0
+    np.testing.assert_allclose(s, g["z1_dense_sigma"][:5], rtol=1e-12)
+    Ad = A.toarray()
+    res = max(np.linalg.norm(Ad @ vh[i].conj() - s[i] * u[:, i]) for i in range(5))
+    assert res < 1e-10 * s[0]
+    # scipy's restarted complex driver is off on this input (recorded)
+    assert np.max(np.abs(g["z1_irl_scipy_sigma"] - g["z1_dense_sigma"][:5])) > 0.1
+
+
+def test_complex_oracle_random_start():
+    """A zero start vector: zgetu0 draws the real and imaginary parts from
+    dlaruv's stream (zlarnv, idist 2)."""
+    import oracle
+    g = _zgolden()
+    A = _zcsr(g, "z2")
+    u, s, vh, bnd, info, kc = oracle.svdp(A, 4, irl_mode=True, kmax=24, tol=1e-12,
+                                          v0=np.zeros(A.shape[0], dtype=np.complex128))
+    assert info == 0 and kc == 4
+    np.testing.assert_allclose(s, g["z2_dense_sigma"][:4], rtol=1e-12)
