@@ -228,6 +228,62 @@ void propack_gpu_csr_saprod_(const char *transa, const int *m, const int *n,
                              const float *x, float *y, float *dparm, int *iparm,
                              size_t transa_len);
 
+/* ---- Complex*16 drivers ------------------------------------------------
+ * ZLANSVD / ZLANSVD_IRL: the argument lists of complex16/zlansvd.F:1-3 and
+ * complex16/zlansvd_irl.F:1-3.  U, V, ZWORK and ZPARM are COMPLEX*16 (a
+ * propack_z16 has the same layout: real part, then imaginary part);
+ * Sigma, bnd, WORK and DOPTION stay DOUBLE PRECISION.  The APROD is the
+ * reference's complex one (complex16/zlanbpro.F:297, :442):
+ *   SUBROUTINE APROD(TRANSA, M, N, X, Y, ZPARM, IPARM)
+ * TRANSA = 'n': Y(1:M) = A X(1:N);  TRANSA = 'c': Y(1:N) = A^H X(1:M).
+ * Always FP64 arithmetic (propack_set_precision does not apply).  ZWORK,
+ * WORK and IWORK are not used. */
+typedef struct {
+    double re, im;
+} propack_z16;
+typedef void (*propack_zaprod_t)(const char *transa, const int *m, const int *n,
+                                 const propack_z16 *x, propack_z16 *y,
+                                 propack_z16 *zparm, int *iparm, size_t transa_len);
+void zlansvd_(const char *jobu, const char *jobv, const int *m, const int *n,
+              int *k, const int *kmax, propack_zaprod_t aprod,
+              propack_z16 *U, const int *ldu, double *sigma, double *bnd,
+              propack_z16 *V, const int *ldv, const double *tolin,
+              double *work, const int *lwork, propack_z16 *zwork,
+              const int *lzwrk, int *iwork, const int *liwork,
+              double *doption, const int *ioption, int *info,
+              propack_z16 *zparm, int *iparm, size_t jobu_len, size_t jobv_len);
+void zlansvd_irl_(const char *which, const char *jobu, const char *jobv,
+                  const int *m, const int *n, const int *dim, const int *p,
+                  int *neig, const int *maxiter, propack_zaprod_t aprod,
+                  propack_z16 *U, const int *ldu, double *sigma, double *bnd,
+                  propack_z16 *V, const int *ldv, const double *tolin,
+                  double *work, const int *lwork, propack_z16 *zwork,
+                  const int *lzwrk, int *iwork, const int *liwork,
+                  double *doption, const int *ioption, int *info,
+                  propack_z16 *zparm, int *iparm,
+                  size_t which_len, size_t jobu_len, size_t jobv_len);
+
+/* Upload a complex m x n CSR matrix (0-based int64 row pointers, int32
+ * column indices, complex*16 values) as a device operator for the complex
+ * drivers.  The device holds its real 2m x 2n form: each entry b + ic of A
+ * becomes the 2x2 block [b -c; c b] on the (re, im) pairs, so one real
+ * SpMV computes A x and the device-transposed one computes A^H x exactly.
+ * Same checks and error codes as propack_csr_create; the handle is freed
+ * with propack_csr_destroy. */
+int propack_zcsr_create(int m, int n, const int64_t *rowptr, const int32_t *colidx, const propack_z16 *val,
+                        int64_t *handle);
+/* The 2x2-block form itself, on the host (used by propack_zcsr_create):
+ * rowptr2 has 2m+1 entries, colidx2 and val2 4 nnz(A) entries.  Returns 0,
+ * or PROPACK_ERR_ARG for a negative size or 4 nnz(A) >= 2^31. */
+int propack_zcsr_expand(int m, int n, const int64_t *rowptr, const int32_t *colidx, const propack_z16 *val,
+                        int64_t *rowptr2, int32_t *colidx2, double *val2);
+/* The complex device operator as a ZAPROD (host complex*16 vectors in and
+ * out); the complex drivers recognise it by address and then keep every
+ * product on the device. */
+void propack_gpu_csr_zaprod_(const char *transa, const int *m, const int *n,
+                             const propack_z16 *x, propack_z16 *y, propack_z16 *zparm,
+                             int *iparm, size_t transa_len);
+
 /* ---- Learned start vector (no reference counterpart) ----------------
  * A row-wise MLP (18 -> 256 -> 256 -> 1, ReLU; BF16 weights, FP32
  * accumulation) that proposes the start vector U(:,1) in place of dgetu0's

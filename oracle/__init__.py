@@ -184,6 +184,13 @@ def clearstat():
     lib().oracle_clearstat()
 
 
+def nelr():
+    """Passes of the extended local reorthogonalisation since clearstat()."""
+    L = lib()
+    L.oracle_nelr.restype = C.c_long
+    return int(L.oracle_nelr())
+
+
 def bdsqr(d, e, nru_vectors=False, ncvt_vectors=False, urow=None):
     """Upper-bidiagonal SVD of the oracle (for pinning against numpy)."""
     n = len(d)

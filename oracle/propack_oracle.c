@@ -58,10 +58,12 @@ typedef void (*aprod_t)(const char *transa, const int *m, const int *n,
 /* Counters of double/stat.h:6-15 (timers are never assigned there). */
 typedef struct {
     long nopx, nreorth, ndot, nitref, nbsvd, nrestart, nlandim, nsing;
+    long nelr; /* passes of the extended local reorthogonalisation (not in stat.h) */
 } oracle_stat_t;
 static oracle_stat_t st;
 
 void oracle_clearstat(void) { memset(&st, 0, sizeof st); }
+long oracle_nelr(void) { return st.nelr; }
 void oracle_getstat(long *out8)
 {
     out8[0] = st.nopx; out8[1] = st.nreorth; out8[2] = st.ndot;
@@ -424,6 +426,7 @@ static void lanbpro(int m, int n, int k0, int *kp, aprod_t aprod, double *U, int
             alpha = v_nrm2(n, vj);
             if (j > 1 && ielr > 0 && alpha < KAPPA_LANBPRO * beta) {
                 for (int i = 1; i <= ielr; i++) {
+                    st.nelr++;
                     s = v_dot(n, vj - ldv, vj);
                     v_axpy(n, -s, vj - ldv, vj);
                     if (beta != 0.0) { beta = beta + s; bbeta[j - 2] = beta; }
@@ -490,6 +493,7 @@ static void lanbpro(int m, int n, int k0, int *kp, aprod_t aprod, double *U, int
         beta = v_nrm2(m, uj1);
         if (ielr > 0 && beta < KAPPA_LANBPRO * alpha) {
             for (int i = 1; i <= ielr; i++) {
+                st.nelr++;
                 s = v_dot(m, uj, uj1);
                 v_axpy(m, -s, uj, uj1);
                 if (alpha != 0.0) { alpha = alpha + s; balpha[j - 1] = alpha; }

@@ -7,6 +7,8 @@ this module is the thin Python host side over it:
   ``_svdp``): same arguments, defaults, start vector and return values, but
   every call runs the GPU drivers ``dlansvd_irl_`` / ``dlansvd_`` through the
   C ABI.
+* Complex matrices go to the complex*16 drivers ``zlansvd_irl_`` /
+  ``zlansvd_`` the same way.
 * ``CsrOperator`` uploads A = S + L diag(w) R' to the device; passing it (or
   a scipy sparse / dense matrix, which is wrapped automatically) makes the
   drivers use the device operator with no host round trips.  A
@@ -23,10 +25,13 @@ import numpy as np
 
 from . import _build
 
-__all__ = ["svdp", "CsrOperator", "load", "get_stats", "clearstat", "printstat", "PropackError", "APROD"]
+__all__ = ["svdp", "CsrOperator", "load", "get_stats", "clearstat", "printstat", "PropackError", "APROD", "ZAPROD"]
 
 APROD = C.CFUNCTYPE(None, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_size_t)
+# the complex*16 APROD of complex16/zlanbpro.F (x, y, zparm: complex*16 arrays)
+ZAPROD = C.CFUNCTYPE(None, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_void_p,
+                     C.c_void_p, C.POINTER(C.c_int), C.c_size_t)
 
 ERR_ARG, ERR_CUDA, ERR_HANDLE, ERR_WAIT = -2, -3, -4, -5
 
@@ -65,6 +70,10 @@ def load(build_if_missing=True):
     L.propack_csr_create.argtypes = [C.c_int, C.c_int, i64p, ip, dp, C.c_int, i64p, ip, dp, i64p, ip, dp, dp, i64p]
     L.propack_csr_destroy.restype = C.c_int
     L.propack_csr_destroy.argtypes = [C.c_int64]
+    L.propack_zcsr_create.restype = C.c_int
+    L.propack_zcsr_create.argtypes = [C.c_int, C.c_int, i64p, ip, C.c_void_p, i64p]
+    L.propack_zcsr_expand.restype = C.c_int
+    L.propack_zcsr_expand.argtypes = [C.c_int, C.c_int, i64p, ip, C.c_void_p, i64p, ip, dp]
     L.propack_last_error.restype = C.c_char_p
     L.propack_get_stats.argtypes = [C.POINTER(_Stats)]
     _lib = L
@@ -136,6 +145,9 @@ class CsrOperator:
         lib = load()
         S = sp.csr_array(S)
         self.shape = S.shape
+        if np.iscomplexobj(S.data):
+            self._init_complex(lib, S, L)
+            return
         self.dtype = np.dtype(np.float64)
         keep = []
 
@@ -166,6 +178,25 @@ class CsrOperator:
         self.aprod = C.cast(lib.propack_gpu_csr_aprod_, APROD)
         self.r = r
 
+    def _init_complex(self, lib, S, L):
+        # a complex S alone (propack_zcsr_create): the device holds its real
+        # 2x2-block form, which the complex drivers apply as A and A^H
+        if L is not None:
+            raise TypeError("a complex operator takes no low-rank term")
+        self.dtype = np.dtype(np.complex128)
+        ptr = np.ascontiguousarray(S.indptr, dtype=np.int64)
+        idx = np.ascontiguousarray(S.indices, dtype=np.int32)
+        val = np.ascontiguousarray(S.data, dtype=np.complex128)
+        h = C.c_int64(0)
+        rc = lib.propack_zcsr_create(S.shape[0], S.shape[1], _i64p(ptr), _ip(idx), C.c_void_p(val.ctypes.data),
+                                     C.byref(h))
+        if rc != 0:
+            raise PropackError(f"propack_zcsr_create failed ({rc}): {last_error()}")
+        self.handle = h.value
+        self.iparm = np.array([h.value & 0xFFFFFFFF, (h.value >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
+        self.aprod = C.cast(lib.propack_gpu_csr_zaprod_, ZAPROD)
+        self.r = 0
+
     @property
     def schedule(self):
         """({'fwd': ..., 'adj': ...} with 'chunked' / 'staged', timed ms per
@@ -193,6 +224,13 @@ class CsrOperator:
 
     def _apply(self, trans, x):
         m, n = self.shape
+        ci = lambda v: C.byref(C.c_int(v))
+        if self.dtype == np.complex128:
+            x = np.ascontiguousarray(x, dtype=np.complex128)
+            y = np.zeros(n if trans else m, dtype=np.complex128)
+            load().propack_gpu_csr_zaprod_(b'c' if trans else b'n', ci(m), ci(n), C.c_void_p(x.ctypes.data),
+                                           C.c_void_p(y.ctypes.data), C.c_void_p(), _ip(self.iparm), C.c_size_t(1))
+            return y
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros(n if trans else m)
         ci = lambda v: C.byref(C.c_int(v))
@@ -220,6 +258,62 @@ def _host_aprod(A):
             x = np.ctypeslib.as_array(px, shape=(n,))
             np.ctypeslib.as_array(py, shape=(m,))[:] = op.matvec(x)
     return APROD(cb)
+
+
+def _host_zaprod(A):
+    """ZAPROD over a complex host operator: 'n' y = A x, 'c' y = A^H x."""
+    from scipy.sparse.linalg import aslinearoperator
+    op = aslinearoperator(A)
+    m, n = op.shape
+
+    def cb(transa, pm, pn, px, py, zparm, iparm, ln):
+        if transa[0:1].lower() == b'n':
+            x = np.ctypeslib.as_array(C.cast(px, C.POINTER(C.c_double)), shape=(2 * n,)).view(np.complex128)
+            y = np.ctypeslib.as_array(C.cast(py, C.POINTER(C.c_double)), shape=(2 * m,)).view(np.complex128)
+            y[:] = op.matvec(x)
+        else:
+            x = np.ctypeslib.as_array(C.cast(px, C.POINTER(C.c_double)), shape=(2 * m,)).view(np.complex128)
+            y = np.ctypeslib.as_array(C.cast(py, C.POINTER(C.c_double)), shape=(2 * n,)).view(np.complex128)
+            y[:] = op.rmatvec(x)
+    return ZAPROD(cb)
+
+
+def zlansvd_irl(which, jobu, jobv, m, n, dim, p, neig, maxiter, aprod, U, sigma, bnd, V, tol, doption, ioption,
+                iparm=None):
+    """Call zlansvd_irl_ with the reference's argument list (complex16/zlansvd_irl.F:1-3); U, V complex128
+    Fortran-ordered.  Returns (neig_conv, info)."""
+    lib = load()
+    ci = lambda v: C.byref(C.c_int(v))
+    ne, info = C.c_int(neig), C.c_int(0)
+    work = np.zeros(1)
+    zwork = np.zeros(1, dtype=np.complex128)
+    iwork = np.zeros(1, dtype=np.int32)
+    zparm = np.zeros(1, dtype=np.complex128)
+    iparm = np.zeros(2, dtype=np.int32) if iparm is None else iparm
+    vp = lambda a: C.c_void_p(a.ctypes.data)
+    lib.zlansvd_irl_(which, jobu, jobv, ci(m), ci(n), ci(dim), ci(p), C.byref(ne), ci(maxiter), aprod, vp(U),
+                     ci(U.shape[0]), _dp(sigma), _dp(bnd), vp(V), ci(V.shape[0]), C.byref(C.c_double(tol)),
+                     _dp(work), ci(1), vp(zwork), ci(1), _ip(iwork), ci(1), _dp(doption), _ip(ioption),
+                     C.byref(info), vp(zparm), _ip(iparm), C.c_size_t(1), C.c_size_t(1), C.c_size_t(1))
+    return ne.value, info.value
+
+
+def zlansvd(jobu, jobv, m, n, k, kmax, aprod, U, sigma, bnd, V, tol, doption, ioption, iparm=None):
+    """Call zlansvd_ with the reference's argument list (complex16/zlansvd.F:1-3).  Returns (k_conv, info)."""
+    lib = load()
+    ci = lambda v: C.byref(C.c_int(v))
+    km, info = C.c_int(k), C.c_int(0)
+    work = np.zeros(1)
+    zwork = np.zeros(1, dtype=np.complex128)
+    iwork = np.zeros(1, dtype=np.int32)
+    zparm = np.zeros(1, dtype=np.complex128)
+    iparm = np.zeros(2, dtype=np.int32) if iparm is None else iparm
+    vp = lambda a: C.c_void_p(a.ctypes.data)
+    lib.zlansvd_(jobu, jobv, ci(m), ci(n), C.byref(km), ci(kmax), aprod, vp(U), ci(U.shape[0]), _dp(sigma),
+                 _dp(bnd), vp(V), ci(V.shape[0]), C.byref(C.c_double(tol)), _dp(work), ci(1), vp(zwork), ci(1),
+                 _ip(iwork), ci(1), _dp(doption), _ip(ioption), C.byref(info), vp(zparm), _ip(iparm),
+                 C.c_size_t(1), C.c_size_t(1))
+    return km.value, info.value
 
 
 def lansvd_irl(which, jobu, jobv, m, n, dim, p, neig, maxiter, aprod, U, sigma, bnd, V, tol, doption, ioption,
@@ -303,6 +397,10 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
     Lanczos vectors, FP64 scalars, FP64 refinement to the requested tol) or
     'fp32' (the FP32 form alone, tol no finer than 16 * 2^-24: the form of
     the single-precision drivers slansvd_ / slansvd_irl_).
+    Complex A (a complex CsrOperator, sparse or dense matrix, or a complex
+    LinearOperator) runs the complex*16 drivers zlansvd_irl_ / zlansvd_
+    (complex16/zlansvd_irl.F, zlansvd.F) in FP64, with scipy's complex start
+    vector (uniform real and imaginary parts).
     Returns (u, sigma, vt, bnd) like scipy's _svdp."""
     from scipy.linalg import LinAlgError
     if rng is None:
@@ -315,13 +413,16 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
     own_op = None
     if isinstance(A, CsrOperator):
         op = A
+        cplx = op.dtype == np.complex128
     elif callable(getattr(A, "matvec", None)) and not hasattr(A, "tocsr"):
         op = None
+        cplx = np.dtype(A.dtype).kind == 'c'
     else:
         import scipy.sparse as sp
-        if np.iscomplexobj(A.data if sp.issparse(A) else np.asarray(A)):
-            raise TypeError("complex matrices are not supported by the GPU drivers")
         op = own_op = CsrOperator(A)
+        cplx = op.dtype == np.complex128
+    if cplx and precision != "fp64":
+        raise ValueError("complex matrices run in FP64 only (zlansvd_ / zlansvd_irl_)")
     m, n = op.shape if op is not None else A.shape
     if (k < 1) or (k > min(m, n)):
         raise ValueError("k must be positive and not greater than m or n")
@@ -335,12 +436,16 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
                          f"but kmax ({kmax}) < k ({k})")
     jobu = b'y' if compute_u else b'n'
     jobv = b'y' if compute_v else b'n'
-    u = np.zeros((m, kmax + 1), order='F')
-    v = np.zeros((n, kmax), order='F')
+    typ = np.complex128 if cplx else np.float64
+    u = np.zeros((m, kmax + 1), order='F', dtype=typ)
+    v = np.zeros((n, kmax), order='F', dtype=typ)
     sigma = np.zeros(k)
     bnd = np.zeros(k)
     if v0 is None:
         u[:, 0] = rng.uniform(size=m)
+        if cplx:
+            # scipy's start vector for complex input: uniform real and imaginary parts
+            u[:, 0] += 1j * rng.uniform(size=m)
     else:
         try:
             u[:, 0] = v0
@@ -364,11 +469,17 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
     if op is not None:
         aprod, iparm = op.aprod, op.iparm
     else:
-        aprod, iparm = _host_aprod(A), None
+        aprod, iparm = (_host_zaprod(A) if cplx else _host_aprod(A)), None
     previous = get_precision()
     set_precision(precision)
     try:
-        if irl_mode:
+        if cplx and irl_mode:
+            kc, info = zlansvd_irl(_which_converter[which], jobu, jobv, m, n, kmax, shifts, k, maxiter, aprod,
+                                   u, sigma, bnd, v, tol, doption, ioption, iparm=iparm)
+        elif cplx:
+            kc, info = zlansvd(jobu, jobv, m, n, k, kmax, aprod, u, sigma, bnd, v, tol, doption, ioption,
+                               iparm=iparm)
+        elif irl_mode:
             kc, info = lansvd_irl(_which_converter[which], jobu, jobv, m, n, kmax, shifts, k, maxiter, aprod,
                                   u, sigma, bnd, v, tol, doption, ioption, iparm=iparm)
         else:

@@ -86,6 +86,9 @@ struct Operator {
     unsigned int *zticket = nullptr;
     int64_t id = 0;
     int device = 0;
+    // 1: a complex m/2 x n/2 matrix held as its real 2x2-block form (fwd
+    // computes A x and adj computes A^H x on (re, im) pairs)
+    int cplx = 0;
 };
 Operator *lookup_operator(int64_t handle);
 
@@ -114,6 +117,12 @@ struct LbCtl {
     // per half-step phase state
     int elr_active, elr_iter;
     double elr_s;           // ELR inner product for the coming iteration
+    // complex*16 vectors (zlanbpro): stored as (re, im) pairs of doubles; the
+    // ELR projection is complex and leaves B alone (zlanbpro.F:318-331),
+    // and its first inner product is formed by the first ELR kernel
+    int cplx;
+    int elr_need_dot;
+    double elr_s_im;
     int reorth_active, reorth_iter, reorth_count;
     int cgs_phase;          // 0: the next CGS kernel forms the projections, 1: it applies them
     double reorth_nrm0;
@@ -143,13 +152,25 @@ struct LbArgs {
     double *mu, *nu;
     int *index;             // reorthogonalisation intervals (1-based)
     int *sel;               // expanded column list (0-based)
-    double *h;              // CGS coefficients
+    double *h;              // CGS coefficients (complex: (re, im) pairs)
     double *part_sq, *part_dot;   // per-CTA partial sums (nb)
     double *part_cols;            // (kmax+1) * nb partial CGS dots, column c at c*nb
+                                  // (complex: 2 (kmax+1) * nb, re at 2c*nb, im at (2c+1)*nb)
     int nb;                 // CTAs of the vector kernels
     int kmax;               // capacity of the column arrays
     Csr fwd, adj;           // device operator (fwd = [S|L], adj = [S'|R])
     const double *z;        // low-rank coefficients of the current product
+};
+// real scalars per element of a Lanczos vector: 1 for double and float, 2
+// for complex*16, held as double2 = (re, im).  LbArgs' ldu, ldv and the
+// rows of its operators count real scalars.
+template <typename T>
+struct VecW {
+    static constexpr int w = 1;
+};
+template <>
+struct VecW<double2> {
+    static constexpr int w = 2;
 };
 template <typename T>
 __host__ __device__ __forceinline__ T *ucol(const LbArgs &a, int c) { return (T *)a.U + (size_t)c * a.ldu; }

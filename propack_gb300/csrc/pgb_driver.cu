@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/propack_gb300.h"
@@ -131,6 +132,51 @@ __global__ void __launch_bounds__(BS) k_gemvn_upd(const T *W, size_t ld, int len
         x[r] -= acc;
     }
 }
+// complex*16 forms of the two above (zgemv 'C' and 'N' of zcgs): column c's
+// partial (re, im) at rows 2c, 2c+1 of part; h as (re, im) pairs
+__global__ void __launch_bounds__(BS) k_zgemvt_part(const double2 *W, size_t ld, int len, int kk, const double2 *x,
+                                                    double *part)
+{
+    const int chunk = (len + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * chunk, r1 = min(len, r0 + chunk);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c = w; c < kk; c += BS / 32) {
+        const double2 *col = W + (size_t)c * ld;
+        double re = 0.0, im = 0.0;
+        for (int r = r0 + lane; r < r1; r += 32) {
+            const double2 a = col[r], b = x[r];
+            re = fma(a.x, b.x, re);
+            re = fma(a.y, b.y, re);
+            im = fma(a.x, b.y, im);
+            im = fma(-a.y, b.x, im);
+        }
+        re = warp_sum(re);
+        im = warp_sum(im);
+        if (lane == 0) {
+            part[(size_t)(2 * c) * gridDim.x + blockIdx.x] = re;
+            part[(size_t)(2 * c + 1) * gridDim.x + blockIdx.x] = im;
+        }
+    }
+}
+__global__ void __launch_bounds__(BS) k_zgemvn_upd(const double2 *W, size_t ld, int len, int kk, const double *h,
+                                                   double2 *x)
+{
+    for (int r = blockIdx.x * BS + threadIdx.x; r < len; r += gridDim.x * BS) {
+        double ar = 0.0, ai = 0.0;
+        for (int c = 0; c < kk; c++) {
+            const double2 w = W[(size_t)c * ld + r];
+            const double hr = h[2 * c], hi = h[2 * c + 1];
+            ar = fma(w.x, hr, ar);
+            ar = fma(-w.y, hi, ar);
+            ai = fma(w.x, hi, ai);
+            ai = fma(w.y, hr, ai);
+        }
+        double2 v = x[r];
+        v.x -= ar;
+        v.y -= ai;
+        x[r] = v;
+    }
+}
 template <typename T>
 __global__ void k_scale(T *x, int n, int mode, double val)
 {
@@ -177,6 +223,7 @@ __global__ void k_sum_cols(const T *U, size_t ldu, int m, int ncols, double *out
 // ------------------------------------------------------------- context
 struct Ctx {
     int m = 0, n = 0, kmax = 0, ldu = 0, ldv = 0, es = 8;
+    int vw = 1;                             // real scalars per vector element (2: complex*16)
     cudaStream_t s = nullptr;
     void *U = nullptr, *V = nullptr;        // Lanczos vectors (double or float)
     LbCtl *ctl = nullptr;
@@ -201,6 +248,8 @@ struct Ctx {
     propack_aprod_t aprod = nullptr;
     double *dparm = nullptr;
     int *iparm = nullptr;
+    propack_zaprod_t zaprod = nullptr;      // complex*16 host APROD and its ZPARM
+    propack_z16 *zparm = nullptr;
     double *hx = nullptr, *hy = nullptr;    // pinned host vectors for a host APROD
     int nb = 0;
     int ntry_spec = 2;
@@ -241,14 +290,14 @@ struct Ctx {
     LbArgs args() const
     {
         LbArgs a;
-        a.ctl = ctl; a.U = U; a.V = V; a.ldu = ldu; a.ldv = ldv;
+        a.ctl = ctl; a.U = U; a.V = V; a.ldu = ldu * vw; a.ldv = ldv * vw;
         a.balpha = balpha; a.bbeta = bbeta; a.mu = mu; a.nu = nu;
         a.index = index; a.sel = sel; a.h = h;
         a.part_sq = part_sq; a.part_dot = part_dot; a.part_cols = part_cols;
         a.nb = nb; a.kmax = kmax;
         if (op) { a.fwd = op->fwd; a.adj = op->adj; a.z = op->zbuf; }
         else {
-            a.fwd.rows = m; a.adj.rows = n; a.z = nullptr;
+            a.fwd.rows = m * vw; a.adj.rows = n * vw; a.z = nullptr;
         }
         return a;
     }
@@ -270,6 +319,7 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
 {
     const Dev &d = device_info();
     c.m = m; c.n = n; c.kmax = kmax; c.es = (int)sizeof(T);
+    c.vw = VecW<T>::w;
     c.ldu = (m + 31) / 32 * 32;
     c.ldv = (n + 31) / 32 * 32;
     c.nb = d.nb;
@@ -287,10 +337,10 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
     c.bbeta = c.dalloc<double>(kmax + 2);
     c.mu = c.dalloc<double>(kmax + 2);
     c.nu = c.dalloc<double>(kmax + 2);
-    c.h = c.dalloc<double>(kmax + 2);
+    c.h = c.dalloc<double>((size_t)(kmax + 2) * c.vw);
     c.part_sq = c.dalloc<double>(c.nb);
     c.part_dot = c.dalloc<double>(c.nb);
-    c.part_cols = c.dalloc<double>((size_t)c.nb * (kmax + 2));
+    c.part_cols = c.dalloc<double>((size_t)c.nb * (kmax + 2) * c.vw);
     c.index = c.dalloc<int>(2 * (size_t)kmax + 8);
     c.sel = c.dalloc<int>(kmax + 2);
     const int mn = std::max(m, n);
@@ -324,20 +374,28 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
 template <typename T>
 static double dev_nrm2(Ctx &c, const T *x, int n)
 {
-    k_sumsq_part<T><<<c.nb, BS, 0, c.s>>>(x, n, c.part_sq);
-    PGB_LAUNCHED();
-    k_sum_final<<<1, BS, 0, c.s>>>(c.part_sq, c.nb, c.scal);
-    PGB_LAUNCHED();
-    PGB_CUDA(cudaMemcpyAsync(c.hscal, c.scal, sizeof(double), cudaMemcpyDeviceToHost, c.s));
-    c.sync();
-    return std::sqrt(c.hscal[0]);
+    if constexpr (VecW<T>::w == 2) {
+        return dev_nrm2<double>(c, (const double *)x, 2 * n);
+    } else {
+        k_sumsq_part<T><<<c.nb, BS, 0, c.s>>>(x, n, c.part_sq);
+        PGB_LAUNCHED();
+        k_sum_final<<<1, BS, 0, c.s>>>(c.part_sq, c.nb, c.scal);
+        PGB_LAUNCHED();
+        PGB_CUDA(cudaMemcpyAsync(c.hscal, c.scal, sizeof(double), cudaMemcpyDeviceToHost, c.s));
+        c.sync();
+        return std::sqrt(c.hscal[0]);
+    }
 }
 template <typename T>
 static void dev_scale(Ctx &c, T *x, int n, int mode, double val)
 {
-    if (mode == 0 || n <= 0) return;
-    k_scale<T><<<c.nb, 256, 0, c.s>>>(x, n, mode, val);
-    PGB_LAUNCHED();
+    if constexpr (VecW<T>::w == 2) {
+        dev_scale<double>(c, (double *)x, 2 * n, mode, val);
+    } else {
+        if (mode == 0 || n <= 0) return;
+        k_scale<T><<<c.nb, 256, 0, c.s>>>(x, n, mode, val);
+        PGB_LAUNCHED();
+    }
 }
 // dsafescal on the device
 template <typename T>
@@ -359,24 +417,38 @@ template <typename T>
 static void dev_aprod(Ctx &c, bool trans, const T *x, T *y)
 {
     const int nin = trans ? c.m : c.n, nout = trans ? c.n : c.m;
-    if (c.op) {
-        op_apply<T>(*c.op, trans, x, y, c.s);
-        return;
-    }
-    const double *xd = (const double *)x;
-    if (sizeof(T) != sizeof(double)) {
-        dev_convert<T, double>(c, x, c.dx, nin);
-        xd = c.dx;
-    }
-    PGB_CUDA(cudaMemcpyAsync(c.hx, xd, sizeof(double) * nin, cudaMemcpyDeviceToHost, c.s));
-    c.sync();
-    const char ta = trans ? 't' : 'n';
-    c.aprod(&ta, &c.m, &c.n, c.hx, c.hy, c.dparm, c.iparm, 1);
-    if (sizeof(T) != sizeof(double)) {
-        PGB_CUDA(cudaMemcpyAsync(c.dy, c.hy, sizeof(double) * nout, cudaMemcpyHostToDevice, c.s));
-        dev_convert<double, T>(c, c.dy, y, nout);
+    if constexpr (VecW<T>::w == 2) {
+        // the device operator is the real 2x2-block form; a host ZAPROD sees
+        // complex*16 vectors with TRANSA 'n' or 'c' (zlanbpro.F:297, :442)
+        if (c.op) {
+            op_apply<double>(*c.op, trans, (const double *)x, (double *)y, c.s);
+            return;
+        }
+        PGB_CUDA(cudaMemcpyAsync(c.hx, x, sizeof(T) * nin, cudaMemcpyDeviceToHost, c.s));
+        c.sync();
+        const char ta = trans ? 'c' : 'n';
+        c.zaprod(&ta, &c.m, &c.n, (const propack_z16 *)c.hx, (propack_z16 *)c.hy, c.zparm, c.iparm, 1);
+        PGB_CUDA(cudaMemcpyAsync(y, c.hy, sizeof(T) * nout, cudaMemcpyHostToDevice, c.s));
     } else {
-        PGB_CUDA(cudaMemcpyAsync((double *)y, c.hy, sizeof(double) * nout, cudaMemcpyHostToDevice, c.s));
+        if (c.op) {
+            op_apply<T>(*c.op, trans, x, y, c.s);
+            return;
+        }
+        const double *xd = (const double *)x;
+        if (sizeof(T) != sizeof(double)) {
+            dev_convert<T, double>(c, x, c.dx, nin);
+            xd = c.dx;
+        }
+        PGB_CUDA(cudaMemcpyAsync(c.hx, xd, sizeof(double) * nin, cudaMemcpyDeviceToHost, c.s));
+        c.sync();
+        const char ta = trans ? 't' : 'n';
+        c.aprod(&ta, &c.m, &c.n, c.hx, c.hy, c.dparm, c.iparm, 1);
+        if (sizeof(T) != sizeof(double)) {
+            PGB_CUDA(cudaMemcpyAsync(c.dy, c.hy, sizeof(double) * nout, cudaMemcpyHostToDevice, c.s));
+            dev_convert<double, T>(c, c.dy, y, nout);
+        } else {
+            PGB_CUDA(cudaMemcpyAsync((double *)y, c.hy, sizeof(double) * nout, cudaMemcpyHostToDevice, c.s));
+        }
     }
 }
 
@@ -388,12 +460,21 @@ static void dev_reorth_full(Ctx &c, const T *W, size_t ld, int len, int kk, T *x
     if (kk <= 0 || len <= 0) return;
     for (int itry = 0; itry < NTRY; itry++) {
         const double nrm0 = *nrm;
-        k_gemvt_part<T><<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, x, c.part_cols);
-        PGB_LAUNCHED();
-        k_gemvt_final<<<1, BS, 0, c.s>>>(c.part_cols, c.nb, kk, c.h);
-        PGB_LAUNCHED();
-        k_gemvn_upd<T><<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, c.h, x);
-        PGB_LAUNCHED();
+        if constexpr (VecW<T>::w == 2) {
+            k_zgemvt_part<<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, x, c.part_cols);
+            PGB_LAUNCHED();
+            k_gemvt_final<<<1, BS, 0, c.s>>>(c.part_cols, c.nb, 2 * kk, c.h);
+            PGB_LAUNCHED();
+            k_zgemvn_upd<<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, c.h, x);
+            PGB_LAUNCHED();
+        } else {
+            k_gemvt_part<T><<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, x, c.part_cols);
+            PGB_LAUNCHED();
+            k_gemvt_final<<<1, BS, 0, c.s>>>(c.part_cols, c.nb, kk, c.h);
+            PGB_LAUNCHED();
+            k_gemvn_upd<T><<<c.nb, BS, 0, c.s>>>(W, ld, len, kk, c.h, x);
+            PGB_LAUNCHED();
+        }
         g_last.ndot += 2 * (int64_t)kk;
         *nrm = dev_nrm2<T>(c, x, len);
         if (*nrm > kappa * nrm0) { g_last.nreorth++; return; }
@@ -413,19 +494,35 @@ static int dev_getu0(Ctx &c, bool trans, int j, int ntry, T *u0, double *u0norm,
     const int rsize = trans ? c.m : c.n, usize = trans ? c.n : c.m;
     T *xr = (T *)c.xr;
     for (int itry = 0; itry < ntry; itry++) {
-        const int nch = (rsize + 63) / 64;
-        k_rng_pm1<T><<<std::max(1, std::min(c.nb, (nch + 255) / 256)), 256, 0, c.s>>>(xr, rsize, seed,
-                                                                                      (long long)itry * rsize);
+        // complex: zlarnv(2) draws the real and imaginary parts as 2 rsize
+        // consecutive values of the same stream
+        const int nval = rsize * VecW<T>::w;
+        const int nch = (nval + 63) / 64;
+        using E = typename std::conditional<VecW<T>::w == 2, double, T>::type;
+        k_rng_pm1<E><<<std::max(1, std::min(c.nb, (nch + 255) / 256)), 256, 0, c.s>>>((E *)xr, nval, seed,
+                                                                                      (long long)itry * nval);
         PGB_LAUNCHED();
         const double nrm = dev_nrm2<T>(c, xr, rsize);
         dev_aprod<T>(c, trans, xr, u0);
         g_last.nopx++;
         *u0norm = dev_nrm2<T>(c, u0, usize);
         *anormest = *u0norm / nrm;
-        if (j >= 1) dev_reorth_full<T>(c, W, ld, usize, j, u0, u0norm, KAPPA_GETU0);
+        // dgetu0.F:30 has a REAL literal, zgetu0.F:30 a DOUBLE one
+        if (j >= 1) dev_reorth_full<T>(c, W, ld, usize, j, u0, u0norm, VecW<T>::w == 2 ? KAPPA : KAPPA_GETU0);
         if (*u0norm > 0) return 0;
     }
     return -1;
+}
+
+// the deferred scale of u (which=0) or v (which=1) applied to its column
+template <typename T>
+static void apply_pend_col(Ctx &c, int which)
+{
+    using E = typename std::conditional<VecW<T>::w == 2, double, T>::type;
+    const int w = VecW<T>::w;
+    k_apply_pend_col<E><<<c.nb, 256, 0, c.s>>>(c.ctl, (E *)c.U, c.ldu * w, (E *)c.V, c.ldv * w, c.m * w, c.n * w,
+                                               which);
+    PGB_LAUNCHED();
 }
 
 // ------------------------------------------------------------ dlanbpro
@@ -444,17 +541,20 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
     // refresh the host copy (counters, pending scales)
     c.get_ctl();
     const int mn = std::max(m, n);
-    h.m = m; h.n = n; h.k = k; h.ldu = c.ldu; h.ldv = c.ldv;
+    h.m = m; h.n = n; h.k = k; h.ldu = c.ldu * c.vw; h.ldv = c.ldv * c.vw;
     h.icgs = ioption[0]; h.ielr = ioption[1];
+    h.cplx = VecW<T>::w == 2;
+    h.elr_need_dot = 0;
     // machine constants of the Lanczos vectors (FP32 vectors: eps = 2^-24)
-    const double eps = sizeof(T) == sizeof(double) ? EPS : 5.9604644775390625e-08;
+    constexpr bool f32 = std::is_same<T, float>::value;
+    const double eps = !f32 ? EPS : 5.9604644775390625e-08;
     h.eps_vec = eps;
     // the breakdown level of alpha/beta: max(m,n)*eps in FP64 (as the
     // reference); with FP32 vectors that worst-case bound reaches ~0.2*||A||
     // at a few million rows, so the FP32 level is the statistical
     // sqrt(max(m,n))*eps (2^-24), which still sits far above the rounding noise
     // of an FP32 product with compensated norms
-    h.epsn = sizeof(T) == sizeof(double) ? (double)mn * eps : std::sqrt((double)mn) * eps;
+    h.epsn = !f32 ? (double)mn * eps : std::sqrt((double)mn) * eps;
     h.epsn2 = std::sqrt((double)mn) * eps;
     h.delta = doption[0] < 0 ? std::sqrt(eps / k) : doption[0];
     h.eta = doption[1] < 0 ? std::pow(eps, 0.75) / std::sqrt((double)k) : doption[1];
@@ -598,9 +698,7 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
                     T *x = side == 0 ? c.Ucol<T>(j - 1) : c.Vcol<T>(j - 1);
                     T *y = side == 0 ? c.Vcol<T>(j - 1) : c.Ucol<T>(j);
                     // the product must see the scaled input
-                    k_apply_pend_col<T><<<c.nb, 256, 0, c.s>>>(c.ctl, (T *)c.U, c.ldu, (T *)c.V, c.ldv, m, n,
-                                                               side == 0 ? 0 : 1);
-                    PGB_LAUNCHED();
+                    apply_pend_col<T>(c, side == 0 ? 0 : 1);
                     k_clear_pend<<<1, 1, 0, c.s>>>(c.ctl, side == 0 ? 0 : 1);
                     PGB_LAUNCHED();
                     dev_aprod<T>(c, side == 0, x, y);
@@ -651,8 +749,7 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
                 // dlanbpro.F:372-405: new random v_j orthogonal to V(:,1:j-1)
                 // (u_j may still carry its deferred scale: apply it first)
                 c.put_ctl();
-                k_apply_pend_col<T><<<c.nb, 256, 0, c.s>>>(c.ctl, (T *)c.U, c.ldu, (T *)c.V, c.ldv, m, n, 0);
-                PGB_LAUNCHED();
+                apply_pend_col<T>(c, 0);
                 k_clear_pend<<<1, 1, 0, c.s>>>(c.ctl, 0);
                 PGB_LAUNCHED();
                 c.get_ctl();
@@ -680,8 +777,7 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
             } else {
                 // dlanbpro.F:503-535: new random u_{j+1} orthogonal to U(:,1:j)
                 c.put_ctl();
-                k_apply_pend_col<T><<<c.nb, 256, 0, c.s>>>(c.ctl, (T *)c.U, c.ldu, (T *)c.V, c.ldv, m, n, 1);
-                PGB_LAUNCHED();
+                apply_pend_col<T>(c, 1);
                 k_clear_pend<<<1, 1, 0, c.s>>>(c.ctl, 1);
                 PGB_LAUNCHED();
                 c.get_ctl();
@@ -734,7 +830,7 @@ template <typename T>
 static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, bool du, bool dv)
 {
     if (ncols <= 0) return;
-    if (sizeof(T) != sizeof(double)) {
+    if constexpr (std::is_same<T, float>::value) {
         // FP32 bases: widen column by column through the FP64 scratch
         for (int side = 0; side < 2; side++) {
             if (side == 0 ? !du : !dv) continue;
@@ -749,21 +845,31 @@ static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, 
             }
         }
         return;
-    }
+    } else {
+    // FP64 or complex*16 (sizeof(T) = 16) bases straight into the caller's arrays
     if (du)
-        PGB_CUDA(cudaMemcpy2DAsync(U, sizeof(double) * ldu, c.U, sizeof(double) * c.ldu, sizeof(double) * c.m, ncols,
+        PGB_CUDA(cudaMemcpy2DAsync(U, sizeof(T) * ldu, c.U, sizeof(T) * c.ldu, sizeof(T) * c.m, ncols,
                                    cudaMemcpyDeviceToHost, c.s));
     if (dv)
-        PGB_CUDA(cudaMemcpy2DAsync(V, sizeof(double) * ldv, c.V, sizeof(double) * c.ldv, sizeof(double) * c.n, ncols,
+        PGB_CUDA(cudaMemcpy2DAsync(V, sizeof(T) * ldv, c.V, sizeof(T) * c.ldv, sizeof(T) * c.n, ncols,
                                    cudaMemcpyDeviceToHost, c.s));
+    }
 }
 
 // A(:,0:nc) <- A(:,0:kk) op(B)   (dgemm_ovwr_left)
+// (complex A times the real B: the real GEMM on the (re, im) rows,
+// zdgemm_ovwr_left of complex16/zgemm_ovwr.F)
 template <typename T>
 static void ovwr_left(Ctx &c, T *A, int lda, int rows, int nc, int kk, const double *B, int ldb, bool tb)
 {
-    gemm<T>(rows, nc, kk, A, lda, false, B, ldb, tb, (T *)c.gout, lda, c.s);
-    copy_cols<T>((T *)c.gout, lda, A, lda, rows, nc, c.s);
+    if constexpr (VecW<T>::w == 2) {
+        gemm<double>(2 * rows, nc, kk, (const double *)A, 2 * lda, false, B, ldb, tb, (double *)c.gout, 2 * lda,
+                     c.s);
+        copy_cols<double>((const double *)c.gout, 2 * lda, (double *)A, 2 * lda, 2 * rows, nc, c.s);
+    } else {
+        gemm<T>(rows, nc, kk, A, lda, false, B, ldb, tb, (T *)c.gout, lda, c.s);
+        copy_cols<T>((T *)c.gout, lda, A, lda, rows, nc, c.s);
+    }
 }
 
 // the bidiagonal analysis; returns the number of converged values
@@ -861,14 +967,18 @@ static void finish_stats(int64_t launches0)
 
 static void setup_operator(Ctx &c, propack_aprod_t aprod, double *dparm, int *iparm)
 {
+    if ((void *)aprod == (void *)propack_gpu_csr_zaprod_) {
+        set_error("a complex operator needs the complex drivers");
+        throw ArgFailure();
+    }
     if (aprod == propack_gpu_csr_aprod_) {
         const Operator *op = lookup_operator(handle_from_iparm(iparm));
         if (!op) {
             set_error("APROD is propack_gpu_csr_aprod_ but iparm holds no live operator handle");
             throw ArgFailure();
         }
-        if (op->m != c.m || op->n != c.n) {
-            set_error("operator shape does not match m, n");
+        if (op->cplx || op->m != c.m || op->n != c.n) {
+            set_error(op->cplx ? "a complex operator needs the complex drivers" : "operator shape does not match m, n");
             throw ArgFailure();
         }
         c.op = op;
@@ -878,6 +988,34 @@ static void setup_operator(Ctx &c, propack_aprod_t aprod, double *dparm, int *ip
         c.iparm = iparm;
         PGB_CUDA(cudaMallocHost(&c.hx, sizeof(double) * std::max(c.m, c.n)));
         PGB_CUDA(cudaMallocHost(&c.hy, sizeof(double) * std::max(c.m, c.n)));
+    }
+}
+
+// the complex drivers: propack_gpu_csr_zaprod_ with a complex operator's
+// handle, or a user ZAPROD called on pinned host complex*16 vectors
+static void setup_zoperator(Ctx &c, propack_zaprod_t aprod, propack_z16 *zparm, int *iparm)
+{
+    if ((void *)aprod == (void *)propack_gpu_csr_aprod_ || (void *)aprod == (void *)propack_gpu_csr_saprod_) {
+        set_error("a real operator needs the real drivers");
+        throw ArgFailure();
+    }
+    if (aprod == propack_gpu_csr_zaprod_) {
+        const Operator *op = lookup_operator(handle_from_iparm(iparm));
+        if (!op) {
+            set_error("APROD is propack_gpu_csr_zaprod_ but iparm holds no live operator handle");
+            throw ArgFailure();
+        }
+        if (!op->cplx || op->m != 2 * c.m || op->n != 2 * c.n) {
+            set_error(!op->cplx ? "a real operator needs the real drivers" : "operator shape does not match m, n");
+            throw ArgFailure();
+        }
+        c.op = op;
+    } else {
+        c.zaprod = aprod;
+        c.zparm = zparm;
+        c.iparm = iparm;
+        PGB_CUDA(cudaMallocHost(&c.hx, sizeof(propack_z16) * std::max(c.m, c.n)));
+        PGB_CUDA(cudaMallocHost(&c.hy, sizeof(propack_z16) * std::max(c.m, c.n)));
     }
 }
 
@@ -936,7 +1074,8 @@ static void irl_loop(Ctx &c, const IrlIn &in, double *doption, const int *ioptio
         }
         if (trace_on())
             fprintf(stderr, "[propack_gb300] irl %s iter %d: dim %d nconv %d ierr %d\n",
-                    sizeof(T) == sizeof(double) ? "fp64" : "fp32", iter, dim, nconv, ierr);
+                    VecW<T>::w == 2 ? "complex" : sizeof(T) == sizeof(double) ? "fp64" : "fp32", iter, dim, nconv,
+                    ierr);
         if (in.stall_limit > 0) {
             if (nconv > best) { best = nconv; since = 0; }
             else if (++since >= in.stall_limit) break;
@@ -983,6 +1122,33 @@ static void irl_loop(Ctx &c, const IrlIn &in, double *doption, const int *ioptio
     }
     out.nconv = nconv;
     out.dim = dim;
+}
+
+// one IRL solve in the vectors' own precision (FP64, or complex*16 through
+// a ZAPROD or a complex operator); U(:,1) in, the Ritz vectors out
+template <typename T>
+static void irl_plain(const IrlIn &in, propack_aprod_t aprod, double *dparm, propack_zaprod_t zaprod,
+                      propack_z16 *zparm, int *iparm, double *U, int ldu, double *V, int ldv, double *doption,
+                      const int *ioption, IrlOut &out)
+{
+    Ctx c;
+    init_ctx<T>(c, in.m, in.n, in.dim);
+    if constexpr (VecW<T>::w == 2) setup_zoperator(c, zaprod, zparm, iparm);
+    else setup_operator(c, aprod, dparm, iparm);
+    PGB_CUDA(cudaEventRecord(c.ev0, c.s));
+    PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(T) * in.m, cudaMemcpyHostToDevice, c.s));
+    PGB_CUDA(cudaEventRecord(c.evs0, c.s));
+    irl_loop<T>(c, in, doption, ioption, out);
+    PGB_CUDA(cudaEventRecord(c.evs1, c.s));
+    copy_out<T>(c, U, ldu, V, ldv, out.nconv, in.du, in.dv);
+    PGB_CUDA(cudaEventRecord(c.ev1, c.s));
+    c.sync();
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    g_last.device_ms = ms;
+    cudaEventElapsedTime(&ms, c.evs0, c.evs1);
+    g_last.solve_ms = ms;
+    add_ctx_counters(c);
 }
 
 static void run_irl(const char *which, const char *jobu, const char *jobv, int m, int n, int dim, int p, int *neig,
@@ -1043,23 +1209,7 @@ static void run_irl(const char *which, const char *jobu, const char *jobv, int m
         g_last.nopx_low = g_last.nopx;
         doption[2] = dop32[2];
     } else if (g_precision == 0 || in.small_side) {
-        Ctx c;
-        init_ctx<double>(c, m, n, in.dim);
-        setup_operator(c, aprod, dparm, iparm);
-        PGB_CUDA(cudaEventRecord(c.ev0, c.s));
-        PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(double) * m, cudaMemcpyHostToDevice, c.s));
-        PGB_CUDA(cudaEventRecord(c.evs0, c.s));
-        irl_loop<double>(c, in, doption, ioption, out);
-        PGB_CUDA(cudaEventRecord(c.evs1, c.s));
-        copy_out<double>(c, U, ldu, V, ldv, out.nconv, in.du, in.dv);
-        PGB_CUDA(cudaEventRecord(c.ev1, c.s));
-        c.sync();
-        float ms = 0;
-        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
-        g_last.device_ms = ms;
-        cudaEventElapsedTime(&ms, c.evs0, c.evs1);
-        g_last.solve_ms = ms;
-        add_ctx_counters(c);
+        irl_plain<double>(in, aprod, dparm, nullptr, nullptr, iparm, U, ldu, V, ldv, doption, ioption, out);
     } else {
         // mixed form: FP32 Lanczos to MIXED_TOL, then FP64 refinement
         Ctx c32;
@@ -1126,21 +1276,25 @@ static void run_irl(const char *which, const char *jobu, const char *jobv, int m
     finish_stats(l0);
 }
 
+// T = complex*16 (double2): U, V are the caller's complex arrays and the
+// operator comes from zaprod / zparm
 template <typename T>
 static void run_lansvd_t(const char *jobu, const char *jobv, int m, int n, int *kp, int kmax, propack_aprod_t aprod,
                        double *U, int ldu, double *sigma, double *bnd, double *V, int ldv, double tolin,
-                       double *doption, const int *ioption, int *info, double *dparm, int *iparm)
+                       double *doption, const int *ioption, int *info, double *dparm, int *iparm,
+                       propack_zaprod_t zaprod = nullptr, propack_z16 *zparm = nullptr)
 {
     const int k = *kp;
-    if (m <= 0 || n <= 0 || k <= 0 || kmax <= 0 || ldu < m || ldv < n || !aprod || !U || !V || !sigma || !bnd ||
-        !doption || !ioption) {
-        set_error("dlansvd_: invalid argument");
+    constexpr bool cplx = VecW<T>::w == 2;
+    if (m <= 0 || n <= 0 || k <= 0 || kmax <= 0 || ldu < m || ldv < n || !(cplx ? (void *)zaprod : (void *)aprod) ||
+        !U || !V || !sigma || !bnd || !doption || !ioption) {
+        set_error(cplx ? "zlansvd_: invalid argument" : "dlansvd_: invalid argument");
         throw ArgFailure();
     }
     const int64_t l0 = g_launches;
     g_last = Stats();
     const int lanmax = std::min(std::min(n + 1, m + 1), kmax);
-    const bool f32 = sizeof(T) != sizeof(double);
+    constexpr bool f32 = std::is_same<T, float>::value;
     const double tol = std::min(1.0, std::max(16.0 * (f32 ? EPS32 : EPS), tolin));
     // the FP32 vectors keep orthogonality at the FP32 levels sqrt(eps), eps^(3/4)
     double dop[4] = {doption[0], doption[1], doption[2], 0.0};
@@ -1148,11 +1302,17 @@ static void run_lansvd_t(const char *jobu, const char *jobv, int m, int n, int *
     if (f32 && dop[1] >= 0) dop[1] = std::max(dop[1], std::pow(EPS32, 0.75));
     Ctx c;
     init_ctx<T>(c, m, n, lanmax);
-    setup_operator(c, aprod, dparm, iparm);
+    if constexpr (cplx) setup_zoperator(c, zaprod, zparm, iparm);
+    else setup_operator(c, aprod, dparm, iparm);
     PGB_CUDA(cudaEventRecord(c.ev0, c.s));
-    PGB_CUDA(cudaMemcpyAsync(c.dx, U, sizeof(double) * m, cudaMemcpyHostToDevice, c.s));
-    PGB_CUDA(cudaEventRecord(c.evs0, c.s));
-    dev_convert<double, T>(c, c.dx, c.Ucol<T>(0), m);
+    if constexpr (cplx) {
+        PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(T) * m, cudaMemcpyHostToDevice, c.s));
+        PGB_CUDA(cudaEventRecord(c.evs0, c.s));
+    } else {
+        PGB_CUDA(cudaMemcpyAsync(c.dx, U, sizeof(double) * m, cudaMemcpyHostToDevice, c.s));
+        PGB_CUDA(cudaEventRecord(c.evs0, c.s));
+        dev_convert<double, T>(c, c.dx, c.Ucol<T>(0), m);
+    }
     double rnorm = dev_nrm2<T>(c, c.Ucol<T>(0), m);
     int ierr = 0;
     double anorm_drv = 0.0;
@@ -1241,6 +1401,47 @@ static void run_lansvd(const char *jobu, const char *jobv, int m, int n, int *kp
                              ioption, info, dparm, iparm);
 }
 
+// ZLANSVD_IRL (complex16/zlansvd_irl.F): the FP64 IRL on complex*16
+// vectors; the precision setting does not apply
+static void run_zirl(const char *which, const char *jobu, const char *jobv, int m, int n, int dim, int p, int *neig,
+                     int maxiter, propack_zaprod_t aprod, propack_z16 *U, int ldu, double *sigma, double *bnd,
+                     propack_z16 *V, int ldv, double tolin, double *doption, const int *ioption, int *info,
+                     propack_z16 *zparm, int *iparm)
+{
+    if (m <= 0 || n <= 0 || dim <= 0 || p < 0 || *neig < 0 || ldu < m || ldv < n || !aprod || !U || !V || !sigma ||
+        !bnd || !doption || !ioption) {
+        set_error("zlansvd_irl_: invalid argument");
+        throw ArgFailure();
+    }
+    const int64_t l0 = g_launches;
+    g_last = Stats();
+    IrlIn in;
+    in.small_side = which && (which[0] == 's' || which[0] == 'S');
+    in.du = yes(jobu);
+    in.dv = yes(jobv);
+    in.m = m;
+    in.n = n;
+    in.dim = std::min(dim, std::min(n + 1, m + 1));
+    in.p = p;
+    in.neig = *neig;
+    in.maxiter = maxiter;
+    in.tol = std::min(1.0, std::max(16.0 * EPS, tolin));
+    const int k = in.dim - p;
+    if (k < 1 || in.neig > k) {
+        set_error("zlansvd_irl_: need 1 <= neig <= dim - p");
+        throw ArgFailure();
+    }
+    IrlOut out;
+    irl_plain<double2>(in, nullptr, nullptr, aprod, zparm, iparm, (double *)U, ldu, (double *)V, ldv, doption,
+                       ioption, out);
+    for (int i = 0; i < out.nconv && i < in.neig; i++) { sigma[i] = out.sigma[i]; bnd[i] = out.bnd[i]; }
+    *info = out.info;
+    *neig = out.nconv;
+    g_last.nlandim = out.dim;
+    prof_collect();
+    finish_stats(l0);
+}
+
 }  // namespace pgb
 
 // ------------------------------------------------------------------ C ABI
@@ -1278,6 +1479,54 @@ extern "C" void dlansvd_(const char *jobu, const char *jobv, const int *m, const
     try {
         run_lansvd(jobu, jobv, *m, *n, k, *kmax, aprod, U, *ldu, sigma, bnd, V, *ldv, *tolin, doption, ioption, info,
                    dparm, iparm);
+    } catch (const CudaFailure &) {
+        *info = PROPACK_ERR_CUDA;
+    } catch (const ArgFailure &) {
+        *info = PROPACK_ERR_ARG;
+    } catch (const WaitFailure &) {
+        *info = PROPACK_ERR_WAIT;
+    }
+}
+
+// ------------------------------------------------------ complex drivers
+// ZLANSVD / ZLANSVD_IRL (complex16/zlansvd.F:1-3, complex16/zlansvd_irl.F:1-3):
+// complex*16 U, V, ZWORK and ZPARM; DOUBLE PRECISION Sigma, bnd, WORK and
+// DOPTION; the APROD takes TRANSA 'n' (y = A x) or 'c' (y = A^H x).
+extern "C" void zlansvd_irl_(const char *which, const char *jobu, const char *jobv, const int *m, const int *n,
+                             const int *dim, const int *p, int *neig, const int *maxiter, propack_zaprod_t aprod,
+                             propack_z16 *U, const int *ldu, double *sigma, double *bnd, propack_z16 *V,
+                             const int *ldv, const double *tolin, double *work, const int *lwork, propack_z16 *zwork,
+                             const int *lzwrk, int *iwork, const int *liwork, double *doption, const int *ioption,
+                             int *info, propack_z16 *zparm, int *iparm, size_t which_len, size_t jobu_len,
+                             size_t jobv_len)
+{
+    (void)work; (void)lwork; (void)zwork; (void)lzwrk; (void)iwork; (void)liwork;
+    (void)which_len; (void)jobu_len; (void)jobv_len;
+    set_error("");
+    try {
+        run_zirl(which, jobu, jobv, *m, *n, *dim, *p, neig, *maxiter, aprod, U, *ldu, sigma, bnd, V, *ldv, *tolin,
+                 doption, ioption, info, zparm, iparm);
+    } catch (const CudaFailure &) {
+        *info = PROPACK_ERR_CUDA;
+    } catch (const ArgFailure &) {
+        *info = PROPACK_ERR_ARG;
+    } catch (const WaitFailure &) {
+        *info = PROPACK_ERR_WAIT;
+    }
+}
+
+extern "C" void zlansvd_(const char *jobu, const char *jobv, const int *m, const int *n, int *k, const int *kmax,
+                         propack_zaprod_t aprod, propack_z16 *U, const int *ldu, double *sigma, double *bnd,
+                         propack_z16 *V, const int *ldv, const double *tolin, double *work, const int *lwork,
+                         propack_z16 *zwork, const int *lzwrk, int *iwork, const int *liwork, double *doption,
+                         const int *ioption, int *info, propack_z16 *zparm, int *iparm, size_t jobu_len,
+                         size_t jobv_len)
+{
+    (void)work; (void)lwork; (void)zwork; (void)lzwrk; (void)iwork; (void)liwork; (void)jobu_len; (void)jobv_len;
+    set_error("");
+    try {
+        run_lansvd_t<double2>(jobu, jobv, *m, *n, k, *kmax, nullptr, (double *)U, *ldu, sigma, bnd, (double *)V,
+                              *ldv, *tolin, doption, ioption, info, nullptr, iparm, aprod, zparm);
     } catch (const CudaFailure &) {
         *info = PROPACK_ERR_CUDA;
     } catch (const ArgFailure &) {

@@ -28,6 +28,8 @@
 // unscaled, the product that reads it through the operator is scaled
 // instead (A(v/a) = (Av)/a), and the next same-side SpMV, which reads it
 // row by row, writes the scaled value back.
+#include <type_traits>
+
 #include "pgb.cuh"
 #include "pgb_f3.cuh"
 #include "pgb_spmv.cuh"
@@ -374,8 +376,11 @@ __device__ void after_spmv(Tail &t, const LbArgs &a, int j, double nrm, double d
             } else if (c.ielr > 0 && c.alpha < KAPPA * c.beta) {
                 c.elr_active = 1;
                 c.elr_iter = 1;
-                c.elr_s = dotp;
-                if (c.beta != 0.0) { c.beta += dotp; a.bbeta[j - 2] = c.beta; }
+                if (c.cplx) c.elr_need_dot = 1;
+                else {
+                    c.elr_s = dotp;
+                    if (c.beta != 0.0) { c.beta += dotp; a.bbeta[j - 2] = c.beta; }
+                }
                 t.go = 0;
             }
         } else {
@@ -384,8 +389,11 @@ __device__ void after_spmv(Tail &t, const LbArgs &a, int j, double nrm, double d
             if (c.ielr > 0 && c.beta < KAPPA * c.alpha) {
                 c.elr_active = 1;
                 c.elr_iter = 1;
-                c.elr_s = dotp;
-                if (c.alpha != 0.0) { c.alpha += dotp; a.balpha[j - 1] = c.alpha; }
+                if (c.cplx) c.elr_need_dot = 1;
+                else {
+                    c.elr_s = dotp;
+                    if (c.alpha != 0.0) { c.alpha += dotp; a.balpha[j - 1] = c.alpha; }
+                }
                 t.go = 0;
             }
         }
@@ -399,8 +407,9 @@ __device__ void after_spmv(Tail &t, const LbArgs &a, int j, double nrm, double d
     }
 }
 
+// dotp_im: the imaginary part of the next projection (complex vectors)
 template <int SIDE>
-__device__ void after_elr(Tail &t, const LbArgs &a, int j, double snrm, double dotp)
+__device__ void after_elr(Tail &t, const LbArgs &a, int j, double snrm, double dotp, double dotp_im = 0.0)
 {
     if (threadIdx.x == 0) {
         LbCtl &c = t.c;
@@ -417,7 +426,8 @@ __device__ void after_elr(Tail &t, const LbArgs &a, int j, double snrm, double d
             cur = snrm;
             c.elr_iter++;
             c.elr_s = dotp;
-            if (oth != 0.0) {
+            if (c.cplx) c.elr_s_im = dotp_im;
+            else if (oth != 0.0) {
                 oth += dotp;
                 if (SIDE == 0) a.bbeta[j - 2] = oth;
                 else a.balpha[j - 1] = oth;
@@ -910,6 +920,200 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd_f3(LbArgs a, int j, int last)
     }
 }
 
+// ------------------------------------------------- complex*16 vectors
+// The complex form (complex16/zlanbpro.F) keeps alpha, beta and the omega
+// recurrences real.  Its vectors are (re, im) pairs of doubles and its
+// operator is the real 2x2-block form of A (pgb_operator.cu), so the fused
+// SpMV, the norms, the deferred scaling and the flush above serve it as
+// they are.  What differs are the inner products, which are conjugated and
+// complex: in the ELR (zlanbpro.F:318-331, :451-464) and in Gram-Schmidt
+// (zreorth.F, zcgs: zgemv 'C' then 'N').
+
+// conj(w) x added to (re, im)
+__device__ __forceinline__ void zdot_acc(double &re, double &im, const double2 &w, const double2 &x)
+{
+    re = fma(w.x, x.x, re);
+    re = fma(w.y, x.y, re);
+    im = fma(w.x, x.y, im);
+    im = fma(-w.y, x.x, im);
+}
+// acc -= w h
+__device__ __forceinline__ void zfms(double2 &acc, const double2 &w, const double2 &h)
+{
+    acc.x = fma(-w.x, h.x, acc.x);
+    acc.x = fma(w.y, h.y, acc.x);
+    acc.y = fma(-w.x, h.y, acc.y);
+    acc.y = fma(-w.y, h.x, acc.y);
+}
+
+// One complex ELR pass: x -= s p, ||x||^2 and the next projection <p, x>.
+// The fused SpMV cannot form the complex <p, x> (the real and imaginary
+// rows of an element are different rows of the 2x2-block operator), so the
+// first pass after it (elr_need_dot set) forms <p, x> alone.
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_zelr(LbArgs a, int j)
+{
+    __shared__ double sred[32];
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->elr_active) return;
+    const bool dot_only = a.ctl->elr_need_dot != 0;
+    const double sr = a.ctl->elr_s, si = a.ctl->elr_s_im;
+    const int len = (SIDE == 0 ? a.adj.rows : a.fwd.rows) / 2;
+    double2 *x = reinterpret_cast<double2 *>(SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j));
+    const double2 *p =
+        reinterpret_cast<const double2 *>(SIDE == 0 ? vcol<double>(a, j - 2) : ucol<double>(a, j - 1));
+    double sq = 0.0, dr = 0.0, di = 0.0;
+    for (int r = blockIdx.x * BS + threadIdx.x; r < len; r += gridDim.x * BS) {
+        const double2 pv = p[r];
+        double2 y = x[r];
+        if (!dot_only) {
+            y.x = fma(-sr, pv.x, y.x);
+            y.x = fma(si, pv.y, y.x);
+            y.y = fma(-sr, pv.y, y.y);
+            y.y = fma(-si, pv.x, y.y);
+            x[r] = y;
+            sq = fma(y.x, y.x, sq);
+            sq = fma(y.y, y.y, sq);
+        }
+        zdot_acc(dr, di, pv, y);
+    }
+    const double sq2 = block_sum<BS>(sq, sred);
+    const double dr2 = block_sum<BS>(dr, sred);
+    const double di2 = block_sum<BS>(di, sred);
+    if (threadIdx.x == 0) {
+        a.part_sq[blockIdx.x] = sq2;
+        a.part_dot[blockIdx.x] = dr2;
+        a.part_cols[blockIdx.x] = di2;  // Gram-Schmidt is idle while the ELR runs
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
+        const double d2 = sum_parts(a.part_dot, gridDim.x, t.red);
+        const double e2 = sum_parts(a.part_cols, gridDim.x, t.red);
+        if (dot_only) {
+            if (threadIdx.x == 0) {
+                t.c.elr_s = d2;
+                t.c.elr_s_im = e2;
+                t.c.elr_need_dot = 0;
+            }
+        } else {
+            after_elr<SIDE>(t, a, j, sqrt(s2), d2, e2);
+        }
+        tail_store(a, t);
+    }
+}
+
+// projections h = W(:,sel)^H x (the zgemv('C') of zcgs): the work layout of
+// k_lb_cgs_dots with one complex element per 16-byte vector; column c's
+// partials go to part_cols rows 2c (re) and 2c+1 (im), and h comes out as
+// (re, im) pairs
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_zcgs_dots(LbArgs a, int j)
+{
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 0) return;
+    const int L = a.ctl->nsel;
+    const int len = (SIDE == 0 ? a.adj.rows : a.fwd.rows) / 2;
+    const size_t ld = (size_t)(SIDE == 0 ? a.ldv : a.ldu) / 2;
+    const double2 *W = reinterpret_cast<const double2 *>(SIDE == 0 ? a.V : a.U);
+    const double2 *x =
+        reinterpret_cast<const double2 *>(SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j));
+    const int chunk = (len + gridDim.x - 1) / gridDim.x;
+    const int v0 = blockIdx.x * chunk, v1 = min(len, v0 + chunk);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c0 = w * DOT_COLS; c0 < L; c0 += (BS / 32) * DOT_COLS) {
+        const int nc = min(DOT_COLS, L - c0);
+        const double2 *col[DOT_COLS];
+#pragma unroll
+        for (int u = 0; u < DOT_COLS; u++) col[u] = W + (size_t)a.sel[c0 + (u < nc ? u : 0)] * ld;
+        double re[DOT_COLS][2], im[DOT_COLS][2];
+#pragma unroll
+        for (int u = 0; u < DOT_COLS; u++) re[u][0] = re[u][1] = im[u][0] = im[u][1] = 0.0;
+        int v = v0 + lane;
+        for (; v + 32 < v1; v += 64) {
+            const double2 x0 = x[v], x1 = x[v + 32];
+            double2 w0[DOT_COLS], w1[DOT_COLS];
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) {
+                w0[u] = col[u][v];
+                w1[u] = col[u][v + 32];
+            }
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) {
+                zdot_acc(re[u][0], im[u][0], w0[u], x0);
+                zdot_acc(re[u][1], im[u][1], w1[u], x1);
+            }
+        }
+        if (v < v1) {
+            const double2 x0 = x[v];
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) zdot_acc(re[u][0], im[u][0], col[u][v], x0);
+        }
+#pragma unroll
+        for (int u = 0; u < DOT_COLS; u++) {
+            const double sr = warp_sum(re[u][0] + re[u][1]);
+            const double si = warp_sum(im[u][0] + im[u][1]);
+            if (lane == 0 && u < nc) {
+                a.part_cols[(size_t)(2 * (c0 + u)) * a.nb + blockIdx.x] = sr;
+                a.part_cols[(size_t)(2 * (c0 + u) + 1) * a.nb + blockIdx.x] = si;
+            }
+        }
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        reduce_cols(a, 2 * L);
+        if (threadIdx.x == 0) t.c.cgs_phase = 1;
+        tail_store(a, t);
+    }
+}
+
+// x -= W(:,sel) h (the zgemv('N') of zcgs) and ||x||^2, one complex element
+// per thread and step; h (as double2) and the selection in shared memory
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_zcgs_upd(LbArgs a, int j, int last)
+{
+    extern __shared__ double dyn[];  // h[L] as (re, im) | sel[L]
+    __shared__ double sred[32];
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 1) return;
+    const int L = a.ctl->nsel;
+    double2 *hs = reinterpret_cast<double2 *>(dyn);
+    int *ssel = reinterpret_cast<int *>(dyn + 2 * (size_t)L);
+    for (int c = threadIdx.x; c < L; c += BS) {
+        hs[c] = make_double2(a.h[2 * c], a.h[2 * c + 1]);
+        ssel[c] = a.sel[c];
+    }
+    __syncthreads();
+    const int len = (SIDE == 0 ? a.adj.rows : a.fwd.rows) / 2;
+    const size_t ld = (size_t)(SIDE == 0 ? a.ldv : a.ldu) / 2;
+    const double2 *W = reinterpret_cast<const double2 *>(SIDE == 0 ? a.V : a.U);
+    double2 *x = reinterpret_cast<double2 *>(SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j));
+    double sq = 0.0;
+    for (int v = blockIdx.x * BS + threadIdx.x; v < len; v += gridDim.x * BS) {
+        double2 acc = x[v];
+        int c = 0;
+        for (; c + CGS_UNROLL <= L; c += CGS_UNROLL) {
+            double2 wv[CGS_UNROLL];
+#pragma unroll
+            for (int u = 0; u < CGS_UNROLL; u++) wv[u] = W[(size_t)ssel[c + u] * ld + v];
+#pragma unroll
+            for (int u = 0; u < CGS_UNROLL; u++) zfms(acc, wv[u], hs[c + u]);
+        }
+        for (; c < L; c++) zfms(acc, W[(size_t)ssel[c] * ld + v], hs[c]);
+        x[v] = acc;
+        sq = fma(acc.x, acc.x, sq);
+        sq = fma(acc.y, acc.y, sq);
+    }
+    const double sq2 = block_sum<BS>(sq, sred);
+    if (threadIdx.x == 0) a.part_sq[blockIdx.x] = sq2;
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
+        after_cgs<SIDE>(t, a, j, sqrt(s2), last);
+        tail_store(a, t);
+    }
+}
+
 // apply the deferred scaling of the newest u and v columns
 template <typename T>
 __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
@@ -955,6 +1159,11 @@ void lb_set_smem_limits(int kmax)
         PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd_f3<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
         PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd_f3<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
     }
+    if (need3 > 48 * 1024) {
+        // the complex update keeps h as (re, im): the same shared memory as the f3 update
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_zcgs_upd<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_zcgs_upd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
+    }
     const size_t need = (sizeof(double) + sizeof(int)) * (size_t)(kmax + 1) + 16;
     if (need > 48 * 1024) {
         set_upd_limits<0, double>(need);
@@ -983,6 +1192,16 @@ static void launch_cgs_pass(const LbArgs &a, int j, int last, cudaStream_t s)
     PGB_LAUNCHED();
 }
 
+// one complex Gram-Schmidt pass
+template <int SIDE>
+static void launch_zcgs_pass(const LbArgs &a, int j, int last, cudaStream_t s)
+{
+    PGB_PROF(PK_CGS_DOTS, s, k_lb_zcgs_dots<SIDE><<<a.nb, BS, 0, s>>>(a, j));
+    PGB_LAUNCHED();
+    PGB_PROF(PK_CGS_UPD, s, k_lb_zcgs_upd<SIDE><<<a.nb, BS, cgs_smem_f3(a), s>>>(a, j, last));
+    PGB_LAUNCHED();
+}
+
 // one wave of CTAs at the fused SpMV's occupancy (partials are summed over gridDim)
 template <int SIDE, typename T, int SHORT>
 static int spmv_grid(int nb)
@@ -1006,10 +1225,43 @@ static void launch_spmv(const LbArgs &a, const Csr &A, int j, bool host_product,
 
 // Enqueue the kernels of one half step.  host_product: the product was
 // written into the output column by a host APROD call.
+// the half step of the complex form: the real fused SpMV on the 2x2-block
+// operator, then one more ELR launch than ielr (the first forms the complex
+// projection), then the complex Gram-Schmidt passes
+static void zenqueue_half(const LbArgs &a, int side, int j, int ielr, int ntry_spec, bool host_product,
+                          cudaStream_t s)
+{
+    const int nb = a.nb;
+    const int nelr = ielr > 0 ? ielr + 1 : 0;
+    if (side == 0) {
+        PGB_PROF(PK_SPMV_ADJ, s, launch_spmv<0, double>(a, a.adj, j, host_product, s));
+        PGB_LAUNCHED();
+        if (j > 1)
+            for (int i = 0; i < nelr; i++) {
+                PGB_PROF(PK_ELR, s, k_lb_zelr<0><<<nb, BS, 0, s>>>(a, j));
+                PGB_LAUNCHED();
+            }
+        for (int i = 0; i < ntry_spec; i++) launch_zcgs_pass<0>(a, j, i == ntry_spec - 1, s);
+    } else {
+        PGB_PROF(PK_SPMV_FWD, s, launch_spmv<1, double>(a, a.fwd, j, host_product, s));
+        PGB_LAUNCHED();
+        for (int i = 0; i < nelr; i++) {
+            PGB_PROF(PK_ELR, s, k_lb_zelr<1><<<nb, BS, 0, s>>>(a, j));
+            PGB_LAUNCHED();
+        }
+        for (int i = 0; i < ntry_spec; i++) launch_zcgs_pass<1>(a, j, i == ntry_spec - 1, s);
+    }
+}
+
 template <typename T>
 void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int ielr, int ntry_spec,
                      bool host_product, cudaStream_t s)
 {
+    if constexpr (VecW<T>::w == 2) {
+        (void)op;
+        zenqueue_half(a, side, j, ielr, ntry_spec, host_product, s);
+        return;
+    } else {
     const int nb = a.nb;
     if (side == 0) {
         if (!host_product && op && op->r > 0)
@@ -1035,6 +1287,7 @@ void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int i
         }
         for (int i = 0; i < ntry_spec; i++) launch_cgs_pass<1, T>(a, j, i == ntry_spec - 1, s);
     }
+    }
 }
 
 // more Gram-Schmidt passes after a suspension with reason 2
@@ -1042,15 +1295,22 @@ template <typename T>
 void lb_enqueue_cgs_more(const LbArgs &a, int side, int j, int passes, cudaStream_t s)
 {
     for (int i = 0; i < passes; i++) {
-        if (side == 0) launch_cgs_pass<0, T>(a, j, i == passes - 1, s);
-        else launch_cgs_pass<1, T>(a, j, i == passes - 1, s);
+        if constexpr (VecW<T>::w == 2) {
+            if (side == 0) launch_zcgs_pass<0>(a, j, i == passes - 1, s);
+            else launch_zcgs_pass<1>(a, j, i == passes - 1, s);
+        } else {
+            if (side == 0) launch_cgs_pass<0, T>(a, j, i == passes - 1, s);
+            else launch_cgs_pass<1, T>(a, j, i == passes - 1, s);
+        }
     }
 }
 
+// (complex: the flush of the real scalars, whose lengths LbArgs counts)
 template <typename T>
 void lb_enqueue_flush(const LbArgs &a, cudaStream_t s)
 {
-    k_lb_flush<T><<<a.nb, BS, 0, s>>>(a);
+    using E = typename std::conditional<VecW<T>::w == 2, double, T>::type;
+    k_lb_flush<E><<<a.nb, BS, 0, s>>>(a);
     PGB_LAUNCHED();
 }
 
@@ -1060,5 +1320,8 @@ template void lb_enqueue_cgs_more<double>(const LbArgs &, int, int, int, cudaStr
 template void lb_enqueue_cgs_more<float>(const LbArgs &, int, int, int, cudaStream_t);
 template void lb_enqueue_flush<double>(const LbArgs &, cudaStream_t);
 template void lb_enqueue_flush<float>(const LbArgs &, cudaStream_t);
+template void lb_enqueue_half<double2>(const LbArgs &, const Operator *, int, int, int, int, bool, cudaStream_t);
+template void lb_enqueue_cgs_more<double2>(const LbArgs &, int, int, int, cudaStream_t);
+template void lb_enqueue_flush<double2>(const LbArgs &, cudaStream_t);
 
 }  // namespace pgb

@@ -900,6 +900,74 @@ extern "C" int propack_csr_create(int m, int n, const int64_t *s_rowptr, const i
 
 extern "C" int propack_csr_destroy(int64_t handle) { return destroy_operator(handle); }
 
+// Row 2i of the real form holds (2j, b), (2j+1, -c) and row 2i+1 holds
+// (2j, c), (2j+1, b) for each entry b + ic of row i at column j, in the
+// order of row i; so [re; im] rows give Re and Im of (A x)_i, and the
+// transposed form gives A^H x on the same pairs.
+extern "C" int propack_zcsr_expand(int m, int n, const int64_t *rowptr, const int32_t *colidx,
+                                   const propack_z16 *val, int64_t *rowptr2, int32_t *colidx2, double *val2)
+{
+    if (m < 0 || n < 0 || !rowptr || !rowptr2 || m > INT32_MAX / 2 || n > INT32_MAX / 2) return PROPACK_ERR_ARG;
+    const int64_t nnz = rowptr[m];
+    if (nnz < 0 || 4 * nnz >= (int64_t)INT32_MAX) return PROPACK_ERR_ARG;
+    if (nnz > 0 && (!colidx || !val || !colidx2 || !val2)) return PROPACK_ERR_ARG;
+    if (rowptr[0] != 0) return PROPACK_ERR_ARG;
+    for (int i = 0; i < m; i++)
+        if (rowptr[i + 1] < rowptr[i]) return PROPACK_ERR_ARG;
+    rowptr2[0] = 0;
+    for (int i = 0; i < m; i++) {
+        const int64_t p0 = rowptr[i], p1 = rowptr[i + 1], len = p1 - p0;
+        const int64_t r0 = 4 * p0, r1 = r0 + 2 * len;  // starts of rows 2i and 2i+1
+        rowptr2[2 * i + 1] = r1;
+        rowptr2[2 * i + 2] = r1 + 2 * len;
+        for (int64_t e = p0; e < p1; e++) {
+            if (colidx[e] < 0 || colidx[e] >= n) return PROPACK_ERR_ARG;
+            const int64_t q = 2 * (e - p0);
+            const int32_t j2 = 2 * colidx[e];
+            const double b = val[e].re, c = val[e].im;
+            colidx2[r0 + q] = j2;
+            val2[r0 + q] = b;
+            colidx2[r0 + q + 1] = j2 + 1;
+            val2[r0 + q + 1] = -c;
+            colidx2[r1 + q] = j2;
+            val2[r1 + q] = c;
+            colidx2[r1 + q + 1] = j2 + 1;
+            val2[r1 + q + 1] = b;
+        }
+    }
+    return 0;
+}
+
+extern "C" int propack_zcsr_create(int m, int n, const int64_t *rowptr, const int32_t *colidx,
+                                   const propack_z16 *val, int64_t *handle)
+{
+    if (m <= 0 || n <= 0 || !rowptr || !handle) {
+        set_error("invalid argument to propack_zcsr_create");
+        return PROPACK_ERR_ARG;
+    }
+    const int64_t nnz = rowptr[m];
+    if (nnz < 0 || 4 * nnz >= (int64_t)INT32_MAX) {
+        set_error("complex operator has 2^29 or more nonzeros (its real form 2^31)");
+        return PROPACK_ERR_ARG;
+    }
+    // the expansion checks row pointers and column indices on the host; the
+    // real form is checked again on the device by propack_csr_create
+    std::vector<int64_t> p2(2 * (size_t)m + 1);
+    std::vector<int32_t> i2(std::max<int64_t>(4 * nnz, 1));
+    std::vector<double> v2(std::max<int64_t>(4 * nnz, 1));
+    if (propack_zcsr_expand(m, n, rowptr, colidx, val, p2.data(), i2.data(), v2.data()) != 0) {
+        set_error(rowptr[0] != 0 ? "row pointers are not monotone from 0 to nnz"
+                                 : "row pointers are not monotone from 0 to nnz, or a column index is out of range");
+        return PROPACK_ERR_ARG;
+    }
+    const int rc = propack_csr_create(2 * m, 2 * n, p2.data(), i2.data(), v2.data(), 0, nullptr, nullptr, nullptr,
+                                      nullptr, nullptr, nullptr, nullptr, handle);
+    if (rc != 0) return rc;
+    Operator *op = lookup_operator(*handle);
+    if (op) op->cplx = 1;
+    return 0;
+}
+
 extern "C" int propack_release_memory(void)
 {
     try {
@@ -951,12 +1019,25 @@ extern "C" void propack_gpu_csr_saprod_(const char *transa, const int *m, const 
     for (int i = 0; i < nout; i++) y[i] = (float)yd[i];
 }
 
+extern "C" void propack_gpu_csr_zaprod_(const char *transa, const int *m, const int *n, const propack_z16 *x,
+                                        propack_z16 *y, propack_z16 *zparm, int *iparm, size_t transa_len)
+{
+    (void)zparm;
+    Operator *op = lookup_operator(handle_from_iparm(iparm));
+    if (!op || !op->cplx) { set_error("propack_gpu_csr_zaprod_: iparm holds no live complex operator"); return; }
+    // the real form is 2m x 2n: 'n' gives A x, anything else A^H x
+    const int m2 = 2 * *m, n2 = 2 * *n;
+    const char t = (transa[0] == 'n' || transa[0] == 'N') ? 'n' : 't';
+    propack_gpu_csr_aprod_(&t, &m2, &n2, (const double *)x, (double *)y, nullptr, iparm, transa_len);
+}
+
 extern "C" void propack_gpu_csr_aprod_(const char *transa, const int *m, const int *n, const double *x, double *y,
                                        double *dparm, int *iparm, size_t transa_len)
 {
     (void)dparm; (void)transa_len;
     Operator *op = lookup_operator(handle_from_iparm(iparm));
     if (!op) { set_error("propack_gpu_csr_aprod_: iparm holds no live operator"); return; }
+    if (op->m != *m || op->n != *n) { set_error("propack_gpu_csr_aprod_: m, n do not match the operator"); return; }
     const bool t = (transa[0] == 't' || transa[0] == 'T');
     const int nin = t ? *m : *n, nout = t ? *n : *m;
     try {
