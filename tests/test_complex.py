@@ -254,9 +254,12 @@ def test_complex_zero_start_and_smallest():
     np.testing.assert_allclose(s, g["z2_dense_sigma"][:4], rtol=SIG_RTOL)
     assert phase_err(u, uo) < VEC_TOL
     # which='SM' with p <= dim/2 (larger p is the reference's known
-    # restart problem for the smallest values, Changelog:56)
+    # restart problem for the smallest values, Changelog:56) and full
+    # reorthogonalisation (delta = 0): with the partial scheme the oracle
+    # itself returns spurious tiny values on 2 of 40 random draws of this
+    # family (seeds 8 and 25), and the draw depends on the host's LAPACK
     B = geometric_complex(seed=2, m=120, n=90, r=90, q=0.97)
-    kw = dict(which='SM', irl_mode=True, kmax=60, shifts=20, tol=1e-10, maxiter=800)
+    kw = dict(which='SM', irl_mode=True, kmax=60, shifts=20, tol=1e-10, maxiter=800, delta=0.0)
     u, s, vh, bnd = pg.svdp(B, 3, rng=np.random.default_rng(0), **kw)
     uo, so, vho, bo, info, kc = oracle.svdp(B, 3, rng=np.random.default_rng(0), **kw)
     dense = np.linalg.svd(B.toarray(), compute_uv=False)
