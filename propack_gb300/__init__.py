@@ -416,7 +416,8 @@ def svdp(A, k, which='LM', irl_mode=True, kmax=None, compute_u=True, compute_v=T
         cplx = op.dtype == np.complex128
     elif callable(getattr(A, "matvec", None)) and not hasattr(A, "tocsr"):
         op = None
-        cplx = np.dtype(A.dtype).kind == 'c'
+        dt = getattr(A, "dtype", None)
+        cplx = dt is not None and np.dtype(dt).kind == 'c'
     else:
         import scipy.sparse as sp
         op = own_op = CsrOperator(A)
