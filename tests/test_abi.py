@@ -23,7 +23,8 @@ def declared_symbols():
 def test_header_declares_the_reference_entry_points():
     names = declared_symbols()
     for n in ("dlansvd_", "dlansvd_irl_", "clearstat_", "printstat_", "propack_gpu_csr_aprod_",
-              "propack_csr_create", "propack_csr_destroy"):
+              "propack_csr_create", "propack_csr_destroy", "slansvd_", "slansvd_irl_", "zlansvd_",
+              "zlansvd_irl_", "propack_zcsr_create", "propack_gpu_csr_zaprod_"):
         assert n in names
 
 
@@ -62,3 +63,15 @@ def test_svdp_argument_validation_matches_scipy():
         pg.svdp(A, 3, which="XX", rng=np.random.default_rng(0))
     with pytest.raises(ValueError):
         pg.svdp(A, 3, which="SM", irl_mode=False, rng=np.random.default_rng(0))
+
+
+def test_complex_input_is_fp64_only():
+    """Complex input goes to the complex*16 drivers, which have no FP32 or
+    mixed form: refused before any device work."""
+    import numpy as np
+    from scipy.sparse.linalg import LinearOperator
+    import propack_gb300 as pg
+    M = np.ones((6, 5)) + 1j * np.eye(6, 5)
+    lo = LinearOperator(M.shape, matvec=lambda x: M @ x, rmatvec=lambda y: M.conj().T @ y, dtype=np.complex128)
+    with pytest.raises(ValueError):
+        pg.svdp(lo, 2, precision="mixed", rng=np.random.default_rng(0))
