@@ -39,7 +39,10 @@ triplets), run in each form of --forms (the first is the chosen form):
 * cpu_baseline / --impl reference: the oracle (the C restatement of
            PROPACK, FP64, OpenMP) on the host cores, timing one complete IRL
            cycle (maxiter=1) of the same workload and scaling it by matvecs
-           to a full FP64 solve.
+           to a full FP64 solve.  The reference line also carries
+           `scipy_propack`: scipy's _svdp (the reference's Fortran as scipy
+           builds it, CSR products through a Python callback), one cycle
+           timed and scaled the same way.
 
 Inputs (operators of hundreds of MB, Lanczos bases of GBs) are far larger
 than the 129 MB L2, so no L2 flush is needed between steps.
@@ -242,6 +245,41 @@ def cpu_sample(S, L, R, w, wl, cores, matvecs_full=None):
     return dt * scale, dict(cycle_ms=dt, cycle_matvecs=st["nopx"], scale=scale, matvecs_full=full)
 
 
+def scipy_sample(S, L, R, w, wl):
+    """scipy's packaging of PROPACK (scipy.sparse.linalg._svdp: the
+    reference's Fortran dlansvd_irl as scipy builds it, its BLAS on all host
+    cores, scipy's CSR products through a Python callback), one IRL cycle
+    (maxiter=1) of the same workload, scaled by matvecs to a full solve."""
+    import numpy as np
+    from scipy.linalg import LinAlgError
+    from scipy.sparse.linalg import LinearOperator
+    from scipy.sparse.linalg._svdp import _svdp
+    St = S.T.tocsr()
+    Rt = None if R is None else R.T.tocsr()
+    cnt = [0]
+
+    def mv(x):
+        cnt[0] += 1
+        y = S @ x
+        return y if L is None else y + L @ (w * (Rt @ x))
+
+    def rmv(x):
+        cnt[0] += 1
+        y = St @ x
+        return y if L is None else y + R @ (w * (L.T @ x))
+
+    op = LinearOperator(S.shape, matvec=mv, rmatvec=rmv, dtype=np.float64)
+    t0 = time.perf_counter()
+    try:
+        _svdp(op, wl["k"], which="LM", irl_mode=True, kmax=wl["kmax"], tol=wl["tol"], maxiter=1,
+              compute_u=False, compute_v=False, rng=np.random.default_rng(0))
+    except LinAlgError:
+        pass  # one cycle does not converge; its time is the sample
+    dt = (time.perf_counter() - t0) * 1e3
+    scale = wl["matvecs_full"] / max(cnt[0], 1)
+    return dt * scale, dict(cycle_ms=dt, cycle_matvecs=cnt[0], scale=scale)
+
+
 def run_reference(args, wl):
     rank, world, local = dist_env()
     if rank != 0:
@@ -258,6 +296,16 @@ def run_reference(args, wl):
         if it >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
+    # the reference's Fortran as scipy packages it, once (not a step: it is
+    # the second CPU baseline the scope table asks for, beside the port)
+    try:
+        sv, sinfo = scipy_sample(S, L, R, w, wl)
+        scipy_line = {"value": sv, "unit": "ms", "kind": "scipy._svdp (reference Fortran, scipy build)",
+                      "sample": f"one IRL cycle (maxiter=1: {sinfo['cycle_matvecs']} matvecs, "
+                                f"{sinfo['cycle_ms']:.0f} ms) scaled by matvecs to {wl['matvecs_full']}; "
+                                f"BLAS threads of the scipy build, single-threaded CSR products via a callback"}
+    except Exception as e:  # scipy without _svdp: report why
+        scipy_line = {"unavailable": f"{type(e).__name__}: {e}"}
     sample = (f"oracle (C restatement of PROPACK dlansvd_irl, OpenMP) on {cores} host cores: one full IRL cycle "
               f"(maxiter=1: {info['cycle_matvecs']} matvecs, {info['cycle_ms']:.0f} ms) of the same workload, "
               f"scaled by matvecs to a full solve ({wl['matvecs_full']} matvecs)")
@@ -268,6 +316,7 @@ def run_reference(args, wl):
             "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "desc": wl["desc"]},
             "cpu_baseline": {"value": value, "unit": "ms", "cores": cores, "kind": "port", "sample": sample},
+            "scipy_propack": scipy_line,
             "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
