@@ -41,6 +41,18 @@ def illc1850():
         return sp.csr_array(data["A_real"].item())
 
 
+def mhd1280b():
+    """The reference's complex example matrix (Examples/mhd1280b.cua) as
+    shipped with scipy's tests, or None."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+    path = os.path.join(os.path.dirname(sla.__file__), "tests", "propack_test_data.npz")
+    if not os.path.exists(path):
+        return None
+    with np.load(path, allow_pickle=True) as data:
+        return sp.csr_array(data["A_complex"].item())
+
+
 def subspace_err(u1, u2):
     """max | |u1_i . u2_i| - 1 | over matched columns."""
     return float(np.max(np.abs(np.abs(np.sum(u1 * u2, axis=0)) - 1.0)))

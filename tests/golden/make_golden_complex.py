@@ -7,7 +7,9 @@ driver as shipped in scipy returns wrong singular values on these inputs
 (relative errors of 0.4 to 0.8 against the dense SVD, for every kmax
 tried), so the restarted cases are pinned to the dense SVD instead; their
 scipy values are stored only to document that.  Inputs are stored with the
-outputs.  Run from the repository root:
+outputs, except the reference's example matrix mhd1280b, which comes from
+scipy's own test data (propack_test_data.npz) wherever the tests run.
+Run from the repository root:
     python tests/golden/make_golden_complex.py
 """
 import os
@@ -61,6 +63,22 @@ Z2 = complex_matrix(150, 400, 0.04, 2)
 put_csr("z2", Z2)
 run("z2_lansvd", Z2, 6, irl_mode=False, kmax=120, tol=1e-12)
 out["z2_dense_sigma"] = np.linalg.svd(Z2.toarray(), compute_uv=False)[:20]
+
+# 3. the reference's complex example matrix mhd1280b (1280 x 1280, PROPACK's
+# Examples/mhd1280b.cua, shipped in scipy's test data): the non-restarted
+# driver at scipy's test configuration (k=200), and the restarted one at
+# k=50, kmax=120, where it converges without a restart and, like any
+# single-vector Lanczos run, misses copies of the repeated value 2
+import scipy.sparse.linalg as sla  # noqa: E402
+path = os.path.join(os.path.dirname(sla.__file__), "tests", "propack_test_data.npz")
+with np.load(path, allow_pickle=True) as d:
+    MHD = sp.csr_array(d["A_complex"].item())
+u, s, vh, bnd = _svdp(MHD, 200, irl_mode=False, rng=np.random.default_rng(0), full_output=True)[:4]
+out["mhd_lansvd_sigma"] = s
+out["mhd_lansvd_bnd"] = bnd
+out["mhd_irl50_sigma"] = _svdp(MHD, 50, irl_mode=True, kmax=120, tol=1e-10, rng=np.random.default_rng(0))[1]
+out["mhd_dense_sigma"] = np.linalg.svd(MHD.toarray(), compute_uv=False)[:200]
+print("mhd1280b", s[:3], "irl50 misses", np.sum(np.abs(out["mhd_irl50_sigma"] - out["mhd_dense_sigma"][:50]) > 1e-8))
 
 np.savez_compressed(os.path.join(HERE, "golden_complex.npz"), **out)
 print("wrote", os.path.join(HERE, "golden_complex.npz"))

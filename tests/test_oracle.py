@@ -261,3 +261,33 @@ def test_complex_oracle_random_start():
                                           v0=np.zeros(A.shape[0], dtype=np.complex128))
     assert info == 0 and kc == 4
     np.testing.assert_allclose(s, g["z2_dense_sigma"][:4], rtol=1e-12)
+
+
+def test_complex_oracle_on_the_reference_example_mhd1280b():
+    """zlansvd restated on PROPACK's complex example matrix (1280 x 1280),
+    against scipy's packaging of the reference at scipy's own test
+    configuration (k=200; orthogonality and reconstruction of the leading
+    27 triplets as scipy checks them) and, for the restarted driver at
+    k=50, kmax=120 (converged without a restart), against scipy's values,
+    which miss the same copies of the repeated singular value 2."""
+    from conftest import mhd1280b
+    import oracle
+    A = mhd1280b()
+    if A is None:
+        pytest.skip("scipy's PROPACK test data is not installed")
+    g = _zgolden()
+    u, s, vh, bnd, info, kc = oracle.svdp(A, 200, irl_mode=False, rng=np.random.default_rng(0))
+    assert info == 0 and kc == 200
+    np.testing.assert_allclose(s, g["mhd_lansvd_sigma"], rtol=1e-12)
+    np.testing.assert_allclose(s, g["mhd_dense_sigma"], rtol=1e-12)
+    c = 27
+    np.testing.assert_allclose(u[:, :c].conj().T @ u[:, :c], np.eye(c), atol=1e-9)
+    np.testing.assert_allclose(vh[:c] @ vh[:c].conj().T, np.eye(c), atol=1e-9)
+    u3, s3, vh3 = np.linalg.svd(A.toarray())
+    recon = (u[:, :c] * s[:c]) @ vh[:c] - (u3[:, :c] * s3[:c]) @ vh3[:c]
+    assert np.linalg.norm(recon) < 1e-9
+    oracle.clearstat()
+    u, s, vh, bnd, info, kc = oracle.svdp(A, 50, irl_mode=True, kmax=120, tol=1e-10, rng=np.random.default_rng(0))
+    assert info == 0 and kc == 50 and oracle.getstat()["nrestart"] == 0
+    np.testing.assert_allclose(s, g["mhd_irl50_sigma"], rtol=1e-12)
+    assert np.sum(np.abs(s - g["mhd_dense_sigma"][:50]) > 1e-8) > 0
