@@ -4,6 +4,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 from conftest import ROOT
@@ -75,3 +76,46 @@ def test_complex_input_is_fp64_only():
     lo = LinearOperator(M.shape, matvec=lambda x: M @ x, rmatvec=lambda y: M.conj().T @ y, dtype=np.complex128)
     with pytest.raises(ValueError):
         pg.svdp(lo, 2, precision="mixed", rng=np.random.default_rng(0))
+
+
+def _outcome(f):
+    import propack_gb300 as pg
+    try:
+        f()
+        return "ran"
+    except ValueError:
+        return "ValueError"
+    except pg.PropackError:
+        return "ran"  # validated, then no usable CUDA device on this host
+
+
+@pytest.mark.parametrize("shifts", (None, -10, 0, 1, 10, 70))
+def test_shifts_validation_matches_scipy(shifts):
+    """The cases of scipy's test_propack.py::test_shifts: svdp refuses
+    exactly the shifts scipy's _svdp refuses, before any device work."""
+    import numpy as np
+    from scipy.sparse.linalg import aslinearoperator
+    from scipy.sparse.linalg._svdp import _svdp
+    import propack_gb300 as pg
+    n, k = 70, 10
+    A = np.random.default_rng(0).random((n, n))
+    ref = _outcome(lambda: _svdp(A, k, shifts=shifts, kmax=5 * k, irl_mode=True, rng=np.random.default_rng(0)))
+    ours = _outcome(lambda: pg.svdp(aslinearoperator(A), k, shifts=shifts, kmax=5 * k, irl_mode=True,
+                                    rng=np.random.default_rng(0)))
+    assert ours == ref
+
+
+@pytest.mark.parametrize("kw", [dict(k=0), dict(k=9), dict(k=3, kmax=2), dict(k=3, v0=np.ones(5)),
+                                dict(k=3, which="SM", irl_mode=False), dict(k=3, which="XX")])
+def test_argument_errors_match_scipy(kw):
+    """k out of range, kmax < k, a start vector of the wrong length, 'SM'
+    without restarts, an unknown `which`: the same ValueError as scipy."""
+    from scipy.sparse.linalg import aslinearoperator
+    from scipy.sparse.linalg._svdp import _svdp
+    import propack_gb300 as pg
+    A = np.random.default_rng(1).random((8, 6))
+    kw = dict(kw)
+    k = kw.pop("k")
+    ref = _outcome(lambda: _svdp(A, k, rng=np.random.default_rng(0), **kw))
+    ours = _outcome(lambda: pg.svdp(aslinearoperator(A), k, rng=np.random.default_rng(0), **kw))
+    assert ref == "ValueError" and ours == ref
