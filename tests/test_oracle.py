@@ -291,3 +291,35 @@ def test_complex_oracle_on_the_reference_example_mhd1280b():
     assert info == 0 and kc == 50 and oracle.getstat()["nrestart"] == 0
     np.testing.assert_allclose(s, g["mhd_irl50_sigma"], rtol=1e-12)
     assert np.sum(np.abs(s - g["mhd_dense_sigma"][:50]) > 1e-8) > 0
+
+
+@pytest.mark.timeout(60)
+@pytest.mark.parametrize("mode", ["nan_after_5", "inf", "nan_always"])
+@pytest.mark.parametrize("irl", [True, False])
+def test_nonfinite_aprod_terminates(mode, irl):
+    """Failure injection on the host: an APROD that returns NaN or Inf ends
+    the restated drivers (the control flow the device drivers share: every
+    data-dependent loop is bounded) with no converged triplet claimed."""
+    from scipy.sparse.linalg import LinearOperator
+    import oracle
+    A = np.random.default_rng(0).random((60, 40))
+    cnt = [0]
+
+    def poison(y, i):
+        if mode == "inf":
+            y[i] = np.inf
+        elif mode == "nan_always" or cnt[0] > 5:
+            y[i] = np.nan
+        return y
+
+    def mv(x):
+        cnt[0] += 1
+        return poison(A @ x, 0)
+
+    def rmv(x):
+        cnt[0] += 1
+        return poison(A.T @ x, 1)
+
+    lo = LinearOperator(A.shape, matvec=mv, rmatvec=rmv, dtype=np.float64)
+    u, s, vt, bnd, info, kc = oracle.svdp(lo, 5, irl_mode=irl, kmax=20, maxiter=50, rng=np.random.default_rng(0))
+    assert kc < 5 and cnt[0] < 200
