@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 import scipy.sparse as sp
 
-from . import CsrOperator, PropackError, last_error, load, svdp
+from . import PropackError, last_error, load, svdp
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
