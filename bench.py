@@ -16,6 +16,10 @@ Workloads (seeded synthetic data, numpy default_rng):
   kernel; --scale sets the fraction of the 4096 problems (default 1).
 * learned: the learned start vector on a matrix family (200000 x 50000,
   rank-32 rotating factors + sparse noise), k = 32, kmax 64, tol 1e-8.
+* complex_zipf (opt-in): the complex*16 drivers (zlansvd_irl_) on a
+  2,000,000-row complex analogue of zipf, the device operator in its 2x2
+  block form; same keys, with the rooflines of the block-form SpMV pair
+  and the complex Gram-Schmidt pair.
 
 A step is one complete DLANSVD_IRL solve (start vector -> k converged Ritz
 triplets), run in each form of --forms (the first is the chosen form):
@@ -75,6 +79,15 @@ WORKLOADS = {
              "N(0,1)*(1+i mod 1000)^-0.7 values (FP32-representable), DLANSVD_IRL k=50 dim=150 p=100 tol=1e-8",
         k=50, kmax=150, tol=1e-8,
         matvecs_full=301,
+    ),
+    "complex_zipf": dict(
+        desc="2000000x2000000 complex CSR, nnz/row Zipf(2) clipped to [4,2000], uniform columns, "
+             "(N(0,1)+iN(0,1))*(1+i mod 1000)^-0.7 values, ZLANSVD_IRL k=50 dim=150 p=100 tol=1e-8 "
+             "(the complex*16 drivers; no reference configuration is complex)",
+        k=50, kmax=150, tol=1e-8,
+        # not yet measured on a GB300: the reference arm needs the matvec
+        # count of a full solve to scale its one-cycle sample
+        matvecs_full=None,
     ),
     "batched": dict(
         desc="independent CSR problems, m~U[500,20000], n~U[200,8000], density 1%, N(0,1) FP32 values; "
@@ -151,6 +164,8 @@ def make_workload(name, scale=1.0):
         return workloads.lowrank_irl(seed=1, m=int(2_000_000 * scale), n=int(500_000 * scale))
     if name == "zipf_mixed":
         return workloads.zipf_mixed(seed=2, m=int(4_000_000 * scale)), None, None, None
+    if name == "complex_zipf":
+        return workloads.zipf_complex(seed=5, m=int(2_000_000 * scale)), None, None, None
     raise ValueError(name)
 
 
@@ -232,7 +247,10 @@ def cpu_sample(S, L, R, w, wl, cores, matvecs_full=None):
     import oracle
     oracle.build()
     oracle.lib().oracle_set_threads(cores)
-    op = oracle.Operator(S, L, R, w) if L is not None else oracle.Operator(S)
+    if np.iscomplexobj(S.data):
+        op = oracle.ZOperator(S)
+    else:
+        op = oracle.Operator(S, L, R, w) if L is not None else oracle.Operator(S)
     oracle.clearstat()
     t0 = time.perf_counter()
     u, s, vt, bnd, info, kc = oracle.svdp(None, wl["k"], irl_mode=True, kmax=wl["kmax"], tol=wl["tol"],
@@ -254,7 +272,7 @@ def scipy_sample(S, L, R, w, wl):
     from scipy.linalg import LinAlgError
     from scipy.sparse.linalg import LinearOperator
     from scipy.sparse.linalg._svdp import _svdp
-    St = S.T.tocsr()
+    St = S.conj().T.tocsr()  # rmatvec is the adjoint (A^H for complex input)
     Rt = None if R is None else R.T.tocsr()
     cnt = [0]
 
@@ -268,7 +286,7 @@ def scipy_sample(S, L, R, w, wl):
         y = St @ x
         return y if L is None else y + R @ (w * (L.T @ x))
 
-    op = LinearOperator(S.shape, matvec=mv, rmatvec=rmv, dtype=np.float64)
+    op = LinearOperator(S.shape, matvec=mv, rmatvec=rmv, dtype=S.dtype)
     t0 = time.perf_counter()
     try:
         _svdp(op, wl["k"], which="LM", irl_mode=True, kmax=wl["kmax"], tol=wl["tol"], maxiter=1,
@@ -285,12 +303,12 @@ def run_reference(args, wl):
     if rank != 0:
         return 0
     cores = os.cpu_count() or 1
-    S, L, R, w = make_workload(args.workload)
-    vals = []
     if wl["matvecs_full"] is None:
         print(json.dumps({"impl": "reference", "unavailable": "matvec count of a full solve of this workload "
                           "not yet measured"}))
         return 0
+    S, L, R, w = make_workload(args.workload)
+    vals = []
     for it in range(args.warmup + args.steps):
         v, info = cpu_sample(S, L, R, w, wl, cores)
         if it >= args.warmup:
@@ -720,9 +738,126 @@ def run_learned(args, wl):
     return 0
 
 
+def run_complex(args, wl):
+    """The complex*16 drivers on the device operator: value = device ms of
+    one zlansvd_irl_ solve (start vector in HBM -> k Ritz triplets); e2e =
+    the same through propack_zcsr_create + zlansvd_irl_ from pinned host
+    arrays (expansion to the 2x2-block form, upload, device transposition,
+    solve, U and V back)."""
+    import ctypes as C
+    import numpy as np
+    import propack_gb300 as pg
+    pg.load()
+    S, _, _, _ = make_workload(args.workload, args.scale)
+    m, n = S.shape
+    k, kmax, tol = wl["k"], wl["kmax"], wl["tol"]
+    maxiter = 1000 if args.scale == 1.0 else 20
+    dop0 = [np.sqrt(np.finfo(float).eps), np.finfo(float).eps ** 0.75, 0.0, 0.002]
+    rng = np.random.default_rng(0)
+    u0 = rng.uniform(size=m) + 1j * rng.uniform(size=m)  # scipy's complex start vector
+
+    def solve(aprod, iparm, u, v):
+        u[:, 0] = u0
+        sig, bnd = np.zeros(k), np.zeros(k)
+        kc, info = pg.zlansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, aprod, u, sig, bnd, v, tol,
+                                  np.array(dop0), np.array([0, 1], dtype=np.int32), iparm=iparm)
+        if args.scale == 1.0:
+            assert info == 0 and kc == k, (info, kc)
+        return sig
+
+    u = np.zeros((m, kmax + 1), order="F", dtype=np.complex128)
+    v = np.zeros((n, kmax), order="F", dtype=np.complex128)
+    op = pg.CsrOperator(S)
+    sampler = ClockSampler(0)
+    sampler.start()
+    for _ in range(args.warmup):
+        solve(op.aprod, op.iparm, u, v)
+    dev, mvs, launches = [], [], 0
+    for _ in range(args.steps):
+        sig = solve(op.aprod, op.iparm, u, v)
+        st = pg.get_stats()
+        dev.append(st["solve_ms"])
+        mvs.append(st["nopx"])
+        launches += st["kernel_launches"]
+    clocks = sampler.stop()
+    res = max(max(np.linalg.norm(op.matvec(v[:, i]) - sig[i] * u[:, i]),
+                  np.linalg.norm(op.rmatvec(u[:, i]) - sig[i] * v[:, i])) for i in range(k)) / sig[0]
+    pg.set_profiling(True)
+    solve(op.aprod, op.iparm, u, v)
+    prof = pg.get_profile()
+    st_prof = pg.get_stats()
+    pg.set_profiling(False)
+    op.close()
+    value = statistics.mean(dev)
+
+    # e2e through the public C ABI from pinned host arrays
+    import torch
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    hp, hi, hv = pin(S.indptr.astype(np.int64)), pin(S.indices.astype(np.int32)), pin(S.data.astype(np.complex128))
+    u_pin = torch.zeros((kmax + 1, m), dtype=torch.complex128).pin_memory().numpy().T
+    v_pin = torch.zeros((kmax, n), dtype=torch.complex128).pin_memory().numpy().T
+    lib = pg.load()
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 2))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        h = C.c_int64(0)
+        rc = lib.propack_zcsr_create(m, n, pg._i64p(hp), pg._ip(hi), C.c_void_p(hv.ctypes.data), C.byref(h))
+        assert rc == 0, pg.last_error()
+        iparm = np.array([h.value & 0xFFFFFFFF, (h.value >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
+        solve(C.cast(lib.propack_gpu_csr_zaprod_, pg.ZAPROD), iparm, u_pin, v_pin)
+        lib.propack_csr_destroy(h.value)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    h2d = hp.nbytes + hi.nbytes + hv.nbytes + m * 16
+    d2h = 2 * k * 8 + k * (m + n) * 16
+
+    # rooflines: the SpMV pair on the 2x2-block form (4 real entries per
+    # complex entry, 2m and 2n real rows) and the complex Gram-Schmidt pair
+    # (16-byte elements)
+    fwd_b, adj_b = spmv_bytes(2 * m, 2 * n, 0, 4 * S.nnz, 0, 0, 8)
+    n_adj, t_adj = prof["spmv_adj"]
+    n_fwd, t_fwd = prof["spmv_fwd"]
+    peak, peak_kind = peaks()
+    a_spmv = (fwd_b * n_fwd + adj_b * n_adj) / max((t_fwd + t_adj) * 1e-3, 1e-12) / 1e9
+    roof = {"bound": "hbm", "kernel": "fused SpMV pair on the 2x2-block form", "achieved": a_spmv, "peak": peak,
+            "peak_source": peak_kind, "unit": "GB/s", "frac": a_spmv / peak, "traffic": None,
+            "algorithmic_bytes_per_launch": {"fwd": fwd_b, "adj": adj_b}, "ms": t_fwd + t_adj}
+    cgs_ms = prof["cgs_dots"][1] + prof["cgs_upd"][1]
+    roof_cgs = None
+    if cgs_ms > 0:
+        cgs_bytes = 2.0 * 16 * (st_prof["cgs_cols_u"] * m + st_prof["cgs_cols_v"] * n)
+        a_cgs = cgs_bytes / (cgs_ms * 1e-3) / 1e9
+        roof_cgs = {"bound": "hbm", "kernel": "complex Gram-Schmidt projection + update pair", "achieved": a_cgs,
+                    "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": a_cgs / peak, "traffic": None,
+                    "algorithmic_bytes": cgs_bytes, "ms": cgs_ms}
+    dominant = roof_cgs if roof_cgs and roof_cgs["ms"] > roof["ms"] else roof
+    cpu = None
+    if not args.no_cpu:
+        cores = os.cpu_count() or 1
+        cv, info = cpu_sample(S, None, None, None, wl, cores, statistics.mean(mvs))
+        cpu = {"value": cv, "unit": "ms", "cores": cores, "kind": "port",
+               "sample": f"complex oracle (zlansvd_irl restated, OpenMP) one IRL cycle ({info['cycle_matvecs']} "
+                         f"matvecs, {info['cycle_ms']:.0f} ms) scaled by matvecs to the device solve's "
+                         f"{info['matvecs_full']:.0f}"}
+    line = {"metric": "ms & matvecs to k=50 complex triplets (zlansvd_irl_), 1 GB300", "value": value, "unit": "ms",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64 pairs)", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "desc": wl["desc"], "scale": args.scale,
+                       "l2": "operator and bases are GBs, larger than L2; no flush"},
+            "matvecs": statistics.mean(mvs), "max_rel_residual": res,
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches), "roofline": dominant, "rooflines": {"spmv_pair": roof,
+                                                                               "gram_schmidt": roof_cgs},
+            "cpu_baseline": cpu, "clocks": clocks,
+            "kernel_breakdown": {kk: {"launches": c, "ms": t} for kk, (c, t) in prof.items() if c}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     wl = WORKLOADS[args.workload]
+    if args.workload == "complex_zipf" and args.impl != "reference":
+        return run_complex(args, wl)
     if args.workload == "batched":
         return run_batched(args, wl)
     if args.workload == "learned":

@@ -19,6 +19,10 @@ distributions of the five solver configurations.
                      entry would.
 * ``zipf_mixed``     m x m CSR, nnz per row Zipf(2) clipped to [4, 2000],
                      uniform columns, N(0,1) * (1 + i mod 1000)^-0.7 values.
+* ``zipf_complex``   the same pattern with complex values, real and
+                     imaginary parts N(0,1) * (1 + i mod 1000)^-0.7 (the
+                     complex*16 drivers' workload; no configuration of the
+                     reference names a complex one).
 """
 import numpy as np
 import scipy.sparse as sp
@@ -123,3 +127,15 @@ def dense_of(S, L=None, R=None, w=None):
     if L is not None:
         A = A + (L.toarray() * w) @ R.toarray().T
     return A
+
+
+def zipf_complex(seed=5, m=2_000_000, alpha=2.0, lo=4, hi=2000):
+    rng = np.random.default_rng(seed)
+    counts = np.clip(rng.zipf(alpha, size=m), lo, hi).astype(np.int64)
+    indptr = np.zeros(m + 1, dtype=np.int64)
+    np.cumsum(counts, out=indptr[1:])
+    nnz = int(indptr[-1])
+    indices = rng.integers(0, m, size=nnz, dtype=np.int32)
+    rw = np.repeat((1.0 + (np.arange(m) % 1000)) ** -0.7, counts)
+    data = (rng.standard_normal(nnz) + 1j * rng.standard_normal(nnz)) * rw
+    return sp.csr_array((data, indices, indptr), shape=(m, m))
