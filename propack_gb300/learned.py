@@ -5,7 +5,7 @@ Lanczos bidiagonalisation in place of dgetu0's random start
 The network, its features and its loss are described in
 include/propack_gb300.h (propack_mlp_*); forward and backward passes and the
 Adam update run on the GPU in the library's own kernels.  The random start
-stays both the fallback and the judge: a solve from the learned start whose
+stays both the fallback and the arbiter: a solve from the learned start whose
 own Ritz error bounds (``bnd <= tol * sigma``, the convergence test of
 dlansvd_irl.F:281) do not certify all k triplets is repeated from the random
 start.
