@@ -650,9 +650,9 @@ def run_batched(args, wl):
     return 0
 
 
-def batched_cpu_sample(mats, u0, wl, budget_s=20.0):
+def batched_cpu_sample(mats, u0, wl, limit_s=20.0):
     """The oracle on the host cores over a prefix of the problems (about
-    budget_s seconds of work; OpenMP inside each solve), scaled to all."""
+    limit_s seconds of work; OpenMP inside each solve), scaled to all."""
     import numpy as np
     import oracle
     oracle.build()
@@ -664,7 +664,7 @@ def batched_cpu_sample(mats, u0, wl, budget_s=20.0):
         oracle.svdp(A, wl["k"], kmax=wl["kmax"], tol=wl["tol"], v0=u, cgs=True, delta=0.0, eta=0.0,
                     rng=np.random.default_rng(0), compute_u=False, compute_v=False)
         done += 1
-        if time.perf_counter() - t0 > budget_s:
+        if time.perf_counter() - t0 > limit_s:
             break
     dt = (time.perf_counter() - t0) * 1e3
     return {"value": dt * len(mats) / done, "unit": "ms", "cores": cores, "kind": "port",
@@ -675,7 +675,7 @@ def batched_cpu_sample(mats, u0, wl, budget_s=20.0):
 def run_batched_reference(args, wl, mats, u0, nprob):
     vals, info = [], None
     for it in range(args.warmup + args.steps):
-        c = batched_cpu_sample(mats, u0, wl, budget_s=10.0)
+        c = batched_cpu_sample(mats, u0, wl, limit_s=10.0)
         if it >= args.warmup:
             vals.append(c["value"])
             info = c

@@ -1,6 +1,6 @@
 """Oracle harness: ctypes access to propack_oracle.c.
 
-TEST INFRASTRUCTURE ONLY -- the checker for the GPU library and the timed
+TEST INFRASTRUCTURE ONLY -- the oracle of the GPU library's tests and the timed
 CPU baseline of bench.py.  The product (propack_gb300/) never imports this.
 
 The entry points take the reference's Fortran argument lists

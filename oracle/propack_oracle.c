@@ -2,7 +2,7 @@
  * propack_oracle.c -- CPU restatement of PROPACK 2.1's double-precision
  * Lanczos bidiagonalisation with partial reorthogonalisation.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the oracle (the checker) for the
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle of the tests of the
  * GPU library in propack_gb300/, and the timed multi-core CPU baseline in
  * bench.py.  Nothing in the product links, loads or calls it.
  *

@@ -5,7 +5,7 @@
 // routine that allocates) while they run.  Typical cases are code on a
 // latency-critical path where an allocation's implicit device
 // synchronisation or allocator lock is unacceptable, code that runs while
-// another component owns all free device memory under a fixed budget, and
+// another component owns all free device memory under a fixed cap, and
 // code that has to stay replayable with the same addresses every time.
 // The regular entry point propack_gpu_csr_aprod_ allocates its device
 // vectors per call; this one takes device pointers from the caller and
