@@ -323,3 +323,19 @@ def test_nonfinite_aprod_terminates(mode, irl):
     lo = LinearOperator(A.shape, matvec=mv, rmatvec=rmv, dtype=np.float64)
     u, s, vt, bnd, info, kc = oracle.svdp(lo, 5, irl_mode=irl, kmax=20, maxiter=50, rng=np.random.default_rng(0))
     assert kc < 5 and cnt[0] < 200
+
+
+@pytest.mark.parametrize("irl", [True, False])
+def test_zero_matrix_matches_scipy(irl):
+    """An operator with no nonzeros: every start vector is annihilated, the
+    bidiagonal is zero, and both drivers report k zero singular values with
+    INFO = 0, as scipy's packaging of the reference does."""
+    import scipy.sparse as sp
+    from scipy.sparse.linalg._svdp import _svdp
+    import oracle
+    Z = sp.csr_array((50, 30))
+    u, s, vt, bnd, info, kc = oracle.svdp(Z, 3, irl_mode=irl, kmax=10, rng=np.random.default_rng(0))
+    ref = _svdp(Z, 3, irl_mode=irl, kmax=10, rng=np.random.default_rng(0))[1]
+    assert info == 0 and kc == 3
+    np.testing.assert_array_equal(s, ref)
+    np.testing.assert_array_equal(s, np.zeros(3))
