@@ -171,19 +171,30 @@ static void cgs(int n, int k, const double *V, int ldv, double *vnew, const int 
     }
 }
 
-/* dmgs (dmgs.risc.F:11-84): modified Gram-Schmidt over the same ranges.
- * Unlike dcgs, an empty range (p > q) ends the sweep. */
+/* dmgs / pdmgs (dmgs.risc.F:11-84, :87-): modified Gram-Schmidt over the
+ * same ranges.  As in the reference, the update with column i-1 and the
+ * projection onto column i share one pass over vnew (vn0 = vnew - coef V_i-1;
+ * newcoef += vn0 V_i), which is the separate dot + axpy of MGS in the same
+ * order of operations.  Unlike dcgs, an empty range (p > q) ends the sweep. */
 static void mgs(int n, int k, const double *V, int ldv, double *vnew, const int *index)
 {
     if (k <= 0 || n <= 0) return;
     int ib = 0, p = index[0], q = index[1];
     while (p <= k && p > 0 && p <= q) {
         st.ndot += q - p + 1;
-        for (int c = p; c <= q; c++) {
-            const double *vc = V + (size_t)(c - 1) * ldv;
-            double coef = v_dot(n, vc, vnew);
-            v_axpy(n, -coef, vc, vnew);
+        double coef = v_dot(n, V + (size_t)(p - 1) * ldv, vnew);
+        for (int i = p + 1; i <= q; i++) {
+            const double *vprev = V + (size_t)(i - 2) * ldv, *vi = V + (size_t)(i - 1) * ldv;
+            double newcoef = 0.0;
+#pragma omp parallel for reduction(+ : newcoef) schedule(static) if (n >= PAR_MIN) num_threads(nthr())
+            for (int j = 0; j < n; j++) {
+                const double vn0 = vnew[j] + (-coef) * vprev[j];
+                newcoef += vi[j] * vn0;
+                vnew[j] = vn0;
+            }
+            coef = newcoef;
         }
+        v_axpy(n, -coef, V + (size_t)(q - 1) * ldv, vnew);
         ib += 2;
         p = index[ib];
         q = index[ib + 1];
