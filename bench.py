@@ -121,6 +121,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink m and n by this factor (profiling captures only; not a bench line)")
+    ap.add_argument("--cgs-arith", default="planes", choices=["planes", "fp64", "f3"],
+                    help="Gram-Schmidt arithmetic of the FP64 form (propack_set_cgs_arith)")
     return ap.parse_args()
 
 
@@ -347,6 +349,7 @@ def run_ours(args, wl):
     import numpy as np
     import propack_gb300 as pg
     pg.load()
+    pg.set_cgs_arith(args.cgs_arith)
     barrier = lambda: None
     dist = None
     if world > 1:
@@ -551,7 +554,7 @@ def run_ours(args, wl):
             "data": "synthetic (seeded numpy default_rng)",
             "config": {"workload": args.workload, "desc": wl["desc"], "chosen_form": chosen, "scale": args.scale,
                        "l2": "inputs larger than L2 (operator and Lanczos basis are GBs); no flush"},
-            "matvecs": results[chosen]["matvecs"], "forms": forms_out,
+            "matvecs": results[chosen]["matvecs"], "cgs_arith": args.cgs_arith, "forms": forms_out,
             "speedup_vs_plain_fp64": {f: per["fp64"] / per[f] for f in forms} if "fp64" in per else None,
             "max_rel_sigma_diff_vs_fp64": sig_err,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),

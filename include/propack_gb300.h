@@ -192,7 +192,12 @@ int propack_get_profile(double *total_ms, int64_t *launches, int n);
  * thread: 0 FP64 FMAs (dgemv as in dreorth.F:85-95, :174); 1 each FP64
  * value split exactly into three FP32 pieces and the products summed at
  * three levels on the FP32 pipe (error ~2^-53 of sum |w x|, like an FP64
- * dot product's own rounding), then one FP64 FMA per row.  Returns 0 or
+ * dot product's own rounding), then one FP64 FMA per row; 2 (the default)
+ * each basis column split once into FP32 (hi, lo) planes kept beside the
+ * FP64 basis (one more basis-sized array of device memory), the products
+ * summed on the FP32 pipe as compensated FP32 pairs (error a few 2^-48 of
+ * sum |w x|), then one FP64 FMA per row.  Mode 2 applies to solves whose
+ * kmax is at most ~2800 and falls back to mode 0 above that.  Returns 0 or
  * PROPACK_ERR_ARG. */
 int propack_set_cgs_arith(int mode);
 

@@ -373,9 +373,10 @@ def release_memory():
 
 def set_cgs_arith(arith):
     """Gram-Schmidt arithmetic of the FP64 form for this host thread:
-    "fp64" (FP64 FMAs) or "f3" (exact three-way FP32 splits summed on the
-    FP32 pipe; propack_set_cgs_arith)."""
-    rc = load().propack_set_cgs_arith({"fp64": 0, "f3": 1}[arith])
+    "planes" (the default: each basis column split once into FP32 (hi, lo)
+    planes, products summed on the FP32 pipe), "fp64" (FP64 FMAs) or "f3"
+    (exact three-way FP32 splits of every element read; propack_set_cgs_arith)."""
+    rc = load().propack_set_cgs_arith({"fp64": 0, "f3": 1, "planes": 2}[arith])
     if rc != 0:
         raise PropackError(f"propack_set_cgs_arith failed ({rc})")
 

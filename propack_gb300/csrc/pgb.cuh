@@ -160,6 +160,13 @@ struct LbArgs {
     int kmax;               // capacity of the column arrays
     Csr fwd, adj;           // device operator (fwd = [S|L], adj = [S'|R])
     const double *z;        // low-rank coefficients of the current product
+    // FP64 form, Gram-Schmidt on the FP32 pipe (null when off): the
+    // basis columns as FP32 (hi, lo) planes with the leading dimensions of
+    // U and V, a flag per column (1: its planes hold the column's current
+    // value), and the planes of the vector being reorthogonalised
+    float2 *Up, *Vp;
+    int *okU, *okV;
+    float2 *xpl;
 };
 // real scalars per element of a Lanczos vector: 1 for double and float, 2
 // for complex*16, held as double2 = (re, im).  LbArgs' ldu, ldv and the
@@ -365,7 +372,11 @@ void copy_cols(const T *src, int lds, T *dst, int ldd, int rows, int cols, cudaS
 
 // ------------------------------------------------ Lanczos step enqueue
 void lb_set_smem_limits(int kmax);
-extern thread_local int g_cgs_f3;  // Gram-Schmidt of the FP64 form on the FP32 pipe (pgb_f3.cuh)
+bool lb_planes_fit(int kmax);
+// Gram-Schmidt arithmetic of the FP64 form: 0 FP64 FMAs, 1 three-way
+// splits on the FP32 pipe (pgb_f3.cuh), 2 split-once planes (the default)
+enum CgsArith { CGS_FP64 = 0, CGS_F3 = 1, CGS_PLANES = 2 };
+extern thread_local int g_cgs_arith;
 template <typename T>
 void lb_enqueue_half(const LbArgs &a, const Operator *op, int side, int j, int ielr, int ntry_spec,
                      bool host_product, cudaStream_t s);

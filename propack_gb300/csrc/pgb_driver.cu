@@ -187,11 +187,12 @@ __global__ void k_scale(T *x, int n, int mode, double val)
 }
 // apply the deferred scale of u (which=0) or v (which=1) to its column now
 template <typename T>
-__global__ void k_apply_pend_col(LbCtl *ctl, T *U, int ldu, T *V, int ldv, int m, int n, int which)
+__global__ void k_apply_pend_col(LbCtl *ctl, T *U, int ldu, T *V, int ldv, int m, int n, int which, int *ok)
 {
     const Pend p = which == 0 ? ctl->pend_u : ctl->pend_v;
     const int col = which == 0 ? ctl->pend_u_col : ctl->pend_v_col;
     if (p.mode != 0 && col >= 0) {
+        if (ok && blockIdx.x == 0 && threadIdx.x == 0) ok[col] = 0;  // its FP32 planes are stale
         T *x = which == 0 ? U + (size_t)col * ldu : V + (size_t)col * ldv;
         const int len = which == 0 ? m : n;
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x)
@@ -243,6 +244,11 @@ struct Ctx {
     double *wz = nullptr;                   // scratch of the lane-parallel bidiagonal kernels
     int *dflag = nullptr;
     void *gout = nullptr;                   // GEMM output scratch (vector type)
+    // FP32 (hi, lo) planes of the FP64 bases for the Gram-Schmidt passes,
+    // their per-column flags and the planes of the vector being
+    // reorthogonalised (null: the FP64 or three-way-split kernels)
+    float2 *Up = nullptr, *Vp = nullptr, *xpl = nullptr;
+    int *okU = nullptr, *okV = nullptr;
     // operator
     const Operator *op = nullptr;
     propack_aprod_t aprod = nullptr;
@@ -299,6 +305,7 @@ struct Ctx {
         else {
             a.fwd.rows = m * vw; a.adj.rows = n * vw; a.z = nullptr;
         }
+        a.Up = Up; a.Vp = Vp; a.okU = okU; a.okV = okV; a.xpl = xpl;
         return a;
     }
     template <typename T>
@@ -367,6 +374,13 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
     c.Mt = c.dalloc<double>(d1 * d1); c.Pr = c.dalloc<double>(d1 * d1); c.Qt = c.dalloc<double>(d1 * d1);
     c.X = c.dalloc<double>(d1 * d1);
     c.gout = c.dalloc<T>((size_t)std::max(c.ldu, c.ldv) * (kmax + 1));
+    if (std::is_same<T, double>::value && g_cgs_arith == CGS_PLANES && lb_planes_fit(kmax)) {
+        c.Up = (float2 *)c.dbytes(sizeof(float2) * (size_t)c.ldu * (kmax + 1));
+        c.Vp = (float2 *)c.dbytes(sizeof(float2) * (size_t)c.ldv * (kmax + 1));
+        c.xpl = c.dalloc<float2>(mn);
+        c.okU = c.dalloc<int>(kmax + 2);
+        c.okV = c.dalloc<int>(kmax + 2);
+    }
     lb_set_smem_limits(kmax);
 }
 
@@ -521,7 +535,7 @@ static void apply_pend_col(Ctx &c, int which)
     using E = typename std::conditional<VecW<T>::w == 2, double, T>::type;
     const int w = VecW<T>::w;
     k_apply_pend_col<E><<<c.nb, 256, 0, c.s>>>(c.ctl, (E *)c.U, c.ldu * w, (E *)c.V, c.ldv * w, c.m * w, c.n * w,
-                                               which);
+                                               which, which == 0 ? c.okU : c.okV);
     PGB_LAUNCHED();
 }
 
@@ -668,6 +682,12 @@ static void dev_lanbpro(Ctx &c, int k0, int *kp, double *rnorm, double *doption,
             throw WaitFailure();
         }
         LbArgs a = c.args();
+        // the host may have written columns since the last round (start
+        // vector, prologue, a suspension's fresh vector): no plane is trusted
+        if (c.okU) {
+            PGB_CUDA(cudaMemsetAsync(c.okU, 0, sizeof(int) * (c.kmax + 2), c.s));
+            PGB_CUDA(cudaMemsetAsync(c.okV, 0, sizeof(int) * (c.kmax + 2), c.s));
+        }
         if (!host_ap) {
             // enqueue in windows of LB_WINDOW steps; before a window goes in,
             // the status word of the window two back is read (its copy was
@@ -1684,8 +1704,8 @@ extern "C" int propack_get_precision(void) { return g_precision; }
 
 extern "C" int propack_set_cgs_arith(int mode)
 {
-    if (mode != 0 && mode != 1) return PROPACK_ERR_ARG;
-    g_cgs_f3 = mode;
+    if (mode != CGS_FP64 && mode != CGS_F3 && mode != CGS_PLANES) return PROPACK_ERR_ARG;
+    g_cgs_arith = mode;
     return 0;
 }
 

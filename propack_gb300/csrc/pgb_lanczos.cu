@@ -442,13 +442,15 @@ __device__ void after_elr(Tail &t, const LbArgs &a, int j, double snrm, double d
 }
 
 // h[c] = sum over CTAs of part_cols[c*nb + b] (one warp per column)
-__device__ void reduce_cols(const LbArgs &a, int L)
+// (nparts partials per column, stored with stride nb; nparts <= nb)
+__device__ void reduce_cols(const LbArgs &a, int L, int nparts = -1)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (nparts < 0) nparts = a.nb;
     for (int c = w; c < L; c += BS / 32) {
         const double *p = a.part_cols + (size_t)c * a.nb;
         double s = 0.0;
-        for (int b = lane; b < a.nb; b += 32) s += p[b];
+        for (int b = lane; b < nparts; b += 32) s += p[b];
         s = warp_sum(s);
         if (lane == 0) a.h[c] = s;
     }
@@ -533,6 +535,13 @@ __global__ void __launch_bounds__(BS, SHORT ? SPMV_SHORT_MINB : 3) k_lb_spmv(LbA
     const Csr &A = SIDE == 0 ? a.adj : a.fwd;
     const double *z = a.z;
     const int n0 = A.ncol0;
+    // this launch rewrites the output column and (deferred scale) the
+    // previous one: their FP32 planes no longer hold them
+    if (a.okU && blockIdx.x == 0 && threadIdx.x == 0) {
+        int *ok = SIDE == 0 ? a.okV : a.okU;
+        ok[SIDE == 0 ? j - 1 : j] = 0;
+        if (has_prev) ok[SIDE == 0 ? j - 2 : j - 1] = 0;
+    }
     Acc<T> sq, dt;
     auto epi = [&](int r, double acc, double pvd) {
         T y = apply_pend((T)acc, pin);
@@ -920,6 +929,291 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd_f3(LbArgs a, int j, int last)
     }
 }
 
+// ------------------------------------------------ split-once planes
+// The FP64 form's Gram-Schmidt on the FP32 pipe, reading each basis element
+// as 8 bytes of FP32 planes: hi = fl32(w), lo = fl32(w - hi), so that
+// hi + lo holds w to 2^-48 relative (a Lanczos column has |w| <= 1; bits
+// below 2^-149 are lost, far below the column's unit norm).  A column is
+// split by the first projection that selects it while its flag is clear;
+// the update of the same pass and every later pass read its planes until
+// the column is rewritten (the SpMV that writes a column, the flush and the
+// deferred-scale kernel clear its flag; the host clears all flags whenever
+// it writes columns itself).  One product w x costs 12 FP32 operations --
+// hi*hi as an exact two-product folded into a two-sum, the cross terms
+// hi*lo and lo*hi into the compensation -- for an error of a few 2^-48 of
+// sum |w_i x_i|, the size of an FP64 dot product's own rounding over a
+// few thousand terms.  A pass streams 8 bytes per element either way; on
+// GB300 the FP64 pipe (2 lanes per clock per SM) holds one FMA per element
+// below the HBM rate, 12 FP32 operations (128 lanes per clock) do not.
+
+// s + c: a sum of products kept as an unevaluated FP32 pair
+struct PlAcc {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float ah, float al, float bh, float bl)
+    {
+        const float p = ah * bh;
+        const float pe = fmaf(ah, bh, -p);  // p + pe = ah bh exactly
+        const float t = s + p;
+        const float bp = t - s;
+        const float err = (s - (t - bp)) + (p - bp);  // t + err = s + p exactly
+        c = fmaf(ah, bl, c);
+        c = fmaf(al, bh, c);
+        c += pe + err;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// the planes of a basis element (rounded to nearest)
+__device__ __forceinline__ float2 pl_split(double w)
+{
+    const float h = __double2float_rn(w);
+    return make_float2(h, __double2float_rn(w - (double)h));
+}
+__device__ __forceinline__ float4 pl_split2(double2 w)
+{
+    const float2 a = pl_split(w.x), b = pl_split(w.y);
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+// x 2^-shift as (hi, lo) planes with integer operations only (the FP64
+// pipe stays free): the leading 24 and the next 23 bits of the value
+__device__ __forceinline__ float2 pl_xsplit(double x, int shift)
+{
+    const F3 f = f3_split(x, shift);
+    return make_float2(f.a, f.b);
+}
+
+// projections h = W(:,sel)' x from the planes.  Each CTA owns a contiguous
+// chunk of 2-element row vectors and each of its warps one eighth of the
+// chunk.  A warp first splits its x values (scaled per thread by a power of
+// two) into the x planes scratch and the rows of its slice of every
+// selected column whose planes are stale (read in FP64, written as planes);
+// it then streams its slice once per group of DOT_COLS columns, reading the
+// planes only, so every warp has the same work whatever the column count.
+// Each lane reads back only the vectors it wrote itself.  Per-warp partial
+// sums are added over the warps in a fixed order, then over the CTAs by the
+// last CTA.  The grid is one wave at the kernel's occupancy (<= nb CTAs).
+constexpr int PL_WARPS = BS / 32;
+constexpr size_t PL_SMEM_MAX = 200 * 1024;  // per-warp partials + selection of the projections
+constexpr int PL_MINB = 4;                  // CTAs per SM the projection kernel is compiled for
+constexpr int PL_SPLIT_UNROLL = 4;          // FP64 loads in flight per lane when a column is split
+template <int SIDE>
+__global__ void __launch_bounds__(BS, PL_MINB) k_lb_cgs_dots_pl(LbArgs a, int j)
+{
+    // [PL_WARPS][kmax + 1] per-warp partial projections | sel[kmax + 1] | fresh[kmax + 1]
+    extern __shared__ double wpart[];
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 0) return;
+    const int L = a.ctl->nsel;
+    const int K1 = a.kmax + 1;
+    int *ssel = reinterpret_cast<int *>(wpart + (size_t)PL_WARPS * K1);
+    int *sfresh = ssel + K1;
+    int *ok = SIDE == 0 ? a.okV : a.okU;
+    for (int c = threadIdx.x; c < L; c += BS) {
+        const int col = a.sel[c];
+        ssel[c] = col;
+        sfresh[c] = ok[col] == 0;
+    }
+    __syncthreads();
+    const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
+    const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
+    const size_t ldq = ld / 2;  // leading dimension in float4 (two elements)
+    const double *W = (const double *)(SIDE == 0 ? a.V : a.U);
+    float2 *Wp = SIDE == 0 ? a.Vp : a.Up;
+    const double *x = SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j);
+    const double2 *xv = reinterpret_cast<const double2 *>(x);
+    float4 *xq = reinterpret_cast<float4 *>(a.xpl);
+    const int nvec = len / 2;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int chunk = (nvec + gridDim.x - 1) / gridDim.x;
+    const int cb0 = min(nvec, blockIdx.x * chunk), cb1 = min(nvec, cb0 + chunk);
+    const int sl = (cb1 - cb0 + PL_WARPS - 1) / PL_WARPS;
+    const int v0 = min(cb1, cb0 + w * sl), v1 = min(cb1, v0 + sl);
+    // the row past the last whole vector (odd lengths): lane 0 of the last warp of the last CTA
+    const bool tail_row = (len & 1) && blockIdx.x == gridDim.x - 1 && w == PL_WARPS - 1 && lane == 0;
+    // this thread's scale (|x 2^-xs| < 2), then its x planes
+    int xe = 0;
+    for (int v = v0 + lane; v < v1; v += 32) {
+        const double2 xx = xv[v];
+        xe = max(xe, max(f3_expo(xx.x), f3_expo(xx.y)));
+    }
+    if (tail_row) xe = max(xe, f3_expo(x[len - 1]));
+    const int xs = xe == 0 ? 0 : xe - 1023;
+    const double back = f3_pow2(xs);
+    for (int v = v0 + lane; v < v1; v += 32) {
+        const double2 xx = xv[v];
+        const float2 p = pl_xsplit(xx.x, xs), q = pl_xsplit(xx.y, xs);
+        xq[v] = make_float4(p.x, p.y, q.x, q.y);
+    }
+    float2 xr = make_float2(0.f, 0.f);
+    if (tail_row) xr = pl_xsplit(x[len - 1], xs);
+    // planes of the stale selected columns, on this lane's rows
+    for (int c = 0; c < L; c++) {
+        if (!sfresh[c]) continue;
+        const int col = ssel[c];
+        float4 *Wq = reinterpret_cast<float4 *>(Wp) + (size_t)col * ldq;
+        const double2 *Wd = reinterpret_cast<const double2 *>(W + (size_t)col * ld);
+        int v = v0 + lane;
+        for (; v + 32 * (PL_SPLIT_UNROLL - 1) < v1; v += 32 * PL_SPLIT_UNROLL) {
+            double2 d[PL_SPLIT_UNROLL];
+#pragma unroll
+            for (int u = 0; u < PL_SPLIT_UNROLL; u++) d[u] = Wd[v + 32 * u];
+#pragma unroll
+            for (int u = 0; u < PL_SPLIT_UNROLL; u++) Wq[v + 32 * u] = pl_split2(d[u]);
+        }
+        for (; v < v1; v += 32) Wq[v] = pl_split2(Wd[v]);
+        if (tail_row) Wp[(size_t)col * ld + len - 1] = pl_split(W[(size_t)col * ld + len - 1]);
+    }
+    for (int cb = 0; cb < L; cb += DOT_COLS) {
+        const int nc = min(DOT_COLS, L - cb);
+        const float4 *Wq[DOT_COLS];
+#pragma unroll
+        for (int u = 0; u < DOT_COLS; u++)
+            Wq[u] = reinterpret_cast<const float4 *>(Wp) + (size_t)ssel[cb + (u < nc ? u : 0)] * ldq;
+        PlAcc acc[DOT_COLS];
+        int v = v0 + lane;
+        for (; v + 32 < v1; v += 64) {
+            float4 w0[DOT_COLS], w1[DOT_COLS];
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) {
+                w0[u] = Wq[u][v];
+                w1[u] = Wq[u][v + 32];
+            }
+            const float4 x0 = xq[v], x1 = xq[v + 32];
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) {
+                acc[u].add(w0[u].x, w0[u].y, x0.x, x0.y);
+                acc[u].add(w0[u].z, w0[u].w, x0.z, x0.w);
+                acc[u].add(w1[u].x, w1[u].y, x1.x, x1.y);
+                acc[u].add(w1[u].z, w1[u].w, x1.z, x1.w);
+            }
+        }
+        if (v < v1) {
+            const float4 x0 = xq[v];
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) {
+                const float4 w0 = Wq[u][v];
+                acc[u].add(w0.x, w0.y, x0.x, x0.y);
+                acc[u].add(w0.z, w0.w, x0.z, x0.w);
+            }
+        }
+        if (tail_row) {
+#pragma unroll
+            for (int u = 0; u < DOT_COLS; u++) {
+                if (u >= nc) break;
+                const float2 wr = Wp[(size_t)ssel[cb + u] * ld + len - 1];
+                acc[u].add(wr.x, wr.y, xr.x, xr.y);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < DOT_COLS; u++) {
+            const double sum = warp_sum(acc[u].value() * back);
+            if (lane == 0 && u < nc) wpart[(size_t)w * K1 + cb + u] = sum;
+        }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < L; c += BS) {
+        double s = 0.0;
+#pragma unroll
+        for (int ww = 0; ww < PL_WARPS; ww++) s += wpart[(size_t)ww * K1 + c];
+        a.part_cols[(size_t)c * a.nb + blockIdx.x] = s;
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        reduce_cols(a, L, gridDim.x);
+        for (int c = threadIdx.x; c < L; c += BS) ok[ssel[c]] = 1;
+        if (threadIdx.x == 0) t.c.cgs_phase = 1;
+        tail_store(a, t);
+    }
+}
+
+// x -= W(:,sel) h from the planes, and ||x||^2: one 2-element row vector
+// per thread and step, the selected columns streamed with CGS_UNROLL
+// 16-byte loads in flight.  h (scaled by the power of two of its largest
+// entry) sits in shared memory as (hi, lo) planes; each row's sum of
+// products is formed on the FP32 pipe and applied with one FP64 FMA.
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_cgs_upd_pl(LbArgs a, int j, int last)
+{
+    extern __shared__ double dyn[];  // h[L] as float2 planes (one double slot each) | sel[L]
+    __shared__ double sred[32];
+    __shared__ int hsh;
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 1) return;
+    const int L = a.ctl->nsel;
+    float2 *hp = reinterpret_cast<float2 *>(dyn);
+    int *ssel = reinterpret_cast<int *>(dyn + L);
+    if (threadIdx.x == 0) hsh = 0;
+    __syncthreads();
+    int he = 0;
+    for (int c = threadIdx.x; c < L; c += BS) he = max(he, f3_expo(a.h[c]));
+    if (he) atomicMax(&hsh, he);
+    __syncthreads();
+    const int hs = hsh == 0 ? 0 : hsh - 1023;  // |h 2^-hs| < 2
+    const double hscale = f3_pow2(-hs), back = f3_pow2(hs);
+    for (int c = threadIdx.x; c < L; c += BS) {
+        hp[c] = pl_split(a.h[c] * hscale);
+        ssel[c] = a.sel[c];
+    }
+    __syncthreads();
+    const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
+    const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
+    const size_t ldq = ld / 2;
+    const float4 *Wq = reinterpret_cast<const float4 *>(SIDE == 0 ? a.Vp : a.Up);
+    const float2 *Wp = SIDE == 0 ? a.Vp : a.Up;
+    double *x = SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j);
+    double2 *xv = reinterpret_cast<double2 *>(x);
+    const int nvec = len / 2;
+    double sq = 0.0;
+    for (int v = blockIdx.x * BS + threadIdx.x; v < nvec; v += gridDim.x * BS) {
+        const double2 x0 = xv[v];
+        PlAcc s0, s1;
+        int c = 0;
+        for (; c + CGS_UNROLL <= L; c += CGS_UNROLL) {
+            float4 wv[CGS_UNROLL];
+#pragma unroll
+            for (int u = 0; u < CGS_UNROLL; u++) wv[u] = Wq[(size_t)ssel[c + u] * ldq + v];
+#pragma unroll
+            for (int u = 0; u < CGS_UNROLL; u++) {
+                const float2 hc = hp[c + u];
+                s0.add(wv[u].x, wv[u].y, hc.x, hc.y);
+                s1.add(wv[u].z, wv[u].w, hc.x, hc.y);
+            }
+        }
+        for (; c < L; c++) {
+            const float4 wc = Wq[(size_t)ssel[c] * ldq + v];
+            const float2 hc = hp[c];
+            s0.add(wc.x, wc.y, hc.x, hc.y);
+            s1.add(wc.z, wc.w, hc.x, hc.y);
+        }
+        double2 y;
+        y.x = fma(-s0.value(), back, x0.x);
+        y.y = fma(-s1.value(), back, x0.y);
+        xv[v] = y;
+        sq = fma(y.x, y.x, sq);
+        sq = fma(y.y, y.y, sq);
+    }
+    if (blockIdx.x == gridDim.x - 1 && (len & 1) && threadIdx.x == 0) {
+        const int r = len - 1;
+        PlAcc sr;
+        for (int c = 0; c < L; c++) {
+            const float2 wc = Wp[(size_t)ssel[c] * ld + r];
+            sr.add(wc.x, wc.y, hp[c].x, hp[c].y);
+        }
+        const double y = fma(-sr.value(), back, x[r]);
+        x[r] = y;
+        sq = fma(y, y, sq);
+    }
+    const double sq2 = block_sum<BS>(sq, sred);
+    if (threadIdx.x == 0) a.part_sq[blockIdx.x] = sq2;
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
+        after_cgs<SIDE>(t, a, j, sqrt(s2), last);
+        tail_store(a, t);
+    }
+}
+
 // ------------------------------------------------- complex*16 vectors
 // The complex form (complex16/zlanbpro.F) keeps alpha, beta and the omega
 // recurrences real.  Its vectors are (re, im) pairs of doubles and its
@@ -1125,6 +1419,10 @@ __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
     const int len = m > n ? m : n;
     T *uc = cu >= 0 ? ucol<T>(a, cu) : nullptr;
     T *vc = cv >= 0 ? vcol<T>(a, cv) : nullptr;
+    if (a.okU && blockIdx.x == 0 && threadIdx.x == 0) {
+        if (pu.mode && cu >= 0) a.okU[cu] = 0;
+        if (pv.mode && cv >= 0) a.okV[cv] = 0;
+    }
     for (int r = blockIdx.x * BS + threadIdx.x; r < len; r += gridDim.x * BS) {
         if (pu.mode && uc && r < m) uc[r] = apply_pend(uc[r], pu);
         if (pv.mode && vc && r < n) vc[r] = apply_pend(vc[r], pv);
@@ -1143,9 +1441,10 @@ template <typename T>
 static size_t cgs_smem(const LbArgs &a) { return (sizeof(double) + sizeof(int)) * (size_t)(a.kmax + 1) + 16; }
 static size_t cgs_smem_f3(const LbArgs &a) { return (2 * sizeof(double) + sizeof(int)) * (size_t)(a.kmax + 1) + 16; }
 
-// Gram-Schmidt arithmetic of the FP64 form (propack_set_cgs_arith): 1 the
-// FP32-pipe kernels of pgb_f3.cuh, 0 FP64 FMAs
-thread_local int g_cgs_f3 = 0;
+// Gram-Schmidt arithmetic of the FP64 form (propack_set_cgs_arith)
+thread_local int g_cgs_arith = CGS_PLANES;
+static size_t pl_smem(int kmax) { return (sizeof(double) * PL_WARPS + 2 * sizeof(int)) * (size_t)(kmax + 1); }
+static size_t cgs_smem_pl(const LbArgs &a) { return pl_smem(a.kmax); }
 
 template <int SIDE, typename T>
 static void set_upd_limits(size_t need)
@@ -1170,7 +1469,37 @@ void lb_set_smem_limits(int kmax)
         set_upd_limits<1, double>(need);
         set_upd_limits<0, float>(need);
         set_upd_limits<1, float>(need);
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd_pl<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd_pl<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
     }
+    const size_t needp = pl_smem(kmax);
+    if (needp > 48 * 1024 && needp <= PL_SMEM_MAX) {
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_dots_pl<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)needp));
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_dots_pl<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)needp));
+    }
+}
+
+// the planes are used when the driver allocated them (FP64 form, kmax small
+// enough for the projections' per-warp partials in shared memory)
+bool lb_planes_fit(int kmax) { return pl_smem(kmax) <= PL_SMEM_MAX; }
+
+// one wave of the plane projections at their occupancy (at most nb CTAs;
+// their partials are summed over gridDim)
+template <int SIDE>
+static int dots_pl_grid(const LbArgs &a)
+{
+    static thread_local int g = 0, dev = -1;
+    static thread_local size_t smem = 0;
+    const Dev &d = device_info();
+    const size_t need = cgs_smem_pl(a);
+    if (g == 0 || dev != d.device || smem != need) {
+        int per = 0;
+        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lb_cgs_dots_pl<SIDE>, BS, need));
+        g = std::max(1, per) * d.sms;
+        dev = d.device;
+        smem = need;
+    }
+    return std::min(g, a.nb);
 }
 
 // one CGS pass: the projections, then the update (each kernel returns at
@@ -1178,7 +1507,14 @@ void lb_set_smem_limits(int kmax)
 template <int SIDE, typename T>
 static void launch_cgs_pass(const LbArgs &a, int j, int last, cudaStream_t s)
 {
-    if (sizeof(T) == 8 && g_cgs_f3) {
+    if (sizeof(T) == 8 && a.Up) {
+        PGB_PROF(PK_CGS_DOTS, s, k_lb_cgs_dots_pl<SIDE><<<dots_pl_grid<SIDE>(a), BS, cgs_smem_pl(a), s>>>(a, j));
+        PGB_LAUNCHED();
+        PGB_PROF(PK_CGS_UPD, s, k_lb_cgs_upd_pl<SIDE><<<a.nb, BS, cgs_smem<T>(a), s>>>(a, j, last));
+        PGB_LAUNCHED();
+        return;
+    }
+    if (sizeof(T) == 8 && g_cgs_arith == CGS_F3) {
         PGB_PROF(PK_CGS_DOTS, s, k_lb_cgs_dots_f3<SIDE><<<a.nb, BS, 0, s>>>(a, j));
         PGB_LAUNCHED();
         PGB_PROF(PK_CGS_UPD, s, k_lb_cgs_upd_f3<SIDE><<<a.nb, BS, cgs_smem_f3(a), s>>>(a, j, last));

@@ -103,8 +103,9 @@ def test_spmv_schedules(mode):
 
 @pytest.mark.parametrize("case", ["plain_irl", "lowrank"])
 def test_cgs_arithmetics_agree(golden, case):
-    # the Gram-Schmidt passes on the FP32 pipe (exact FP64 splits) give the
-    # FP64 result: same matvecs, sigma to 1e-12, the same subspaces
+    # the Gram-Schmidt passes on the FP32 pipe (exact three-way splits, or
+    # the split-once (hi, lo) planes) give the FP64 result: same matvecs
+    # within a restart, sigma to 1e-12, the same subspaces
     if case == "plain_irl":
         A, k, kw = csr_from(golden, "plain"), 10, dict(irl_mode=True, kmax=30, tol=1e-12)
     else:
@@ -112,17 +113,19 @@ def test_cgs_arithmetics_agree(golden, case):
         A, k, kw = pg.CsrOperator(S, L, R, w), 8, dict(irl_mode=True, kmax=40, tol=1e-10)
     out = {}
     try:
-        for arith in ("fp64", "f3"):
+        for arith in ("fp64", "f3", "planes"):
             pg.set_cgs_arith(arith)
             u, s, vt, bnd = pg.svdp(A, k, rng=rng0(), **kw)
             out[arith] = (u, s, vt, pg.get_stats())
     finally:
-        pg.set_cgs_arith("fp64")
-    (u0, s0, vt0, st0), (u1, s1, vt1, st1) = out["fp64"], out["f3"]
-    np.testing.assert_allclose(s1, s0, rtol=1e-12)
-    assert subspace_err(u1, u0) < 1e-9 and subspace_err(vt1.T, vt0.T) < 1e-9
-    assert abs(st1["nopx"] - st0["nopx"]) <= 2 * 30
-    assert st1["cgs_cols_u"] + st1["cgs_cols_v"] > 0
+        pg.set_cgs_arith("planes")
+    u0, s0, vt0, st0 = out["fp64"]
+    for arith in ("f3", "planes"):
+        u1, s1, vt1, st1 = out[arith]
+        np.testing.assert_allclose(s1, s0, rtol=1e-12)
+        assert subspace_err(u1, u0) < 1e-9 and subspace_err(vt1.T, vt0.T) < 1e-9
+        assert abs(st1["nopx"] - st0["nopx"]) <= 2 * 30
+        assert st1["cgs_cols_u"] + st1["cgs_cols_v"] > 0
 
 
 # -------------------------------------------------- golden (reference) cases
