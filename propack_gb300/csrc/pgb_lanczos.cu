@@ -931,9 +931,9 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd_f3(LbArgs a, int j, int last)
 
 // ------------------------------------------------ split-once planes
 // The FP64 form's Gram-Schmidt on the FP32 pipe, reading each basis element
-// as 8 bytes of FP32 planes: hi = fl32(w), lo = fl32(w - hi), so that
-// hi + lo holds w to 2^-48 relative (a Lanczos column has |w| <= 1; bits
-// below 2^-149 are lost, far below the column's unit norm).  A column is
+// as 8 bytes of FP32 planes: hi = the leading 24 bits of w, lo = the next
+// 23, so that hi + lo holds w to 2^-47 relative (a Lanczos column has
+// |w| <= 1; parts below 2^-74 are dropped, far below the column's unit norm).  A column is
 // split by the first projection that selects it while its flag is clear;
 // the update of the same pass and every later pass read its planes until
 // the column is rewritten (the SpMV that writes a column, the flush and the
@@ -964,11 +964,57 @@ struct PlAcc {
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
-// the planes of a basis element (rounded to nearest)
+// f as an FP64 value with integer operations only (no FP64-pipe conversion);
+// FP32 subnormals (|f| < 2^-126) become 0, infinities and NaNs stay so
+__device__ __forceinline__ double pl_f2d(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
+    const unsigned long long ee = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
+    const unsigned long long m = (unsigned long long)(u & 0x7fffffu) << 29;
+    return e == 0 ? 0.0 : __longlong_as_double((long long)(sgn | (ee << 52) | m));
+}
+
+// (s, c) += (s2, c2) for compensated pairs: the leading parts by a two-sum
+__device__ __forceinline__ void pl_pair_add(float &s, float &c, float s2, float c2)
+{
+    const float t = s + s2;
+    const float bp = t - s;
+    const float e = (s - (t - bp)) + (s2 - bp);
+    c = (c + c2) + e;
+    s = t;
+}
+// Sum four compensated pairs over the warp with FP32 operations only, by a
+// transposed butterfly: at offset 16 a lane keeps two of the four sums and
+// sends the other two, at offset 8 one of its two, then one sum travels
+// the last three offsets (12 shuffles instead of 40).  Lanes 8u .. 8u+7
+// end with the total of acc[u].  The order of additions is fixed.
+__device__ __forceinline__ PlAcc pl_warp_sum4(const PlAcc *acc)
+{
+    const unsigned F = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool b4 = lane & 16, b3 = lane & 8;
+    PlAcc k0 = b4 ? acc[2] : acc[0], k1 = b4 ? acc[3] : acc[1];
+    const PlAcc g0 = b4 ? acc[0] : acc[2], g1 = b4 ? acc[1] : acc[3];
+    pl_pair_add(k0.s, k0.c, __shfl_xor_sync(F, g0.s, 16), __shfl_xor_sync(F, g0.c, 16));
+    pl_pair_add(k1.s, k1.c, __shfl_xor_sync(F, g1.s, 16), __shfl_xor_sync(F, g1.c, 16));
+    PlAcc k = b3 ? k1 : k0;
+    const PlAcc g = b3 ? k0 : k1;
+    pl_pair_add(k.s, k.c, __shfl_xor_sync(F, g.s, 8), __shfl_xor_sync(F, g.c, 8));
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) pl_pair_add(k.s, k.c, __shfl_xor_sync(F, k.s, o), __shfl_xor_sync(F, k.c, o));
+    return k;
+}
+
+// the planes of a basis element, with integer operations only: the leading
+// 24 and the next 23 bits of w (|w| <= 1; parts below 2^-74 are dropped).
+// Conversions between FP64 and FP32 run on the FP64 pipe, which retires two
+// lanes per clock per SM on GB300.
 __device__ __forceinline__ float2 pl_split(double w)
 {
-    const float h = __double2float_rn(w);
-    return make_float2(h, __double2float_rn(w - (double)h));
+    const F3 f = f3_split(w, 0);
+    return make_float2(f.a, f.b);
 }
 __device__ __forceinline__ float4 pl_split2(double2 w)
 {
@@ -985,14 +1031,15 @@ __device__ __forceinline__ float2 pl_xsplit(double x, int shift)
 
 // projections h = W(:,sel)' x from the planes.  Each CTA owns a contiguous
 // chunk of 2-element row vectors and each of its warps one eighth of the
-// chunk.  A warp first splits its x values (scaled per thread by a power of
-// two) into the x planes scratch and the rows of its slice of every
+// chunk.  A warp first splits its x values (scaled by a power of two per
+// warp) into the x planes scratch and the rows of its slice of every
 // selected column whose planes are stale (read in FP64, written as planes);
 // it then streams its slice once per group of DOT_COLS columns, reading the
 // planes only, so every warp has the same work whatever the column count.
-// Each lane reads back only the vectors it wrote itself.  Per-warp partial
-// sums are added over the warps in a fixed order, then over the CTAs by the
-// last CTA.  The grid is one wave at the kernel's occupancy (<= nb CTAs).
+// Each lane reads back only the vectors it wrote itself.  A group's sums
+// are reduced over the warp as compensated FP32 pairs (no FP64 operation
+// per group), then added over the warps in a fixed order, then over the
+// CTAs by the last CTA.  The grid is one wave at the kernel's occupancy (<= nb CTAs).
 constexpr int PL_WARPS = BS / 32;
 constexpr size_t PL_SMEM_MAX = 200 * 1024;  // per-warp partials + selection of the projections
 constexpr int PL_MINB = 4;                  // CTAs per SM the projection kernel is compiled for
@@ -1031,13 +1078,14 @@ __global__ void __launch_bounds__(BS, PL_MINB) k_lb_cgs_dots_pl(LbArgs a, int j)
     const int v0 = min(cb1, cb0 + w * sl), v1 = min(cb1, v0 + sl);
     // the row past the last whole vector (odd lengths): lane 0 of the last warp of the last CTA
     const bool tail_row = (len & 1) && blockIdx.x == gridDim.x - 1 && w == PL_WARPS - 1 && lane == 0;
-    // this thread's scale (|x 2^-xs| < 2), then its x planes
+    // this warp's scale (|x 2^-xs| < 2), then its x planes
     int xe = 0;
     for (int v = v0 + lane; v < v1; v += 32) {
         const double2 xx = xv[v];
         xe = max(xe, max(f3_expo(xx.x), f3_expo(xx.y)));
     }
     if (tail_row) xe = max(xe, f3_expo(x[len - 1]));
+    xe = __reduce_max_sync(0xffffffffu, xe);
     const int xs = xe == 0 ? 0 : xe - 1023;
     const double back = f3_pow2(xs);
     for (int v = v0 + lane; v < v1; v += 32) {
@@ -1072,12 +1120,14 @@ __global__ void __launch_bounds__(BS, PL_MINB) k_lb_cgs_dots_pl(LbArgs a, int j)
             Wq[u] = reinterpret_cast<const float4 *>(Wp) + (size_t)ssel[cb + (u < nc ? u : 0)] * ldq;
         PlAcc acc[DOT_COLS];
         int v = v0 + lane;
+        // the planes stream through once (evict-first), so that the x
+        // planes, read again by every group, stay in L2
         for (; v + 32 < v1; v += 64) {
             float4 w0[DOT_COLS], w1[DOT_COLS];
 #pragma unroll
             for (int u = 0; u < DOT_COLS; u++) {
-                w0[u] = Wq[u][v];
-                w1[u] = Wq[u][v + 32];
+                w0[u] = __ldcs(Wq[u] + v);
+                w1[u] = __ldcs(Wq[u] + v + 32);
             }
             const float4 x0 = xq[v], x1 = xq[v + 32];
 #pragma unroll
@@ -1092,7 +1142,7 @@ __global__ void __launch_bounds__(BS, PL_MINB) k_lb_cgs_dots_pl(LbArgs a, int j)
             const float4 x0 = xq[v];
 #pragma unroll
             for (int u = 0; u < DOT_COLS; u++) {
-                const float4 w0 = Wq[u][v];
+                const float4 w0 = __ldcs(Wq[u] + v);
                 acc[u].add(w0.x, w0.y, x0.x, x0.y);
                 acc[u].add(w0.z, w0.w, x0.z, x0.w);
             }
@@ -1105,11 +1155,9 @@ __global__ void __launch_bounds__(BS, PL_MINB) k_lb_cgs_dots_pl(LbArgs a, int j)
                 acc[u].add(wr.x, wr.y, xr.x, xr.y);
             }
         }
-#pragma unroll
-        for (int u = 0; u < DOT_COLS; u++) {
-            const double sum = warp_sum(acc[u].value() * back);
-            if (lane == 0 && u < nc) wpart[(size_t)w * K1 + cb + u] = sum;
-        }
+        static_assert(DOT_COLS == 4, "pl_warp_sum4 sums four columns");
+        const PlAcc tot = pl_warp_sum4(acc);
+        if ((lane & 7) == 0 && (lane >> 3) < nc) wpart[(size_t)w * K1 + cb + (lane >> 3)] = tot.value() * back;
     }
     __syncthreads();
     for (int c = threadIdx.x; c < L; c += BS) {
@@ -1187,8 +1235,8 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd_pl(LbArgs a, int j, int last)
             s1.add(wc.z, wc.w, hc.x, hc.y);
         }
         double2 y;
-        y.x = fma(-s0.value(), back, x0.x);
-        y.y = fma(-s1.value(), back, x0.y);
+        y.x = fma(-pl_f2d(s0.c), back, fma(-pl_f2d(s0.s), back, x0.x));
+        y.y = fma(-pl_f2d(s1.c), back, fma(-pl_f2d(s1.s), back, x0.y));
         xv[v] = y;
         sq = fma(y.x, y.x, sq);
         sq = fma(y.y, y.y, sq);
