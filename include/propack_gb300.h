@@ -201,6 +201,11 @@ int propack_get_profile(double *total_ms, int64_t *launches, int n);
  * PROPACK_ERR_ARG. */
 int propack_set_cgs_arith(int mode);
 
+/* The binary (SASS) version of the library's kernels as the CUDA runtime
+ * loaded them on the current device: 103 for sm_103a.  Returns it, or
+ * PROPACK_ERR_CUDA when no device is usable.  No reference counterpart. */
+int propack_kernel_binary_version(void);
+
 /* ---- Single-precision drivers ------------------------------------------
  * SLANSVD / SLANSVD_IRL: the argument lists of single/slansvd.F:1-3 and
  * single/slansvd_irl.F:1-3 (REAL arrays, REAL tolin/doption/dparm, a REAL

@@ -278,6 +278,31 @@ def _host_zaprod(A):
     return ZAPROD(cb)
 
 
+def work_sizes(m, n, kmax, vectors=True, irl=True, cplx=False):
+    """LWORK, LIWORK and (complex drivers) LZWRK as the reference documents
+    them (double/dlansvd.F:55-65, double/dlansvd_irl.F:65-75, with the
+    block size NB = 32 that scipy's _svdp uses).  The drivers here validate
+    the declared sizes (they refuse less than the reference itself writes)
+    but never read or write WORK, IWORK or ZWORK."""
+    nb = 32
+    if vectors:
+        lwork = m + n + (10 if irl else 9) * kmax + 5 * kmax ** 2 + 4 + max(3 * kmax ** 2 + 4 * kmax + 4,
+                                                                           nb * max(m, n))
+        liwork = 8 * kmax
+    else:
+        lwork = m + n + (10 if irl else 9) * kmax + 2 * kmax ** 2 + (5 if irl else 4) + max(m + n, 4 * kmax + 4)
+        liwork = 2 * kmax + 2
+    return lwork, liwork, (m + n + kmax if cplx else 0)
+
+
+def _workspace(m, n, kmax, irl, cplx=False, dtype=np.float64):
+    """Workspace arrays of the documented sizes (np.empty: never touched, so
+    never paged in) and their sizes."""
+    lwork, liwork, lzwrk = work_sizes(m, n, kmax, True, irl, cplx)
+    return (np.empty(lwork, dtype=dtype), lwork, np.empty(liwork, dtype=np.int32), liwork,
+            np.empty(max(lzwrk, 1), dtype=np.complex128), lzwrk)
+
+
 def zlansvd_irl(which, jobu, jobv, m, n, dim, p, neig, maxiter, aprod, U, sigma, bnd, V, tol, doption, ioption,
                 iparm=None):
     """Call zlansvd_irl_ with the reference's argument list (complex16/zlansvd_irl.F:1-3); U, V complex128
@@ -285,15 +310,13 @@ def zlansvd_irl(which, jobu, jobv, m, n, dim, p, neig, maxiter, aprod, U, sigma,
     lib = load()
     ci = lambda v: C.byref(C.c_int(v))
     ne, info = C.c_int(neig), C.c_int(0)
-    work = np.zeros(1)
-    zwork = np.zeros(1, dtype=np.complex128)
-    iwork = np.zeros(1, dtype=np.int32)
+    work, lwork, iwork, liwork, zwork, lzwrk = _workspace(m, n, dim, True, True)
     zparm = np.zeros(1, dtype=np.complex128)
     iparm = np.zeros(2, dtype=np.int32) if iparm is None else iparm
     vp = lambda a: C.c_void_p(a.ctypes.data)
     lib.zlansvd_irl_(which, jobu, jobv, ci(m), ci(n), ci(dim), ci(p), C.byref(ne), ci(maxiter), aprod, vp(U),
                      ci(U.shape[0]), _dp(sigma), _dp(bnd), vp(V), ci(V.shape[0]), C.byref(C.c_double(tol)),
-                     _dp(work), ci(1), vp(zwork), ci(1), _ip(iwork), ci(1), _dp(doption), _ip(ioption),
+                     _dp(work), ci(lwork), vp(zwork), ci(lzwrk), _ip(iwork), ci(liwork), _dp(doption), _ip(ioption),
                      C.byref(info), vp(zparm), _ip(iparm), C.c_size_t(1), C.c_size_t(1), C.c_size_t(1))
     return ne.value, info.value
 
@@ -303,15 +326,13 @@ def zlansvd(jobu, jobv, m, n, k, kmax, aprod, U, sigma, bnd, V, tol, doption, io
     lib = load()
     ci = lambda v: C.byref(C.c_int(v))
     km, info = C.c_int(k), C.c_int(0)
-    work = np.zeros(1)
-    zwork = np.zeros(1, dtype=np.complex128)
-    iwork = np.zeros(1, dtype=np.int32)
+    work, lwork, iwork, liwork, zwork, lzwrk = _workspace(m, n, kmax, False, True)
     zparm = np.zeros(1, dtype=np.complex128)
     iparm = np.zeros(2, dtype=np.int32) if iparm is None else iparm
     vp = lambda a: C.c_void_p(a.ctypes.data)
     lib.zlansvd_(jobu, jobv, ci(m), ci(n), C.byref(km), ci(kmax), aprod, vp(U), ci(U.shape[0]), _dp(sigma),
-                 _dp(bnd), vp(V), ci(V.shape[0]), C.byref(C.c_double(tol)), _dp(work), ci(1), vp(zwork), ci(1),
-                 _ip(iwork), ci(1), _dp(doption), _ip(ioption), C.byref(info), vp(zparm), _ip(iparm),
+                 _dp(bnd), vp(V), ci(V.shape[0]), C.byref(C.c_double(tol)), _dp(work), ci(lwork), vp(zwork),
+                 ci(lzwrk), _ip(iwork), ci(liwork), _dp(doption), _ip(ioption), C.byref(info), vp(zparm), _ip(iparm),
                  C.c_size_t(1), C.c_size_t(1))
     return km.value, info.value
 
@@ -322,14 +343,12 @@ def lansvd_irl(which, jobu, jobv, m, n, dim, p, neig, maxiter, aprod, U, sigma, 
     lib = load()
     ci = lambda v: C.byref(C.c_int(v))
     ne, info = C.c_int(neig), C.c_int(0)
-    lwork = m + n + 10 * dim + 5 * dim ** 2 + 4 + max(3 * dim ** 2 + 4 * dim + 4, 32 * max(m, n))
-    work = np.zeros(1)
-    iwork = np.zeros(1, dtype=np.int32)
+    work, lwork, iwork, liwork, _, _ = _workspace(m, n, dim, True)
     iparm = np.zeros(2, dtype=np.int32) if iparm is None else iparm
     dparm = np.zeros(1) if dparm is None else dparm
     lib.dlansvd_irl_(which, jobu, jobv, ci(m), ci(n), ci(dim), ci(p), C.byref(ne), ci(maxiter), aprod, _dp(U),
                      ci(U.shape[0]), _dp(sigma), _dp(bnd), _dp(V), ci(V.shape[0]), C.byref(C.c_double(tol)),
-                     _dp(work), ci(lwork), _ip(iwork), ci(8 * dim), _dp(doption), _ip(ioption), C.byref(info),
+                     _dp(work), ci(lwork), _ip(iwork), ci(liwork), _dp(doption), _ip(ioption), C.byref(info),
                      _dp(dparm), _ip(iparm), C.c_size_t(1), C.c_size_t(1), C.c_size_t(1))
     return ne.value, info.value
 
@@ -339,14 +358,12 @@ def lansvd(jobu, jobv, m, n, k, kmax, aprod, U, sigma, bnd, V, tol, doption, iop
     lib = load()
     ci = lambda v: C.byref(C.c_int(v))
     km, info = C.c_int(k), C.c_int(0)
-    work = np.zeros(1)
-    iwork = np.zeros(1, dtype=np.int32)
+    work, lwork, iwork, liwork, _, _ = _workspace(m, n, kmax, False)
     iparm = np.zeros(2, dtype=np.int32) if iparm is None else iparm
     dparm = np.zeros(1) if dparm is None else dparm
-    lwork = m + n + 9 * kmax + 5 * kmax ** 2 + 4 + max(3 * kmax ** 2 + 4 * kmax + 4, 32 * max(m, n))
     lib.dlansvd_(jobu, jobv, ci(m), ci(n), C.byref(km), ci(kmax), aprod, _dp(U), ci(U.shape[0]), _dp(sigma),
                  _dp(bnd), _dp(V), ci(V.shape[0]), C.byref(C.c_double(tol)), _dp(work), ci(lwork), _ip(iwork),
-                 ci(8 * kmax), _dp(doption), _ip(ioption), C.byref(info), _dp(dparm), _ip(iparm), C.c_size_t(1),
+                 ci(liwork), _dp(doption), _ip(ioption), C.byref(info), _dp(dparm), _ip(iparm), C.c_size_t(1),
                  C.c_size_t(1))
     return km.value, info.value
 

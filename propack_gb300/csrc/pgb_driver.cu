@@ -1467,6 +1467,46 @@ static void run_zirl(const char *which, const char *jobu, const char *jobv, int 
 // ------------------------------------------------------------------ C ABI
 using namespace pgb;
 
+// LWORK / LIWORK (/ LZWRK) as the reference's drivers use them: the leading
+// part of WORK that they always clear (dzero of 8*dim+3+2*dim^2 entries,
+// double/dlansvd_irl.F:177-188; 7*lanmax+2+2*lanmax^2, double/dlansvd.F:
+// 151-160) plus the max(m,n) vector that dgetu0 and dlanbpro take from its
+// tail; IWORK holds dlanbpro's 2*dim+1 interval bounds; ZWORK (complex
+// drivers) the max(m,n) complex vector of zgetu0.  The device path keeps
+// its own workspace and never reads or writes WORK, IWORK or ZWORK; a call
+// that declares less than the reference would overrun is refused with
+// PROPACK_ERR_ARG.
+static void check_work(const char *who, bool irl, int m, int n, int dim, const int *lwork, const int *liwork,
+                       const int *lzwrk, bool cplx)
+{
+    if (!lwork || !liwork || (cplx && !lzwrk)) {
+        set_error(std::string(who) + ": LWORK, LIWORK" + (cplx ? " and LZWRK" : "") + " are required");
+        throw ArgFailure();
+    }
+    const long long d = std::max(0, std::min(dim, std::min(m, n) + 1));
+    const long long mn = std::max(m, n);
+    const long long need = (irl ? 2 * d * d + 8 * d + 3 : 2 * d * d + 7 * d + 2) + mn;
+    const long long needi = 2 * d + 1;
+    char msg[256];
+    if (*lwork < need) {
+        snprintf(msg, sizeof msg, "%s: LWORK = %d is below %lld (%s + max(m,n))", who, *lwork, need,
+                 irl ? "2*dim^2+8*dim+3" : "2*kmax^2+7*kmax+2");
+        set_error(msg);
+        throw ArgFailure();
+    }
+    if (*liwork < needi) {
+        snprintf(msg, sizeof msg, "%s: LIWORK = %d is below 2*%s+1 = %lld", who, *liwork, irl ? "dim" : "kmax",
+                 needi);
+        set_error(msg);
+        throw ArgFailure();
+    }
+    if (cplx && *lzwrk < mn) {
+        snprintf(msg, sizeof msg, "%s: LZWRK = %d is below max(m,n) = %lld", who, *lzwrk, mn);
+        set_error(msg);
+        throw ArgFailure();
+    }
+}
+
 extern "C" void dlansvd_irl_(const char *which, const char *jobu, const char *jobv, const int *m, const int *n,
                              const int *dim, const int *p, int *neig, const int *maxiter, propack_aprod_t aprod,
                              double *U, const int *ldu, double *sigma, double *bnd, double *V, const int *ldv,
@@ -1474,9 +1514,10 @@ extern "C" void dlansvd_irl_(const char *which, const char *jobu, const char *jo
                              double *doption, const int *ioption, int *info, double *dparm, int *iparm,
                              size_t which_len, size_t jobu_len, size_t jobv_len)
 {
-    (void)work; (void)lwork; (void)iwork; (void)liwork; (void)which_len; (void)jobu_len; (void)jobv_len;
+    (void)work; (void)iwork; (void)which_len; (void)jobu_len; (void)jobv_len;
     set_error("");
     try {
+        if (m && n && dim) check_work("dlansvd_irl_", true, *m, *n, *dim, lwork, liwork, nullptr, false);
         run_irl(which, jobu, jobv, *m, *n, *dim, *p, neig, *maxiter, aprod, U, *ldu, sigma, bnd, V, *ldv, *tolin,
                 doption, ioption, info, dparm, iparm);
     } catch (const CudaFailure &) {
@@ -1494,9 +1535,10 @@ extern "C" void dlansvd_(const char *jobu, const char *jobv, const int *m, const
                          const int *liwork, double *doption, const int *ioption, int *info, double *dparm, int *iparm,
                          size_t jobu_len, size_t jobv_len)
 {
-    (void)work; (void)lwork; (void)iwork; (void)liwork; (void)jobu_len; (void)jobv_len;
+    (void)work; (void)iwork; (void)jobu_len; (void)jobv_len;
     set_error("");
     try {
+        if (m && n && kmax) check_work("dlansvd_", false, *m, *n, *kmax, lwork, liwork, nullptr, false);
         run_lansvd(jobu, jobv, *m, *n, k, *kmax, aprod, U, *ldu, sigma, bnd, V, *ldv, *tolin, doption, ioption, info,
                    dparm, iparm);
     } catch (const CudaFailure &) {
@@ -1520,10 +1562,11 @@ extern "C" void zlansvd_irl_(const char *which, const char *jobu, const char *jo
                              int *info, propack_z16 *zparm, int *iparm, size_t which_len, size_t jobu_len,
                              size_t jobv_len)
 {
-    (void)work; (void)lwork; (void)zwork; (void)lzwrk; (void)iwork; (void)liwork;
+    (void)work; (void)zwork; (void)iwork;
     (void)which_len; (void)jobu_len; (void)jobv_len;
     set_error("");
     try {
+        if (m && n && dim) check_work("zlansvd_irl_", true, *m, *n, *dim, lwork, liwork, lzwrk, true);
         run_zirl(which, jobu, jobv, *m, *n, *dim, *p, neig, *maxiter, aprod, U, *ldu, sigma, bnd, V, *ldv, *tolin,
                  doption, ioption, info, zparm, iparm);
     } catch (const CudaFailure &) {
@@ -1542,9 +1585,10 @@ extern "C" void zlansvd_(const char *jobu, const char *jobv, const int *m, const
                          const int *ioption, int *info, propack_z16 *zparm, int *iparm, size_t jobu_len,
                          size_t jobv_len)
 {
-    (void)work; (void)lwork; (void)zwork; (void)lzwrk; (void)iwork; (void)liwork; (void)jobu_len; (void)jobv_len;
+    (void)work; (void)zwork; (void)iwork; (void)jobu_len; (void)jobv_len;
     set_error("");
     try {
+        if (m && n && kmax) check_work("zlansvd_", false, *m, *n, *kmax, lwork, liwork, lzwrk, true);
         run_lansvd_t<double2>(jobu, jobv, *m, *n, k, *kmax, nullptr, (double *)U, *ldu, sigma, bnd, (double *)V,
                               *ldv, *tolin, doption, ioption, info, nullptr, iparm, aprod, zparm);
     } catch (const CudaFailure &) {
@@ -1626,7 +1670,7 @@ extern "C" void slansvd_irl_(const char *which, const char *jobu, const char *jo
                              float *soption, const int *ioption, int *info, float *sparm, int *iparm,
                              size_t which_len, size_t jobu_len, size_t jobv_len)
 {
-    (void)work; (void)lwork; (void)iwork; (void)liwork; (void)which_len; (void)jobu_len; (void)jobv_len;
+    (void)work; (void)iwork; (void)which_len; (void)jobu_len; (void)jobv_len;
     set_error("");
     const int saved = g_precision;
     try {
@@ -1635,6 +1679,7 @@ extern "C" void slansvd_irl_(const char *which, const char *jobu, const char *jo
             set_error("slansvd_irl_: invalid argument");
             throw ArgFailure();
         }
+        check_work("slansvd_irl_", true, *m, *n, *dim, lwork, liwork, nullptr, false);
         SArgs w;
         const int k0 = *neig;
         s_prepare(w, aprod, *m, *n, *dim + 1, *dim, *ldu, *ldv, U, k0, soption, 4, sparm);
@@ -1662,7 +1707,7 @@ extern "C" void slansvd_(const char *jobu, const char *jobv, const int *m, const
                          const int *liwork, float *soption, const int *ioption, int *info, float *sparm, int *iparm,
                          size_t jobu_len, size_t jobv_len)
 {
-    (void)work; (void)lwork; (void)iwork; (void)liwork; (void)jobu_len; (void)jobv_len;
+    (void)work; (void)iwork; (void)jobu_len; (void)jobv_len;
     set_error("");
     const int saved = g_precision;
     try {
@@ -1671,6 +1716,7 @@ extern "C" void slansvd_(const char *jobu, const char *jobv, const int *m, const
             set_error("slansvd_: invalid argument");
             throw ArgFailure();
         }
+        check_work("slansvd_", false, *m, *n, *kmax, lwork, liwork, nullptr, false);
         SArgs w;
         const int k0 = *k;
         s_prepare(w, aprod, *m, *n, *kmax + 1, *kmax, *ldu, *ldv, U, k0, soption, 3, sparm);
@@ -1701,6 +1747,16 @@ extern "C" int propack_set_precision(int mode)
     return 0;
 }
 extern "C" int propack_get_precision(void) { return g_precision; }
+
+extern "C" int propack_kernel_binary_version(void)
+{
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k_sum_final) != cudaSuccess) {
+        set_error("cudaFuncGetAttributes failed (no usable CUDA device?)");
+        return PROPACK_ERR_CUDA;
+    }
+    return fa.binaryVersion;
+}
 
 extern "C" int propack_set_cgs_arith(int mode)
 {

@@ -45,13 +45,64 @@ def test_library_loads():
         assert hasattr(L, n)
 
 
-def test_kernels_compiled_for_sm103a():
+def test_kernels_compiled_for_sm103a_only():
+    # the build recipe compiles every translation unit and links for sm_103a
+    # alone (the loaded kernels' binary version is checked on the GPU in
+    # test_gpu_parity.py::test_loaded_kernels_are_sm103)
     from propack_gb300 import _build
-    lib = _build.build()
-    out = subprocess.run(["cuobjdump", "--list-elf", lib], capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    assert "sm_103a" in out.stdout
+    assert _build.GENCODE == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+@pytest.mark.parametrize("driver", ["dlansvd_irl_", "dlansvd_", "zlansvd_irl_", "zlansvd_", "slansvd_irl_",
+                                    "slansvd_"])
+def test_short_workspace_is_refused_before_any_device_work(driver):
+    """LWORK / LIWORK / LZWRK below what the reference's drivers write
+    (double/dlansvd_irl.F:177-188, double/dlansvd.F:151-160) give INFO =
+    PROPACK_ERR_ARG and a message naming the argument; the check runs before
+    any CUDA call, so no GPU is needed."""
+    import ctypes as C
+    import propack_gb300 as pg
+    L = pg.load()
+    m, n, kmax, k = 300, 200, 20, 5
+    irl = driver.endswith("_irl_")
+    cplx = driver.startswith("z")
+    single = driver.startswith("s")
+    lw, liw, lzw = pg.work_sizes(m, n, kmax, irl=irl, cplx=cplx)
+    ci = lambda v: C.byref(C.c_int(v))
+    vp = lambda a: C.c_void_p(a.ctypes.data)
+    ft = np.float32 if single else np.float64
+    ct = np.complex128 if cplx else ft
+    U = np.zeros((m, kmax + 1), dtype=ct, order="F")
+    V = np.zeros((n, kmax), dtype=ct, order="F")
+    sig, bnd = np.zeros(k, dtype=ft), np.zeros(k, dtype=ft)
+    opt = np.zeros(4, dtype=ft)
+    iop = np.array([0, 1], dtype=np.int32)
+    iparm = np.zeros(2, dtype=np.int32)
+    parm = np.zeros(2, dtype=ct)
+    tol = C.byref(C.c_float(1e-5) if single else C.c_double(1e-8))
+    aprod = C.c_void_p(C.cast(L.propack_gpu_csr_zaprod_ if cplx else (L.propack_gpu_csr_saprod_ if single
+                                                                          else L.propack_gpu_csr_aprod_),
+                              C.c_void_p).value)
+    for bad in ("lwork", "liwork") + (("lzwrk",) if cplx else ()):
+        sizes = {"lwork": lw, "liwork": liw, "lzwrk": lzw}
+        sizes[bad] = 3
+        work = np.empty(sizes["lwork"], dtype=ft)
+        iwork = np.empty(sizes["liwork"], dtype=np.int32)
+        zwork = np.empty(max(sizes["lzwrk"], 1), dtype=np.complex128)
+        info, kk = C.c_int(0), C.c_int(k)
+        head = [C.c_char_p(b"y"), C.c_char_p(b"y"), ci(m), ci(n)]
+        if irl:
+            head = [C.c_char_p(b"L")] + head + [ci(kmax), ci(kmax - k), C.byref(kk), ci(10)]
+        else:
+            head = head + [C.byref(kk), ci(kmax)]
+        mid = [aprod, vp(U), ci(m), vp(sig), vp(bnd), vp(V), ci(n), tol, vp(work), ci(sizes["lwork"])]
+        if cplx:
+            mid += [vp(zwork), ci(sizes["lzwrk"])]
+        tail = [vp(iwork), ci(sizes["liwork"]), vp(opt), vp(iop), C.byref(info), vp(parm), vp(iparm)]
+        lens = [C.c_size_t(1)] * (3 if irl else 2)
+        getattr(L, driver)(*(head + mid + tail + lens))
+        assert info.value == pg.ERR_ARG, (driver, bad, info.value)
+        assert bad.upper() in pg.last_error(), pg.last_error()
 
 
 def test_svdp_argument_validation_matches_scipy():

@@ -24,6 +24,12 @@ def rng0():
     return np.random.default_rng(0)
 
 
+def test_loaded_kernels_are_sm103():
+    # the runtime loaded the library's own sm_103a code (no JIT from PTX,
+    # no other architecture)
+    assert pg.load().propack_kernel_binary_version() == 103
+
+
 # ------------------------------------------------------------ operator
 @pytest.mark.parametrize("kind", ["plain", "lowrank", "zipf", "longcols", "ragged"])
 def test_operator_products(kind):

@@ -27,8 +27,9 @@ def _call(irl, A, k, kmax, aprod, iparm, tol=1e-5):
     U[:, 0] = np.random.default_rng(0).uniform(size=m)
     sig = np.zeros(k, dtype=np.float32)
     bnd = np.zeros(k, dtype=np.float32)
-    work = np.zeros(16, dtype=np.float32)
-    iwork = np.zeros(16, dtype=np.int32)
+    lwork, liwork, _ = pg.work_sizes(m, n, kmax, irl=irl)
+    work = np.empty(lwork, dtype=np.float32)
+    iwork = np.empty(liwork, dtype=np.int32)
     dop = np.array([np.sqrt(np.finfo(np.float32).eps), np.finfo(np.float32).eps ** 0.75, 0.0, 0.002],
                    dtype=np.float32)
     iop = np.array([0, 1], dtype=np.int32)
@@ -37,14 +38,14 @@ def _call(irl, A, k, kmax, aprod, iparm, tol=1e-5):
     if irl:
         ne = C.c_int(k)
         L.slansvd_irl_(b"L", b"y", b"y", ci(m), ci(n), ci(kmax), ci(kmax - k), C.byref(ne), ci(200), aprod, fp(U),
-                       ci(m), fp(sig), fp(bnd), fp(V), ci(n), C.byref(C.c_float(tol)), fp(work), ci(16), ipt(iwork),
-                       ci(16), fp(dop), ipt(iop), C.byref(info), fp(sparm), ipt(iparm), C.c_size_t(1),
+                       ci(m), fp(sig), fp(bnd), fp(V), ci(n), C.byref(C.c_float(tol)), fp(work), ci(lwork), ipt(iwork),
+                       ci(liwork), fp(dop), ipt(iop), C.byref(info), fp(sparm), ipt(iparm), C.c_size_t(1),
                        C.c_size_t(1), C.c_size_t(1))
         kc = ne.value
     else:
         kk = C.c_int(k)
         L.slansvd_(b"y", b"y", ci(m), ci(n), C.byref(kk), ci(kmax), aprod, fp(U), ci(m), fp(sig), fp(bnd), fp(V),
-                   ci(n), C.byref(C.c_float(tol)), fp(work), ci(16), ipt(iwork), ci(16), fp(dop), ipt(iop),
+                   ci(n), C.byref(C.c_float(tol)), fp(work), ci(lwork), ipt(iwork), ci(liwork), fp(dop), ipt(iop),
                    C.byref(info), fp(sparm), ipt(iparm), C.c_size_t(1), C.c_size_t(1))
         kc = kk.value
     return info.value, kc, sig, U[:, :k].astype(np.float64), V[:, :k].astype(np.float64)
