@@ -64,6 +64,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
+    "plain_lansvd": dict(
+        desc="2000x1000 CSR, 5 distinct uniform columns/row, N(0,1)*(1+i)^-0.5 values, "
+             "DLANSVD (non-restarted) k=10 kmax=200 tol=1e-12",
+        k=10, kmax=200, tol=1e-12, irl=False,
+        matvecs_full=None,
+    ),
     "lowrank_irl": dict(
         desc="2000000x500000 CSR 20nnz/row N(0,1) + rank-64 sparse factored term (w_i=100*0.9^i), "
              "DLANSVD_IRL k=50 dim=150 p=100 tol=1e-10",
@@ -123,7 +129,47 @@ def parse():
                     help="shrink m and n by this factor (profiling captures only; not a bench line)")
     ap.add_argument("--cgs-arith", default="planes", choices=["planes", "fp64", "f3"],
                     help="Gram-Schmidt arithmetic of the FP64 form (propack_set_cgs_arith)")
+    ap.add_argument("--no-other", action="store_true",
+                    help="skip the other configurations that the default headline run appends")
     return ap.parse_args()
+
+
+# The scope's other configurations, each run by this script in a process of
+# its own after the headline workload, its JSON line kept under
+# "other_configs": config[0] (the reference's CPU-runnable case), config[1]
+# at full size, and the batched config on a stated fraction of its 4096
+# problems (the whole batch takes minutes to generate and solve).  The
+# learned-start family (config[4]) stays opt-in: --workload learned.
+OTHER_CONFIGS = [
+    ("plain_lansvd", ["--steps", "20", "--warmup", "3", "--e2e-steps", "5"]),
+    ("lowrank_irl", ["--steps", "2", "--warmup", "1", "--e2e-steps", "1"]),
+    ("batched", ["--steps", "1", "--warmup", "1", "--scale", "0.25"]),
+]
+
+
+def run_other_configs(args):
+    out = {}
+    for name, extra in OTHER_CONFIGS:
+        cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", name, "--forms", "fp64", "--no-other",
+               "--cgs-arith", args.cgs_arith] + extra + (["--no-cpu"] if args.no_cpu else [])
+        t0 = time.perf_counter()
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        wall = time.perf_counter() - t0
+        line = None
+        for ln in reversed(r.stdout.splitlines()):
+            if ln.startswith("{"):
+                try:
+                    line = json.loads(ln)
+                    break
+                except ValueError:
+                    pass
+        if r.returncode != 0 or line is None:
+            out[name] = {"error": f"rc={r.returncode}: {(r.stderr or r.stdout)[-400:]}", "wall_s": wall}
+        else:
+            line.pop("kernel_breakdown", None)
+            line["wall_s"] = wall
+            out[name] = line
+    return out
 
 
 def dist_env():
@@ -159,9 +205,22 @@ def reduce_ranks(vals, op, world):
     return t.tolist()
 
 
+def metric_name(wl):
+    return (f"ms & matvecs to k={wl['k']} triplets at resid<=1e-8*||A||: chosen form vs plain FP64, 1 GB300")
+
+
+def config_of(args, wl):
+    """The workload as both arms name it (the same dict on both)."""
+    l2 = ("inputs larger than L2 (operator and Lanczos basis are GBs); no flush" if args.workload != "plain_lansvd"
+          else "inputs (2000x1000, 10k nonzeros) fit in L2; no flush: the reference's CPU-runnable case")
+    return {"workload": args.workload, "desc": wl["desc"], "scale": args.scale, "l2": l2}
+
+
 def make_workload(name, scale=1.0):
     """(S, L, R, w) with A = S + L diag(w) R' (L = R = w = None for plain CSR)."""
     from propack_gb300 import workloads
+    if name == "plain_lansvd":
+        return workloads.plain_lansvd(0), None, None, None
     if name == "lowrank_irl":
         return workloads.lowrank_irl(seed=1, m=int(2_000_000 * scale), n=int(500_000 * scale))
     if name == "zipf_mixed":
@@ -255,9 +314,14 @@ def cpu_sample(S, L, R, w, wl, cores, matvecs_full=None):
         op = oracle.Operator(S, L, R, w) if L is not None else oracle.Operator(S)
     oracle.clearstat()
     t0 = time.perf_counter()
-    u, s, vt, bnd, info, kc = oracle.svdp(None, wl["k"], irl_mode=True, kmax=wl["kmax"], tol=wl["tol"],
-                                          maxiter=1, rng=np.random.default_rng(0), op=op, compute_u=False,
-                                          compute_v=False)
+    # the Ritz vectors are formed whenever the sampled cycle converges (the
+    # GPU arm forms them too)
+    if wl.get("irl", True):
+        u, s, vt, bnd, info, kc = oracle.svdp(None, wl["k"], irl_mode=True, kmax=wl["kmax"], tol=wl["tol"],
+                                              maxiter=1, rng=np.random.default_rng(0), op=op)
+    else:
+        u, s, vt, bnd, info, kc = oracle.svdp(None, wl["k"], irl_mode=False, kmax=wl["kmax"], tol=wl["tol"],
+                                              rng=np.random.default_rng(0), op=op)
     dt = (time.perf_counter() - t0) * 1e3
     st = oracle.getstat()
     full = matvecs_full or wl["matvecs_full"] or st["nopx"]
@@ -305,7 +369,7 @@ def run_reference(args, wl):
     if rank != 0:
         return 0
     cores = os.cpu_count() or 1
-    if wl["matvecs_full"] is None:
+    if wl["matvecs_full"] is None and wl.get("irl", True):
         print(json.dumps({"impl": "reference", "unavailable": "matvec count of a full solve of this workload "
                           "not yet measured"}))
         return 0
@@ -326,15 +390,19 @@ def run_reference(args, wl):
                                 f"BLAS threads of the scipy build, single-threaded CSR products via a callback"}
     except Exception as e:  # scipy without _svdp: report why
         scipy_line = {"unavailable": f"{type(e).__name__}: {e}"}
-    sample = (f"oracle (C restatement of PROPACK dlansvd_irl, OpenMP) on {cores} host cores: one full IRL cycle "
-              f"(maxiter=1: {info['cycle_matvecs']} matvecs, {info['cycle_ms']:.0f} ms) of the same workload, "
-              f"scaled by matvecs to a full solve ({wl['matvecs_full']} matvecs)")
-    line = {"impl": "reference",
-            "metric": "ms & matvecs to k=50 triplets at resid<=1e-8*||A||: chosen form vs plain FP64, 1 GB300",
+    if wl.get("irl", True):
+        sample = (f"oracle (C restatement of PROPACK dlansvd_irl, OpenMP) on {cores} host cores: one full IRL "
+                  f"cycle (maxiter=1: {info['cycle_matvecs']} matvecs, {info['cycle_ms']:.0f} ms; Ritz vectors "
+                  f"formed when the cycle converges, as on the GPU) of the same workload, scaled by matvecs to a "
+                  f"full solve ({info['matvecs_full']} matvecs)")
+    else:
+        sample = (f"oracle (C restatement of PROPACK dlansvd, OpenMP) on {cores} host cores: the whole solve "
+                  f"({info['cycle_matvecs']} matvecs, Ritz vectors included)")
+    line = {"impl": "reference", "metric": metric_name(wl),
             "value": value, "unit": "ms", "higher_is_better": False, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": args.workload, "desc": wl["desc"]},
+            "config": config_of(args, wl),
             "cpu_baseline": {"value": value, "unit": "ms", "cores": cores, "kind": "port", "sample": sample},
             "scipy_propack": scipy_line,
             "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -368,15 +436,23 @@ def run_ours(args, wl):
     maxiter = 1000 if args.scale == 1.0 else 20
     dop0 = [np.sqrt(np.finfo(float).eps), np.finfo(float).eps ** 0.75, 0.0, 0.002]  # scipy's defaults
 
+    irl = wl.get("irl", True)
+
+    def driver(aprod, iparm, u, sig, bnd, v):
+        """dlansvd_irl_ (or dlansvd_ for the non-restarted workload) through the C ABI."""
+        iop = np.array([0, 1], dtype=np.int32)
+        if irl:
+            return pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, aprod, u, sig, bnd, v, tol,
+                                 np.array(dop0), iop, iparm=iparm)
+        return pg.lansvd(b"y", b"y", m, n, k, kmax, aprod, u, sig, bnd, v, tol, np.array(dop0[:3]), iop,
+                         iparm=iparm)
+
     def solve(op, u0=None):
         u = np.zeros((m, kmax + 1), order="F")
         v = np.zeros((n, kmax), order="F")
         sig, bnd = np.zeros(k), np.zeros(k)
         u[:, 0] = np.random.default_rng(0).uniform(size=m) if u0 is None else u0
-        dop = np.array(dop0)
-        iop = np.array([0, 1], dtype=np.int32)
-        kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, op.aprod, u, sig, bnd, v, tol,
-                                 dop, iop, iparm=op.iparm)
+        kc, info = driver(op.aprod, op.iparm, u, sig, bnd, v)
         return kc, info, sig, u, v
 
     op = pg.CsrOperator(S, L, R, w)
@@ -439,41 +515,55 @@ def run_ours(args, wl):
     lib = pg.load()
     import ctypes as C
     nul64, nul32, nuld = C.POINTER(C.c_int64)(), C.POINTER(C.c_int)(), C.POINTER(C.c_double)()
+    def e2e_run(parts, hw, u_host, v_host, steps):
+        """create + driver call + destroy through the C ABI from host arrays;
+        mean ms per step and its phases"""
+        ph = {"create": 0.0, "solve_call": 0.0, "solve_device": 0.0, "destroy": 0.0}
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ta = time.perf_counter()
+            h = C.c_int64(0)
+            sp_, si, sv = parts["S"]
+            if r:
+                (lp, li, lv), (rp, ri, rv) = parts["L"], parts["R"]
+                rc = lib.propack_csr_create(m, n, pg._i64p(sp_), pg._ip(si), pg._dp(sv), r, pg._i64p(lp),
+                                            pg._ip(li), pg._dp(lv), pg._i64p(rp), pg._ip(ri), pg._dp(rv), pg._dp(hw),
+                                            C.byref(h))
+            else:
+                rc = lib.propack_csr_create(m, n, pg._i64p(sp_), pg._ip(si), pg._dp(sv), 0, nul64, nul32, nuld,
+                                            nul64, nul32, nuld, nuld, C.byref(h))
+            assert rc == 0, pg.last_error()
+            tb = time.perf_counter()
+            iparm = np.array([h.value & 0xFFFFFFFF, (h.value >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
+            aprod = C.cast(lib.propack_gpu_csr_aprod_, pg.APROD)
+            u_host[:, 0] = u0
+            sig, bnd = np.zeros(k), np.zeros(k)
+            kc, info = driver(aprod, iparm, u_host, sig, bnd, v_host)
+            tc = time.perf_counter()
+            if args.scale == 1.0:
+                assert info == 0 and kc == k
+            ph["solve_device"] += pg.get_stats()["solve_ms"]
+            lib.propack_csr_destroy(h.value)
+            td = time.perf_counter()
+            ph["create"] += (tb - ta) * 1e3
+            ph["solve_call"] += (tc - tb) * 1e3
+            ph["destroy"] += (td - tc) * 1e3
+        return (time.perf_counter() - t0) * 1e3 / steps, {kk: v / steps for kk, v in ph.items()}
+
     barrier()
-    phases = {"create": 0.0, "solve_call": 0.0, "solve_device": 0.0, "destroy": 0.0}
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        ta = time.perf_counter()
-        h = C.c_int64(0)
-        sp_, si, sv = h_parts["S"]
-        if r:
-            (lp, li, lv), (rp, ri, rv) = h_parts["L"], h_parts["R"]
-            rc = lib.propack_csr_create(m, n, pg._i64p(sp_), pg._ip(si), pg._dp(sv), r, pg._i64p(lp), pg._ip(li),
-                                        pg._dp(lv), pg._i64p(rp), pg._ip(ri), pg._dp(rv), pg._dp(h_w), C.byref(h))
-        else:
-            rc = lib.propack_csr_create(m, n, pg._i64p(sp_), pg._ip(si), pg._dp(sv), 0, nul64, nul32, nuld, nul64,
-                                        nul32, nuld, nuld, C.byref(h))
-        assert rc == 0, pg.last_error()
-        tb = time.perf_counter()
-        iparm = np.array([h.value & 0xFFFFFFFF, (h.value >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
-        aprod = C.cast(lib.propack_gpu_csr_aprod_, pg.APROD)
-        u_pin[:, 0] = u0
-        sig, bnd = np.zeros(k), np.zeros(k)
-        dop = np.array(dop0)
-        iop = np.array([0, 1], dtype=np.int32)
-        kc, info = pg.lansvd_irl(b"L", b"y", b"y", m, n, kmax, kmax - k, k, maxiter, aprod, u_pin, sig, bnd, v_pin,
-                                 tol, dop, iop, iparm=iparm)
-        tc = time.perf_counter()
-        if args.scale == 1.0:
-            assert info == 0 and kc == k
-        phases["solve_device"] += pg.get_stats()["solve_ms"]
-        lib.propack_csr_destroy(h.value)
-        td = time.perf_counter()
-        phases["create"] += (tb - ta) * 1e3
-        phases["solve_call"] += (tc - tb) * 1e3
-        phases["destroy"] += (td - tc) * 1e3
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
-    phases = {kk: v / e2e_steps for kk, v in phases.items()}
+    e2e_ms, phases = e2e_run(h_parts, h_w, u_pin, v_pin, e2e_steps)
+    # the same with ordinary (pageable) host arrays, as a Fortran or numpy
+    # caller has them: allocated once, pages touched by one untimed call
+    pg_parts = {}
+    for nm, M in (("S", S), ("L", L), ("R", R)):
+        if M is not None:
+            M = sp.csr_array(M)
+            pg_parts[nm] = (np.ascontiguousarray(M.indptr, dtype=np.int64),
+                            np.ascontiguousarray(M.indices, dtype=np.int32), np.ascontiguousarray(M.data))
+    u_pg, v_pg = np.zeros((m, kmax + 1), order="F"), np.zeros((n, kmax), order="F")
+    e2e_run(pg_parts, w, u_pg, v_pg, 1)
+    e2e_pg_ms, phases_pg = e2e_run(pg_parts, w, u_pg, v_pg, e2e_steps)
+    del u_pg, v_pg
     barrier()
     pg.set_precision("fp64")
     h2d = sum(a.nbytes for t in h_parts.values() for a in t) + (h_w.nbytes if h_w is not None else 0) + m * 8
@@ -547,21 +637,24 @@ def run_ours(args, wl):
             if f != "fp64":
                 s1, s2 = results["fp64"]["sigma"], results[f]["sigma"]
                 sig_err[f] = float(np.max(np.abs(s1 - s2) / s1))
-    line = {"metric": "ms & matvecs to k=50 triplets at resid<=1e-8*||A||: chosen form vs plain FP64, 1 GB300",
+    line = {"metric": metric_name(wl),
             "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 vectors + f64 scalars" if chosen == "mixed" else "f64",
             "data": "synthetic (seeded numpy default_rng)",
-            "config": {"workload": args.workload, "desc": wl["desc"], "chosen_form": chosen, "scale": args.scale,
-                       "l2": "inputs larger than L2 (operator and Lanczos basis are GBs); no flush"},
+            "config": config_of(args, wl), "chosen_form": chosen,
             "matvecs": results[chosen]["matvecs"], "cgs_arith": args.cgs_arith, "forms": forms_out,
             "speedup_vs_plain_fp64": {f: per["fp64"] / per[f] for f in forms} if "fp64" in per else None,
             "max_rel_sigma_diff_vs_fp64": sig_err,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "phases_ms": phases},
+                    "phases_ms": phases, "host_buffers": "pinned",
+                    "pageable": {"value": e2e_pg_ms, "unit": "ms", "phases_ms": phases_pg,
+                                 "host_buffers": "ordinary numpy arrays (CSR inputs, U and V), allocated once"}},
             "gpu_launches": int(sum(results[f]["launches"] for f in forms)), "roofline": dominant,
             "rooflines": {"spmv_pair": roof, "gram_schmidt": roof_cgs},
             "cpu_baseline": cpu, "clocks": clocks, "kernel_breakdown": breakdown}
+    if (not args.no_other and args.workload == "zipf_mixed" and args.scale == 1.0 and world == 1):
+        line["other_configs"] = run_other_configs(args)
     print(json.dumps(line))
     return 0
 

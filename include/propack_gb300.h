@@ -128,8 +128,18 @@ void propack_gpu_csr_aprod_(const char *transa, const int *m, const int *n,
  * the GPU (different streams, different host threads) race and must be
  * serialised by the caller.  The first call on each device looks up the
  * array's device address (no allocation); make that first call before
- * any stream capture.  No counterpart exists in the reference.
- * Returns 0 or a negative PROPACK_ERR_* code. */
+ * any stream capture.  That first call (on each device, and the first on
+ * each host thread) may also make the CUDA runtime load the library's
+ * kernels onto the device (lazy module loading), which takes device
+ * memory: callers should make one warm-up call before the section that
+ * must not allocate.  x and y must be memory the operator's device can
+ * address (device memory of that device, managed memory, or mapped host
+ * memory); anything else is refused with PROPACK_ERR_ARG before any
+ * launch.  A complex operator (propack_zcsr_create) is applied in its
+ * real 2x2-block form: x holds n (trans: m) complex entries as
+ * interleaved (re, im) doubles, 2n doubles, and y receives 2m (trans:
+ * 2n) doubles; trans != 0 applies A^H.  No counterpart exists in the
+ * reference.  Returns 0 or a negative PROPACK_ERR_* code. */
 #define PROPACK_NOALLOC_MAX_DOUBLES 65536
 int propack_csr_apply_noalloc(int64_t handle, int trans, const double *x,
                               double *y, void *stream);
@@ -359,6 +369,7 @@ typedef struct {
 } propack_batch_stats_t;
 int propack_batch_get_stats(propack_batch_stats_t *out);
 
+
 /* ---- FP64 product on the tensor cores --------------------------------
  * C (mr x nc, column-major ldc) = A (mr x kk, column-major lda) op(B), with
  * op(B)(l, j) = B[j * ldb + l] (tb = 0) or B[l * ldb + j] (tb = 1); all
@@ -374,7 +385,10 @@ int propack_gemm_f64_tc(int impl, int mr, int nc, int kk, const double *A, int l
 /* Device memory of the library's operators and solves comes from its own
  * stream-ordered pool, which keeps freed memory for the next call instead
  * of returning it to the driver (repeated solves skip the mapping of GBs
- * of device memory).  This returns all of it that is not in use.
+ * of device memory).  This returns all of it that is not in use, and frees
+ * the idle pinned host buffers through which results are copied into
+ * pageable (ordinary) host arrays (two 64 MiB halves per copy that ran
+ * concurrently; kept between calls for the same reason).
  * Returns 0 or PROPACK_ERR_CUDA. */
 int propack_release_memory(void);
 

@@ -403,6 +403,7 @@ const Dev &device_info();
 // for mapping GBs of device memory each time; propack_release_memory()
 // gives it back.
 cudaMemPool_t lib_pool();
+void release_bounce_buffers();  // the idle pinned bounce buffers of pageable result copies
 void *pool_alloc(size_t bytes, cudaStream_t s);  // zero bytes allowed; never returns null
 inline void pool_free(void *p, cudaStream_t s)
 {

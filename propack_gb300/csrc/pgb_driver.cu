@@ -14,6 +14,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -846,6 +850,215 @@ static thread_local int g_precision = 0;
 constexpr double EPS32 = 5.9604644775390625e-08;
 constexpr double MIXED_TOL = 1e-6;  // convergence level of the FP32 phase
 
+// ---------------------------------------- results to pageable host memory
+// A caller's U and V are often ordinary (pageable) arrays: a Fortran
+// program's arrays, numpy's.  A device-to-pageable cudaMemcpy goes through
+// the driver's own staging and the first touch of each destination page on
+// one thread; here such copies go through a pinned bounce buffer of two
+// BOUNCE_BYTES halves instead: one cudaMemcpy2DAsync per chunk of whole
+// columns into one half while host threads copy the previous chunk out of
+// the other half in parallel.
+
+// A small pool of host threads for the copies out of the bounce buffer.
+class HostPool {
+public:
+    static HostPool &get()
+    {
+        static HostPool p;
+        return p;
+    }
+    // run f(i) for i in [0, n) on the pool and the calling thread; returns
+    // when all are done (one job at a time: concurrent callers take turns)
+    void run(int n, const std::function<void(int)> &f)
+    {
+        if (n <= 1 || workers_.empty()) {
+            for (int i = 0; i < n; i++) f(i);
+            return;
+        }
+        std::lock_guard<std::mutex> one(run_mu_);
+        std::unique_lock<std::mutex> lk(mu_);
+        job_ = &f;
+        njob_ = n;
+        next_ = 0;
+        done_ = 0;
+        ++gen_;
+        cv_.notify_all();
+        lk.unlock();
+        work();
+        lk.lock();
+        done_cv_.wait(lk, [&] { return done_ == njob_; });
+        job_ = nullptr;
+    }
+    int threads() const { return (int)workers_.size() + 1; }
+
+private:
+    HostPool()
+    {
+        const unsigned hc = std::thread::hardware_concurrency();
+        const int nt = (int)std::min(16u, std::max(1u, hc)) - 1;
+        for (int i = 0; i < nt; i++) workers_.emplace_back([this] { loop(); });
+    }
+    ~HostPool()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+            cv_.notify_all();
+        }
+        for (auto &t : workers_) t.join();
+    }
+    void work()
+    {
+        for (;;) {
+            int i;
+            const std::function<void(int)> *f;
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                if (!job_ || next_ >= njob_) return;
+                i = next_++;
+                f = job_;
+            }
+            (*f)(i);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (++done_ == njob_) done_cv_.notify_all();
+        }
+    }
+    void loop()
+    {
+        long long seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+            }
+            work();
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(int)> *job_ = nullptr;
+    int njob_ = 0, next_ = 0, done_ = 0;
+    long long gen_ = 0;
+    bool stop_ = false;
+};
+
+constexpr size_t BOUNCE_BYTES = (size_t)64 << 20;
+
+// bounce buffers (two halves of BOUNCE_BYTES, pinned) and their events,
+// kept in a process-wide free list: a copy takes one for its duration, so
+// there are as many as copies ever ran at once; propack_release_memory()
+// frees the idle ones
+struct Bounce {
+    char *buf = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+static std::mutex g_bounce_mu;
+static std::vector<Bounce> g_bounce_free;
+struct BounceLease {
+    Bounce b;
+    BounceLease()
+    {
+        {
+            std::lock_guard<std::mutex> lk(g_bounce_mu);
+            if (!g_bounce_free.empty()) {
+                b = g_bounce_free.back();
+                g_bounce_free.pop_back();
+                return;
+            }
+        }
+        PGB_CUDA(cudaMallocHost(&b.buf, 2 * BOUNCE_BYTES));
+        for (cudaEvent_t &e : b.ev) PGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    ~BounceLease()
+    {
+        std::lock_guard<std::mutex> lk(g_bounce_mu);
+        g_bounce_free.push_back(b);
+    }
+};
+void release_bounce_buffers()
+{
+    std::lock_guard<std::mutex> lk(g_bounce_mu);
+    for (Bounce &b : g_bounce_free) {
+        cudaFreeHost(b.buf);
+        for (cudaEvent_t e : b.ev) cudaEventDestroy(e);
+    }
+    g_bounce_free.clear();
+}
+
+// host memory the GPU's copy engines can reach directly (page-locked or
+// registered, or managed)
+static bool host_pinned(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type != cudaMemoryTypeUnregistered;
+}
+
+// ncols columns of `colbytes` bytes from device src (pitch spitch) to host
+// dst (pitch dpitch): straight when dst is pinned, through the bounce
+// buffer otherwise
+static void d2h_columns(char *dst, size_t dpitch, const char *src, size_t spitch, size_t colbytes, int ncols,
+                        cudaStream_t s)
+{
+    if (ncols <= 0 || colbytes == 0) return;
+    if (host_pinned(dst)) {
+        PGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, colbytes, ncols, cudaMemcpyDeviceToHost, s));
+        return;
+    }
+    BounceLease lease;
+    Bounce &b = lease.b;
+    HostPool &pool = HostPool::get();
+    // pieces: whole columns per chunk, or slices of one column when a column exceeds a half
+    struct Piece {
+        int c0, nc;
+        size_t off, bytes;  // within the column (nc == 1 slices) or whole columns
+    };
+    std::vector<Piece> pieces;
+    if (colbytes <= BOUNCE_BYTES) {
+        const int per = (int)std::max<size_t>(1, BOUNCE_BYTES / colbytes);
+        for (int c0 = 0; c0 < ncols; c0 += per) pieces.push_back({c0, std::min(per, ncols - c0), 0, colbytes});
+    } else {
+        for (int c = 0; c < ncols; c++)
+            for (size_t off = 0; off < colbytes; off += BOUNCE_BYTES)
+                pieces.push_back({c, 1, off, std::min(BOUNCE_BYTES, colbytes - off)});
+    }
+    auto issue = [&](size_t i) {
+        const Piece &p = pieces[i];
+        char *half = b.buf + (i & 1) * BOUNCE_BYTES;
+        PGB_CUDA(cudaMemcpy2DAsync(half, p.bytes, src + (size_t)p.c0 * spitch + p.off, spitch, p.bytes, p.nc,
+                                   cudaMemcpyDeviceToHost, s));
+        PGB_CUDA(cudaEventRecord(b.ev[i & 1], s));
+    };
+    auto drain = [&](size_t i) {
+        const Piece &p = pieces[i];
+        PGB_CUDA(cudaEventSynchronize(b.ev[i & 1]));
+        const char *half = b.buf + (i & 1) * BOUNCE_BYTES;
+        const size_t total = p.bytes * p.nc;
+        const int parts = (int)std::min<size_t>((size_t)pool.threads() * 2, std::max<size_t>(1, total >> 20));
+        const size_t step = (total + parts - 1) / parts;
+        pool.run(parts, [&](int q) {
+            size_t a = (size_t)q * step, e = std::min(total, a + step);
+            while (a < e) {
+                const size_t col = a / p.bytes, within = a % p.bytes;
+                const size_t len = std::min(e - a, p.bytes - within);
+                memcpy(dst + (p.c0 + col) * dpitch + p.off + within, half + a, len);
+                a += len;
+            }
+        });
+    };
+    issue(0);
+    for (size_t i = 0; i < pieces.size(); i++) {
+        if (i + 1 < pieces.size()) issue(i + 1);  // the other half is free: piece i-1 was drained
+        drain(i);
+    }
+}
+
 template <typename T>
 static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, bool du, bool dv)
 {
@@ -866,13 +1079,11 @@ static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, 
         }
         return;
     } else {
-    // FP64 or complex*16 (sizeof(T) = 16) bases straight into the caller's arrays
+    // FP64 or complex*16 (sizeof(T) = 16) bases into the caller's arrays
     if (du)
-        PGB_CUDA(cudaMemcpy2DAsync(U, sizeof(T) * ldu, c.U, sizeof(T) * c.ldu, sizeof(T) * c.m, ncols,
-                                   cudaMemcpyDeviceToHost, c.s));
+        d2h_columns((char *)U, sizeof(T) * ldu, (const char *)c.U, sizeof(T) * c.ldu, sizeof(T) * c.m, ncols, c.s);
     if (dv)
-        PGB_CUDA(cudaMemcpy2DAsync(V, sizeof(T) * ldv, c.V, sizeof(T) * c.ldv, sizeof(T) * c.n, ncols,
-                                   cudaMemcpyDeviceToHost, c.s));
+        d2h_columns((char *)V, sizeof(T) * ldv, (const char *)c.V, sizeof(T) * c.ldv, sizeof(T) * c.n, ncols, c.s);
     }
 }
 

@@ -1590,11 +1590,13 @@ static void launch_zcgs_pass(const LbArgs &a, int j, int last, cudaStream_t s)
 template <int SIDE, typename T, int SHORT>
 static int spmv_grid(int nb)
 {
-    static thread_local int g = 0;
-    if (g == 0) {
+    static thread_local int g = 0, dev = -1;
+    const Dev &d = device_info();
+    if (g == 0 || dev != d.device) {
         int per = 0;
         PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lb_spmv<SIDE, T, SHORT>, BS, 0));
-        g = std::max(1, per) * device_info().sms;
+        g = std::max(1, per) * d.sms;
+        dev = d.device;
     }
     return std::min(g, nb);
 }

@@ -81,6 +81,24 @@ static double *scratch_address(int dev)
     return g_scratch_addr[dev];
 }
 
+// a pointer the kernels may dereference on device `dev`: device memory of
+// that device, managed memory, or host memory mapped for it (its
+// devicePointer is the pointer itself).  cudaPointerGetAttributes
+// allocates nothing; a plain host pointer is refused here instead of
+// faulting in a kernel.
+static bool usable_on(const void *p, int dev)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (at.type == cudaMemoryTypeManaged) return true;
+    if (at.type == cudaMemoryTypeDevice) return at.device == dev;
+    if (at.type == cudaMemoryTypeHost) return at.devicePointer == p;
+    return false;
+}
+
 static int apply_noalloc(int64_t handle, int trans, const double *x, double *y, cudaStream_t s)
 {
     const Operator *op = lookup_operator(handle);
@@ -96,6 +114,10 @@ static int apply_noalloc(int64_t handle, int trans, const double *x, double *y, 
     PGB_CUDA(cudaGetDevice(&dev));
     if (dev != op->device) {
         set_error("propack_csr_apply_noalloc: the operator lives on another device than the current one");
+        return PROPACK_ERR_ARG;
+    }
+    if (!usable_on(x, dev) || !usable_on(y, dev)) {
+        set_error("propack_csr_apply_noalloc: x and y must be device (or managed) memory of the operator's device");
         return PROPACK_ERR_ARG;
     }
     double *base = scratch_address(dev);

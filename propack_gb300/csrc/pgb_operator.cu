@@ -573,14 +573,18 @@ __global__ void __launch_bounds__(BS) k_spmv_plain(Csr A, const T *__restrict__ 
 }
 
 // one wave of CTAs at the kernel's occupancy
+// (cached per host thread for the current device; recomputed when the
+// thread moves to another device)
 template <typename T>
 static int spmv_plain_grid()
 {
-    static thread_local int g = 0;
-    if (g == 0) {
+    static thread_local int g = 0, dev = -1;
+    const Dev &d = device_info();
+    if (g == 0 || dev != d.device) {
         int per = 0;
         PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv_plain<T>, BS, 0));
-        g = std::max(1, per) * device_info().sms;
+        g = std::max(1, per) * d.sms;
+        dev = d.device;
     }
     return g;
 }
@@ -973,6 +977,7 @@ extern "C" int propack_release_memory(void)
     try {
         PGB_CUDA(cudaDeviceSynchronize());
         PGB_CUDA(cudaMemPoolTrimTo(lib_pool(), 0));
+        release_bounce_buffers();
     } catch (const CudaFailure &) {
         return PROPACK_ERR_CUDA;
     }

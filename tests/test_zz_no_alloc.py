@@ -47,6 +47,74 @@ def test_noalloc_matches_allocating_entry_point_twice():
     op.close()
 
 
+def test_noalloc_takes_no_device_memory_after_warm_up():
+    # the property the entry point exists for: once a first call has loaded
+    # the kernels and looked up the scratch address, further calls leave the
+    # device's free memory and torch's allocator untouched
+    torch = pytest.importorskip("torch")
+    lib = pg.load()
+    S, L, R, w = workloads.lowrank_irl(seed=22, m=20000, n=6000, nnz_row=10, rank=8, udens=0.05, vdens=0.1)
+    op = pg.CsrOperator(S, L, R, w)
+    m, n = op.shape
+    xd = torch.ones(n, dtype=torch.float64, device="cuda")
+    yd = torch.zeros(m, dtype=torch.float64, device="cuda")
+    assert _noalloc(lib, op.handle, 0, xd.data_ptr(), yd.data_ptr()) == 0, pg.last_error()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    alloc0 = torch.cuda.memory_stats().get("allocated_bytes.all.current", 0)
+    for _ in range(3):
+        assert _noalloc(lib, op.handle, 0, xd.data_ptr(), yd.data_ptr()) == 0, pg.last_error()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_stats().get("allocated_bytes.all.current", 0) == alloc0
+    np.testing.assert_allclose(yd.cpu().numpy(), op.matvec(np.ones(n)), rtol=1e-12, atol=1e-12)
+    op.close()
+
+
+def test_noalloc_refuses_host_pointers():
+    # a host buffer passed by mistake is refused (cudaPointerGetAttributes,
+    # before any launch) instead of faulting in a kernel
+    torch = pytest.importorskip("torch")
+    lib = pg.load()
+    S, L, R, w = workloads.lowrank_irl(seed=23, m=3000, n=1000, nnz_row=6, rank=4, udens=0.05, vdens=0.1)
+    op = pg.CsrOperator(S, L, R, w)
+    m, n = op.shape
+    xh = np.ones(n)
+    yd = torch.zeros(m, dtype=torch.float64, device="cuda")
+    rc = _noalloc(lib, op.handle, 0, xh.ctypes.data, yd.data_ptr())
+    assert rc == pg.ERR_ARG and "device" in pg.last_error()
+    xd = torch.ones(n, dtype=torch.float64, device="cuda")
+    yh = np.zeros(m)
+    assert _noalloc(lib, op.handle, 0, xd.data_ptr(), yh.ctypes.data) == pg.ERR_ARG
+    op.close()
+
+
+def test_noalloc_complex_operator_in_block_form():
+    # a complex operator takes interleaved (re, im) doubles and applies A
+    # (trans 0) or A^H (trans 1), twice in a row
+    torch = pytest.importorskip("torch")
+    import scipy.sparse as sp
+    lib = pg.load()
+    rng = np.random.default_rng(7)
+    m, n, k = 700, 500, 6
+    rows = np.repeat(np.arange(m), k)
+    A = sp.csr_array((rng.standard_normal(m * k) + 1j * rng.standard_normal(m * k),
+                      (rows, rng.integers(0, n, m * k))), shape=(m, n))
+    op = pg.CsrOperator(A)
+    for call in range(2):
+        for trans in (0, 1):
+            x = rng.standard_normal(m if trans else n) + 1j * rng.standard_normal(m if trans else n)
+            ref = A.conj().T @ x if trans else A @ x
+            xd = torch.tensor(x.view(np.float64), dtype=torch.float64, device="cuda")
+            yd = torch.full((2 * (n if trans else m),), np.nan, dtype=torch.float64, device="cuda")
+            assert _noalloc(lib, op.handle, trans, xd.data_ptr(), yd.data_ptr()) == 0, pg.last_error()
+            torch.cuda.synchronize()
+            got = yd.cpu().numpy().view(np.complex128)
+            np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max(),
+                                       err_msg=f"call {call}, trans {trans}")
+    op.close()
+
+
 def test_noalloc_rejects_scratch_beyond_the_limit():
     torch = pytest.importorskip("torch")
     import scipy.sparse as sp
