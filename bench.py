@@ -689,8 +689,10 @@ def run_batched(args, wl):
     mtot = sum(A.shape[0] for A in all_mats)
     ntot = sum(A.shape[1] for A in all_mats)
     B = batch.Batch(mats)
-    for _ in range(args.warmup):
-        B.solve(k, kmax=kmax, tol=tol, maxiter=100, u0=u0, vectors=False)
+    tune_ms = 0.0
+    for _ in range(max(1, args.warmup)):
+        B.solve(k, kmax=kmax, tol=tol, maxiter=100, u0=u0, vectors=False)  # the first solve runs the autotuner
+        tune_ms += B.stats["tune_ms"]
     sampler = ClockSampler(0)
     sampler.start()
     dev, stats_l, info = [], [], None
@@ -699,6 +701,12 @@ def run_batched(args, wl):
         dev.append(B.stats["device_ms"])
         stats_l.append(B.stats)
     clocks = sampler.stop()
+    table = B.tuning()
+    # the same batch with one configuration for every problem (row split 1,
+    # projection tile 1: the kernel before the autotuner), for comparison
+    B.set_tuning([1] * batch.NCLASS, [1] * batch.NCLASS)
+    B.solve(k, kmax=kmax, tol=tol, maxiter=100, u0=u0, vectors=False)
+    one_shape_ms = B.stats["device_ms"]
     B.close()
     value = statistics.mean(dev)
     st = stats_l[-1]
@@ -733,6 +741,8 @@ def run_batched(args, wl):
             "config": {"workload": "batched", "desc": wl["desc"], "nprob": nprob, "nnz": int(nnz),
                        "fraction_of_4096": nprob / 4096, "l2": "batch data (GBs) larger than L2; no flush"},
             "problems_per_s": nprob / (value * 1e-3), "converged": conv, "matvecs": st["nopx"],
+            "autotuner": {"table": table, "tune_ms": tune_ms, "one_shape_ms": one_shape_ms,
+                          "speedup_vs_one_shape": one_shape_ms / value},
             "cycles": st["cycles"], "persistent_grid": st["grid"],
             "e2e": {"value": e2e_ms, "unit": "ms",
                     "h2d_bytes_per_step": int(nnz * 8 + (mtot + nprob) * 4 + mtot * 8),

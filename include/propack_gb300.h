@@ -366,9 +366,30 @@ typedef struct {
     int64_t cycles;          /* CUDA-graph replays of the restart cycle */
     int64_t grid;            /* CTAs of the persistent kernel */
     int64_t kernel_launches;
+    double tune_ms;          /* host ms of the autotuner in this call (0: the batch was tuned before) */
 } propack_batch_stats_t;
 int propack_batch_get_stats(propack_batch_stats_t *out);
 
+/* The batched kernel's autotuner.  The problems fall into
+ * PROPACK_BATCH_CLASSES size classes (quarters of the batch by decreasing
+ * nonzeros + 8 (m + n)).  Before the first solve of a batch, every
+ * candidate pair (g, dc) -- g lanes per row in the sparse products (1, 4, 8
+ * or 32: the row split), dc columns per warp in the Gram-Schmidt
+ * projections (1, 2 or 4: the tile) -- is timed on a sample of each class
+ * (one CTA per sampled problem: both products and one set of projections,
+ * CUDA events), and the fastest is kept; the defaults (1, 1) stay unless a
+ * candidate is more than 3 % faster.  dc does not change any result; g
+ * changes the summation order of the products (results differ at rounding
+ * level between choices), so a caller who needs the same bits across
+ * batches pins the table with propack_batch_set_tuning.
+ * propack_batch_get_tuning writes per class g, dc and the probe's ms with
+ * them and with (1, 1) (0 when the table was set by the caller) and returns
+ * 0 (not tuned yet), 1 (timed) or 2 (set by the caller), or
+ * PROPACK_ERR_HANDLE.  propack_batch_set_tuning(h, NULL, NULL) asks for a
+ * new timing at the next solve.  No reference counterpart. */
+#define PROPACK_BATCH_CLASSES 4
+int propack_batch_get_tuning(int64_t handle, int *g, int *dc, float *ms_tuned, float *ms_default);
+int propack_batch_set_tuning(int64_t handle, const int *g, const int *dc);
 
 /* ---- FP64 product on the tensor cores --------------------------------
  * C (mr x nc, column-major ldc) = A (mr x kk, column-major lda) op(B), with

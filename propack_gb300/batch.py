@@ -24,7 +24,9 @@ _fp = C.POINTER(C.c_float)
 class BatchStats(C.Structure):
     _fields_ = [("nopx", C.c_int64), ("nreorth", C.c_int64), ("converged", C.c_int64), ("fallback", C.c_int64),
                 ("device_ms", C.c_double), ("cycles", C.c_int64), ("grid", C.c_int64),
-                ("kernel_launches", C.c_int64)]
+                ("kernel_launches", C.c_int64), ("tune_ms", C.c_double)]
+
+NCLASS = 4  # PROPACK_BATCH_CLASSES: size classes of the autotuner
 
 
 def _lib():
@@ -35,6 +37,8 @@ def _lib():
         L.propack_batch_solve.argtypes = [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, _ip,
                                           _dp, _dp]
         L.propack_batch_get_stats.argtypes = [C.POINTER(BatchStats)]
+        L.propack_batch_get_tuning.argtypes = [C.c_int64, _ip, _ip, _fp, _fp]
+        L.propack_batch_set_tuning.argtypes = [C.c_int64, _ip, _ip]
         L._batch_bound = True
     return L
 
@@ -62,6 +66,33 @@ class Batch:
         if rc != 0:
             raise PropackError(f"propack_batch_create failed ({rc}): {last_error()}")
         self.handle = h.value
+
+    def tuning(self):
+        """The autotuner's table: per size class (quarters of the batch by
+        decreasing size) the SpMV row split g, the projection tile dc and the
+        probe's ms with them and with (1, 1); state 0 untuned, 1 timed, 2 set."""
+        g = np.zeros(NCLASS, dtype=np.int32)
+        dc = np.zeros(NCLASS, dtype=np.int32)
+        mt = np.zeros(NCLASS, dtype=np.float32)
+        md = np.zeros(NCLASS, dtype=np.float32)
+        st = self._L.propack_batch_get_tuning(self.handle, g.ctypes.data_as(_ip), dc.ctypes.data_as(_ip),
+                                              mt.ctypes.data_as(_fp), md.ctypes.data_as(_fp))
+        if st < 0:
+            raise PropackError(f"propack_batch_get_tuning failed ({st}): {last_error()}")
+        return {"state": st, "g": g.tolist(), "dc": dc.tolist(), "probe_ms": mt.tolist(),
+                "probe_ms_default": md.tolist()}
+
+    def set_tuning(self, g=None, dc=None):
+        """Pin the table (lists of NCLASS values), or with no arguments ask
+        for a new timing at the next solve."""
+        if g is None or dc is None:
+            rc = self._L.propack_batch_set_tuning(self.handle, None, None)
+        else:
+            ga = np.ascontiguousarray(g, dtype=np.int32)
+            da = np.ascontiguousarray(dc, dtype=np.int32)
+            rc = self._L.propack_batch_set_tuning(self.handle, ga.ctypes.data_as(_ip), da.ctypes.data_as(_ip))
+        if rc != 0:
+            raise PropackError(f"propack_batch_set_tuning failed ({rc}): {last_error()}")
 
     def close(self):
         if self.handle:

@@ -20,6 +20,7 @@
 // with a fresh random vector, dgetu0.F) is marked for the single-problem
 // driver.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -56,6 +57,8 @@ struct BProb {
     double *sig, *bnd;        // neig each (outputs)
     double rnorm, anorm;
     int k0, iter, status, nconv, nopx, nreorth;
+    int g;    // SpMV row split: lanes per row (1, 4, 8 or 32), chosen by the autotuner
+    int dc;   // Gram-Schmidt projections: columns per warp (1, 2 or 4), chosen by the autotuner
 };
 
 struct BCfg {
@@ -124,44 +127,81 @@ __device__ void cta_safescal(int n, double a, double *x)
     }
     __syncthreads();
 }
-// y = A x (A: rows x *, CSR with FP32 values), one thread per row: every
-// thread keeps a row in flight (rows of ~1% density are tens of nonzeros),
-// four (index, value) pairs and four gathers at a time
-__device__ void cta_spmv(const int *ptr, const int *idx, const float *val, int rows, const double *x, double *y)
+// y = A x (A: rows x *, CSR with FP32 values) with g lanes per row (the row
+// split, g a power of two <= 32): a group of g lanes takes a row, each lane
+// every g-th nonzero with four (index, value) pairs and four gathers in
+// flight, then the group adds its partial sums by a shuffle tree.  g = 1 is
+// one thread per row.  The autotuner picks g per problem class: long rows
+// and few of them favour wide groups, many short rows g = 1.
+__device__ void cta_spmv(const int *ptr, const int *idx, const float *val, int rows, const double *x, double *y,
+                         int g)
 {
-    for (int r = threadIdx.x; r < rows; r += BT) {
-        const int e1 = ptr[r + 1];
-        int e = ptr[r];
+    const int grp = threadIdx.x / g, lig = threadIdx.x % g, ngrp = BT / g;
+    for (int r0 = 0; r0 < rows; r0 += ngrp) {
+        const int r = r0 + grp;
         double s = 0.0;
-        for (; e + 3 < e1; e += 4) {
-            const int c0 = idx[e], c1 = idx[e + 1], c2 = idx[e + 2], c3 = idx[e + 3];
-            const float v0 = val[e], v1 = val[e + 1], v2 = val[e + 2], v3 = val[e + 3];
-            const double x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
-            s = fma((double)v0, x0, s);
-            s = fma((double)v1, x1, s);
-            s = fma((double)v2, x2, s);
-            s = fma((double)v3, x3, s);
+        if (r < rows) {
+            const int e1 = ptr[r + 1];
+            int e = ptr[r] + lig;
+            for (; e + 3 * g < e1; e += 4 * g) {
+                const int c0 = idx[e], c1 = idx[e + g], c2 = idx[e + 2 * g], c3 = idx[e + 3 * g];
+                const float v0 = val[e], v1 = val[e + g], v2 = val[e + 2 * g], v3 = val[e + 3 * g];
+                const double x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+                s = fma((double)v0, x0, s);
+                s = fma((double)v1, x1, s);
+                s = fma((double)v2, x2, s);
+                s = fma((double)v3, x3, s);
+            }
+            for (; e < e1; e += g) s = fma((double)val[e], x[idx[e]], s);
         }
-        for (; e < e1; e++) s = fma((double)val[e], x[idx[e]], s);
-        y[r] = s;
+        // every lane of a warp takes part (rows past the end add zeros)
+        for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, g);
+        if (r < rows && lig == 0) y[r] = s;
     }
     __syncthreads();
 }
 // dreorth with iterated CGS (dreorth.F:106-210): x against the first ncols
 // columns of W (leading dimension ld); *nrm is ||x|| on entry and exit
-__device__ void cta_reorth(const double *W, int ld, int ncols, double *x, int len, double *nrm, BShared &S, int &count)
+// projections h = W(:, 0:ncols)' x into S.h: each warp takes dc adjacent
+// columns at a time and reads each x element once for all of them (the
+// autotuner's choice of dc; every column's sum is formed in the same order
+// whatever dc is, so the choice does not change the result)
+template <int DC>
+__device__ void cta_proj(const double *W, int ld, int ncols, const double *x, int len, BShared &S)
+{
+    const int lane = threadIdx.x & 31;
+    for (int c0 = (threadIdx.x >> 5) * DC; c0 < ncols; c0 += BW * DC) {
+        const int nc = min(DC, ncols - c0);
+        double s[DC];
+#pragma unroll
+        for (int u = 0; u < DC; u++) s[u] = 0.0;
+        for (int i = lane; i < len; i += 32) {
+            const double xi = x[i];
+#pragma unroll
+            for (int u = 0; u < DC; u++)
+                if (u < nc) s[u] = fma(W[(size_t)(c0 + u) * ld + i], xi, s[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < DC; u++) {
+            const double t = warp_sum(s[u]);
+            if (lane == 0 && u < nc) S.h[c0 + u] = t;
+        }
+    }
+}
+__device__ void cta_proj_dc(const double *W, int ld, int ncols, const double *x, int len, BShared &S, int dc)
+{
+    if (dc >= 4) cta_proj<4>(W, ld, ncols, x, len, S);
+    else if (dc == 2) cta_proj<2>(W, ld, ncols, x, len, S);
+    else cta_proj<1>(W, ld, ncols, x, len, S);
+}
+
+__device__ void cta_reorth(const double *W, int ld, int ncols, double *x, int len, double *nrm, BShared &S, int &count,
+                           int dc)
 {
     if (ncols <= 0) return;
     double nrm0 = *nrm;
-    const int lane = threadIdx.x & 31;
     for (int it = 0; it < NTRY; it++) {
-        for (int c = threadIdx.x >> 5; c < ncols; c += BW) {
-            const double *w = W + (size_t)c * ld;
-            double s = 0.0;
-            for (int i = lane; i < len; i += 32) s = fma(w[i], x[i], s);
-            s = warp_sum(s);
-            if (lane == 0) S.h[c] = s;
-        }
+        cta_proj_dc(W, ld, ncols, x, len, S, dc);
         __syncthreads();
         double a = 0.0;
         for (int i = threadIdx.x; i < len; i += BT) {
@@ -218,7 +258,7 @@ __device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S)
         for (int i = threadIdx.x; i < m; i += BT) uk[i] *= P.rnorm;
         __syncthreads();
         double r = P.rnorm;
-        cta_reorth(U, m, k0, uk, m, &r, S, nre);
+        cta_reorth(U, m, k0, uk, m, &r, S, nre, P.dc);
         cta_safescal(m, r, uk);
         beta = r;
         if (threadIdx.x == 0) bb[k0 - 1] = beta;
@@ -243,7 +283,7 @@ __device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S)
     for (int j = j0; j <= dim; j++) {
         double *vj = V + (size_t)(j - 1) * n, *uj = U + (size_t)(j - 1) * m, *uj1 = U + (size_t)j * m;
         // alpha_j v_j = A' u_j - beta_j v_{j-1}
-        cta_spmv(P.tptr, P.tidx, P.tval, n, uj, vj);
+        cta_spmv(P.tptr, P.tidx, P.tval, n, uj, vj, P.g);
         nopx++;
         if (j == 1) {
             alpha = cta_nrm2(vj, n, S);
@@ -276,12 +316,12 @@ __device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S)
             }
             anorm = fmax(anorm, a1);
         }
-        if (alpha != 0.0) cta_reorth(V, n, j - 1, vj, n, &alpha, S, nre);
+        if (alpha != 0.0) cta_reorth(V, n, j - 1, vj, n, &alpha, S, nre, P.dc);
         if (alpha < anorm * epsn && j < dim) { ok = false; break; }
         if (threadIdx.x == 0) ba[j - 1] = alpha;
         if (alpha != 0.0) cta_safescal(n, alpha, vj);
         // beta_{j+1} u_{j+1} = A v_j - alpha_j u_j
-        cta_spmv(P.ptr, P.idx, P.val, m, vj, uj1);
+        cta_spmv(P.ptr, P.idx, P.val, m, vj, uj1, P.g);
         nopx++;
         cta_axpy(m, -alpha, uj, uj1);
         beta = cta_nrm2(uj1, m, S);
@@ -308,7 +348,7 @@ __device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S)
             a1 = amax * sqrt(a1 * a1 + (beta / amax) * (beta / amax) + a1 * bb[j - 2] / amax);
         }
         anorm = fmax(anorm, a1);
-        if (beta != 0.0) cta_reorth(U, m, j, uj1, m, &beta, S, nre);
+        if (beta != 0.0) cta_reorth(U, m, j, uj1, m, &beta, S, nre, P.dc);
         if (beta < anorm * epsn && j < dim) { ok = false; break; }
         if (threadIdx.x == 0) bb[j - 1] = beta;
         if (beta != 0.0) cta_safescal(m, beta, uj1);
@@ -598,7 +638,7 @@ __device__ bool b_ritz(BProb &P, const BCfg &c, BShared &S, double *scr, const B
 }
 
 // ------------------------------------------------------- the cycle kernel
-__global__ void __launch_bounds__(BT) k_batch_cycle(BProb *probs, const int *order, int nprob, BCfg c,
+__global__ void __launch_bounds__(BT, 2) k_batch_cycle(BProb *probs, const int *order, int nprob, BCfg c,
                                                     double *scratch, size_t scr_stride, int *ticket, int *active,
                                                     int cycles_per_launch)
 {
@@ -640,6 +680,27 @@ __global__ void __launch_bounds__(BT) k_batch_cycle(BProb *probs, const int *ord
             __syncthreads();
         }
         if (threadIdx.x == 0 && P.status == BS_ACTIVE) atomicAdd(active, 1);
+        __syncthreads();
+    }
+}
+
+// The autotuner's probe: for each sampled problem (one CTA each) the two
+// products and the Gram-Schmidt projections of one vector against ncols
+// columns on both sides, with the candidate row split g and projection tile
+// dc.  The operands are the problem's own basis arrays, zeroed beforehand:
+// U(:,0) -> V(:,0) -> U(:,1), and column ncols of each side against the
+// ncols before it.
+__global__ void __launch_bounds__(BT) k_batch_probe(const BProb *probs, const int *sample, int ns, int g, int dc,
+                                                    int ncols)
+{
+    __shared__ BShared S;
+    for (int q = blockIdx.x; q < ns; q += gridDim.x) {
+        const BProb &P = probs[sample[q]];
+        cta_spmv(P.tptr, P.tidx, P.tval, P.n, P.U, P.V, g);
+        cta_spmv(P.ptr, P.idx, P.val, P.m, P.V, P.U + P.m, g);
+        cta_proj_dc(P.U, P.m, ncols, P.U + (size_t)ncols * P.m, P.m, S, dc);
+        __syncthreads();
+        cta_proj_dc(P.V, P.n, ncols, P.V + (size_t)ncols * P.n, P.n, S, dc);
         __syncthreads();
     }
 }
@@ -719,11 +780,77 @@ struct Batch {
     float *d_val = nullptr, *d_tval = nullptr;
     int64_t total_m = 0, total_n = 0, total_nnz = 0;
     std::vector<int> order;  // problems by decreasing cost
+    // autotuner: per size class (quarters of `order`) the row split and the
+    // projection tile, the probe's ms with them and with the defaults (1, 1)
+    int tuned = 0;           // 0: tune at the next solve, 1: timed, 2: set by the caller
+    int g[PROPACK_BATCH_CLASSES], dc[PROPACK_BATCH_CLASSES];
+    float ms_best[PROPACK_BATCH_CLASSES], ms_default[PROPACK_BATCH_CLASSES];
+    int cls(int pos) const { return std::min(PROPACK_BATCH_CLASSES - 1, pos * PROPACK_BATCH_CLASSES / nprob); }
 };
 static std::mutex g_batch_mu;
 static std::map<int64_t, Batch *> g_batches;
 static int64_t g_batch_next = 1;
 static thread_local propack_batch_stats_t g_batch_stats;
+
+// Time every candidate (row split g, projection tile dc) on a sample of each
+// size class and keep the fastest; the defaults (1, 1) stay unless a
+// candidate is more than 3 % faster, so that near-ties do not flip the
+// choice (and with it the SpMV's summation order) between batches.
+static void batch_tune(Batch *B, BProb *dprob, int grid, int dim, cudaStream_t s)
+{
+    static const int gs[] = {1, 4, 8, 32};
+    static const int dcs[] = {1, 2, 4};
+    const int np = B->nprob, ncols = std::max(1, dim / 2);
+    int *dsample = nullptr;
+    PGB_CUDA(cudaMalloc(&dsample, sizeof(int) * std::max(1, np)));
+    cudaEvent_t e0, e1;
+    PGB_CUDA(cudaEventCreate(&e0));
+    PGB_CUDA(cudaEventCreate(&e1));
+    for (int c = 0; c < PROPACK_BATCH_CLASSES; c++) {
+        const int p0 = c * np / PROPACK_BATCH_CLASSES, p1 = (c + 1) * np / PROPACK_BATCH_CLASSES;
+        B->g[c] = 1;
+        B->dc[c] = 1;
+        B->ms_best[c] = B->ms_default[c] = 0.f;
+        if (p1 <= p0) continue;
+        const int ns = std::min(p1 - p0, grid);
+        std::vector<int> sample(ns);
+        for (int q = 0; q < ns; q++) sample[q] = B->order[p0 + (int)((int64_t)q * (p1 - p0) / ns)];
+        PGB_CUDA(cudaMemcpyAsync(dsample, sample.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        float best = 0.f, def = 0.f;
+        for (int g : gs)
+            for (int dc : dcs) {
+                k_batch_probe<<<ns, BT, 0, s>>>(dprob, dsample, ns, g, dc, ncols);
+                PGB_LAUNCHED();
+                PGB_CUDA(cudaEventRecord(e0, s));
+                for (int r = 0; r < 2; r++) {
+                    k_batch_probe<<<ns, BT, 0, s>>>(dprob, dsample, ns, g, dc, ncols);
+                    PGB_LAUNCHED();
+                }
+                PGB_CUDA(cudaEventRecord(e1, s));
+                PGB_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                PGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                ms *= 0.5f;
+                if (g == 1 && dc == 1) def = ms;
+                if (best == 0.f || ms < best) {
+                    best = ms;
+                    B->g[c] = g;
+                    B->dc[c] = dc;
+                }
+            }
+        if (!(best < 0.97f * def)) {
+            B->g[c] = 1;
+            B->dc[c] = 1;
+            best = def;
+        }
+        B->ms_best[c] = best;
+        B->ms_default[c] = def;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(dsample);
+    B->tuned = 1;
+}
 
 }  // namespace pgb
 
@@ -872,6 +999,7 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
             throw ArgFailure();
         }
         g_batch_stats = propack_batch_stats_t();
+        g_batch_stats.tune_ms = 0.0;
         const int64_t l0 = g_launches;
         cudaStream_t s;
         PGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
@@ -927,6 +1055,23 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
             P.bnd = P.sig + neig;
             mo += B->m[p];
             no += B->n[p];
+        }
+        // the tuning (once per batch, before its first solve's timing) and
+        // every problem's choice by its size class
+        for (int p = 0; p < np; p++) hp[p].g = hp[p].dc = 1;
+        if (!B->tuned) {
+            const auto t0 = std::chrono::steady_clock::now();
+            PGB_CUDA(cudaMemcpyAsync(dprob, hp.data(), sizeof(BProb) * np, cudaMemcpyHostToDevice, s));
+            PGB_CUDA(cudaMemsetAsync(dU, 0, sizeof(double) * (size_t)B->total_m * d1, s));
+            PGB_CUDA(cudaMemsetAsync(dV, 0, sizeof(double) * (size_t)B->total_n * dim, s));
+            batch_tune(B, dprob, grid, dim, s);
+            g_batch_stats.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                                        .count();
+        }
+        for (int pos = 0; pos < np; pos++) {
+            const int c = B->cls(pos);
+            hp[B->order[pos]].g = B->g[c];
+            hp[B->order[pos]].dc = B->dc[c];
         }
         PGB_CUDA(cudaMemcpyAsync(dprob, hp.data(), sizeof(BProb) * np, cudaMemcpyHostToDevice, s));
         PGB_CUDA(cudaMemcpyAsync(dorder, B->order.data(), sizeof(int) * np, cudaMemcpyHostToDevice, s));
@@ -1011,6 +1156,48 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
         cudaFreeHost(hactive);
         cudaStreamDestroy(s);
     })
+}
+
+extern "C" int propack_batch_get_tuning(int64_t handle, int *g, int *dc, float *ms_tuned, float *ms_default)
+{
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    auto it = g_batches.find(handle);
+    if (it == g_batches.end()) return PROPACK_ERR_HANDLE;
+    const Batch *B = it->second;
+    for (int c = 0; c < PROPACK_BATCH_CLASSES; c++) {
+        if (g) g[c] = B->tuned ? B->g[c] : 0;
+        if (dc) dc[c] = B->tuned ? B->dc[c] : 0;
+        if (ms_tuned) ms_tuned[c] = B->tuned == 1 ? B->ms_best[c] : 0.f;
+        if (ms_default) ms_default[c] = B->tuned == 1 ? B->ms_default[c] : 0.f;
+    }
+    return B->tuned;
+}
+
+extern "C" int propack_batch_set_tuning(int64_t handle, const int *g, const int *dc)
+{
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    auto it = g_batches.find(handle);
+    if (it == g_batches.end()) return PROPACK_ERR_HANDLE;
+    Batch *B = it->second;
+    if (!g || !dc) {
+        B->tuned = 0;  // time again at the next solve
+        return 0;
+    }
+    for (int c = 0; c < PROPACK_BATCH_CLASSES; c++) {
+        const bool okg = g[c] == 1 || g[c] == 2 || g[c] == 4 || g[c] == 8 || g[c] == 16 || g[c] == 32;
+        const bool okd = dc[c] == 1 || dc[c] == 2 || dc[c] == 4;
+        if (!okg || !okd) {
+            set_error("propack_batch_set_tuning: g must be 1, 2, 4, 8, 16 or 32 and dc 1, 2 or 4");
+            return PROPACK_ERR_ARG;
+        }
+    }
+    for (int c = 0; c < PROPACK_BATCH_CLASSES; c++) {
+        B->g[c] = g[c];
+        B->dc[c] = dc[c];
+        B->ms_best[c] = B->ms_default[c] = 0.f;
+    }
+    B->tuned = 2;
+    return 0;
 }
 
 extern "C" int propack_batch_get_stats(propack_batch_stats_t *out)

@@ -73,3 +73,35 @@ def test_batch_uneven_sizes_single_call():
         s_ref = np.linalg.svd(A.toarray(), compute_uv=False)[:6]
         np.testing.assert_allclose(sig[p], s_ref, rtol=1e-10)
     B.close()
+
+
+def test_autotuner_table_and_pinned_choices():
+    """The autotuner times its candidates once per batch; every choice of the
+    table solves correctly; the projection tile dc changes no bit, and a
+    pinned table gives the same bits on every solve."""
+    mats = batch.random_batch(24, m_range=(300, 3000), n_range=(100, 900), density=0.02, seed=9)
+    rng = np.random.default_rng(3)
+    u0 = [rng.uniform(size=A.shape[0]) for A in mats]
+    dense = [np.linalg.svd(A.toarray(), compute_uv=False)[:6] for A in mats]
+    B = batch.Batch(mats)
+    assert B.tuning()["state"] == 0
+    sig, bnd, info, U, V = B.solve(6, kmax=20, tol=1e-12, maxiter=200, u0=u0, vectors=False)
+    t = B.tuning()
+    assert t["state"] == 1 and B.stats["tune_ms"] > 0
+    assert all(g in (1, 4, 8, 32) for g in t["g"]) and all(d in (1, 2, 4) for d in t["dc"])
+    assert all(b <= d * 1.0001 for b, d in zip(t["probe_ms"], t["probe_ms_default"]))
+    for p in range(len(mats)):
+        np.testing.assert_allclose(sig[p], dense[p], rtol=1e-10)
+    sig2, _, _, _, _ = B.solve(6, kmax=20, tol=1e-12, maxiter=200, u0=u0, vectors=False)
+    assert B.stats["tune_ms"] == 0.0 and np.array_equal(sig, sig2)
+    out = {}
+    for g, dc in ((1, 1), (1, 4), (32, 2), (8, 1)):
+        B.set_tuning([g] * batch.NCLASS, [dc] * batch.NCLASS)
+        assert B.tuning()["state"] == 2
+        out[(g, dc)] = B.solve(6, kmax=20, tol=1e-12, maxiter=200, u0=u0, vectors=False)[0]
+        for p in range(len(mats)):
+            np.testing.assert_allclose(out[(g, dc)][p], dense[p], rtol=1e-10)
+    assert np.array_equal(out[(1, 1)], out[(1, 4)])
+    B.set_tuning()
+    assert B.tuning()["state"] == 0
+    B.close()
