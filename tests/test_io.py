@@ -1,7 +1,8 @@
 """Matrix files (propack_gb300.io): the Harwell-Boeing reader against scipy's
 reader on real files and against hand-written complex / symmetric /
 Hermitian / skew / pattern files, and complex data through the Matrix
-Market, coordinate and dense readers.  Host code only."""
+Market, coordinate and dense readers (host code), and, on the GPU, the
+device operator built from files of each kind."""
 import numpy as np
 import pytest
 import scipy.io as sio
@@ -134,3 +135,40 @@ def test_complex_matrix_market_coordinate_and_dense(tmp_path):
         f.write(f"{D.shape[0]} {D.shape[1]}\n")
         f.write("\n".join(f"{float(z.real)!r} {float(z.imag)!r}" for z in D.ravel(order="F")))
     np.testing.assert_array_equal(pio.read(str(p)).toarray(), D)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fmt", ["mtx", "rua", "coord", "cua"])
+def test_device_operator_from_a_matrix_file(tmp_path, fmt):
+    """io.load builds the device operator from a file (upload, device
+    checks and transposition, SpMV schedule): its products equal scipy's on
+    the matrix read back, and a solve on it gives the dense SVD's values."""
+    import propack_gb300 as pg
+    rng = np.random.default_rng(11)
+    m, n = 300, 180
+    A = sp.csr_array(sp.random_array((m, n), density=0.05, format="csr", random_state=rng))
+    if fmt == "cua":
+        A = sp.csr_array(A + 1j * sp.csr_array(sp.random_array((m, n), density=0.05, format="csr",
+                                                              random_state=rng)))
+    p = tmp_path / f"a.{fmt}"
+    if fmt == "mtx":
+        sio.mmwrite(str(p), A)
+    elif fmt == "rua":
+        sio.hb_write(str(p), sp.csc_array(A))
+    elif fmt == "coord":
+        C = A.tocoo()
+        with open(p, "w") as f:
+            f.write(f"{m} {n} {C.nnz}\n")
+            for i, j, v in zip(C.row, C.col, C.data):
+                f.write(f"{i + 1} {j + 1} {float(v)!r}\n")
+    else:
+        sio.mmwrite(str(p), A)  # complex data through the Matrix Market reader
+    ref = pio.read(str(p))
+    op = pio.load(str(p))
+    x = rng.standard_normal(n) + (1j * rng.standard_normal(n) if fmt == "cua" else 0)
+    y = rng.standard_normal(m) + (1j * rng.standard_normal(m) if fmt == "cua" else 0)
+    np.testing.assert_allclose(op.matvec(x), ref @ x, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(op.rmatvec(y), ref.conj().T @ y, rtol=1e-12, atol=1e-12)
+    u, s, vt, bnd = pg.svdp(op, 5, kmax=40, tol=1e-12, rng=np.random.default_rng(0))
+    np.testing.assert_allclose(s, np.linalg.svd(ref.toarray(), compute_uv=False)[:5], rtol=1e-10)
+    op.close()
