@@ -11,7 +11,10 @@
 //   h1 = relu(W1 f + b1), h2 = relu(W2 h1 + b2), u0_i = w3 . h2 + b3
 // (18 -> 256 -> 256 -> 1).  Weights are held in FP32 (Adam master copy) and
 // used as BF16; every product accumulates in FP32.  The 256 x 256 layer runs
-// on the BF16 tensor cores (mma.sync m16n8k16), forward and backward.
+// on the 5th-generation tensor cores (tcgen05.mma, FP32 accumulators in
+// tensor memory), forward and backward through its input; the mma.sync
+// kernel it replaced stays selectable (propack_mlp_set_impl) as the
+// reference implementation.
 //
 // Training (propack_mlp_train_step) minimises, for a matrix whose leading k
 // left singular vectors U are known,
@@ -27,8 +30,11 @@
 #include <map>
 #include <vector>
 
+#include <atomic>
+
 #include "../../include/propack_gb300.h"
 #include "pgb.cuh"
+#include "pgb_tc.cuh"
 
 namespace pgb {
 
@@ -50,6 +56,7 @@ struct Mlp {
     bf16 *H1 = nullptr, *H2 = nullptr, *D2 = nullptr;
     double *Y = nullptr, *om = nullptr, *U = nullptr, *red = nullptr, *coef = nullptr;
     float *part = nullptr;  // per-CTA partial sums of the reductions
+    int *err = nullptr;     // set by the tensor-core kernel when a bounded wait runs out
     int device = 0;
     cudaStream_t s = nullptr;
 };
@@ -194,6 +201,139 @@ __global__ void __launch_bounds__(256) k_mlp_mm(int m, const bf16 *X, const bf16
                 }
             }
     }
+}
+
+// The same product on the 5th-generation tensor cores.  A persistent CTA
+// (256 threads, one per SM: 192 KB of shared memory) keeps Wt in shared
+// memory in the no-swizzle K-major layout of pgb_tc.cuh (16 K steps of 256
+// rows x 16 K) and takes tiles of 128 rows of X in turn: the threads write
+// the tile into the same layout (two lanes per 32-byte sector of a row, so
+// that the loads are whole sectors and a warp's stores take the minimum
+// four wavefronts), thread 0 issues the 16 MMAs (M = 128, N = 256, K = 16,
+// BF16 x BF16 -> FP32) into TMEM columns 0..255 and commits them to an
+// mbarrier, and every warp reads 32 TMEM lanes (rows; lanes 32 (w mod 4)..)
+// x 128 columns (half w / 4) with tcgen05.ld and applies k_mlp_mm's
+// epilogue.  Every wait is bounded; one that runs out sets *err and the CTA
+// stops after its MMAs in flight are done.
+constexpr int TM_BM = 128, TM_N = MLP_H, TM_KSTEPS = MLP_H / 16;
+constexpr int TM_ATILE = TM_BM * 16 * 2;  // 4096 bytes per K step
+constexpr int TM_BTILE = TM_N * 16 * 2;   // 8192 bytes per K step
+constexpr int TM_SMEM = TM_KSTEPS * (TM_ATILE + TM_BTILE) + 128;
+constexpr uint32_t TM_IDESC = tc_idesc_bf16(TM_BM, TM_N);
+constexpr unsigned TM_TMEM_COLS = TM_N;
+constexpr long TM_WAIT_LIMIT = 1L << 22;
+static_assert(TM_SMEM <= 227 * 1024, "shared memory");
+
+template <int MODE>
+__global__ void __launch_bounds__(256, 1) k_mlp_mm_tc(int m, const bf16 *X, const bf16 *Wt, const float *bias,
+                                                      const bf16 *mask, bf16 *Ob, float *Of, int *err)
+{
+    extern __shared__ __align__(1024) unsigned char tm_sm[];
+    const uint32_t a_s = tc_smem(tm_sm), b_s = a_s + TM_KSTEPS * TM_ATILE;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(tm_sm + TM_KSTEPS * (TM_ATILE + TM_BTILE));
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+    int *sbad = reinterpret_cast<int *>(tslot + 1);
+    const uint32_t bar_s = tc_smem(bar);
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int ntiles = (m + TM_BM - 1) / TM_BM;
+    if (tid == 0) {
+        tc_bar_init(bar_s, 1);
+        *sbad = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (w == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tslot)),
+                     "r"(TM_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // Wt (256 rows n x 256 K) into shared memory, once per CTA
+    for (int q = tid; q < TM_N * (MLP_H / 8); q += blockDim.x) {
+        const int n = (q >> 1) & (TM_N - 1), kc = ((q >> 9) << 1) | (q & 1);
+        const uint4 v = *reinterpret_cast<const uint4 *>(Wt + (size_t)n * MLP_H + kc * 8);
+        tc_st16(b_s + (kc >> 1) * TM_BTILE + (n >> 3) * 256 + (kc & 1) * 128 + (n & 7) * 16, v);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    int it = 0;
+    bool bad = false;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+        const int row0 = t * TM_BM;
+        // the tile of X (rows past m read as zeros)
+        for (int q = tid; q < TM_BM * (MLP_H / 8); q += blockDim.x) {
+            const int r = (q >> 1) & (TM_BM - 1), kc = ((q >> 8) << 1) | (q & 1);
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (row0 + r < m) v = *reinterpret_cast<const uint4 *>(X + (size_t)(row0 + r) * MLP_H + kc * 8);
+            tc_st16(a_s + (kc >> 1) * TM_ATILE + (r >> 3) * 256 + (kc & 1) * 128 + (r & 7) * 16, v);
+        }
+        tc_fence_proxy();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int ks = 0; ks < TM_KSTEPS; ks++)
+                tc_mma(tmem, tc_desc(a_s + ks * TM_ATILE), tc_desc(b_s + ks * TM_BTILE), TM_IDESC, ks > 0 ? 1u : 0u);
+            tc_commit(bar_s);
+        }
+        const bool ok = tc_bar_wait(bar_s, (unsigned)(it & 1), TM_WAIT_LIMIT);
+        if (__syncthreads_or(!ok)) {
+            bad = true;
+            break;
+        }
+        tc_fence_after();
+        {
+            const int L = 32 * (w & 3), cb = (w >> 2) * (TM_N / 2);
+            const int row = row0 + L + lane;
+#pragma unroll 1
+            for (int cc = 0; cc < TM_N / 2; cc += 8) {
+                uint32_t v[8];
+                tc_ld8(tmem + ((uint32_t)L << 16) + (uint32_t)(cb + cc), v);
+                tc_wait_ld();
+                if (row >= m) continue;
+                const int c = cb + cc;
+                if (MODE == 0) {
+                    uint32_t pk[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const float z0 = fmaxf(__uint_as_float(v[2 * j]) + bias[c + 2 * j], 0.f);
+                        const float z1 = fmaxf(__uint_as_float(v[2 * j + 1]) + bias[c + 2 * j + 1], 0.f);
+                        __nv_bfloat162 h;
+                        h.x = __float2bfloat16_rn(z0);
+                        h.y = __float2bfloat16_rn(z1);
+                        pk[j] = *reinterpret_cast<uint32_t *>(&h);
+                    }
+                    *reinterpret_cast<uint4 *>(Ob + (size_t)row * MLP_H + c) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                } else {
+                    const uint4 mk = *reinterpret_cast<const uint4 *>(mask + (size_t)row * MLP_H + c);
+                    const uint32_t mw[4] = {mk.x, mk.y, mk.z, mk.w};
+                    float o[8];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&mw[j]);
+                        o[2 * j] = __bfloat162float(h.x) > 0.f ? __uint_as_float(v[2 * j]) : 0.f;
+                        o[2 * j + 1] = __bfloat162float(h.y) > 0.f ? __uint_as_float(v[2 * j + 1]) : 0.f;
+                    }
+                    float4 *dst = reinterpret_cast<float4 *>(Of + (size_t)row * MLP_H + c);
+                    dst[0] = make_float4(o[0], o[1], o[2], o[3]);
+                    dst[1] = make_float4(o[4], o[5], o[6], o[7]);
+                }
+            }
+        }
+        // the TMEM reads are done before the next tile's MMAs overwrite the
+        // accumulators, and the MMAs before the next tile's X overwrites A
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (bad) {
+        if (tid == 0) atomicExch(err, 1);
+        tc_bar_wait(bar_s, (unsigned)(it & 1), TM_WAIT_LIMIT);  // the MMAs in flight (bounded)
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TM_TMEM_COLS) : "memory");
 }
 
 // u0_i = w3 . h2_i + b3, one warp per row
@@ -429,13 +569,40 @@ static void mlp_features(Mlp &M, const Operator &op, unsigned long long seed)
 
 static size_t mm_smem() { return sizeof(unsigned short) * MLP_H * W2S; }
 
+// the 256 x 256 layer: 1 the tcgen05 kernel (default), 0 the mma.sync one
+static std::atomic<int> g_mlp_impl{1};
+
+// Z = X Wt' with the layer's epilogue (MODE 0 forward, 1 backward)
+template <int MODE>
+static void mlp_mm(Mlp &M, int m, const bf16 *X, const bf16 *Wt, const float *bias, const bf16 *mask, bf16 *Ob,
+                   float *Of)
+{
+    if (g_mlp_impl.load() == 1) {
+        const int g = std::max(1, std::min(device_info().sms, (m + TM_BM - 1) / TM_BM));
+        k_mlp_mm_tc<MODE><<<g, 256, TM_SMEM, M.s>>>(m, X, Wt, bias, mask, Ob, Of, M.err);
+    } else {
+        const int g = std::min(device_info().sms, (m + 127) / 128);
+        k_mlp_mm<MODE><<<g, 256, mm_smem(), M.s>>>(m, X, Wt, bias, mask, Ob, Of);
+    }
+    PGB_LAUNCHED();
+}
+// after the stream has been synchronised: a wait of the tensor-core kernel that ran out
+static void mlp_check(Mlp &M)
+{
+    int e = 0;
+    PGB_CUDA(cudaMemcpy(&e, M.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        PGB_CUDA(cudaMemset(M.err, 0, sizeof(int)));
+        set_error("learned start: a tensor-core wait ran out");
+        throw WaitFailure();
+    }
+}
+
 static void mlp_forward(Mlp &M, int m)
 {
     k_mlp_l1<<<std::min(8192, m), MLP_H, 0, M.s>>>(m, M.F, M.W1b, M.p + OB1, M.H1);
     PGB_LAUNCHED();
-    const int g = std::min(device_info().sms, (m + 127) / 128);
-    k_mlp_mm<0><<<g, 256, mm_smem(), M.s>>>(m, M.H1, M.W2b, M.p + OB2, nullptr, M.H2, nullptr);
-    PGB_LAUNCHED();
+    mlp_mm<0>(M, m, M.H1, M.W2b, M.p + OB2, nullptr, M.H2, nullptr);
     k_mlp_l3<<<std::min(4096, (m + 7) / 8), 256, 0, M.s>>>(m, M.H2, M.w3b, M.p + OB3, M.out);
     PGB_LAUNCHED();
 }
@@ -477,9 +644,7 @@ static double mlp_backward(Mlp &M, int m, int k)
     PGB_LAUNCHED();
     k_mlp_sum_dw2<<<(MLP_H * MLP_H + MLP_H + 255) / 256, 256, 0, M.s>>>(MLP_DW2_CHUNKS, M.part, M.g);
     PGB_LAUNCHED();
-    const int g = std::min(device_info().sms, (m + 127) / 128);
-    k_mlp_mm<1><<<g, 256, mm_smem(), M.s>>>(m, M.D2, M.W2Tb, nullptr, M.H1, nullptr, M.D1);
-    PGB_LAUNCHED();
+    mlp_mm<1>(M, m, M.D2, M.W2Tb, nullptr, M.H1, nullptr, M.D1);
     k_mlp_dw1<<<MLP_GRID, MLP_H, 0, M.s>>>(m, M.D1, M.F, pf);
     PGB_LAUNCHED();
     k_mlp_sum_dw1<<<(MLP_H * (MLP_IN + 1) + 255) / 256, 256, 0, M.s>>>(MLP_GRID, pf, M.g);
@@ -553,6 +718,10 @@ extern "C" int propack_mlp_create(uint64_t seed, int64_t *handle)
         PGB_CUDA(cudaMalloc(&M->part, sizeof(float) * (size_t)MLP_DW2_CHUNKS * (MLP_H * MLP_H + MLP_H)));
         PGB_CUDA(cudaFuncSetAttribute(k_mlp_mm<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mm_smem()));
         PGB_CUDA(cudaFuncSetAttribute(k_mlp_mm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mm_smem()));
+        PGB_CUDA(cudaFuncSetAttribute(k_mlp_mm_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, TM_SMEM));
+        PGB_CUDA(cudaFuncSetAttribute(k_mlp_mm_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TM_SMEM));
+        PGB_CUDA(cudaMalloc(&M->err, sizeof(int)));
+        PGB_CUDA(cudaMemset(M->err, 0, sizeof(int)));
         mlp_cast(*M);
         PGB_CUDA(cudaStreamSynchronize(M->s));
         std::lock_guard<std::mutex> lk(g_mlp_mu);
@@ -575,7 +744,7 @@ extern "C" int propack_mlp_destroy(int64_t handle)
     for (void *q : {(void *)M->p, (void *)M->g, (void *)M->m1, (void *)M->m2, (void *)M->W1b, (void *)M->W2b,
                     (void *)M->W2Tb, (void *)M->w3b, (void *)M->F, (void *)M->out, (void *)M->gout, (void *)M->D1,
                     (void *)M->H1, (void *)M->H2, (void *)M->D2, (void *)M->Y, (void *)M->om, (void *)M->U,
-                    (void *)M->red, (void *)M->coef, (void *)M->part})
+                    (void *)M->red, (void *)M->coef, (void *)M->part, (void *)M->err})
         if (q) cudaFree(q);
     cudaStreamDestroy(M->s);
     delete M;
@@ -597,6 +766,13 @@ extern "C" int propack_mlp_params(int64_t handle, float *get, const float *set)
 }
 
 extern "C" int propack_mlp_nparams(void) { return MLP_NP; }
+
+extern "C" int propack_mlp_set_impl(int impl)
+{
+    if (impl != 0 && impl != 1) return PROPACK_ERR_ARG;
+    g_mlp_impl.store(impl);
+    return 0;
+}
 
 extern "C" int propack_mlp_features(int64_t handle, int64_t op_handle, uint64_t seed, float *F)
 {
@@ -623,6 +799,7 @@ extern "C" int propack_mlp_start(int64_t handle, int64_t op_handle, uint64_t see
         std::vector<float> o(m);
         PGB_CUDA(cudaMemcpyAsync(o.data(), M->out, sizeof(float) * m, cudaMemcpyDeviceToHost, M->s));
         PGB_CUDA(cudaStreamSynchronize(M->s));
+        mlp_check(*M);
         for (int i = 0; i < m; i++) u0[i] = o[i];
     })
 }
@@ -646,6 +823,7 @@ extern "C" int propack_mlp_grad(int64_t handle, int64_t op_handle, uint64_t seed
         if (loss) *loss = L;
         if (grad) PGB_CUDA(cudaMemcpyAsync(grad, M->g, sizeof(float) * MLP_NP, cudaMemcpyDeviceToHost, M->s));
         PGB_CUDA(cudaStreamSynchronize(M->s));
+        mlp_check(*M);
     })
 }
 
@@ -672,5 +850,6 @@ extern "C" int propack_mlp_train_step(int64_t handle, int64_t op_handle, uint64_
         PGB_LAUNCHED();
         mlp_cast(*M);
         PGB_CUDA(cudaStreamSynchronize(M->s));
+        mlp_check(*M);
     })
 }

@@ -32,10 +32,17 @@ def _lib():
         L.propack_mlp_features.argtypes = [C.c_int64, C.c_int64, C.c_uint64, _fp]
         L.propack_mlp_start.argtypes = [C.c_int64, C.c_int64, C.c_uint64, _dp]
         L.propack_mlp_grad.argtypes = [C.c_int64, C.c_int64, C.c_uint64, _dp, C.c_int, C.c_int, _fp, _dp]
+        L.propack_mlp_set_impl.argtypes = [C.c_int]
         L.propack_mlp_train_step.argtypes = [C.c_int64, C.c_int64, C.c_uint64, _dp, C.c_int, C.c_int, C.c_double,
                                              _dp]
         L._mlp_bound = True
     return L
+
+
+def set_layer_impl(impl):
+    """The 256 x 256 layer's kernel (process-wide): "tcgen05" (default) or
+    "mma_sync" (the reference implementation)."""
+    _check(_lib().propack_mlp_set_impl({"mma_sync": 0, "tcgen05": 1}[impl]), "propack_mlp_set_impl")
 
 
 def _check(rc, what):

@@ -77,6 +77,32 @@ def test_gradients_match_oracle():
     model.close()
 
 
+def test_tcgen05_layer_matches_mma_sync():
+    """The 256 x 256 layer on tcgen05 (TMEM accumulators) against the
+    mma.sync kernel: start vectors and gradients agree to the FP32
+    accumulation order (H2 is rounded to BF16, so a few entries may move by
+    one BF16 unit), on a row count that is not a multiple of the 128-row
+    tile."""
+    op, A = _family_op(m=3001, n=800)
+    k = 6
+    U = np.linalg.svd(A, full_matrices=False)[0][:, :k]
+    model = learned.StartModel(seed=3)
+    out = {}
+    try:
+        for impl in ("mma_sync", "tcgen05"):
+            learned.set_layer_impl(impl)
+            out[impl] = (model.start(op), model.grad(op, U))
+    finally:
+        learned.set_layer_impl("tcgen05")
+    u_ref, (l_ref, g_ref) = out["mma_sync"]
+    u_tc, (l_tc, g_tc) = out["tcgen05"]
+    assert np.linalg.norm(u_tc - u_ref) <= 1e-2 * np.linalg.norm(u_ref)
+    assert abs(l_tc - l_ref) <= 1e-3 * abs(l_ref)
+    assert np.linalg.norm(g_tc - g_ref) <= 2e-2 * np.linalg.norm(g_ref)
+    op.close()
+    model.close()
+
+
 def test_training_lowers_the_loss():
     op, A = _family_op()
     k = 6
