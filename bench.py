@@ -16,10 +16,10 @@ Workloads (seeded synthetic data, numpy default_rng):
   kernel; --scale sets the fraction of the 4096 problems (default 1).
 * learned: the learned start vector on a matrix family (200000 x 50000,
   rank-32 rotating factors + sparse noise), k = 32, kmax 64, tol 1e-8.
-* complex_zipf (opt-in): the complex*16 drivers (zlansvd_irl_) on a
-  2,000,000-row complex analogue of zipf, the device operator in its 2x2
-  block form; same keys, with the rooflines of the block-form SpMV pair
-  and the complex Gram-Schmidt pair.
+* complex_zipf: the complex*16 drivers (zlansvd_irl_) on a 2,000,000-row
+  complex analogue of zipf, the device operator in its native complex form
+  (the real 2x2-block form timed beside it); same keys, with the rooflines
+  of the native complex SpMV pair and the complex Gram-Schmidt pair.
 
 A step is one complete DLANSVD_IRL solve (start vector -> k converged Ritz
 triplets), run in each form of --forms (the first is the chosen form):
@@ -129,6 +129,8 @@ def parse():
                     help="shrink m and n by this factor (profiling captures only; not a bench line)")
     ap.add_argument("--cgs-arith", default="planes", choices=["planes", "fp64", "f3"],
                     help="Gram-Schmidt arithmetic of the FP64 form (propack_set_cgs_arith)")
+    ap.add_argument("--batch-arith", default="fp64", choices=["fp64", "planes"],
+                    help="batched workload: arithmetic of its products and Gram-Schmidt (propack_batch_set_arith)")
     ap.add_argument("--no-other", action="store_true",
                     help="skip the other configurations that the default headline run appends")
     return ap.parse_args()
@@ -599,11 +601,21 @@ def run_ours(args, wl):
     n_fwd, t_fwd = prof[kfwd]
     achieved = (fwd_b * n_fwd + adj_b * n_adj) / max((t_fwd + t_adj) * 1e-3, 1e-12) / 1e9
     peak, peak_kind = peaks()
+    # the gather ceiling of this matrix's products on this GPU (flat random
+    # reads of the input vector with the index/value stream, no rows)
+    gc = {}
+    for nm, n_in, nz in (("fwd", n + r, S.nnz + nnz_l), ("adj", m + r, S.nnz + nnz_r)):
+        ms_c = C.c_float(0.0)
+        if lib.propack_gather_ceiling(C.c_int(int(n_in)), C.c_int64(int(nz)), C.byref(ms_c)) == 0:
+            gc[nm] = ms_c.value
     roof = {"bound": "hbm", "kernel": f"fused SpMV pair ({'FP32, mixed form' if vb == 4 else 'FP64'})",
             "achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
             "traffic": SPMV_TRAFFIC_BYTES.get(args.workload, {}).get(chosen) if SPMV_TRAFFIC_BYTES else None,
             "algorithmic_bytes_per_launch": {"fwd": fwd_b, "adj": adj_b},
-            "mean_launch_ms": {"fwd": t_fwd / max(n_fwd, 1), "adj": t_adj / max(n_adj, 1)}}
+            "mean_launch_ms": {"fwd": t_fwd / max(n_fwd, 1), "adj": t_adj / max(n_adj, 1)},
+            "gather_ceiling_ms": gc,
+            "frac_of_gather_ceiling": {d: gc[d] / max((t_fwd / max(n_fwd, 1)) if d == "fwd" else
+                                                      (t_adj / max(n_adj, 1)), 1e-12) for d in gc}}
     # Gram-Schmidt: a pass over l basis columns of length len reads them in
     # the projection and again in the update (2*l*len*vb bytes; the x reads
     # and writes, 3*len*vb per pass, are left out)
@@ -700,6 +712,7 @@ def run_batched(args, wl):
     mtot = sum(A.shape[0] for A in all_mats)
     ntot = sum(A.shape[1] for A in all_mats)
     B = batch.Batch(mats)
+    B.set_arith(args.batch_arith)
     tune_ms = 0.0
     for _ in range(max(1, args.warmup)):
         B.solve(k, kmax=kmax, tol=tol, maxiter=100, u0=u0, vectors=False)  # the first solve runs the autotuner
@@ -724,6 +737,7 @@ def run_batched(args, wl):
     # e2e: host CSR arrays -> batch -> sigma/U/V back
     t0 = time.perf_counter()
     B2 = batch.Batch(mats)
+    B2.set_arith(args.batch_arith)
     sig, bnd, info2, U, V = B2.solve(k, kmax=kmax, tol=tol, maxiter=100, u0=u0, vectors=True)
     B2.close()
     e2e_ms = (time.perf_counter() - t0) * 1e3
@@ -731,8 +745,9 @@ def run_batched(args, wl):
     launches = int(sum(s_["kernel_launches"] for s_ in stats_l))
     # whole job: the slowest rank's times, every rank's counts
     value, e2e_ms = reduce_ranks([value, e2e_ms], "max", world)
-    conv, nopx, launches = (int(v) for v in reduce_ranks([conv, st["nopx"], launches], "sum", world))
-    st = dict(st, nopx=nopx)
+    conv, nopx, launches, nre, nfb = (int(v) for v in reduce_ranks(
+        [conv, st["nopx"], launches, st["nreorth"], st["fallback"]], "sum", world))
+    st = dict(st, nopx=nopx, nreorth=nre, fallback=nfb)
     if rank != 0:
         return 0
     mats, u0 = all_mats, all_u0
@@ -752,6 +767,7 @@ def run_batched(args, wl):
             "config": {"workload": "batched", "desc": wl["desc"], "nprob": nprob, "nnz": int(nnz),
                        "fraction_of_4096": nprob / 4096, "l2": "batch data (GBs) larger than L2; no flush"},
             "problems_per_s": nprob / (value * 1e-3), "converged": conv, "matvecs": st["nopx"],
+            "reorthogonalisations": st["nreorth"], "handed_back": st["fallback"], "batch_arith": args.batch_arith,
             "autotuner": {"table": table, "tune_ms": tune_ms, "one_shape_ms": one_shape_ms,
                           "speedup_vs_one_shape": one_shape_ms / value},
             "cycles": st["cycles"], "persistent_grid": st["grid"],
@@ -857,10 +873,11 @@ def run_learned(args, wl):
 
 def run_complex(args, wl):
     """The complex*16 drivers on the device operator: value = device ms of
-    one zlansvd_irl_ solve (start vector in HBM -> k Ritz triplets); e2e =
-    the same through propack_zcsr_create + zlansvd_irl_ from pinned host
-    arrays (expansion to the 2x2-block form, upload, device transposition,
-    solve, U and V back)."""
+    one zlansvd_irl_ solve (start vector in HBM -> k Ritz triplets) on the
+    native complex operator; e2e = the same through propack_zcsr_create +
+    zlansvd_irl_ from pinned host arrays (upload, device checks and
+    conjugate transposition, solve, U and V back).  The real 2x2-block form
+    of the same matrix is timed beside it (`block_form`)."""
     import ctypes as C
     import numpy as np
     import propack_gb300 as pg
@@ -884,28 +901,45 @@ def run_complex(args, wl):
 
     u = np.zeros((m, kmax + 1), order="F", dtype=np.complex128)
     v = np.zeros((n, kmax), order="F", dtype=np.complex128)
-    op = pg.CsrOperator(S)
-    sampler = ClockSampler(0)
-    sampler.start()
-    for _ in range(args.warmup):
+
+    def measure(form, steps, warmup, sampler=None):
+        pg.set_complex_form(form)
+        try:
+            op = pg.CsrOperator(S)
+        finally:
+            pg.set_complex_form("native")
+        if sampler:
+            sampler.start()
+        for _ in range(warmup):
+            solve(op.aprod, op.iparm, u, v)
+        dev, mvs, launches = [], [], 0
+        for _ in range(steps):
+            sig = solve(op.aprod, op.iparm, u, v)
+            st = pg.get_stats()
+            dev.append(st["solve_ms"])
+            mvs.append(st["nopx"])
+            launches += st["kernel_launches"]
+        clocks = sampler.stop() if sampler else None
+        res = max(max(np.linalg.norm(op.matvec(v[:, i]) - sig[i] * u[:, i]),
+                      np.linalg.norm(op.rmatvec(u[:, i]) - sig[i] * v[:, i])) for i in range(k)) / sig[0]
+        pg.set_profiling(True)
         solve(op.aprod, op.iparm, u, v)
-    dev, mvs, launches = [], [], 0
-    for _ in range(args.steps):
-        sig = solve(op.aprod, op.iparm, u, v)
-        st = pg.get_stats()
-        dev.append(st["solve_ms"])
-        mvs.append(st["nopx"])
-        launches += st["kernel_launches"]
-    clocks = sampler.stop()
-    res = max(max(np.linalg.norm(op.matvec(v[:, i]) - sig[i] * u[:, i]),
-                  np.linalg.norm(op.rmatvec(u[:, i]) - sig[i] * v[:, i])) for i in range(k)) / sig[0]
-    pg.set_profiling(True)
-    solve(op.aprod, op.iparm, u, v)
-    prof = pg.get_profile()
-    st_prof = pg.get_stats()
-    pg.set_profiling(False)
-    op.close()
-    value = statistics.mean(dev)
+        prof = pg.get_profile()
+        st_prof = pg.get_stats()
+        pg.set_profiling(False)
+        op.close()
+        return dict(ms=statistics.mean(dev), matvecs=statistics.mean(mvs), launches=launches, clocks=clocks,
+                    res=res, prof=prof, st_prof=st_prof, sig=sig)
+
+    nat = measure("native", args.steps, args.warmup, ClockSampler(0))
+    blk = measure("block", max(1, min(args.steps, 3)), 1)
+    value, mvs, launches, clocks, res = nat["ms"], nat["matvecs"], nat["launches"], nat["clocks"], nat["res"]
+    prof, st_prof = nat["prof"], nat["st_prof"]
+    block_form = {"ms": blk["ms"], "matvecs": blk["matvecs"], "max_rel_residual": blk["res"],
+                  "spmv_pair_ms": blk["prof"]["spmv_adj"][1] + blk["prof"]["spmv_fwd"][1],
+                  "elr": {"launches": blk["prof"]["elr"][0], "ms": blk["prof"]["elr"][1]},
+                  "max_rel_sigma_diff": float(np.max(np.abs(blk["sig"] - nat["sig"]) / nat["sig"])),
+                  "speedup_native_vs_block": blk["ms"] / nat["ms"]}
 
     # e2e through the public C ABI from pinned host arrays
     import torch
@@ -927,17 +961,22 @@ def run_complex(args, wl):
     h2d = hp.nbytes + hi.nbytes + hv.nbytes + m * 16
     d2h = 2 * k * 8 + k * (m + n) * 16
 
-    # rooflines: the SpMV pair on the 2x2-block form (4 real entries per
-    # complex entry, 2m and 2n real rows) and the complex Gram-Schmidt pair
-    # (16-byte elements)
-    fwd_b, adj_b = spmv_bytes(2 * m, 2 * n, 0, 4 * S.nnz, 0, 0, 8)
+    # rooflines: the native complex SpMV pair (an int32 index and a 16-byte
+    # value per entry, 16-byte gathers and vector elements) and the complex
+    # Gram-Schmidt pair (16-byte elements); the block form's pair reads 4
+    # real entries of 12 bytes per complex entry
+    fwd_b = S.nnz * 20 + (m + 1) * 4 + n * 16 + 3 * m * 16
+    adj_b = S.nnz * 20 + (n + 1) * 4 + m * 16 + 3 * n * 16
+    blk_fwd_b, blk_adj_b = spmv_bytes(2 * m, 2 * n, 0, 4 * S.nnz, 0, 0, 8)
+    block_form["spmv_algorithmic_bytes_per_launch"] = {"fwd": blk_fwd_b, "adj": blk_adj_b}
     n_adj, t_adj = prof["spmv_adj"]
     n_fwd, t_fwd = prof["spmv_fwd"]
     peak, peak_kind = peaks()
     a_spmv = (fwd_b * n_fwd + adj_b * n_adj) / max((t_fwd + t_adj) * 1e-3, 1e-12) / 1e9
-    roof = {"bound": "hbm", "kernel": "fused SpMV pair on the 2x2-block form", "achieved": a_spmv, "peak": peak,
+    roof = {"bound": "hbm", "kernel": "fused native complex SpMV pair", "achieved": a_spmv, "peak": peak,
             "peak_source": peak_kind, "unit": "GB/s", "frac": a_spmv / peak, "traffic": None,
-            "algorithmic_bytes_per_launch": {"fwd": fwd_b, "adj": adj_b}, "ms": t_fwd + t_adj}
+            "algorithmic_bytes_per_launch": {"fwd": fwd_b, "adj": adj_b},
+            "mean_launch_ms": {"fwd": t_fwd / max(n_fwd, 1), "adj": t_adj / max(n_adj, 1)}, "ms": t_fwd + t_adj}
     cgs_ms = prof["cgs_dots"][1] + prof["cgs_upd"][1]
     roof_cgs = None
     if cgs_ms > 0:
@@ -950,7 +989,7 @@ def run_complex(args, wl):
     cpu = None
     if not args.no_cpu:
         cores = os.cpu_count() or 1
-        cv, info = cpu_sample(S, None, None, None, wl, cores, statistics.mean(mvs))
+        cv, info = cpu_sample(S, None, None, None, wl, cores, mvs)
         cpu = {"value": cv, "unit": "ms", "cores": cores, "kind": "port",
                "sample": f"complex oracle (zlansvd_irl restated, OpenMP) one IRL cycle ({info['cycle_matvecs']} "
                          f"matvecs, {info['cycle_ms']:.0f} ms) scaled by matvecs to the device solve's "
@@ -960,7 +999,8 @@ def run_complex(args, wl):
             "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64 pairs)", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "desc": wl["desc"], "scale": args.scale,
                        "l2": "operator and bases are GBs, larger than L2; no flush"},
-            "matvecs": statistics.mean(mvs), "max_rel_residual": res,
+            "matvecs": mvs, "max_rel_residual": res, "operator_form": "native complex CSR",
+            "block_form": block_form,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "roofline": dominant, "rooflines": {"spmv_pair": roof,
                                                                                "gram_schmidt": roof_cgs},

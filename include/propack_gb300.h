@@ -135,11 +135,12 @@ void propack_gpu_csr_aprod_(const char *transa, const int *m, const int *n,
  * must not allocate.  x and y must be memory the operator's device can
  * address (device memory of that device, managed memory, or mapped host
  * memory); anything else is refused with PROPACK_ERR_ARG before any
- * launch.  A complex operator (propack_zcsr_create) is applied in its
- * real 2x2-block form: x holds n (trans: m) complex entries as
- * interleaved (re, im) doubles, 2n doubles, and y receives 2m (trans:
- * 2n) doubles; trans != 0 applies A^H.  No counterpart exists in the
- * reference.  Returns 0 or a negative PROPACK_ERR_* code. */
+ * launch.  A complex operator (propack_zcsr_create, either form): x
+ * holds n (trans: m) complex entries as interleaved (re, im) doubles, 2n
+ * doubles, and y receives 2m (trans: 2n) doubles; trans != 0 applies A^H.
+ * For the native form x and y must be 16-byte aligned (PROPACK_ERR_ARG
+ * otherwise).  No counterpart exists in the reference.  Returns 0 or a
+ * negative PROPACK_ERR_* code. */
 #define PROPACK_NOALLOC_MAX_DOUBLES 65536
 int propack_csr_apply_noalloc(int64_t handle, int trans, const double *x,
                               double *y, void *stream);
@@ -285,13 +286,23 @@ void zlansvd_irl_(const char *which, const char *jobu, const char *jobv,
 
 /* Upload a complex m x n CSR matrix (0-based int64 row pointers, int32
  * column indices, complex*16 values) as a device operator for the complex
- * drivers.  The device holds its real 2m x 2n form: each entry b + ic of A
- * becomes the 2x2 block [b -c; c b] on the (re, im) pairs, so one real
- * SpMV computes A x and the device-transposed one computes A^H x exactly.
- * Same checks and error codes as propack_csr_create; the handle is freed
- * with propack_csr_destroy. */
+ * drivers.  Default (native) form: the device keeps the complex CSR (an
+ * int32 index and a complex*16 value per entry, 20 bytes) and its
+ * conjugate transpose, built on the device; the complex SpMV accumulates
+ * in complex arithmetic and, inside the Lanczos steps, also forms the
+ * complex projection that the local reorthogonalisation subtracts.  Block
+ * form (propack_set_zcsr_form(1)): the device holds the real 2m x 2n
+ * matrix in which each entry b + ic becomes the 2x2 block [b -c; c b] on
+ * the (re, im) pairs (48 bytes per complex entry), applied by the real
+ * kernels.  Both give A x and A^H x to rounding.  Same checks and error
+ * codes as propack_csr_create (native: fewer than 2^31 entries; block
+ * form: 4 nnz < 2^31); the handle is freed with propack_csr_destroy. */
 int propack_zcsr_create(int m, int n, const int64_t *rowptr, const int32_t *colidx, const propack_z16 *val,
                         int64_t *handle);
+/* The form of complex operators created afterwards (process-wide): 0
+ * native complex CSR (default), 1 the real 2x2-block form.  Returns 0, or
+ * PROPACK_ERR_ARG for another value. */
+int propack_set_zcsr_form(int form);
 /* The 2x2-block form itself, on the host (used by propack_zcsr_create):
  * rowptr2 has 2m+1 entries, colidx2 and val2 4 nnz(A) entries.  Returns 0,
  * or PROPACK_ERR_ARG for a negative size or 4 nnz(A) >= 2^31. */
@@ -333,6 +344,11 @@ int propack_mlp_grad(int64_t handle, int64_t op_handle, uint64_t seed, const dou
 /* one Adam step (beta 0.9 / 0.999) with learning rate lr on (operator, U) */
 int propack_mlp_train_step(int64_t handle, int64_t op_handle, uint64_t seed, const double *U, int ldu, int k,
                            double lr, double *loss);
+/* the kernel of the 256 x 256 layer, process-wide: 1 (default) tcgen05.mma
+ * with FP32 accumulators in tensor memory, 0 the mma.sync kernel (the
+ * reference implementation; results differ only in the FP32 accumulation
+ * order).  Returns 0 or PROPACK_ERR_ARG. */
+int propack_mlp_set_impl(int impl);
 
 /* ---- Batched solver (no reference counterpart) -----------------------
  * nprob independent CSR matrices with FP32 values, solved by dlansvd_irl
@@ -390,6 +406,13 @@ int propack_batch_get_stats(propack_batch_stats_t *out);
 #define PROPACK_BATCH_CLASSES 4
 int propack_batch_get_tuning(int64_t handle, int *g, int *dc, float *ms_tuned, float *ms_default);
 int propack_batch_set_tuning(int64_t handle, const int *g, const int *dc);
+/* Arithmetic of a batch's products and Gram-Schmidt passes: 0 FP64 FMAs on
+ * the FP64 bases (default), 2 FP32 (hi, lo) planes of every basis column,
+ * split once per final column, summed as compensated FP32 pairs (results
+ * agree with the FP64 ones to rounding; on a GB300 the batched workload
+ * measured slower with planes).  A timed autotuner table is redone when the
+ * arithmetic changes.  Returns 0, PROPACK_ERR_ARG or PROPACK_ERR_HANDLE. */
+int propack_batch_set_arith(int64_t handle, int arith);
 
 /* ---- FP64 product on the tensor cores --------------------------------
  * C (mr x nc, column-major ldc) = A (mr x kk, column-major lda) op(B), with
@@ -412,6 +435,15 @@ int propack_gemm_f64_tc(int impl, int mr, int nc, int kk, const double *A, int l
  * concurrently; kept between calls for the same reason).
  * Returns 0 or PROPACK_ERR_CUDA. */
 int propack_release_memory(void);
+
+/* Roofline calibration of the sparse products: the device ms of one pass of
+ * nnz random 8-byte reads from an n-entry FP64 vector (which stays in L2 for
+ * n up to ~16 M) with their 12-byte (int32 index, FP64 value) stream, flat,
+ * four independent entries in flight per thread -- the fastest a product
+ * with uniformly random columns can run on this GPU, whatever its rows.
+ * Median of five passes after three.  Returns 0 or a negative
+ * PROPACK_ERR_*.  No reference counterpart. */
+int propack_gather_ceiling(int n, int64_t nnz, float *ms);
 
 /* Last error message for the calling thread ("" if none). */
 const char *propack_last_error(void);

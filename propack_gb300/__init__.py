@@ -74,6 +74,8 @@ def load(build_if_missing=True):
     L.propack_zcsr_create.argtypes = [C.c_int, C.c_int, i64p, ip, C.c_void_p, i64p]
     L.propack_zcsr_expand.restype = C.c_int
     L.propack_zcsr_expand.argtypes = [C.c_int, C.c_int, i64p, ip, C.c_void_p, i64p, ip, dp]
+    L.propack_set_zcsr_form.restype = C.c_int
+    L.propack_set_zcsr_form.argtypes = [C.c_int]
     L.propack_last_error.restype = C.c_char_p
     L.propack_get_stats.argtypes = [C.POINTER(_Stats)]
     _lib = L
@@ -179,8 +181,9 @@ class CsrOperator:
         self.r = r
 
     def _init_complex(self, lib, S, L):
-        # a complex S alone (propack_zcsr_create): the device holds its real
-        # 2x2-block form, which the complex drivers apply as A and A^H
+        # a complex S alone (propack_zcsr_create): the device holds it as a
+        # native complex CSR (or its real 2x2-block form, set_complex_form),
+        # which the complex drivers apply as A and A^H
         if L is not None:
             raise TypeError("a complex operator takes no low-rank term")
         self.dtype = np.dtype(np.complex128)
@@ -396,6 +399,16 @@ def set_cgs_arith(arith):
     rc = load().propack_set_cgs_arith({"fp64": 0, "f3": 1, "planes": 2}[arith])
     if rc != 0:
         raise PropackError(f"propack_set_cgs_arith failed ({rc})")
+
+
+def set_complex_form(form):
+    """Form of complex device operators created afterwards (process-wide):
+    "native" (the default: complex CSR, one index and one complex value per
+    entry, complex SpMV) or "block" (the real 2x2-block form applied by the
+    real kernels; propack_set_zcsr_form)."""
+    rc = load().propack_set_zcsr_form({"native": 0, "block": 1}[form])
+    if rc != 0:
+        raise PropackError(f"propack_set_zcsr_form failed ({rc})")
 
 
 def get_precision():

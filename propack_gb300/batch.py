@@ -39,6 +39,7 @@ def _lib():
         L.propack_batch_get_stats.argtypes = [C.POINTER(BatchStats)]
         L.propack_batch_get_tuning.argtypes = [C.c_int64, _ip, _ip, _fp, _fp]
         L.propack_batch_set_tuning.argtypes = [C.c_int64, _ip, _ip]
+        L.propack_batch_set_arith.argtypes = [C.c_int64, C.c_int]
         L._batch_bound = True
     return L
 
@@ -93,6 +94,14 @@ class Batch:
             rc = self._L.propack_batch_set_tuning(self.handle, ga.ctypes.data_as(_ip), da.ctypes.data_as(_ip))
         if rc != 0:
             raise PropackError(f"propack_batch_set_tuning failed ({rc}): {last_error()}")
+
+    def set_arith(self, arith):
+        """Arithmetic of the products and Gram-Schmidt passes: "fp64" (the
+        default) or "planes" (FP32 (hi, lo) planes of the bases;
+        propack_batch_set_arith)."""
+        rc = self._L.propack_batch_set_arith(self.handle, {"fp64": 0, "planes": 2}[arith])
+        if rc != 0:
+            raise PropackError(f"propack_batch_set_arith failed ({rc})")
 
     def close(self):
         if self.handle:

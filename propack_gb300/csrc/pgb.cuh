@@ -73,6 +73,11 @@ struct Csr {
     int *cidx = nullptr;      // 32 * tbase[tiles] (padding: column 0, value 0)
     double *cval = nullptr;
     float *cvalf = nullptr;
+    // a native complex matrix (Operator::cplx == 2): (re, im) values in CSR
+    // order and run-interleaved for the chunked schedule, which it always
+    // uses; val, valf and cval stay null
+    double2 *zval = nullptr;  // nnz
+    double2 *czval = nullptr; // 32 * tbase[tiles]
 };
 
 // A = S + L diag(w) R'.  fwd = [S | L] (m x (n+r)), adj = [S' | R]
@@ -87,7 +92,9 @@ struct Operator {
     int64_t id = 0;
     int device = 0;
     // 1: a complex m/2 x n/2 matrix held as its real 2x2-block form (fwd
-    // computes A x and adj computes A^H x on (re, im) pairs)
+    // computes A x and adj computes A^H x on (re, im) pairs); 2: a complex
+    // m x n matrix held natively (index + complex value per entry, adj its
+    // conjugate transpose)
     int cplx = 0;
 };
 Operator *lookup_operator(int64_t handle);
@@ -159,6 +166,7 @@ struct LbArgs {
     int nb;                 // CTAs of the vector kernels
     int kmax;               // capacity of the column arrays
     Csr fwd, adj;           // device operator (fwd = [S|L], adj = [S'|R])
+    Csr zfwd, zadj;         // a native complex operator (A, A^H; rows = 0 otherwise)
     const double *z;        // low-rank coefficients of the current product
     // FP64 form, Gram-Schmidt on the FP32 pipe (null when off): the
     // basis columns as FP32 (hi, lo) planes with the leading dimensions of
@@ -372,7 +380,7 @@ void copy_cols(const T *src, int lds, T *dst, int ldd, int rows, int cols, cudaS
 
 // ------------------------------------------------ Lanczos step enqueue
 void lb_set_smem_limits(int kmax);
-bool lb_planes_fit(int kmax);
+bool lb_planes_fit(int kmax, bool cplx);
 // Gram-Schmidt arithmetic of the FP64 form: 0 FP64 FMAs, 1 three-way
 // splits on the FP32 pipe (pgb_f3.cuh), 2 split-once planes (the default)
 enum CgsArith { CGS_FP64 = 0, CGS_F3 = 1, CGS_PLANES = 2 };
@@ -416,5 +424,10 @@ int scan_excl(const int *in, int *out, int n, cudaStream_t s);
 // operator application on device vectors (no Lanczos fusion)
 template <typename T>
 void op_apply(const Operator &op, bool trans, const T *x, T *y, cudaStream_t s);
+// y = A x (trans: A^H x) for a complex operator of either form, on complex
+// device vectors
+void op_zapply(const Operator &op, bool trans, const double2 *x, double2 *y, cudaStream_t s);
+// the plain complex product of one side of a native complex operator
+void op_zspmv_plain_launch(const Csr &A, const double2 *x, double2 *y, cudaStream_t s);
 
 }  // namespace pgb

@@ -4,7 +4,9 @@
 // runs dlansvd_irl (double/dlansvd_irl.F:160-419) on every problem with full
 // reorthogonalisation (dlanbpro.F with delta = 0: every new Lanczos vector
 // is orthogonalised against all previous ones by iterated classical
-// Gram-Schmidt, dreorth.F:106-210) and FP64 vectors.
+// Gram-Schmidt, dreorth.F:106-210) and FP64 vectors.  Optionally the products
+// and the Gram-Schmidt passes read the bases as FP32 (hi, lo) planes, split
+// once per final column (pgb_planes.cuh; propack_batch_set_arith).
 //
 // Execution: one CTA owns one problem at a time.  A persistent grid pulls
 // problems from a work queue ordered by decreasing cost (an atomic ticket)
@@ -30,6 +32,7 @@
 #include "../../include/propack_gb300.h"
 #include "pgb.cuh"
 #include "pgb_bidiag.cuh"
+#include "pgb_planes.cuh"
 #include "pgb_scalar.cuh"
 
 namespace pgb {
@@ -53,6 +56,7 @@ struct BProb {
     const int *tptr, *tidx;   // A' (n x m)
     const float *tval;
     double *U, *V;            // m x (dim+1), n x dim (leading dimensions m, n)
+    float2 *Up, *Vp;          // their FP32 (hi, lo) planes, written when a column is final
     double *alpha, *beta;     // dim + 1 each
     double *sig, *bnd;        // neig each (outputs)
     double rnorm, anorm;
@@ -93,7 +97,8 @@ struct BShared {
     double cs[BDIM_MAX + 2], sn[BDIM_MAX + 2];
     double shifts[BDIM_MAX + 2];
     double scal[8];
-    int flag;
+    float2 hp[BDIM_MAX + 2];  // Gram-Schmidt coefficients as planes
+    int flag, xe;
 };
 
 // ------------------------------------------------------ CTA vector helpers
@@ -233,12 +238,162 @@ __device__ void cta_reorth(const double *W, int ld, int ncols, double *x, int le
     count++;
 }
 
+// ---------------------------------------------------- on the FP32 pipe
+// With propack_batch_set_arith(h, 2) the cycle's products and Gram-Schmidt
+// passes read the bases as FP32 (hi, lo) planes (pgb_planes.cuh): every
+// basis column is split once, when it is final (normalised, or rewritten by
+// a restart), and every later product or projection that reads it runs on
+// the FP32 pipe instead of the FP64 pipe.  Measured on a GB300 (1024
+// problems of the batched workload) it is not faster: 4899 ms and 635,328
+// matvecs against 4299 ms and 581,632 with the FP64 routines above, which
+// stay the default.
+
+__device__ void cta_split_col(const double *w, float2 *wp, int len)
+{
+    for (int i = threadIdx.x; i < len; i += BT) wp[i] = pl_split(w[i]);
+}
+
+// y = A x with x given by its planes: each product val * (hi + lo) with the
+// FP32 value exact, summed as a compensated pair, the row split g as in
+// cta_spmv; y in FP64
+__device__ void cta_spmv_pl(const int *ptr, const int *idx, const float *val, int rows, const float2 *xp, double *y,
+                            int g)
+{
+    const int grp = threadIdx.x / g, lig = threadIdx.x % g, ngrp = BT / g;
+    for (int r0 = 0; r0 < rows; r0 += ngrp) {
+        const int r = r0 + grp;
+        PlAcc acc;
+        if (r < rows) {
+            const int e1 = ptr[r + 1];
+            int e = ptr[r] + lig;
+            for (; e + 3 * g < e1; e += 4 * g) {
+                const int c0 = idx[e], c1 = idx[e + g], c2 = idx[e + 2 * g], c3 = idx[e + 3 * g];
+                const float v0 = val[e], v1 = val[e + g], v2 = val[e + 2 * g], v3 = val[e + 3 * g];
+                const float2 x0 = xp[c0], x1 = xp[c1], x2 = xp[c2], x3 = xp[c3];
+                acc.add(v0, 0.f, x0.x, x0.y);
+                acc.add(v1, 0.f, x1.x, x1.y);
+                acc.add(v2, 0.f, x2.x, x2.y);
+                acc.add(v3, 0.f, x3.x, x3.y);
+            }
+            for (; e < e1; e += g) {
+                const float2 xv = xp[idx[e]];
+                acc.add(val[e], 0.f, xv.x, xv.y);
+            }
+        }
+        for (int o = g >> 1; o > 0; o >>= 1)
+            pl_pair_add(acc.s, acc.c, __shfl_xor_sync(0xffffffffu, acc.s, o, g),
+                        __shfl_xor_sync(0xffffffffu, acc.c, o, g));
+        if (r < rows && lig == 0) y[r] = acc.value_int();
+    }
+    __syncthreads();
+}
+
+// projections S.h = Wp(:, 0:ncols)' xq * back from the planes, dc adjacent
+// columns per warp (every column's sum in the same order whatever dc is)
+template <int DC>
+__device__ void cta_proj_pl(const float2 *Wp, int ld, int ncols, const float2 *xq, int len, double back, BShared &S)
+{
+    const int lane = threadIdx.x & 31;
+    for (int c0 = (threadIdx.x >> 5) * DC; c0 < ncols; c0 += BW * DC) {
+        const int nc = min(DC, ncols - c0);
+        PlAcc acc[DC];
+        for (int i = lane; i < len; i += 32) {
+            const float2 xv = xq[i];
+#pragma unroll
+            for (int u = 0; u < DC; u++)
+                if (u < nc) {
+                    const float2 wv = Wp[(size_t)(c0 + u) * ld + i];
+                    acc[u].add(wv.x, wv.y, xv.x, xv.y);
+                }
+        }
+#pragma unroll
+        for (int u = 0; u < DC; u++) {
+            const double t = warp_sum(acc[u].value_int());
+            if (lane == 0 && u < nc) S.h[c0 + u] = t * back;
+        }
+    }
+}
+__device__ void cta_proj_pl_dc(const float2 *Wp, int ld, int ncols, const float2 *xq, int len, double back, BShared &S,
+                               int dc)
+{
+    if (dc >= 4) cta_proj_pl<4>(Wp, ld, ncols, xq, len, back, S);
+    else if (dc == 2) cta_proj_pl<2>(Wp, ld, ncols, xq, len, back, S);
+    else cta_proj_pl<1>(Wp, ld, ncols, xq, len, back, S);
+}
+
+// x (len) as planes in xq, scaled by 2^-xs for the CTA's largest exponent
+// (|x 2^-xs| < 2); returns 2^xs
+__device__ double cta_xplanes(const double *x, int len, float2 *xq, BShared &S)
+{
+    if (threadIdx.x == 0) S.xe = 0;
+    __syncthreads();
+    int e = 0;
+    for (int i = threadIdx.x; i < len; i += BT) e = max(e, f3_expo(x[i]));
+    if (e) atomicMax(&S.xe, e);
+    __syncthreads();
+    const int xs = S.xe == 0 ? 0 : S.xe - 1023;
+    for (int i = threadIdx.x; i < len; i += BT) xq[i] = pl_xsplit(x[i], xs);
+    __syncthreads();
+    return f3_pow2(xs);
+}
+
+// dreorth with iterated CGS on the planes of W (dreorth.F:106-210); the same
+// control flow as cta_reorth.  xq: len float2 of scratch
+__device__ void cta_reorth_pl(const float2 *Wp, int ld, int ncols, double *x, int len, double *nrm, BShared &S,
+                              int &count, int dc, float2 *xq)
+{
+    if (ncols <= 0) return;
+    double nrm0 = *nrm;
+    for (int it = 0; it < NTRY; it++) {
+        const double back = cta_xplanes(x, len, xq, S);
+        cta_proj_pl_dc(Wp, ld, ncols, xq, len, back, S, dc);
+        __syncthreads();
+        // h as planes, scaled by the power of two of its largest entry
+        if (threadIdx.x == 0) S.xe = 0;
+        __syncthreads();
+        int he = 0;
+        for (int c = threadIdx.x; c < ncols; c += BT) he = max(he, f3_expo(S.h[c]));
+        if (he) atomicMax(&S.xe, he);
+        __syncthreads();
+        const int hs = S.xe == 0 ? 0 : S.xe - 1023;
+        for (int c = threadIdx.x; c < ncols; c += BT) S.hp[c] = pl_xsplit(S.h[c], hs);
+        __syncthreads();
+        const double hback = f3_pow2(hs);
+        double a = 0.0;
+        for (int i = threadIdx.x; i < len; i += BT) {
+            PlAcc sm;
+            for (int c = 0; c < ncols; c++) {
+                const float2 wv = Wp[(size_t)c * ld + i];
+                sm.add(wv.x, wv.y, S.hp[c].x, S.hp[c].y);
+            }
+            double v = x[i];
+            v = fma(-pl_f2d(sm.s), hback, v);
+            v = fma(-pl_f2d(sm.c), hback, v);
+            x[i] = v;
+            a = fma(v, v, a);
+        }
+        const double s = sqrt(cta_sum(a, S));
+        if (s > KAPPA * nrm0) {
+            *nrm = s;
+            count++;
+            return;
+        }
+        nrm0 = s;
+    }
+    for (int i = threadIdx.x; i < len; i += BT) x[i] = 0.0;
+    __syncthreads();
+    *nrm = 0.0;
+    count++;
+}
+
 // ------------------------------------------------------------- Lanczos
 // dlanbpro.F:146-549 with full reorthogonalisation, from k0 to dim.
 // Returns false when the problem must go to the single-problem driver.
-__device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S)
+template <bool PL>
+__device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S, float2 *xq)
 {
     const int m = P.m, n = P.n, dim = c.dim, k0 = P.k0;
+    float2 *Up = P.Up, *Vp = P.Vp;
     int nopx = 0, nre = 0;  // counted redundantly by every thread, stored by thread 0
     bool ok = true;
     const int mn = m > n ? m : n;
@@ -250,16 +405,28 @@ __device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S)
         beta = P.rnorm;
         alpha = 0.0;
         cta_safescal(m, beta, U);
+        if (PL) cta_split_col(U, Up, m);
+        __syncthreads();
         j0 = 1;
     } else {
         alpha = ba[k0 - 1];
         beta = P.rnorm;
+        // the restart rewrote U(:, 0:k0) and V(:, 0:k0): their planes
+        if (PL)
+            for (int q = 0; q < k0; q++) {
+                cta_split_col(U + (size_t)q * m, Up + (size_t)q * m, m);
+                cta_split_col(V + (size_t)q * n, Vp + (size_t)q * n, n);
+            }
+        __syncthreads();
         double *uk = U + (size_t)k0 * m;
         for (int i = threadIdx.x; i < m; i += BT) uk[i] *= P.rnorm;
         __syncthreads();
         double r = P.rnorm;
-        cta_reorth(U, m, k0, uk, m, &r, S, nre, P.dc);
+        if (PL) cta_reorth_pl(Up, m, k0, uk, m, &r, S, nre, P.dc, xq);
+        else cta_reorth(U, m, k0, uk, m, &r, S, nre, P.dc);
         cta_safescal(m, r, uk);
+        if (PL) cta_split_col(uk, Up + (size_t)k0 * m, m);
+        __syncthreads();
         beta = r;
         if (threadIdx.x == 0) bb[k0 - 1] = beta;
         __syncthreads();
@@ -283,7 +450,8 @@ __device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S)
     for (int j = j0; j <= dim; j++) {
         double *vj = V + (size_t)(j - 1) * n, *uj = U + (size_t)(j - 1) * m, *uj1 = U + (size_t)j * m;
         // alpha_j v_j = A' u_j - beta_j v_{j-1}
-        cta_spmv(P.tptr, P.tidx, P.tval, n, uj, vj, P.g);
+        if (PL) cta_spmv_pl(P.tptr, P.tidx, P.tval, n, Up + (size_t)(j - 1) * m, vj, P.g);
+        else cta_spmv(P.tptr, P.tidx, P.tval, n, uj, vj, P.g);
         nopx++;
         if (j == 1) {
             alpha = cta_nrm2(vj, n, S);
@@ -316,12 +484,20 @@ __device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S)
             }
             anorm = fmax(anorm, a1);
         }
-        if (alpha != 0.0) cta_reorth(V, n, j - 1, vj, n, &alpha, S, nre, P.dc);
+        if (alpha != 0.0) {
+            if (PL) cta_reorth_pl(Vp, n, j - 1, vj, n, &alpha, S, nre, P.dc, xq);
+            else cta_reorth(V, n, j - 1, vj, n, &alpha, S, nre, P.dc);
+        }
         if (alpha < anorm * epsn && j < dim) { ok = false; break; }
         if (threadIdx.x == 0) ba[j - 1] = alpha;
         if (alpha != 0.0) cta_safescal(n, alpha, vj);
+        if (PL) {
+            cta_split_col(vj, Vp + (size_t)(j - 1) * n, n);
+            __syncthreads();
+        }
         // beta_{j+1} u_{j+1} = A v_j - alpha_j u_j
-        cta_spmv(P.ptr, P.idx, P.val, m, vj, uj1, P.g);
+        if (PL) cta_spmv_pl(P.ptr, P.idx, P.val, m, Vp + (size_t)(j - 1) * n, uj1, P.g);
+        else cta_spmv(P.ptr, P.idx, P.val, m, vj, uj1, P.g);
         nopx++;
         cta_axpy(m, -alpha, uj, uj1);
         beta = cta_nrm2(uj1, m, S);
@@ -348,10 +524,17 @@ __device__ bool b_lanbpro(BProb &P, const BCfg &c, BShared &S)
             a1 = amax * sqrt(a1 * a1 + (beta / amax) * (beta / amax) + a1 * bb[j - 2] / amax);
         }
         anorm = fmax(anorm, a1);
-        if (beta != 0.0) cta_reorth(U, m, j, uj1, m, &beta, S, nre, P.dc);
+        if (beta != 0.0) {
+            if (PL) cta_reorth_pl(Up, m, j, uj1, m, &beta, S, nre, P.dc, xq);
+            else cta_reorth(U, m, j, uj1, m, &beta, S, nre, P.dc);
+        }
         if (beta < anorm * epsn && j < dim) { ok = false; break; }
         if (threadIdx.x == 0) bb[j - 1] = beta;
         if (beta != 0.0) cta_safescal(m, beta, uj1);
+        if (PL) {
+            cta_split_col(uj1, Up + (size_t)j * m, m);
+            __syncthreads();
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -638,6 +821,7 @@ __device__ bool b_ritz(BProb &P, const BCfg &c, BShared &S, double *scr, const B
 }
 
 // ------------------------------------------------------- the cycle kernel
+template <bool PL>
 __global__ void __launch_bounds__(BT, 2) k_batch_cycle(BProb *probs, const int *order, int nprob, BCfg c,
                                                     double *scratch, size_t scr_stride, int *ticket, int *active,
                                                     int cycles_per_launch)
@@ -655,7 +839,7 @@ __global__ void __launch_bounds__(BT, 2) k_batch_cycle(BProb *probs, const int *
         // up to cycles_per_launch restart cycles of this problem, then it is
         // handed back to the queue of the next replay
         for (int rep = 0; rep < cycles_per_launch && P.status == BS_ACTIVE; rep++) {
-            bool ok = b_lanbpro(P, c, S);
+            bool ok = b_lanbpro<PL>(P, c, S, reinterpret_cast<float2 *>(scr + L.W));
             int nconv = ok ? b_analyse(P, c, S, scr, L) : -1;
             if (nconv < 0) {
                 if (threadIdx.x == 0) P.status = BS_FALLBACK;
@@ -687,20 +871,29 @@ __global__ void __launch_bounds__(BT, 2) k_batch_cycle(BProb *probs, const int *
 // The autotuner's probe: for each sampled problem (one CTA each) the two
 // products and the Gram-Schmidt projections of one vector against ncols
 // columns on both sides, with the candidate row split g and projection tile
-// dc.  The operands are the problem's own basis arrays, zeroed beforehand:
-// U(:,0) -> V(:,0) -> U(:,1), and column ncols of each side against the
-// ncols before it.
+// dc.  The operands are the problem's own basis arrays and planes, zeroed
+// beforehand: U(:,0) -> V(:,0) -> U(:,1), and column ncols of each side
+// against the ncols before it.
+template <bool PL>
 __global__ void __launch_bounds__(BT) k_batch_probe(const BProb *probs, const int *sample, int ns, int g, int dc,
                                                     int ncols)
 {
     __shared__ BShared S;
     for (int q = blockIdx.x; q < ns; q += gridDim.x) {
         const BProb &P = probs[sample[q]];
-        cta_spmv(P.tptr, P.tidx, P.tval, P.n, P.U, P.V, g);
-        cta_spmv(P.ptr, P.idx, P.val, P.m, P.V, P.U + P.m, g);
-        cta_proj_dc(P.U, P.m, ncols, P.U + (size_t)ncols * P.m, P.m, S, dc);
-        __syncthreads();
-        cta_proj_dc(P.V, P.n, ncols, P.V + (size_t)ncols * P.n, P.n, S, dc);
+        if (PL) {
+            cta_spmv_pl(P.tptr, P.tidx, P.tval, P.n, P.Up, P.V, g);
+            cta_spmv_pl(P.ptr, P.idx, P.val, P.m, P.Vp, P.U + P.m, g);
+            cta_proj_pl_dc(P.Up, P.m, ncols, P.Up + (size_t)ncols * P.m, P.m, 1.0, S, dc);
+            __syncthreads();
+            cta_proj_pl_dc(P.Vp, P.n, ncols, P.Vp + (size_t)ncols * P.n, P.n, 1.0, S, dc);
+        } else {
+            cta_spmv(P.tptr, P.tidx, P.tval, P.n, P.U, P.V, g);
+            cta_spmv(P.ptr, P.idx, P.val, P.m, P.V, P.U + P.m, g);
+            cta_proj_dc(P.U, P.m, ncols, P.U + (size_t)ncols * P.m, P.m, S, dc);
+            __syncthreads();
+            cta_proj_dc(P.V, P.n, ncols, P.V + (size_t)ncols * P.n, P.n, S, dc);
+        }
         __syncthreads();
     }
 }
@@ -783,6 +976,8 @@ struct Batch {
     // autotuner: per size class (quarters of `order`) the row split and the
     // projection tile, the probe's ms with them and with the defaults (1, 1)
     int tuned = 0;           // 0: tune at the next solve, 1: timed, 2: set by the caller
+    int tuned_pl = -1;       // the arithmetic the timed table was made for (1: planes)
+    int planes = 0;          // products and Gram-Schmidt on FP32 planes (propack_batch_set_arith)
     int g[PROPACK_BATCH_CLASSES], dc[PROPACK_BATCH_CLASSES];
     float ms_best[PROPACK_BATCH_CLASSES], ms_default[PROPACK_BATCH_CLASSES];
     int cls(int pos) const { return std::min(PROPACK_BATCH_CLASSES - 1, pos * PROPACK_BATCH_CLASSES / nprob); }
@@ -796,6 +991,7 @@ static thread_local propack_batch_stats_t g_batch_stats;
 // size class and keep the fastest; the defaults (1, 1) stay unless a
 // candidate is more than 3 % faster, so that near-ties do not flip the
 // choice (and with it the SpMV's summation order) between batches.
+template <bool PL>
 static void batch_tune(Batch *B, BProb *dprob, int grid, int dim, cudaStream_t s)
 {
     static const int gs[] = {1, 4, 8, 32};
@@ -819,11 +1015,11 @@ static void batch_tune(Batch *B, BProb *dprob, int grid, int dim, cudaStream_t s
         float best = 0.f, def = 0.f;
         for (int g : gs)
             for (int dc : dcs) {
-                k_batch_probe<<<ns, BT, 0, s>>>(dprob, dsample, ns, g, dc, ncols);
+                k_batch_probe<PL><<<ns, BT, 0, s>>>(dprob, dsample, ns, g, dc, ncols);
                 PGB_LAUNCHED();
                 PGB_CUDA(cudaEventRecord(e0, s));
                 for (int r = 0; r < 2; r++) {
-                    k_batch_probe<<<ns, BT, 0, s>>>(dprob, dsample, ns, g, dc, ncols);
+                    k_batch_probe<PL><<<ns, BT, 0, s>>>(dprob, dsample, ns, g, dc, ncols);
                     PGB_LAUNCHED();
                 }
                 PGB_CUDA(cudaEventRecord(e1, s));
@@ -850,6 +1046,7 @@ static void batch_tune(Batch *B, BProb *dprob, int grid, int dim, cudaStream_t s
     cudaEventDestroy(e1);
     cudaFree(dsample);
     B->tuned = 1;
+    B->tuned_pl = PL ? 1 : 0;
 }
 
 }  // namespace pgb
@@ -1018,6 +1215,14 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
         };
         alloc((void **)&dU, sizeof(double) * (size_t)B->total_m * d1);
         alloc((void **)&dV, sizeof(double) * (size_t)B->total_n * dim);
+        // the plane arithmetic (propack_batch_set_arith(h, 2)) keeps FP32
+        // (hi, lo) planes of both bases; the default uses the FP64 bases
+        const bool pl = B->planes != 0;
+        float2 *dUp = nullptr, *dVp = nullptr;
+        if (pl) {
+            alloc((void **)&dUp, sizeof(float2) * (size_t)B->total_m * d1);
+            alloc((void **)&dVp, sizeof(float2) * (size_t)B->total_n * dim);
+        }
         alloc((void **)&dab, sizeof(double) * (size_t)np * 2 * (d1 + 1));
         alloc((void **)&dsb, sizeof(double) * (size_t)np * 2 * neig);
         alloc((void **)&dprob, sizeof(BProb) * np);
@@ -1026,7 +1231,8 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
         alloc((void **)&dactive, sizeof(int));
         PGB_CUDA(cudaMallocHost(&hactive, sizeof(int)));
         int occ = 0;
-        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_cycle, BT, 0));
+        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pl ? k_batch_cycle<true> : k_batch_cycle<false>,
+                                                               BT, 0));
         const int grid = std::max(1, std::min(np, std::max(1, occ) * device_info().sms));
         const BScrLayout L = bscr_layout(dim, maxrows);
         const size_t stride = (L.total + 31) / 32 * 32;
@@ -1049,6 +1255,8 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
             P.tval = B->d_tval;
             P.U = dU + mo * d1;
             P.V = dV + no * dim;
+            P.Up = pl ? dUp + mo * d1 : nullptr;
+            P.Vp = pl ? dVp + no * dim : nullptr;
             P.alpha = dab + (size_t)p * 2 * (d1 + 1);
             P.beta = P.alpha + (d1 + 1);
             P.sig = dsb + (size_t)p * 2 * neig;
@@ -1059,12 +1267,19 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
         // the tuning (once per batch, before its first solve's timing) and
         // every problem's choice by its size class
         for (int p = 0; p < np; p++) hp[p].g = hp[p].dc = 1;
-        if (!B->tuned) {
+        // a timed table is redone when the arithmetic changed since
+        if (!B->tuned || (B->tuned == 1 && B->tuned_pl != (pl ? 1 : 0))) {
             const auto t0 = std::chrono::steady_clock::now();
             PGB_CUDA(cudaMemcpyAsync(dprob, hp.data(), sizeof(BProb) * np, cudaMemcpyHostToDevice, s));
             PGB_CUDA(cudaMemsetAsync(dU, 0, sizeof(double) * (size_t)B->total_m * d1, s));
             PGB_CUDA(cudaMemsetAsync(dV, 0, sizeof(double) * (size_t)B->total_n * dim, s));
-            batch_tune(B, dprob, grid, dim, s);
+            if (pl) {
+                PGB_CUDA(cudaMemsetAsync(dUp, 0, sizeof(float2) * (size_t)B->total_m * d1, s));
+                PGB_CUDA(cudaMemsetAsync(dVp, 0, sizeof(float2) * (size_t)B->total_n * dim, s));
+                batch_tune<true>(B, dprob, grid, dim, s);
+            } else {
+                batch_tune<false>(B, dprob, grid, dim, s);
+            }
             g_batch_stats.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
                                         .count();
         }
@@ -1099,8 +1314,12 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
         PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         PGB_CUDA(cudaMemsetAsync(dticket, 0, sizeof(int), s));
         PGB_CUDA(cudaMemsetAsync(dactive, 0, sizeof(int), s));
-        k_batch_cycle<<<grid, BT, 0, s>>>(dprob, dorder, np, cfg, scratch, stride, dticket, dactive,
-                                          BATCH_CYCLES_PER_LAUNCH);
+        if (pl)
+            k_batch_cycle<true><<<grid, BT, 0, s>>>(dprob, dorder, np, cfg, scratch, stride, dticket, dactive,
+                                                    BATCH_CYCLES_PER_LAUNCH);
+        else
+            k_batch_cycle<false><<<grid, BT, 0, s>>>(dprob, dorder, np, cfg, scratch, stride, dticket, dactive,
+                                                     BATCH_CYCLES_PER_LAUNCH);
         PGB_CUDA(cudaMemcpyAsync(hactive, dactive, sizeof(int), cudaMemcpyDeviceToHost, s));
         PGB_CUDA(cudaStreamEndCapture(s, &graph));
         PGB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
@@ -1156,6 +1375,16 @@ extern "C" int propack_batch_solve(int64_t handle, int dim, int neig, int maxite
         cudaFreeHost(hactive);
         cudaStreamDestroy(s);
     })
+}
+
+extern "C" int propack_batch_set_arith(int64_t handle, int arith)
+{
+    if (arith != 0 && arith != 2) return PROPACK_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    auto it = g_batches.find(handle);
+    if (it == g_batches.end()) return PROPACK_ERR_HANDLE;
+    it->second->planes = arith == 2 ? 1 : 0;
+    return 0;
 }
 
 extern "C" int propack_batch_get_tuning(int64_t handle, int *g, int *dc, float *ms_tuned, float *ms_default)

@@ -267,12 +267,25 @@ struct Ctx {
     cudaEvent_t wev[2] = {nullptr, nullptr};
     std::vector<void *> allocs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
+    // the left Ritz vectors are final (recorded by dev_ritzvec): their copy
+    // to the host may run on s2 while the right ones are formed on s
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev_u = nullptr, ev_s2 = nullptr;
+    bool u_final = false;
 
+    // zero-filled device memory from the library's pool
     void *dbytes(size_t bytes)
+    {
+        void *p = dbytes_raw(bytes);
+        PGB_CUDA(cudaMemsetAsync(p, 0, std::max<size_t>(bytes, 16), s));
+        return p;
+    }
+    // device memory left as it is: only for arrays that are always written
+    // before they are read
+    void *dbytes_raw(size_t bytes)
     {
         bytes = std::max<size_t>(bytes, 16);
         void *p = pool_alloc(bytes, s);
-        PGB_CUDA(cudaMemsetAsync(p, 0, bytes, s));
         allocs.push_back(p);
         return p;
     }
@@ -295,6 +308,9 @@ struct Ctx {
         if (ev1) cudaEventDestroy(ev1);
         if (evs0) cudaEventDestroy(evs0);
         if (evs1) cudaEventDestroy(evs1);
+        if (ev_u) cudaEventDestroy(ev_u);
+        if (ev_s2) cudaEventDestroy(ev_s2);
+        if (s2) cudaStreamDestroy(s2);
         if (s) cudaStreamDestroy(s);
     }
     LbArgs args() const
@@ -305,8 +321,14 @@ struct Ctx {
         a.index = index; a.sel = sel; a.h = h;
         a.part_sq = part_sq; a.part_dot = part_dot; a.part_cols = part_cols;
         a.nb = nb; a.kmax = kmax;
-        if (op) { a.fwd = op->fwd; a.adj = op->adj; a.z = op->zbuf; }
-        else {
+        if (op && op->cplx == 2) {
+            // a native complex operator: its own kernels read zfwd / zadj;
+            // fwd and adj carry only the vector lengths in real scalars
+            a.zfwd = op->fwd; a.zadj = op->adj;
+            a.fwd.rows = m * vw; a.adj.rows = n * vw; a.z = nullptr;
+        } else if (op) {
+            a.fwd = op->fwd; a.adj = op->adj; a.z = op->zbuf;
+        } else {
             a.fwd.rows = m * vw; a.adj.rows = n * vw; a.z = nullptr;
         }
         a.Up = Up; a.Vp = Vp; a.okU = okU; a.okV = okV; a.xpl = xpl;
@@ -324,6 +346,17 @@ struct Ctx {
     }
     void put_ctl() { PGB_CUDA(cudaMemcpyAsync(ctl, hctl, sizeof(LbCtl), cudaMemcpyHostToDevice, s)); }
 };
+
+// CTAs of the vector kernels: about 2048 vector elements or 16384 nonzeros
+// each, at most the four per SM that the partial-sum arrays hold.  A small
+// problem then runs its many short kernels on a few CTAs instead of
+// launching four per SM that mostly find no work.
+static int vec_grid(int64_t elems, int64_t nnz)
+{
+    const int64_t cap = device_info().nb;
+    const int64_t want = std::max((elems + 2047) / 2048, (nnz + 16383) / 16384);
+    return (int)std::max<int64_t>(1, std::min(cap, want));
+}
 
 template <typename T>
 static void init_ctx(Ctx &c, int m, int n, int kmax)
@@ -377,11 +410,17 @@ static void init_ctx(Ctx &c, int m, int n, int kmax)
     c.D = c.dalloc<double>(d1); c.E = c.dalloc<double>(d1);
     c.Mt = c.dalloc<double>(d1 * d1); c.Pr = c.dalloc<double>(d1 * d1); c.Qt = c.dalloc<double>(d1 * d1);
     c.X = c.dalloc<double>(d1 * d1);
-    c.gout = c.dalloc<T>((size_t)std::max(c.ldu, c.ldv) * (kmax + 1));
-    if (std::is_same<T, double>::value && g_cgs_arith == CGS_PLANES && lb_planes_fit(kmax)) {
-        c.Up = (float2 *)c.dbytes(sizeof(float2) * (size_t)c.ldu * (kmax + 1));
-        c.Vp = (float2 *)c.dbytes(sizeof(float2) * (size_t)c.ldv * (kmax + 1));
-        c.xpl = c.dalloc<float2>(mn);
+    // the restart/Ritz product's output: written by the GEMM before it is read
+    c.gout = c.dbytes_raw(sizeof(T) * (size_t)std::max(c.ldu, c.ldv) * (kmax + 1));
+    // the partial-sum arrays above hold d.nb CTAs; the grid follows the size
+    c.nb = vec_grid((int64_t)std::max(m, n) * c.vw, 0);
+    constexpr bool fp64 = std::is_same<T, double>::value || std::is_same<T, double2>::value;
+    if (fp64 && g_cgs_arith == CGS_PLANES && lb_planes_fit(kmax, c.vw == 2)) {
+        // planes of every real scalar (complex: of re and im); written (flag
+        // set) before any kernel reads them
+        c.Up = (float2 *)c.dbytes_raw(sizeof(float2) * (size_t)c.ldu * c.vw * (kmax + 1));
+        c.Vp = (float2 *)c.dbytes_raw(sizeof(float2) * (size_t)c.ldv * c.vw * (kmax + 1));
+        c.xpl = c.dalloc<float2>((size_t)mn * c.vw);
         c.okU = c.dalloc<int>(kmax + 2);
         c.okV = c.dalloc<int>(kmax + 2);
     }
@@ -436,10 +475,11 @@ static void dev_aprod(Ctx &c, bool trans, const T *x, T *y)
 {
     const int nin = trans ? c.m : c.n, nout = trans ? c.n : c.m;
     if constexpr (VecW<T>::w == 2) {
-        // the device operator is the real 2x2-block form; a host ZAPROD sees
-        // complex*16 vectors with TRANSA 'n' or 'c' (zlanbpro.F:297, :442)
+        // the device operator (native, or the real 2x2-block form); a host
+        // ZAPROD sees complex*16 vectors with TRANSA 'n' or 'c'
+        // (zlanbpro.F:297, :442)
         if (c.op) {
-            op_apply<double>(*c.op, trans, (const double *)x, (double *)y, c.s);
+            op_zapply(*c.op, trans, (const double2 *)x, (double2 *)y, c.s);
             return;
         }
         PGB_CUDA(cudaMemcpyAsync(c.hx, x, sizeof(T) * nin, cudaMemcpyDeviceToHost, c.s));
@@ -1079,9 +1119,24 @@ static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, 
         }
         return;
     } else {
-    // FP64 or complex*16 (sizeof(T) = 16) bases into the caller's arrays
-    if (du)
-        d2h_columns((char *)U, sizeof(T) * ldu, (const char *)c.U, sizeof(T) * c.ldu, sizeof(T) * c.m, ncols, c.s);
+    // FP64 or complex*16 (sizeof(T) = 16) bases into the caller's arrays.
+    // When the left vectors were final before the right ones were formed,
+    // their copy runs on a second stream, behind that point only, so that
+    // it overlaps the right vectors' product.
+    if (du) {
+        cudaStream_t su = c.s;
+        if (c.u_final && dv) {
+            if (!c.s2) PGB_CUDA(cudaStreamCreateWithFlags(&c.s2, cudaStreamNonBlocking));
+            if (!c.ev_s2) PGB_CUDA(cudaEventCreateWithFlags(&c.ev_s2, cudaEventDisableTiming));
+            PGB_CUDA(cudaStreamWaitEvent(c.s2, c.ev_u, 0));
+            su = c.s2;
+        }
+        d2h_columns((char *)U, sizeof(T) * ldu, (const char *)c.U, sizeof(T) * c.ldu, sizeof(T) * c.m, ncols, su);
+        if (su != c.s) {
+            PGB_CUDA(cudaEventRecord(c.ev_s2, su));
+            PGB_CUDA(cudaStreamWaitEvent(c.s, c.ev_s2, 0));
+        }
+    }
     if (dv)
         d2h_columns((char *)V, sizeof(T) * ldv, (const char *)c.V, sizeof(T) * c.ldv, sizeof(T) * c.n, ncols, c.s);
     }
@@ -1146,7 +1201,12 @@ static void dev_ritzvec(Ctx &c, bool small_side, bool du, bool dv, int k, int di
     // X = P' Mt(1:dim, 1:dim+1)   (dim x dim+1, ld dim+1)
     gemm<double>(dim, dp1, dim, c.Pr, dim, true, c.Mt, dp1, false, c.X, dp1, c.s);
     const int mstart = small_side ? dim - k + 1 : 1;
-    if (du) ovwr_left<T>(c, (T *)c.U, c.ldu, c.m, k, dp1, c.X + (mstart - 1), dp1, true);
+    if (du) {
+        ovwr_left<T>(c, (T *)c.U, c.ldu, c.m, k, dp1, c.X + (mstart - 1), dp1, true);
+        if (!c.ev_u) PGB_CUDA(cudaEventCreateWithFlags(&c.ev_u, cudaEventDisableTiming));
+        PGB_CUDA(cudaEventRecord(c.ev_u, c.s));
+        c.u_final = true;
+    }
     if (dv) ovwr_left<T>(c, (T *)c.V, c.ldv, c.n, k, dim, c.Qt + (mstart - 1), dim, true);
 }
 
@@ -1213,6 +1273,7 @@ static void setup_operator(Ctx &c, propack_aprod_t aprod, double *dparm, int *ip
             throw ArgFailure();
         }
         c.op = op;
+        c.nb = std::max(c.nb, vec_grid(0, std::max(op->fwd.nnz, op->adj.nnz)));
     } else {
         c.aprod = aprod;
         c.dparm = dparm;
@@ -1236,11 +1297,14 @@ static void setup_zoperator(Ctx &c, propack_zaprod_t aprod, propack_z16 *zparm, 
             set_error("APROD is propack_gpu_csr_zaprod_ but iparm holds no live operator handle");
             throw ArgFailure();
         }
-        if (!op->cplx || op->m != 2 * c.m || op->n != 2 * c.n) {
+        // the real 2x2-block form is 2m x 2n, the native form m x n
+        const int f = op->cplx == 1 ? 2 : 1;
+        if (!op->cplx || op->m != f * c.m || op->n != f * c.n) {
             set_error(!op->cplx ? "a real operator needs the real drivers" : "operator shape does not match m, n");
             throw ArgFailure();
         }
         c.op = op;
+        c.nb = std::max(c.nb, vec_grid(0, std::max(op->fwd.nnz, op->adj.nnz)));
     } else {
         c.zaprod = aprod;
         c.zparm = zparm;

@@ -32,6 +32,7 @@
 
 #include "pgb.cuh"
 #include "pgb_f3.cuh"
+#include "pgb_planes.cuh"
 #include "pgb_spmv.cuh"
 
 namespace pgb {
@@ -360,8 +361,11 @@ __device__ void u_finish_beta(Tail &t, const LbArgs &a, int j)
 }
 
 // ------------------------------------------------ continuations by phase
+// cdot: the launch formed the complex projection <prev, y> = (dotp,
+// dotp_im) (the native complex SpMV), so the ELR needs no pass to form it
 template <int SIDE>
-__device__ void after_spmv(Tail &t, const LbArgs &a, int j, double nrm, double dotp)
+__device__ void after_spmv(Tail &t, const LbArgs &a, int j, double nrm, double dotp, double dotp_im = 0.0,
+                           bool cdot = false)
 {
     if (threadIdx.x == 0) {
         LbCtl &c = t.c;
@@ -376,8 +380,11 @@ __device__ void after_spmv(Tail &t, const LbArgs &a, int j, double nrm, double d
             } else if (c.ielr > 0 && c.alpha < KAPPA * c.beta) {
                 c.elr_active = 1;
                 c.elr_iter = 1;
-                if (c.cplx) c.elr_need_dot = 1;
-                else {
+                if (c.cplx) {
+                    c.elr_need_dot = cdot ? 0 : 1;
+                    c.elr_s = dotp;
+                    c.elr_s_im = dotp_im;
+                } else {
                     c.elr_s = dotp;
                     if (c.beta != 0.0) { c.beta += dotp; a.bbeta[j - 2] = c.beta; }
                 }
@@ -389,8 +396,11 @@ __device__ void after_spmv(Tail &t, const LbArgs &a, int j, double nrm, double d
             if (c.ielr > 0 && c.beta < KAPPA * c.alpha) {
                 c.elr_active = 1;
                 c.elr_iter = 1;
-                if (c.cplx) c.elr_need_dot = 1;
-                else {
+                if (c.cplx) {
+                    c.elr_need_dot = cdot ? 0 : 1;
+                    c.elr_s = dotp;
+                    c.elr_s_im = dotp_im;
+                } else {
                     c.elr_s = dotp;
                     if (c.alpha != 0.0) { c.alpha += dotp; a.balpha[j - 1] = c.alpha; }
                 }
@@ -946,89 +956,6 @@ __global__ void __launch_bounds__(BS) k_lb_cgs_upd_f3(LbArgs a, int j, int last)
 // GB300 the FP64 pipe (2 lanes per clock per SM) holds one FMA per element
 // below the HBM rate, 12 FP32 operations (128 lanes per clock) do not.
 
-// s + c: a sum of products kept as an unevaluated FP32 pair
-struct PlAcc {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float ah, float al, float bh, float bl)
-    {
-        const float p = ah * bh;
-        const float pe = fmaf(ah, bh, -p);  // p + pe = ah bh exactly
-        const float t = s + p;
-        const float bp = t - s;
-        const float err = (s - (t - bp)) + (p - bp);  // t + err = s + p exactly
-        c = fmaf(ah, bl, c);
-        c = fmaf(al, bh, c);
-        c += pe + err;
-        s = t;
-    }
-    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
-};
-
-// f as an FP64 value with integer operations only (no FP64-pipe conversion);
-// FP32 subnormals (|f| < 2^-126) become 0, infinities and NaNs stay so
-__device__ __forceinline__ double pl_f2d(float f)
-{
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xffu;
-    const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
-    const unsigned long long ee = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
-    const unsigned long long m = (unsigned long long)(u & 0x7fffffu) << 29;
-    return e == 0 ? 0.0 : __longlong_as_double((long long)(sgn | (ee << 52) | m));
-}
-
-// (s, c) += (s2, c2) for compensated pairs: the leading parts by a two-sum
-__device__ __forceinline__ void pl_pair_add(float &s, float &c, float s2, float c2)
-{
-    const float t = s + s2;
-    const float bp = t - s;
-    const float e = (s - (t - bp)) + (s2 - bp);
-    c = (c + c2) + e;
-    s = t;
-}
-// Sum four compensated pairs over the warp with FP32 operations only, by a
-// transposed butterfly: at offset 16 a lane keeps two of the four sums and
-// sends the other two, at offset 8 one of its two, then one sum travels
-// the last three offsets (12 shuffles instead of 40).  Lanes 8u .. 8u+7
-// end with the total of acc[u].  The order of additions is fixed.
-__device__ __forceinline__ PlAcc pl_warp_sum4(const PlAcc *acc)
-{
-    const unsigned F = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const bool b4 = lane & 16, b3 = lane & 8;
-    PlAcc k0 = b4 ? acc[2] : acc[0], k1 = b4 ? acc[3] : acc[1];
-    const PlAcc g0 = b4 ? acc[0] : acc[2], g1 = b4 ? acc[1] : acc[3];
-    pl_pair_add(k0.s, k0.c, __shfl_xor_sync(F, g0.s, 16), __shfl_xor_sync(F, g0.c, 16));
-    pl_pair_add(k1.s, k1.c, __shfl_xor_sync(F, g1.s, 16), __shfl_xor_sync(F, g1.c, 16));
-    PlAcc k = b3 ? k1 : k0;
-    const PlAcc g = b3 ? k0 : k1;
-    pl_pair_add(k.s, k.c, __shfl_xor_sync(F, g.s, 8), __shfl_xor_sync(F, g.c, 8));
-#pragma unroll
-    for (int o = 4; o > 0; o >>= 1) pl_pair_add(k.s, k.c, __shfl_xor_sync(F, k.s, o), __shfl_xor_sync(F, k.c, o));
-    return k;
-}
-
-// the planes of a basis element, with integer operations only: the leading
-// 24 and the next 23 bits of w (|w| <= 1; parts below 2^-74 are dropped).
-// Conversions between FP64 and FP32 run on the FP64 pipe, which retires two
-// lanes per clock per SM on GB300.
-__device__ __forceinline__ float2 pl_split(double w)
-{
-    const F3 f = f3_split(w, 0);
-    return make_float2(f.a, f.b);
-}
-__device__ __forceinline__ float4 pl_split2(double2 w)
-{
-    const float2 a = pl_split(w.x), b = pl_split(w.y);
-    return make_float4(a.x, a.y, b.x, b.y);
-}
-// x 2^-shift as (hi, lo) planes with integer operations only (the FP64
-// pipe stays free): the leading 24 and the next 23 bits of the value
-__device__ __forceinline__ float2 pl_xsplit(double x, int shift)
-{
-    const F3 f = f3_split(x, shift);
-    return make_float2(f.a, f.b);
-}
-
 // projections h = W(:,sel)' x from the planes.  Each CTA owns a contiguous
 // chunk of 2-element row vectors and each of its warps one eighth of the
 // chunk.  A warp first splits its x values (scaled by a power of two per
@@ -1345,6 +1272,81 @@ __global__ void __launch_bounds__(BS) k_lb_zelr(LbArgs a, int j)
     }
 }
 
+// The fused complex SpMV of one half step on a native complex operator
+// (zlanbpro.F:297-311 and :442-450): y = op(A) x with complex
+// accumulation (one index and one 16-byte value per entry, 16-byte gathers),
+// the deferred scale of x and of the previous vector, y -= coef prev (coef
+// real), and the partial sums of ||y||^2 and of the complex projection
+// <prev, y> = sum conj(prev) y that the first ELR pass subtracts
+// (pzdotc), in the same launch.  host_product: the caller's ZAPROD already
+// wrote y.
+constexpr int ZSPMV_MINB = 3;  // CTAs per SM the complex SpMV is compiled for (wider values and gathers)
+template <int SIDE>
+__global__ void __launch_bounds__(BS, ZSPMV_MINB) k_lb_zspmv(LbArgs a, int j, int host_product)
+{
+    __shared__ ChunkStage<double2> cst[SPMV_WARPS];
+    __shared__ double sred[32];
+    __shared__ Tail t;
+    if (a.ctl->status != 0) return;
+    const Pend pin = SIDE == 0 ? a.ctl->pend_u : a.ctl->pend_v;
+    const Pend pprev = SIDE == 0 ? a.ctl->pend_v : a.ctl->pend_u;
+    const bool has_prev = SIDE == 1 || j > 1;
+    const double coef = SIDE == 0 ? a.ctl->beta : a.ctl->alpha;
+    const double2 *x = reinterpret_cast<const double2 *>(SIDE == 0 ? ucol<double>(a, j - 1) : vcol<double>(a, j - 1));
+    double2 *out = reinterpret_cast<double2 *>(SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j));
+    double2 *prev = has_prev ? reinterpret_cast<double2 *>(SIDE == 0 ? vcol<double>(a, j - 2) : ucol<double>(a, j - 1))
+                             : nullptr;
+    const Csr &A = SIDE == 0 ? a.zadj : a.zfwd;
+    // this launch rewrites the output column and (deferred scale) the
+    // previous one: their planes no longer hold them
+    if (a.okU && blockIdx.x == 0 && threadIdx.x == 0) {
+        int *ok = SIDE == 0 ? a.okV : a.okU;
+        ok[SIDE == 0 ? j - 1 : j] = 0;
+        if (has_prev) ok[SIDE == 0 ? j - 2 : j - 1] = 0;
+    }
+    double sq = 0.0, dr = 0.0, di = 0.0;
+    auto scale = [](double2 v, const Pend &p) { return make_double2(apply_pend(v.x, p), apply_pend(v.y, p)); };
+    auto epi = [&](int r, double2 acc, double2 pv) {
+        double2 y = scale(acc, pin);
+        if (has_prev) {
+            if (pprev.mode) {
+                pv = scale(pv, pprev);
+                prev[r] = pv;
+            }
+            y.x = fma(-coef, pv.x, y.x);
+            y.y = fma(-coef, pv.y, y.y);
+            zdot_acc(dr, di, pv, y);
+        }
+        out[r] = y;
+        sq = fma(y.x, y.x, sq);
+        sq = fma(y.y, y.y, sq);
+    };
+    auto pre = [&](int r) -> double2 { return has_prev ? prev[r] : make_double2(0.0, 0.0); };
+    if (!host_product) {
+        auto xl = [&](int c) -> double2 { return x[c]; };
+        csr_rows_chunked<double2, double2>(A.ptr, A.tbase, A.cidx, A.czval, A.rows, xl, pre, epi, cst);
+    } else {
+        const int rows = (SIDE == 0 ? a.adj.rows : a.fwd.rows) / 2;
+        for (int r = blockIdx.x * BS + threadIdx.x; r < rows; r += gridDim.x * BS) epi(r, out[r], pre(r));
+    }
+    const double sq2 = block_sum<BS>(sq, sred);
+    const double dr2 = block_sum<BS>(dr, sred);
+    const double di2 = block_sum<BS>(di, sred);
+    if (threadIdx.x == 0) {
+        a.part_sq[blockIdx.x] = sq2;
+        a.part_dot[blockIdx.x] = dr2;
+        a.part_cols[blockIdx.x] = di2;  // Gram-Schmidt is idle while the SpMV runs
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
+        const double d2 = sum_parts(a.part_dot, gridDim.x, t.red);
+        const double e2 = sum_parts(a.part_cols, gridDim.x, t.red);
+        after_spmv<SIDE>(t, a, j, sqrt(s2), d2, e2, true);
+        tail_store(a, t);
+    }
+}
+
 // projections h = W(:,sel)^H x (the zgemv('C') of zcgs): the work layout of
 // k_lb_cgs_dots with one complex element per 16-byte vector; column c's
 // partials go to part_cols rows 2c (re) and 2c+1 (im), and h comes out as
@@ -1456,6 +1458,209 @@ __global__ void __launch_bounds__(BS) k_lb_zcgs_upd(LbArgs a, int j, int last)
     }
 }
 
+// ------------------------------------ complex Gram-Schmidt on the planes
+// The complex basis read as its real (re, im) arrays: one complex element is
+// one float4 of planes (re hi, re lo, im hi, im lo), split, flagged and
+// scaled exactly as in the real kernels above.  The projection
+// h = sum conj(w) x has Re h = sum (w.re x.re + w.im x.im), the real dot of
+// the two arrays, and Im h = sum (w.re x.im - w.im x.re), the same loaded
+// values with the parts of x swapped and one negated: two compensated sums
+// per column, four plane products per element, on the FP32 pipe where the
+// FP64 kernels spend four FP64 FMAs per 16 bytes.
+
+// projections h = W(:,sel)^H x (zgemv 'C' of zcgs, zreorth.F) from the
+// planes: the work layout of k_lb_cgs_dots_pl with two columns per group
+// (their re and im sums are the four sums of pl_warp_sum4); partials of
+// column c go to part_cols rows 2c (re) and 2c+1 (im), h comes out as
+// (re, im) pairs
+constexpr int ZPL_COLS = 2;
+template <int SIDE>
+__global__ void __launch_bounds__(BS, PL_MINB) k_lb_zcgs_dots_pl(LbArgs a, int j)
+{
+    // [PL_WARPS][2 (kmax + 1)] per-warp partials | sel[kmax + 1] | fresh[kmax + 1]
+    extern __shared__ double wpart[];
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 0) return;
+    const int L = a.ctl->nsel;
+    const int K1 = a.kmax + 1, K2 = 2 * K1;
+    int *ssel = reinterpret_cast<int *>(wpart + (size_t)PL_WARPS * K2);
+    int *sfresh = ssel + K1;
+    int *ok = SIDE == 0 ? a.okV : a.okU;
+    for (int c = threadIdx.x; c < L; c += BS) {
+        const int col = a.sel[c];
+        ssel[c] = col;
+        sfresh[c] = ok[col] == 0;
+    }
+    __syncthreads();
+    const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;  // real scalars: twice the complex length
+    const size_t ld = SIDE == 0 ? a.ldv : a.ldu;
+    const size_t ldq = ld / 2;  // leading dimension in float4 (one complex element)
+    const double *W = (const double *)(SIDE == 0 ? a.V : a.U);
+    float2 *Wp = SIDE == 0 ? a.Vp : a.Up;
+    const double *x = SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j);
+    const double2 *xv = reinterpret_cast<const double2 *>(x);
+    float4 *xq = reinterpret_cast<float4 *>(a.xpl);
+    const int nvec = len / 2;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int chunk = (nvec + gridDim.x - 1) / gridDim.x;
+    const int cb0 = min(nvec, blockIdx.x * chunk), cb1 = min(nvec, cb0 + chunk);
+    const int sl = (cb1 - cb0 + PL_WARPS - 1) / PL_WARPS;
+    const int v0 = min(cb1, cb0 + w * sl), v1 = min(cb1, v0 + sl);
+    int xe = 0;
+    for (int v = v0 + lane; v < v1; v += 32) {
+        const double2 xx = xv[v];
+        xe = max(xe, max(f3_expo(xx.x), f3_expo(xx.y)));
+    }
+    xe = __reduce_max_sync(0xffffffffu, xe);
+    const int xs = xe == 0 ? 0 : xe - 1023;
+    const double back = f3_pow2(xs);
+    for (int v = v0 + lane; v < v1; v += 32) {
+        const double2 xx = xv[v];
+        const float2 p = pl_xsplit(xx.x, xs), q = pl_xsplit(xx.y, xs);
+        xq[v] = make_float4(p.x, p.y, q.x, q.y);
+    }
+    for (int c = 0; c < L; c++) {
+        if (!sfresh[c]) continue;
+        const int col = ssel[c];
+        float4 *Wq = reinterpret_cast<float4 *>(Wp) + (size_t)col * ldq;
+        const double2 *Wd = reinterpret_cast<const double2 *>(W + (size_t)col * ld);
+        int v = v0 + lane;
+        for (; v + 32 * (PL_SPLIT_UNROLL - 1) < v1; v += 32 * PL_SPLIT_UNROLL) {
+            double2 d[PL_SPLIT_UNROLL];
+#pragma unroll
+            for (int u = 0; u < PL_SPLIT_UNROLL; u++) d[u] = Wd[v + 32 * u];
+#pragma unroll
+            for (int u = 0; u < PL_SPLIT_UNROLL; u++) Wq[v + 32 * u] = pl_split2(d[u]);
+        }
+        for (; v < v1; v += 32) Wq[v] = pl_split2(Wd[v]);
+    }
+    // conj(w) x into (re, im): w = (w.x + w.y, w.z + w.w), x likewise
+    auto zacc = [](PlAcc &re, PlAcc &im, const float4 &wv, const float4 &xq4) {
+        re.add(wv.x, wv.y, xq4.x, xq4.y);
+        re.add(wv.z, wv.w, xq4.z, xq4.w);
+        im.add(wv.x, wv.y, xq4.z, xq4.w);
+        im.add(wv.z, wv.w, -xq4.x, -xq4.y);
+    };
+    for (int cb = 0; cb < L; cb += ZPL_COLS) {
+        const int nc = min(ZPL_COLS, L - cb);
+        const float4 *Wq[ZPL_COLS];
+#pragma unroll
+        for (int u = 0; u < ZPL_COLS; u++)
+            Wq[u] = reinterpret_cast<const float4 *>(Wp) + (size_t)ssel[cb + (u < nc ? u : 0)] * ldq;
+        PlAcc acc[2 * ZPL_COLS];  // re, im of column cb, then of column cb + 1
+        int v = v0 + lane;
+        for (; v + 32 < v1; v += 64) {
+            float4 w0[ZPL_COLS], w1[ZPL_COLS];
+#pragma unroll
+            for (int u = 0; u < ZPL_COLS; u++) {
+                w0[u] = __ldcs(Wq[u] + v);
+                w1[u] = __ldcs(Wq[u] + v + 32);
+            }
+            const float4 x0 = xq[v], x1 = xq[v + 32];
+#pragma unroll
+            for (int u = 0; u < ZPL_COLS; u++) {
+                zacc(acc[2 * u], acc[2 * u + 1], w0[u], x0);
+                zacc(acc[2 * u], acc[2 * u + 1], w1[u], x1);
+            }
+        }
+        if (v < v1) {
+            const float4 x0 = xq[v];
+#pragma unroll
+            for (int u = 0; u < ZPL_COLS; u++) zacc(acc[2 * u], acc[2 * u + 1], __ldcs(Wq[u] + v), x0);
+        }
+        static_assert(2 * ZPL_COLS == 4, "pl_warp_sum4 sums four accumulators");
+        const PlAcc tot = pl_warp_sum4(acc);
+        const int q = lane >> 3;  // accumulator q: column cb + q / 2, part q % 2
+        if ((lane & 7) == 0 && (q >> 1) < nc) wpart[(size_t)w * K2 + 2 * cb + q] = tot.value() * back;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < 2 * L; c += BS) {
+        double s = 0.0;
+#pragma unroll
+        for (int ww = 0; ww < PL_WARPS; ww++) s += wpart[(size_t)ww * K2 + c];
+        a.part_cols[(size_t)c * a.nb + blockIdx.x] = s;
+    }
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        reduce_cols(a, 2 * L, gridDim.x);
+        for (int c = threadIdx.x; c < L; c += BS) ok[ssel[c]] = 1;
+        if (threadIdx.x == 0) t.c.cgs_phase = 1;
+        tail_store(a, t);
+    }
+}
+
+// x -= W(:,sel) h (zgemv 'N' of zcgs) from the planes, and ||x||^2: one
+// complex element per thread and step; h (scaled by the power of two of its
+// largest part) in shared memory as float4 planes (re hi, re lo, im hi,
+// im lo); Re and Im of each row's sum formed on the FP32 pipe and applied
+// with FP64 FMAs
+template <int SIDE>
+__global__ void __launch_bounds__(BS) k_lb_zcgs_upd_pl(LbArgs a, int j, int last)
+{
+    extern __shared__ double dyn[];  // h[L] as float4 planes (two double slots each) | sel[L]
+    __shared__ double sred[32];
+    __shared__ int hsh;
+    __shared__ Tail t;
+    if (a.ctl->status != 0 || !a.ctl->reorth_active || a.ctl->cgs_phase != 1) return;
+    const int L = a.ctl->nsel;
+    float4 *hp = reinterpret_cast<float4 *>(dyn);
+    int *ssel = reinterpret_cast<int *>(dyn + 2 * (size_t)L);
+    if (threadIdx.x == 0) hsh = 0;
+    __syncthreads();
+    int he = 0;
+    for (int c = threadIdx.x; c < 2 * L; c += BS) he = max(he, f3_expo(a.h[c]));
+    if (he) atomicMax(&hsh, he);
+    __syncthreads();
+    const int hs = hsh == 0 ? 0 : hsh - 1023;  // |h 2^-hs| < 2
+    const double hscale = f3_pow2(-hs), back = f3_pow2(hs);
+    for (int c = threadIdx.x; c < L; c += BS) {
+        const float2 hr = pl_split(a.h[2 * c] * hscale), hi = pl_split(a.h[2 * c + 1] * hscale);
+        hp[c] = make_float4(hr.x, hr.y, hi.x, hi.y);
+        ssel[c] = a.sel[c];
+    }
+    __syncthreads();
+    const int len = SIDE == 0 ? a.adj.rows : a.fwd.rows;
+    const size_t ldq = (size_t)(SIDE == 0 ? a.ldv : a.ldu) / 2;
+    const float4 *Wq = reinterpret_cast<const float4 *>(SIDE == 0 ? a.Vp : a.Up);
+    double2 *xv = reinterpret_cast<double2 *>(SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j));
+    const int nvec = len / 2;
+    // w h into (re, im)
+    auto zmul = [](PlAcc &re, PlAcc &im, const float4 &wv, const float4 &h) {
+        re.add(wv.x, wv.y, h.x, h.y);
+        re.add(wv.z, wv.w, -h.z, -h.w);
+        im.add(wv.x, wv.y, h.z, h.w);
+        im.add(wv.z, wv.w, h.x, h.y);
+    };
+    double sq = 0.0;
+    for (int v = blockIdx.x * BS + threadIdx.x; v < nvec; v += gridDim.x * BS) {
+        const double2 x0 = xv[v];
+        PlAcc sr, si;
+        int c = 0;
+        for (; c + CGS_UNROLL <= L; c += CGS_UNROLL) {
+            float4 wv[CGS_UNROLL];
+#pragma unroll
+            for (int u = 0; u < CGS_UNROLL; u++) wv[u] = Wq[(size_t)ssel[c + u] * ldq + v];
+#pragma unroll
+            for (int u = 0; u < CGS_UNROLL; u++) zmul(sr, si, wv[u], hp[c + u]);
+        }
+        for (; c < L; c++) zmul(sr, si, Wq[(size_t)ssel[c] * ldq + v], hp[c]);
+        double2 y;
+        y.x = fma(-pl_f2d(sr.c), back, fma(-pl_f2d(sr.s), back, x0.x));
+        y.y = fma(-pl_f2d(si.c), back, fma(-pl_f2d(si.s), back, x0.y));
+        xv[v] = y;
+        sq = fma(y.x, y.x, sq);
+        sq = fma(y.y, y.y, sq);
+    }
+    const double sq2 = block_sum<BS>(sq, sred);
+    if (threadIdx.x == 0) a.part_sq[blockIdx.x] = sq2;
+    if (last_cta(&a.ctl->ticket)) {
+        tail_load(a, t);
+        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
+        after_cgs<SIDE>(t, a, j, sqrt(s2), last);
+        tail_store(a, t);
+    }
+}
+
 // apply the deferred scaling of the newest u and v columns
 template <typename T>
 __global__ void __launch_bounds__(BS) k_lb_flush(LbArgs a)
@@ -1492,6 +1697,8 @@ static size_t cgs_smem_f3(const LbArgs &a) { return (2 * sizeof(double) + sizeof
 // Gram-Schmidt arithmetic of the FP64 form (propack_set_cgs_arith)
 thread_local int g_cgs_arith = CGS_PLANES;
 static size_t pl_smem(int kmax) { return (sizeof(double) * PL_WARPS + 2 * sizeof(int)) * (size_t)(kmax + 1); }
+// the complex projections keep (re, im) partials per warp
+static size_t zpl_smem(int kmax) { return (2 * sizeof(double) * PL_WARPS + 2 * sizeof(int)) * (size_t)(kmax + 1); }
 static size_t cgs_smem_pl(const LbArgs &a) { return pl_smem(a.kmax); }
 
 template <int SIDE, typename T>
@@ -1507,9 +1714,16 @@ void lb_set_smem_limits(int kmax)
         PGB_CUDA(cudaFuncSetAttribute(k_lb_cgs_upd_f3<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
     }
     if (need3 > 48 * 1024) {
-        // the complex update keeps h as (re, im): the same shared memory as the f3 update
+        // the complex updates keep h as (re, im) or its planes: the same shared memory as the f3 update
         PGB_CUDA(cudaFuncSetAttribute(k_lb_zcgs_upd<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
         PGB_CUDA(cudaFuncSetAttribute(k_lb_zcgs_upd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_zcgs_upd_pl<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_zcgs_upd_pl<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3));
+    }
+    const size_t needz = zpl_smem(kmax);
+    if (needz > 48 * 1024 && needz <= PL_SMEM_MAX) {
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_zcgs_dots_pl<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)needz));
+        PGB_CUDA(cudaFuncSetAttribute(k_lb_zcgs_dots_pl<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)needz));
     }
     const size_t need = (sizeof(double) + sizeof(int)) * (size_t)(kmax + 1) + 16;
     if (need > 48 * 1024) {
@@ -1528,8 +1742,9 @@ void lb_set_smem_limits(int kmax)
 }
 
 // the planes are used when the driver allocated them (FP64 form, kmax small
-// enough for the projections' per-warp partials in shared memory)
-bool lb_planes_fit(int kmax) { return pl_smem(kmax) <= PL_SMEM_MAX; }
+// enough for the projections' per-warp partials in shared memory; complex
+// vectors keep twice the partials)
+bool lb_planes_fit(int kmax, bool cplx) { return (cplx ? zpl_smem(kmax) : pl_smem(kmax)) <= PL_SMEM_MAX; }
 
 // one wave of the plane projections at their occupancy (at most nb CTAs;
 // their partials are summed over gridDim)
@@ -1576,10 +1791,35 @@ static void launch_cgs_pass(const LbArgs &a, int j, int last, cudaStream_t s)
     PGB_LAUNCHED();
 }
 
-// one complex Gram-Schmidt pass
+template <int SIDE>
+static int zdots_pl_grid(const LbArgs &a)
+{
+    static thread_local int g = 0, dev = -1;
+    static thread_local size_t smem = 0;
+    const Dev &d = device_info();
+    const size_t need = zpl_smem(a.kmax);
+    if (g == 0 || dev != d.device || smem != need) {
+        int per = 0;
+        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lb_zcgs_dots_pl<SIDE>, BS, need));
+        g = std::max(1, per) * d.sms;
+        dev = d.device;
+        smem = need;
+    }
+    return std::min(g, a.nb);
+}
+
+// one complex Gram-Schmidt pass (on the planes when the driver keeps them)
 template <int SIDE>
 static void launch_zcgs_pass(const LbArgs &a, int j, int last, cudaStream_t s)
 {
+    if (a.Up) {
+        PGB_PROF(PK_CGS_DOTS, s,
+                 k_lb_zcgs_dots_pl<SIDE><<<zdots_pl_grid<SIDE>(a), BS, zpl_smem(a.kmax), s>>>(a, j));
+        PGB_LAUNCHED();
+        PGB_PROF(PK_CGS_UPD, s, k_lb_zcgs_upd_pl<SIDE><<<a.nb, BS, cgs_smem_f3(a), s>>>(a, j, last));
+        PGB_LAUNCHED();
+        return;
+    }
     PGB_PROF(PK_CGS_DOTS, s, k_lb_zcgs_dots<SIDE><<<a.nb, BS, 0, s>>>(a, j));
     PGB_LAUNCHED();
     PGB_PROF(PK_CGS_UPD, s, k_lb_zcgs_upd<SIDE><<<a.nb, BS, cgs_smem_f3(a), s>>>(a, j, last));
@@ -1609,6 +1849,20 @@ static void launch_spmv(const LbArgs &a, const Csr &A, int j, bool host_product,
         k_lb_spmv<SIDE, T, 0><<<spmv_grid<SIDE, T, 0>(a.nb), BS, 0, s>>>(a, j, host_product ? 1 : 0);
 }
 
+template <int SIDE>
+static void launch_zspmv(const LbArgs &a, int j, bool host_product, cudaStream_t s)
+{
+    static thread_local int g = 0, dev = -1;
+    const Dev &d = device_info();
+    if (g == 0 || dev != d.device) {
+        int per = 0;
+        PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lb_zspmv<SIDE>, BS, 0));
+        g = std::max(1, per) * d.sms;
+        dev = d.device;
+    }
+    k_lb_zspmv<SIDE><<<std::min(g, a.nb), BS, 0, s>>>(a, j, host_product ? 1 : 0);
+}
+
 // Enqueue the kernels of one half step.  host_product: the product was
 // written into the output column by a host APROD call.
 // the half step of the complex form: the real fused SpMV on the 2x2-block
@@ -1618,7 +1872,26 @@ static void zenqueue_half(const LbArgs &a, int side, int j, int ielr, int ntry_s
                           cudaStream_t s)
 {
     const int nb = a.nb;
-    const int nelr = ielr > 0 ? ielr + 1 : 0;
+    // the native complex SpMV (and the host-product epilogue, which shares
+    // it) forms the complex projection itself: ielr ELR launches suffice
+    const bool native = host_product || a.zfwd.rows > 0;
+    const int nelr = ielr > 0 ? ielr + (native ? 0 : 1) : 0;
+    if (native) {
+        if (side == 0) PGB_PROF(PK_SPMV_ADJ, s, launch_zspmv<0>(a, j, host_product, s));
+        else PGB_PROF(PK_SPMV_FWD, s, launch_zspmv<1>(a, j, host_product, s));
+        PGB_LAUNCHED();
+        if (side == 1 || j > 1)
+            for (int i = 0; i < nelr; i++) {
+                if (side == 0) PGB_PROF(PK_ELR, s, k_lb_zelr<0><<<nb, BS, 0, s>>>(a, j));
+                else PGB_PROF(PK_ELR, s, k_lb_zelr<1><<<nb, BS, 0, s>>>(a, j));
+                PGB_LAUNCHED();
+            }
+        for (int i = 0; i < ntry_spec; i++) {
+            if (side == 0) launch_zcgs_pass<0>(a, j, i == ntry_spec - 1, s);
+            else launch_zcgs_pass<1>(a, j, i == ntry_spec - 1, s);
+        }
+        return;
+    }
     if (side == 0) {
         PGB_PROF(PK_SPMV_ADJ, s, launch_spmv<0, double>(a, a.adj, j, host_product, s));
         PGB_LAUNCHED();

@@ -120,6 +120,18 @@ static int apply_noalloc(int64_t handle, int trans, const double *x, double *y, 
         set_error("propack_csr_apply_noalloc: x and y must be device (or managed) memory of the operator's device");
         return PROPACK_ERR_ARG;
     }
+    if (op->cplx == 2) {
+        // a native complex operator: x and y hold (re, im) pairs, read as
+        // 16-byte vectors
+        if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15u) {
+            set_error("propack_csr_apply_noalloc: complex x and y must be 16-byte aligned");
+            return PROPACK_ERR_ARG;
+        }
+        op_zspmv_plain_launch(trans ? op->adj : op->fwd, reinterpret_cast<const double2 *>(x),
+                              reinterpret_cast<double2 *>(y), s);
+        PGB_CUDA(cudaGetLastError());
+        return 0;
+    }
     double *base = scratch_address(dev);
     const Csr &A = trans ? op->adj : op->fwd;
     const double *z = nullptr;

@@ -148,6 +148,30 @@ template <>
 __device__ __forceinline__ const double *chunk_vals<double>(const Csr &A) { return A.cval; }
 template <>
 __device__ __forceinline__ const float *chunk_vals<float>(const Csr &A) { return A.cvalf; }
+template <>
+__device__ __forceinline__ const double2 *chunk_vals<double2>(const Csr &A) { return A.czval; }
+
+// The chunked schedule's arithmetic on its accumulation type: real (float,
+// double) or complex (double2 = (re, im); a complex entry costs four FP64
+// FMAs on one index and one 16-byte gather, where the 2x2-block real form
+// reads four entries)
+template <typename AT>
+__device__ __forceinline__ AT spmv_zero() { return (AT)0; }
+template <>
+__device__ __forceinline__ double2 spmv_zero<double2>() { return make_double2(0.0, 0.0); }
+__device__ __forceinline__ float spmv_mac(float v, float x, float acc) { return fmaf(v, x, acc); }
+__device__ __forceinline__ double spmv_mac(double v, double x, double acc) { return fma(v, x, acc); }
+__device__ __forceinline__ double2 spmv_mac(double2 v, double2 x, double2 acc)
+{
+    acc.x = fma(v.x, x.x, acc.x);
+    acc.x = fma(-v.y, x.y, acc.x);
+    acc.y = fma(v.x, x.y, acc.y);
+    acc.y = fma(v.y, x.x, acc.y);
+    return acc;
+}
+__device__ __forceinline__ float spmv_add(float a, float b) { return a + b; }
+__device__ __forceinline__ double spmv_add(double a, double b) { return a + b; }
+__device__ __forceinline__ double2 spmv_add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
 template <typename AT>
 struct ChunkStage {
@@ -223,10 +247,11 @@ __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, co
         end_c = end_n;
         t0_c = t0_n;
         t1_c = t1_n;
-        const double pre = r < nrows ? pre_load(r) : 0.0;
+        using PT = decltype(pre_load(0));
+        const PT pre = r < nrows ? pre_load(r) : PT{};
         cs.bnd[lane] = lo;
         if (lane == 31) cs.bnd[32] = hi;
-        cs.part[lane] = (AT)0;
+        cs.part[lane] = spmv_zero<AT>();
         __syncwarp();
         // the row holding the run's first entry p0: the last q with
         // bnd[q] <= p0 (a non-empty row), or 32 when p0 is past the entries
@@ -238,16 +263,16 @@ __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, co
         if (cs.bnd[32] <= p0) q = 32;
         int nend = q < 32 ? cs.bnd[q + 1] : INT_MAX;
         int p = p0;
-        AT acc = (AT)0;
+        AT acc = spmv_zero<AT>();
         const size_t off = (size_t)t0 * 32 + lane;
         const int *ci = cidx + off;
         const VT *cv = cval + off;
         // one entry of the run; closes row q when it ends at this entry
         auto step = [&](VT v, AT xv) {
-            acc = fma((AT)v, xv, acc);
+            acc = spmv_mac((AT)v, xv, acc);
             if (++p == nend) {
                 cs.part[q] = acc;
-                acc = (AT)0;
+                acc = spmv_zero<AT>();
                 do { ++q; } while (q < 32 && cs.bnd[q + 1] == p);
                 nend = q < 32 ? cs.bnd[q + 1] : INT_MAX;
             }
@@ -268,18 +293,18 @@ __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, co
         cs.tail[lane] = acc;
         __syncwarp();
         // row `lane`: its runs ls .. le, added in lane order
-        AT tot = (AT)0;
+        AT tot = spmv_zero<AT>();
         if (lo < hi) {
             const int ls = lo / C, le = (hi - 1) / C;
             if (ls == le) {
                 tot = cs.part[lane];
             } else {
                 tot = cs.tail[ls];
-                for (int l2 = ls + 1; l2 < le; l2++) tot += cs.tail[l2];
-                tot += cs.part[lane];
+                for (int l2 = ls + 1; l2 < le; l2++) tot = spmv_add(tot, cs.tail[l2]);
+                tot = spmv_add(tot, cs.part[lane]);
             }
         }
-        if (r < nrows) epi(r, (double)tot, pre);
+        if (r < nrows) epi(r, tot, pre);
         __syncwarp();
     }
 }

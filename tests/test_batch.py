@@ -105,3 +105,29 @@ def test_autotuner_table_and_pinned_choices():
     B.set_tuning()
     assert B.tuning()["state"] == 0
     B.close()
+
+
+def test_plane_and_fp64_arithmetics_agree():
+    """The batched kernel's FP32-plane products and Gram-Schmidt passes
+    (propack_batch_set_arith(h, 2)) against its FP64 ones (the default) on
+    the same batch: every problem converges, values agree to 1e-10 and with
+    LAPACK's, and the matvec counts stay close (the two differ by rounding
+    only)."""
+    mats = batch.random_batch(16, m_range=(300, 3000), n_range=(100, 900), density=0.02, seed=12)
+    rng = np.random.default_rng(6)
+    u0 = [rng.uniform(size=A.shape[0]) for A in mats]
+    out = {}
+    for arith in ("planes", "fp64"):
+        B = batch.Batch(mats)
+        B.set_arith(arith)
+        B.set_tuning([1] * batch.NCLASS, [1] * batch.NCLASS)
+        sig, bnd, info, U, V = B.solve(6, kmax=20, tol=1e-10, maxiter=200, u0=u0, vectors=True)
+        out[arith] = (sig, info, U, V, B.stats["nopx"])
+        B.close()
+    (s1, i1, U1, V1, n1), (s2, i2, U2, V2, n2) = out["planes"], out["fp64"]
+    assert np.all(i1 == 0) and np.all(i2 == 0)
+    for p, A in enumerate(mats):
+        np.testing.assert_allclose(s1[p], s2[p], rtol=1e-10)
+        np.testing.assert_allclose(s1[p], np.linalg.svd(A.toarray(), compute_uv=False)[:6], rtol=1e-9)
+        assert subspace_err(U1[p], U2[p]) < 1e-7 and subspace_err(V1[p], V2[p]) < 1e-7
+    assert abs(n1 - n2) <= 0.1 * n2

@@ -1,9 +1,10 @@
 """The complex*16 drivers (zlansvd_, zlansvd_irl_ through the C ABI) against
 the complex oracle and scipy's zlansvd outputs (tests/golden/golden_complex.npz).
 
-The device holds a complex operator as its real 2x2-block form; the CPU
-tests pin that form (propack_zcsr_expand, host code) against complex
-products.  GPU tolerances are those of the FP64 path: singular values 1e-10
+The device holds a complex operator natively (complex CSR and its
+conjugate transpose, complex SpMV) or, on request, as its real 2x2-block
+form; the CPU tests pin the block form (propack_zcsr_expand, host code)
+against complex products, and a GPU test holds the two forms to each other.  GPU tolerances are those of the FP64 path: singular values 1e-10
 relative, phase-free vector agreement | |<u_gpu, u_ref>| - 1 | < 1e-8,
 operator products 1e-12 relative."""
 import ctypes as C
@@ -284,3 +285,78 @@ def test_complex_operator_is_refused_by_the_real_drivers():
     assert info == pg.ERR_ARG
     assert "complex" in pg.last_error()
     op.close()
+
+
+@pytest.mark.gpu
+def test_native_and_block_forms_agree():
+    """The native complex operator (complex CSR, complex SpMV that also
+    forms the ELR's complex projection) against the real 2x2-block form on
+    the same matrices: products to 1e-12, the same zlansvd_irl_ results and
+    matvec counts within rounding, and one ELR launch fewer per triggered
+    ELR step in the native form (same ELR passes)."""
+    rng = np.random.default_rng(3)
+    out = {}
+    for form in ("native", "block"):
+        pg.set_complex_form(form)
+        try:
+            ops = [pg.CsrOperator(ragged_complex(11, 3001, 700)), pg.CsrOperator(geometric_complex())]
+        finally:
+            pg.set_complex_form("native")
+        res = []
+        for op in ops:
+            m, n = op.shape
+            x = np.random.default_rng(5).standard_normal(n) + 1j * np.random.default_rng(6).standard_normal(n)
+            y = np.random.default_rng(7).standard_normal(m) + 1j * np.random.default_rng(8).standard_normal(m)
+            prods = (op.matvec(x), op.rmatvec(y))
+            pg.set_profiling(True)
+            u, s, vh, bnd = pg.svdp(op, 6, irl_mode=True, kmax=40, tol=1e-12, rng=np.random.default_rng(0))
+            prof = pg.get_profile()
+            pg.set_profiling(False)
+            res.append((prods, s, u, vh, pg.get_stats(), prof))
+            op.close()
+        out[form] = res
+    for (pn, sn, un, vn, stn, prn), (pb, sb, ub, vb, stb, prb), A in zip(
+            out["native"], out["block"], (ragged_complex(11, 3001, 700), geometric_complex())):
+        for got, ref in zip(pn, pb):
+            np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+        np.testing.assert_allclose(sn, sb, rtol=SIG_RTOL)
+        np.testing.assert_allclose(sn, np.linalg.svd(A.toarray(), compute_uv=False)[:6], rtol=SIG_RTOL)
+        assert phase_err(un, ub) < VEC_TOL and phase_err(vn, vb, axis=1) < VEC_TOL
+        assert abs(stn["nopx"] - stb["nopx"]) <= 0.05 * stb["nopx"] + 4
+    # the block form enqueues one more ELR launch per half step (the pass
+    # that forms the complex projection)
+    prn, prb = out["native"][1][5], out["block"][1][5]
+    assert 0 < prn["elr"][0] < prb["elr"][0]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["native", "block"])
+def test_complex_plane_gram_schmidt_agrees_with_fp64(form):
+    """The complex Gram-Schmidt passes on FP32 (hi, lo) planes (the default)
+    against the complex FP64 kernels (propack_set_cgs_arith(0)), with both
+    operator forms: values to 1e-12, the same vectors up to phase, matvec
+    counts within a restart; the plane kernels stream columns."""
+    g = zgolden()
+    cases = [(zcsr(g, "z1"), 5, dict(irl_mode=True, kmax=30, tol=1e-12, cgs=True)),
+             (geometric_complex(), 6, dict(irl_mode=True, kmax=40, tol=1e-12)),
+             (ragged_complex(5, 4100, 600), 5, dict(irl_mode=True, kmax=24, tol=1e-10))]
+    pg.set_complex_form(form)
+    try:
+        ops = [(pg.CsrOperator(A), k, kw) for A, k, kw in cases]
+    finally:
+        pg.set_complex_form("native")
+    try:
+        for op, k, kw in ops:
+            out = {}
+            for arith in ("fp64", "planes"):
+                pg.set_cgs_arith(arith)
+                u, s, vh, bnd = pg.svdp(op, k, rng=np.random.default_rng(0), **kw)
+                out[arith] = (u, s, vh, pg.get_stats())
+            (u0, s0, vh0, st0), (u1, s1, vh1, st1) = out["fp64"], out["planes"]
+            np.testing.assert_allclose(s1, s0, rtol=1e-12)
+            assert phase_err(u1, u0) < VEC_TOL and phase_err(vh1, vh0, axis=1) < VEC_TOL
+            assert abs(st1["nopx"] - st0["nopx"]) <= 2 * kw["kmax"]
+            assert st1["cgs_cols_u"] + st1["cgs_cols_v"] > 0
+            op.close()
+    finally:
+        pg.set_cgs_arith("planes")

@@ -138,7 +138,7 @@ def test_complex_matrix_market_coordinate_and_dense(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("fmt", ["mtx", "rua", "coord", "cua"])
+@pytest.mark.parametrize("fmt", ["mtx", "rua", "coord", "complex_mtx"])
 def test_device_operator_from_a_matrix_file(tmp_path, fmt):
     """io.load builds the device operator from a file (upload, device
     checks and transposition, SpMV schedule): its products equal scipy's on
@@ -147,10 +147,11 @@ def test_device_operator_from_a_matrix_file(tmp_path, fmt):
     rng = np.random.default_rng(11)
     m, n = 300, 180
     A = sp.csr_array(sp.random_array((m, n), density=0.05, format="csr", random_state=rng))
-    if fmt == "cua":
+    if fmt == "complex_mtx":
         A = sp.csr_array(A + 1j * sp.csr_array(sp.random_array((m, n), density=0.05, format="csr",
                                                               random_state=rng)))
-    p = tmp_path / f"a.{fmt}"
+    # the Matrix Market writer appends ".mtx" to a name without it
+    p = tmp_path / ("a.mtx" if fmt.endswith("mtx") else f"a.{fmt}")
     if fmt == "mtx":
         sio.mmwrite(str(p), A)
     elif fmt == "rua":
@@ -165,8 +166,8 @@ def test_device_operator_from_a_matrix_file(tmp_path, fmt):
         sio.mmwrite(str(p), A)  # complex data through the Matrix Market reader
     ref = pio.read(str(p))
     op = pio.load(str(p))
-    x = rng.standard_normal(n) + (1j * rng.standard_normal(n) if fmt == "cua" else 0)
-    y = rng.standard_normal(m) + (1j * rng.standard_normal(m) if fmt == "cua" else 0)
+    x = rng.standard_normal(n) + (1j * rng.standard_normal(n) if fmt == "complex_mtx" else 0)
+    y = rng.standard_normal(m) + (1j * rng.standard_normal(m) if fmt == "complex_mtx" else 0)
     np.testing.assert_allclose(op.matvec(x), ref @ x, rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(op.rmatvec(y), ref.conj().T @ y, rtol=1e-12, atol=1e-12)
     u, s, vt, bnd = pg.svdp(op, 5, kmax=40, tol=1e-12, rng=np.random.default_rng(0))

@@ -89,9 +89,12 @@ def test_noalloc_refuses_host_pointers():
     op.close()
 
 
-def test_noalloc_complex_operator_in_block_form():
-    # a complex operator takes interleaved (re, im) doubles and applies A
-    # (trans 0) or A^H (trans 1), twice in a row
+@pytest.mark.parametrize("form", ["native", "block"])
+def test_noalloc_complex_operator(form):
+    # a complex operator (native complex CSR, or the real 2x2-block form)
+    # takes interleaved (re, im) doubles and applies A (trans 0) or A^H
+    # (trans 1), twice in a row; the native form refuses vectors that are
+    # not 16-byte aligned before any launch
     torch = pytest.importorskip("torch")
     import scipy.sparse as sp
     lib = pg.load()
@@ -100,7 +103,15 @@ def test_noalloc_complex_operator_in_block_form():
     rows = np.repeat(np.arange(m), k)
     A = sp.csr_array((rng.standard_normal(m * k) + 1j * rng.standard_normal(m * k),
                       (rows, rng.integers(0, n, m * k))), shape=(m, n))
-    op = pg.CsrOperator(A)
+    pg.set_complex_form(form)
+    try:
+        op = pg.CsrOperator(A)
+    finally:
+        pg.set_complex_form("native")
+    if form == "native":
+        buf = torch.zeros(2 * max(m, n) + 2, dtype=torch.float64, device="cuda")
+        assert _noalloc(lib, op.handle, 0, buf.data_ptr() + 8, buf.data_ptr()) == pg.ERR_ARG
+        assert "aligned" in pg.last_error()
     for call in range(2):
         for trans in (0, 1):
             x = rng.standard_normal(m if trans else n) + 1j * rng.standard_normal(m if trans else n)
