@@ -293,6 +293,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def form_phases(prof):
+    """Device ms of one profiled solve by phase: the FP32 Lanczos phase of
+    the mixed form (its SpMVs and Gram-Schmidt passes), the FP64 phase
+    (the FP64 form itself, or the mixed form's refinement), and what both
+    share (ELR passes, bidiagonal analysis and restarts, Ritz vectors)."""
+    g = lambda *ks: sum(prof[k][1] for k in ks if k in prof)
+    return {"fp32_spmv": g("spmv_adj_fp32", "spmv_fwd_fp32"),
+            "fp32_gram_schmidt": g("cgs_dots_fp32", "cgs_upd_fp32"),
+            "fp64_spmv": g("spmv_adj", "spmv_fwd", "lowrank_prepass"),
+            "fp64_gram_schmidt": g("cgs_dots", "cgs_upd"),
+            "elr": g("elr"), "bidiagonal_restarts_ritz": g("analyse", "sweeps", "gemm", "ritz_prep")}
+
+
 def spmv_bytes(m, n, r, nnz_s, nnz_l, nnz_r, vb=8):
     """Algorithmic bytes of one fused SpMV launch with vb-byte values and
     vectors (8: FP64 form, 4: mixed form) and int32 indices: values+indices,
@@ -499,6 +512,12 @@ def run_ours(args, wl):
                 for a, b in ((ref_uv[0][:, i], u[:, i]), (ref_uv[1][:, i], v[:, i])):
                     ang = max(ang, min(np.linalg.norm(a - b), np.linalg.norm(a + b)))
             results[form]["max_vector_angle"] = float(ang)
+        if form != chosen:
+            # where a non-chosen form's time goes: one more, profiled solve
+            pg.set_profiling(True)
+            solve(op)
+            results[form]["phases_ms"] = form_phases(pg.get_profile())
+            pg.set_profiling(False)
     clocks = sampler.stop() if sampler else None
     # per-kernel profile of one more solve of the chosen form
     pg.set_precision(chosen)
@@ -650,9 +669,11 @@ def run_ours(args, wl):
                          f"{info['cycle_ms']:.0f} ms) scaled by matvecs to a full FP64 solve "
                          f"({info['matvecs_full']:.0f} matvecs)"}
     breakdown = {kk: {"launches": c, "ms": t} for kk, (c, t) in prof.items() if c}
+    results[chosen]["phases_ms"] = form_phases(prof)
     forms_out = {f: {"ms": per[f], "matvecs": results[f]["matvecs"], "matvecs_fp32": results[f]["matvecs_fp32"],
                      "restarts": results[f]["restarts"], "max_rel_residual": results[f]["rel_resid"],
-                     "wall_ms_per_step": results[f]["wall_ms"] / args.steps} for f in forms}
+                     "wall_ms_per_step": results[f]["wall_ms"] / args.steps,
+                     "phases_ms": results[f]["phases_ms"]} for f in forms}
     sig_err = {}
     if "fp64" in results:
         for f in forms:
