@@ -1280,7 +1280,8 @@ __global__ void __launch_bounds__(BS) k_lb_zelr(LbArgs a, int j)
 // <prev, y> = sum conj(prev) y that the first ELR pass subtracts
 // (pzdotc), in the same launch.  host_product: the caller's ZAPROD already
 // wrote y.
-constexpr int ZSPMV_MINB = 3;  // CTAs per SM the complex SpMV is compiled for (wider values and gathers)
+constexpr int ZSPMV_MINB = 3;    // CTAs per SM the complex SpMV is compiled for (wider values and gathers)
+constexpr int ZSPMV_UNROLL = 4;  // its (index, value) pairs and gathers in flight per lane
 template <int SIDE>
 __global__ void __launch_bounds__(BS, ZSPMV_MINB) k_lb_zspmv(LbArgs a, int j, int host_product)
 {
@@ -1324,7 +1325,7 @@ __global__ void __launch_bounds__(BS, ZSPMV_MINB) k_lb_zspmv(LbArgs a, int j, in
     auto pre = [&](int r) -> double2 { return has_prev ? prev[r] : make_double2(0.0, 0.0); };
     if (!host_product) {
         auto xl = [&](int c) -> double2 { return x[c]; };
-        csr_rows_chunked<double2, double2>(A.ptr, A.tbase, A.cidx, A.czval, A.rows, xl, pre, epi, cst);
+        csr_rows_chunked<double2, double2, ZSPMV_UNROLL>(A.ptr, A.tbase, A.cidx, A.czval, A.rows, xl, pre, epi, cst);
     } else {
         const int rows = (SIDE == 0 ? a.adj.rows : a.fwd.rows) / 2;
         for (int r = blockIdx.x * BS + threadIdx.x; r < rows; r += gridDim.x * BS) epi(r, out[r], pre(r));

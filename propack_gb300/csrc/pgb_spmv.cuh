@@ -205,7 +205,7 @@ __device__ __forceinline__ int warp_lower_bound(const int *__restrict__ t, int n
     return m ? lo + __ffs(m) - 1 : hi;
 }
 
-template <typename VT, typename AT, typename XF, typename PF, typename EPI>
+template <typename VT, typename AT, int UNROLL = CHUNK_UNROLL, typename XF, typename PF, typename EPI>
 __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, const int *__restrict__ tbase,
                                                  const int *__restrict__ cidx, const VT *__restrict__ cval,
                                                  int nrows, XF xload, PF pre_load, EPI epi, ChunkStage<AT> *stages)
@@ -278,16 +278,16 @@ __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, co
             }
         };
         int i = 0;
-        for (; i + CHUNK_UNROLL - 1 < C; i += CHUNK_UNROLL) {
-            int c[CHUNK_UNROLL];
-            VT v[CHUNK_UNROLL];
-            AT xv[CHUNK_UNROLL];
+        for (; i + UNROLL - 1 < C; i += UNROLL) {
+            int c[UNROLL];
+            VT v[UNROLL];
+            AT xv[UNROLL];
 #pragma unroll
-            for (int u = 0; u < CHUNK_UNROLL; u++) { c[u] = ci[32 * (i + u)]; v[u] = cv[32 * (i + u)]; }
+            for (int u = 0; u < UNROLL; u++) { c[u] = ci[32 * (i + u)]; v[u] = cv[32 * (i + u)]; }
 #pragma unroll
-            for (int u = 0; u < CHUNK_UNROLL; u++) xv[u] = (AT)xload(c[u]);
+            for (int u = 0; u < UNROLL; u++) xv[u] = (AT)xload(c[u]);
 #pragma unroll
-            for (int u = 0; u < CHUNK_UNROLL; u++) step(v[u], xv[u]);
+            for (int u = 0; u < UNROLL; u++) step(v[u], xv[u]);
         }
         for (; i < C; i++) step(cv[32 * i], (AT)xload(ci[32 * i]));
         cs.tail[lane] = acc;
