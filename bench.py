@@ -129,6 +129,8 @@ def parse():
                     help="shrink m and n by this factor (profiling captures only; not a bench line)")
     ap.add_argument("--cgs-arith", default="planes", choices=["planes", "fp64", "f3"],
                     help="Gram-Schmidt arithmetic of the FP64 form (propack_set_cgs_arith)")
+    ap.add_argument("--gemm-impl", type=int, default=None, choices=[1, 2],
+                    help="tcgen05 kernel of the restart/Ritz products (propack_set_gemm_impl; default: the library's)")
     ap.add_argument("--batch-arith", default="fp64", choices=["fp64", "planes"],
                     help="batched workload: arithmetic of its products and Gram-Schmidt (propack_batch_set_arith)")
     ap.add_argument("--no-other", action="store_true",
@@ -433,6 +435,8 @@ def run_ours(args, wl):
     import propack_gb300 as pg
     pg.load()
     pg.set_cgs_arith(args.cgs_arith)
+    if getattr(args, "gemm_impl", None) is not None:
+        pg.load().propack_set_gemm_impl(args.gemm_impl)
     barrier = lambda: None
     dist = None
     if world > 1:

@@ -421,10 +421,17 @@ int propack_batch_set_arith(int64_t handle, int arith);
  * dlansvd_irl.F:371-398 and dritzvec.F:130-198 (dgemm_ovwr.F:56-87) as the
  * drivers run it: an error-free split of both operands into seven BF16
  * digits, exact FP32 level sums, int64 recombination.  impl 1 is the
- * tcgen05 kernel the drivers use, impl 0 the mma.sync kernel; both give the
- * same bits.  Requires mr >= 1, 1 <= kk <= 256, lda, ldc >= mr. */
+ * tcgen05 kernel (every thread splits digits, one issues the MMAs between
+ * CTA barriers), impl 2 the warp-specialised tcgen05 kernel (sixteen
+ * splitting warps and one MMA warp meeting on mbarriers), impl 0 the
+ * mma.sync kernel; all give the same bits.  The drivers use the kernel set
+ * by propack_set_gemm_impl (1 or 2).  Requires mr >= 1, 1 <= kk <= 256,
+ * lda, ldc >= mr. */
 int propack_gemm_f64_tc(int impl, int mr, int nc, int kk, const double *A, int lda, const double *B, int ldb,
                         int tb, double *C, int ldc);
+/* The tcgen05 kernel of the drivers' restart and Ritz products (1 or 2,
+ * default 2; process-wide).  Returns 0 or PROPACK_ERR_ARG. */
+int propack_set_gemm_impl(int impl);
 
 /* Device memory of the library's operators and solves comes from its own
  * stream-ordered pool, which keeps freed memory for the next call instead

@@ -23,6 +23,7 @@
 // The digits of A are produced in registers from the FP64 bits with integer
 // operations, straight into mma.sync fragments (m16n8k16, row.col); the
 // digits of B come from a small pre-pass and are staged in shared memory.
+#include <atomic>
 #include <algorithm>
 
 #include "../../include/propack_gb300.h"
@@ -656,6 +657,295 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_oz_umma(int mr, int nc, int k
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
 }
 
+// ===========================================================================
+// The same product, warp-specialised.  Sixteen producer warps (four threads
+// per row, as above) split A into digit planes; one more warp, the MMA warp,
+// copies B's digit planes in (cp.async.bulk) and issues the MMAs.  The two
+// roles meet only on mbarriers, so no CTA-wide barrier sits between a
+// stage's digits and its MMAs:
+//
+//   full[b]   the producers' 512 arrivals: stage buffer b holds its A digits
+//             (each thread fences its shared-memory writes into the async
+//             proxy first)
+//   bfull[b]  the bulk copy of B's digits for the stage in buffer b landed
+//   empty[b]  tcgen05.commit of the stage's MMAs: buffer b may be rewritten
+//   tfull     tcgen05.commit after a tile's last stage: TMEM holds its levels
+//   tempty    the producers' 512 arrivals after reading TMEM: the next
+//             tile's first MMAs may overwrite the levels
+//
+// Stage g uses buffer g % 2, phase (g / 2) % 2 of full/bfull/empty; tile tt
+// (of this CTA) phase tt % 2 of tfull/tempty.  No barrier can run two phases
+// ahead of its waiter: refilling a buffer waits for the MMAs that read it,
+// which wait for the fill before.  Every wait is bounded; a wait that runs
+// out sets the CTA's flag, which every loop checks, and the kernel reports
+// it through *err after the MMAs in flight have finished (bounded) and the
+// tensor memory is freed.  The row exponents of the next tile are folded
+// into the current tile's stages as above and exchanged among the producers
+// only (named barrier 1).  Results are bit-identical to k_oz_umma.
+constexpr int WS_PROD = 512;              // producer threads
+constexpr int WS_THREADS = WS_PROD + 32;  // + the MMA warp
+__device__ __forceinline__ void ws_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void ws_prod_sync() { asm volatile("bar.sync 1, %0;" ::"n"(WS_PROD) : "memory"); }
+// a barrier of the producers only that also ORs a flag over them
+__device__ __forceinline__ bool ws_prod_or(bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.or.pred q, 1, %2, p;\nselp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "n"(WS_PROD)
+        : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ bool ws_bad(const int *sbad) { return *(volatile const int *)sbad != 0; }
+// bounded wait that gives up early once the CTA's flag is set
+__device__ __forceinline__ bool ws_wait(uint32_t bar, unsigned parity, int *sbad)
+{
+    for (long it = 0; it < UM_WAIT_LIMIT; it++) {
+        if (um_bar_try(bar, parity)) return true;
+        if ((it & 255) == 255 && ws_bad(sbad)) return false;
+    }
+    *(volatile int *)sbad = 1;
+    return false;
+}
+
+__global__ void __launch_bounds__(WS_THREADS, 1) k_oz_umma_ws(int mr, int nc, int kk, const double *__restrict__ A,
+                                                             int lda, const unsigned short *__restrict__ Bimg,
+                                                             const int *__restrict__ Fe, int nstage,
+                                                             double *__restrict__ C, int ldc, int *err)
+{
+    extern __shared__ __align__(1024) unsigned char um_sm[];
+    unsigned char *As = um_sm;
+    unsigned char *Bs = um_sm + 2 * UM_ASTAGE;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(Bs + 2 * UM_BSTAGE);
+    // [0..1] full, [2..3] bfull, [4..5] empty, [6] tfull, [7] tempty
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 8);
+    int *sbad = reinterpret_cast<int *>(tslot + 1);
+    int *Ep = reinterpret_cast<int *>(tslot + 4);  // [4][UM_BM]
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int ntc = (nc + UM_BN - 1) / UM_BN;
+    const int ntiles = (mr + UM_BM - 1) / UM_BM * ntc;
+    const uint32_t a_s = um_smem(As), b_s = um_smem(Bs), bar_s = um_smem(bar);
+    const uint32_t FULL = bar_s, BFULL = bar_s + 16, EMPTY = bar_s + 32, TFULL = bar_s + 48, TEMPTY = bar_s + 56;
+    if (tid == 0) {
+        um_bar_init(FULL, WS_PROD);
+        um_bar_init(FULL + 8, WS_PROD);
+        um_bar_init(BFULL, 1);
+        um_bar_init(BFULL + 8, 1);
+        um_bar_init(EMPTY, 1);
+        um_bar_init(EMPTY + 8, 1);
+        um_bar_init(TFULL, 1);
+        um_bar_init(TEMPTY, WS_PROD);
+        *sbad = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (w == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(um_smem(tslot)),
+                     "r"(UM_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+
+    if (tid >= WS_PROD) {
+        // ------------------------------------------------------ MMA warp
+        if (lane == 0) {
+            int g = 0, tt = 0;
+            // the bulk copy of B's digits for stage g (tile t, stage c) into buffer g % 2
+            auto copy_b = [&](int t, int c, int gg) {
+                const uint32_t bb = BFULL + 8 * (gg & 1);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bb), "r"(UM_BSTAGE)
+                             : "memory");
+                const unsigned short *src = Bimg + ((size_t)(t % ntc) * nstage + c) * (UM_BSTAGE / 2);
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        b_s + (gg & 1) * UM_BSTAGE),
+                    "l"(src), "r"(UM_BSTAGE), "r"(bb)
+                    : "memory");
+            };
+            // stage after (t, c): (t, c + 1) or (t + grid, 0)
+            auto next_stage = [&](int &t, int &c) {
+                if (++c == nstage) {
+                    c = 0;
+                    t += gridDim.x;
+                }
+            };
+            int tb = blockIdx.x, cb = 0;  // the stage whose B copy goes out next (stage g + 1 in the loop)
+            if (tb < ntiles) {
+                copy_b(tb, cb, 0);
+                next_stage(tb, cb);
+            }
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, tt++) {
+                if (tt > 0 && !ws_wait(TEMPTY, (tt - 1) & 1, sbad)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                for (int c = 0; c < nstage; c++, g++) {
+                    const int b = g & 1;
+                    if (!ws_wait(FULL + 8 * b, (g >> 1) & 1, sbad) || !ws_wait(BFULL + 8 * b, (g >> 1) & 1, sbad)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint64_t ad0 = um_desc(a_s + b * UM_ASTAGE), bd0 = um_desc(b_s + b * UM_BSTAGE);
+#pragma unroll
+                    for (int st = 0; st < 2; st++)
+#pragma unroll
+                        for (int p = 0; p < OZ_S; p++)
+#pragma unroll
+                            for (int q = 0; p + q < OZ_S; q++)
+                                um_mma(tmem + (uint32_t)((p + q) * UM_BN),
+                                       ad0 + (uint64_t)(((p * 2 + st) * UM_ATILE) >> 4),
+                                       bd0 + (uint64_t)(((q * 2 + st) * UM_BTILE) >> 4),
+                                       (c == 0 && st == 0 && p == 0) ? 0u : 1u);
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     EMPTY + 8 * b)
+                                 : "memory");
+                    if (c == nstage - 1)
+                        asm volatile(
+                            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(TFULL)
+                            : "memory");
+                    // the other buffer is free once stage g - 1's MMAs are done
+                    // (issued before this stage's): the B copy of stage g + 1
+                    // goes into it
+                    if (tb < ntiles) {
+                        if (g >= 1 && !ws_wait(EMPTY + 8 * (b ^ 1), ((g - 1) >> 1) & 1, sbad)) {
+                            ok = false;
+                            break;
+                        }
+                        copy_b(tb, cb, g + 1);
+                        next_stage(tb, cb);
+                    }
+                }
+            }
+            if (!ok) *(volatile int *)sbad = 1;
+            // the MMAs issued last are done before the columns are freed
+            if (g > 0) um_bar_wait(EMPTY + 8 * ((g - 1) & 1), ((g - 1) >> 1) & 1);
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------------------------ producer warps
+        const int r = tid & (UM_BM - 1), h = tid >> 7;
+        auto tile_row = [&](int t) { return (t / ntc) * UM_BM + r; };
+        auto scan_load = [&](int t, int c, double (&sv)[8]) {
+            const int row = tile_row(t);
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int l = h + 4 * (8 * c + u);
+                sv[u] = (t < ntiles && row < mr && l < kk) ? A[(size_t)l * lda + row] : 0.0;
+            }
+        };
+        auto scan_fold = [&](int &Eacc, const double (&sv)[8]) {
+#pragma unroll
+            for (int u = 0; u < 8; u++) Eacc = max(Eacc, oz_exp_of(sv[u]));
+        };
+        double xv[8];
+        auto load_stage = [&](int t, int c) {
+            const int row = tile_row(t), k0 = c * UM_KC + h * 8;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int l = k0 + i;
+                xv[i] = (t < ntiles && row < mr && l < kk) ? A[(size_t)l * lda + row] : 0.0;
+            }
+        };
+        int t = blockIdx.x;
+        int E = -2000;
+        for (int c = 0; c < nstage; c++) {
+            double sv[8];
+            scan_load(t, c, sv);
+            scan_fold(E, sv);
+        }
+        Ep[h * UM_BM + r] = E;
+        load_stage(t, 0);
+        ws_prod_sync();
+        E = max(max(Ep[r], Ep[UM_BM + r]), max(Ep[2 * UM_BM + r], Ep[3 * UM_BM + r]));
+        if (E == -2000) E = 0;
+        ws_prod_sync();  // Ep is written again at the end of the first tile
+        const uint32_t arow_off = (uint32_t)((h >> 1) * UM_ATILE + (r >> 3) * 256 + (h & 1) * 128 + (r & 7) * 16);
+        // Control flow is the same in every producer thread (the named
+        // barriers need all of them): a wait that fails marks the thread,
+        // which then skips its TMEM reads and stores, and the producers stop
+        // together at the end of the tile
+        int g = 0, tt = 0;
+        bool ok = true;
+        for (; t < ntiles; t += gridDim.x, tt++) {
+            const int tn = t + gridDim.x;
+            const int col0 = (t % ntc) * UM_BN, row0 = (t / ntc) * UM_BM;
+            int En = -2000;
+            double sv[8];
+            for (int c = 0; c < nstage; c++, g++) {
+                const int b = g & 1;
+                if (g >= 2 && ok && !ws_wait(EMPTY + 8 * b, ((g - 2) >> 1) & 1, sbad)) ok = false;
+                if (c > 0) scan_fold(En, sv);
+                unsigned long long Mb[8];
+                float sg[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    unsigned ng;
+                    Mb[i] = oz_fixed(xv[i], E, ng);
+                    sg[i] = ng ? -1.0f : 1.0f;
+                }
+                if (c + 1 < nstage) load_stage(t, c + 1);
+                else load_stage(tn, 0);
+                scan_load(tn, c, sv);
+                const uint32_t arow = a_s + b * UM_ASTAGE + arow_off;
+                um_plane<0>(arow, Mb, sg);
+                um_plane<1>(arow, Mb, sg);
+                um_plane<2>(arow, Mb, sg);
+                um_plane<3>(arow, Mb, sg);
+                um_plane<4>(arow, Mb, sg);
+                um_plane<5>(arow, Mb, sg);
+                um_plane<6>(arow, Mb, sg);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                ws_arrive(FULL + 8 * b);
+            }
+            if (ok && !ws_wait(TFULL, tt & 1, sbad)) ok = false;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            scan_fold(En, sv);
+            Ep[h * UM_BM + r] = En;
+            if (ok) {
+                const int L = 32 * (w & 3), hc = w >> 2;
+                const int orow = row0 + L + lane;
+#pragma unroll
+                for (int ph = 0; ph < 2; ph++) {
+                    const int cb = hc * 16 + ph * 8;
+                    uint32_t v[OZ_S][8];
+#pragma unroll
+                    for (int gg = 0; gg < OZ_S; gg++)
+                        um_ld8(tmem + ((uint32_t)L << 16) + (uint32_t)(gg * UM_BN + cb), v[gg]);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                    for (int jj = 0; jj < 8; jj++) {
+                        const int col = col0 + cb + jj;
+                        int T[OZ_S];
+#pragma unroll
+                        for (int gg = 0; gg < OZ_S; gg++) T[gg] = __float2int_rn(__uint_as_float(v[gg][jj]));
+                        if (orow < mr && col < nc)
+                            C[(size_t)col * ldc + orow] = oz_levels(T, E + Fe[col] - 14 - 7 * (OZ_S - 1));
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            ws_arrive(TEMPTY);
+            const bool stop = ws_prod_or(!ok || ws_bad(sbad));
+            E = max(max(Ep[r], Ep[UM_BM + r]), max(Ep[2 * UM_BM + r], Ep[3 * UM_BM + r]));
+            if (E == -2000) E = 0;
+            if (stop) break;
+        }
+        if (!ok) *(volatile int *)sbad = 1;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (tid == 0 && *sbad) atomicExch(err, 1);
+    if (w == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
+}
+
 // scratch for the digits of B (grown on demand, per host thread)
 struct OzScratch {
     unsigned short *bd = nullptr;
@@ -698,19 +988,21 @@ static void oz_scratch(OzScratch &sc, size_t need, int nfe)
     }
 }
 
-// impl 0: mma.sync kernel; impl 1: tcgen05 kernel
+// impl 0: mma.sync kernel; impl 1: tcgen05 kernel; impl 2: tcgen05,
+// warp-specialised
 static void oz_gemm_launch(int impl, int mr, int nc, int kk, const double *A, int lda, const double *B, int ldb,
                            bool tb, double *C, int ldc, cudaStream_t s)
 {
     static thread_local OzScratch sc;
-    if (impl == 1) {
+    if (impl == 1 || impl == 2) {
         const int ntc = (nc + UM_BN - 1) / UM_BN;
         const int nstage = (kk + UM_KC - 1) / UM_KC;
         oz_scratch(sc, (size_t)ntc * nstage * UM_BSTAGE / 2, ntc * UM_BN);
-        static thread_local bool attr = false;
-        if (!attr) {
+        static thread_local int attr = -1;
+        if (attr != 1) {
             PGB_CUDA(cudaFuncSetAttribute(k_oz_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
-            attr = true;
+            PGB_CUDA(cudaFuncSetAttribute(k_oz_umma_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
+            attr = 1;
         }
         PGB_CUDA(cudaMemsetAsync(sc.err, 0, sizeof(int), s));
         PGB_PROF(PK_GEMM, s, {
@@ -718,7 +1010,11 @@ static void oz_gemm_launch(int impl, int mr, int nc, int kk, const double *A, in
             PGB_LAUNCHED();
             const int ntiles = (mr + UM_BM - 1) / UM_BM * ntc;
             const int grid = std::min(ntiles, device_info().sms);  // persistent: one CTA per SM
-            k_oz_umma<<<grid, UM_THREADS, UM_SMEM, s>>>(mr, nc, kk, A, lda, sc.bd, sc.fe, nstage, C, ldc, sc.err);
+            if (impl == 2)
+                k_oz_umma_ws<<<grid, WS_THREADS, UM_SMEM, s>>>(mr, nc, kk, A, lda, sc.bd, sc.fe, nstage, C, ldc,
+                                                              sc.err);
+            else
+                k_oz_umma<<<grid, UM_THREADS, UM_SMEM, s>>>(mr, nc, kk, A, lda, sc.bd, sc.fe, nstage, C, ldc, sc.err);
             PGB_LAUNCHED();
         });
         PGB_CUDA(cudaMemcpyAsync(sc.herr, sc.err, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -747,25 +1043,38 @@ static void oz_gemm_launch(int impl, int mr, int nc, int kk, const double *A, in
     });
 }
 
+// the tcgen05 kernel of the library's restart and Ritz products
+// (propack_set_gemm_impl: 1 or 2; the warp-specialised one measured 1.3x
+// faster on the zipf restart products)
+static std::atomic<int> g_gemm_impl{2};
+
 bool gemm_f64_tc(int mr, int nc, int kk, const double *A, int lda, const double *B, int ldb, bool tb, double *C,
                  int ldc, cudaStream_t s)
 {
     if (mr < 4096 || nc <= 0 || kk <= 0 || kk > OZ_KMAX) return false;
-    oz_gemm_launch(1, mr, nc, kk, A, lda, B, ldb, tb, C, ldc, s);
+    oz_gemm_launch(g_gemm_impl.load(), mr, nc, kk, A, lda, B, ldb, tb, C, ldc, s);
     return true;
 }
 
 }  // namespace pgb
 
-// C = A op(B) with device operands through one of the two tensor-core
-// kernels (0: mma.sync, 1: tcgen05); both give the same bits.  Used by the
+extern "C" int propack_set_gemm_impl(int impl)
+{
+    if (impl != 1 && impl != 2) return PROPACK_ERR_ARG;
+    pgb::g_gemm_impl.store(impl);
+    return 0;
+}
+
+// C = A op(B) with device operands through one of the tensor-core kernels
+// (0: mma.sync, 1: tcgen05, 2: tcgen05 warp-specialised); all give the same
+// bits.  Used by the
 // tests to hold the kernels against each other and against FP64 products.
 extern "C" int propack_gemm_f64_tc(int impl, int mr, int nc, int kk, const double *A, int lda, const double *B,
                                    int ldb, int tb, double *C, int ldc)
 {
     using namespace pgb;
     set_error("");
-    if (mr <= 0 || nc <= 0 || kk <= 0 || kk > OZ_KMAX || (impl != 0 && impl != 1) || lda < mr || ldc < mr)
+    if (mr <= 0 || nc <= 0 || kk <= 0 || kk > OZ_KMAX || impl < 0 || impl > 2 || lda < mr || ldc < mr)
         return PROPACK_ERR_ARG;
     try {
         oz_gemm_launch(impl, mr, nc, kk, A, lda, B, ldb, tb != 0, C, ldc, 0);

@@ -1,6 +1,7 @@
 """The FP64 restart/Ritz product on the tensor cores (error-free digit
-split, dlansvd_irl.F:371-398, dritzvec.F:130-198): the tcgen05 kernel and
-the mma.sync kernel must give the same bits, and both must match an FP64
+split, dlansvd_irl.F:371-398, dritzvec.F:130-198): the tcgen05 kernels
+(barrier-staged and warp-specialised) and the mma.sync kernel must give the
+same bits, and all must match an FP64
 product to the split's error bound (operands kept to 2^-49 of their row and
 column maxima, digit products below 2^-56 dropped; the level sums
 themselves are exact)."""
@@ -48,13 +49,13 @@ def test_tcgen05_matches_mma_sync_and_fp64(mr, kk, nc, tb):
     A_t = torch.from_numpy(Amem).to(dev)
     B_t = torch.from_numpy(Bmem).to(dev)
     outs = []
-    for impl in (0, 1):
+    for impl in (0, 1, 2):
         C_t = torch.full((nc, ldc), np.nan, dtype=torch.float64, device=dev)
         _call(impl, A_t, lda, B_t, ldb, tb, C_t, ldc, mr, nc, kk)
         Cm = C_t.cpu().numpy()
         assert np.all(np.isnan(Cm[:, mr:]))  # rows past mr untouched
         outs.append(Cm[:, :mr].T)
-    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
     # the split keeps every operand to 2^-49 of its row (column) maximum and
     # drops the digit products below 2^-56: |error| <= K 2^-45 max|A(i,:)| max|B(:,j)|
     ref = A @ Bop
@@ -70,7 +71,27 @@ def test_aligned_signs_take_the_wide_path():
     dev = torch.device("cuda:0")
     A_t = torch.ones((kk, mr), dtype=torch.float64, device=dev)
     B_t = torch.ones((nc, kk), dtype=torch.float64, device=dev)
-    for impl in (0, 1):
+    for impl in (0, 1, 2):
         C_t = torch.zeros((nc, mr), dtype=torch.float64, device=dev)
         _call(impl, A_t, mr, B_t, kk, 0, C_t, mr, mr, nc, kk)
         assert torch.all(C_t == float(kk))
+
+
+def test_warp_specialised_kernel_in_the_solve():
+    """The drivers' restart products on either tcgen05 kernel give the same
+    bits (propack_set_gemm_impl)."""
+    pytest.importorskip("torch")
+    import scipy.sparse as sp
+    rng = np.random.default_rng(4)
+    A = sp.random_array((6000, 1500), density=0.004, format="csr", random_state=rng)
+    out = []
+    try:
+        for impl in (1, 2):
+            assert pg.load().propack_set_gemm_impl(impl) == 0
+            u, s, vt, bnd = pg.svdp(A, 6, irl_mode=True, kmax=24, tol=1e-10, rng=np.random.default_rng(0))
+            assert pg.get_stats()["nrestart"] > 0
+            out.append((u, s, vt))
+    finally:
+        pg.load().propack_set_gemm_impl(2)
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
