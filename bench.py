@@ -141,13 +141,15 @@ def parse():
 # The scope's other configurations, each run by this script in a process of
 # its own after the headline workload, its JSON line kept under
 # "other_configs": config[0] (the reference's CPU-runnable case), config[1]
-# at full size, and the batched config on a stated fraction of its 4096
-# problems (the whole batch takes minutes to generate and solve).  The
-# learned-start family (config[4]) stays opt-in: --workload learned.
+# at full size, the batched config on a stated fraction of its 4096
+# problems (the whole batch takes minutes to generate and solve), and the
+# complex*16 drivers on the complex zipf analogue.  The learned-start family
+# (config[4]) stays opt-in: --workload learned.
 OTHER_CONFIGS = [
     ("plain_lansvd", ["--steps", "20", "--warmup", "3", "--e2e-steps", "5"]),
     ("lowrank_irl", ["--steps", "2", "--warmup", "1", "--e2e-steps", "1"]),
     ("batched", ["--steps", "1", "--warmup", "1", "--scale", "0.25"]),
+    ("complex_zipf", ["--steps", "3", "--warmup", "2", "--e2e-steps", "1"]),
 ]
 
 
