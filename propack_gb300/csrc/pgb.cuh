@@ -164,6 +164,7 @@ struct LbArgs {
     double *part_cols;            // (kmax+1) * nb partial CGS dots, column c at c*nb
                                   // (complex: 2 (kmax+1) * nb, re at 2c*nb, im at (2c+1)*nb)
     int nb;                 // CTAs of the vector kernels
+    int nb_spmv;            // CTAs the fused SpMV may use (>= nb; the partial-sum arrays hold it)
     int kmax;               // capacity of the column arrays
     Csr fwd, adj;           // device operator (fwd = [S|L], adj = [S'|R])
     Csr zfwd, zadj;         // a native complex operator (A, A^H; rows = 0 otherwise)

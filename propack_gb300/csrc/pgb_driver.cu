@@ -235,6 +235,7 @@ struct Ctx {
     LbCtl *hctl = nullptr;  // pinned host copy
     double *balpha = nullptr, *bbeta = nullptr, *mu = nullptr, *nu = nullptr, *h = nullptr;
     double *part_sq = nullptr, *part_dot = nullptr, *part_cols = nullptr;
+    int nb_spmv = 0;  // grid bound of the fused SpMV (spmv_grid_bound)
     int *index = nullptr, *sel = nullptr;
     void *xr = nullptr, *yr = nullptr;      // max(m,n) scratch of the vector type
     double *dx = nullptr, *dy = nullptr;    // max(m,n) FP64 scratch
@@ -321,6 +322,7 @@ struct Ctx {
         a.index = index; a.sel = sel; a.h = h;
         a.part_sq = part_sq; a.part_dot = part_dot; a.part_cols = part_cols;
         a.nb = nb; a.kmax = kmax;
+        a.nb_spmv = std::max(nb, nb_spmv);
         if (op && op->cplx == 2) {
             // a native complex operator: its own kernels read zfwd / zadj;
             // fwd and adj carry only the vector lengths in real scalars
@@ -356,6 +358,16 @@ static int vec_grid(int64_t elems, int64_t nnz)
     const int64_t cap = device_info().nb;
     const int64_t want = std::max((elems + 2047) / 2048, (nnz + 16383) / 16384);
     return (int)std::max<int64_t>(1, std::min(cap, want));
+}
+// CTAs the fused SpMV may use: one per 256 rows (a 32-row tile per warp),
+// at most the four per SM that the partial-sum arrays hold.  The SpMV's
+// latency chain (row bounds, indices, gathers) runs once per tile, so a
+// small matrix wants its tiles spread over warps rather than its nonzeros
+// over few CTAs.
+static int spmv_grid_bound(int64_t rows)
+{
+    const int64_t cap = device_info().nb;
+    return (int)std::max<int64_t>(1, std::min(cap, (rows + 255) / 256));
 }
 
 template <typename T>
@@ -1274,6 +1286,7 @@ static void setup_operator(Ctx &c, propack_aprod_t aprod, double *dparm, int *ip
         }
         c.op = op;
         c.nb = std::max(c.nb, vec_grid(0, std::max(op->fwd.nnz, op->adj.nnz)));
+        c.nb_spmv = spmv_grid_bound(std::max(op->fwd.rows, op->adj.rows));
     } else {
         c.aprod = aprod;
         c.dparm = dparm;
@@ -1305,6 +1318,7 @@ static void setup_zoperator(Ctx &c, propack_zaprod_t aprod, propack_z16 *zparm, 
         }
         c.op = op;
         c.nb = std::max(c.nb, vec_grid(0, std::max(op->fwd.nnz, op->adj.nnz)));
+        c.nb_spmv = spmv_grid_bound(std::max(op->fwd.rows, op->adj.rows));
     } else {
         c.zaprod = aprod;
         c.zparm = zparm;

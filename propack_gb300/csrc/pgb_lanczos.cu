@@ -1845,9 +1845,9 @@ template <int SIDE, typename T>
 static void launch_spmv(const LbArgs &a, const Csr &A, int j, bool host_product, cudaStream_t s)
 {
     if (host_product || A.short_rows)
-        k_lb_spmv<SIDE, T, 1><<<spmv_grid<SIDE, T, 1>(a.nb), BS, 0, s>>>(a, j, host_product ? 1 : 0);
+        k_lb_spmv<SIDE, T, 1><<<spmv_grid<SIDE, T, 1>(a.nb_spmv), BS, 0, s>>>(a, j, host_product ? 1 : 0);
     else
-        k_lb_spmv<SIDE, T, 0><<<spmv_grid<SIDE, T, 0>(a.nb), BS, 0, s>>>(a, j, host_product ? 1 : 0);
+        k_lb_spmv<SIDE, T, 0><<<spmv_grid<SIDE, T, 0>(a.nb_spmv), BS, 0, s>>>(a, j, host_product ? 1 : 0);
 }
 
 template <int SIDE>
@@ -1861,7 +1861,7 @@ static void launch_zspmv(const LbArgs &a, int j, bool host_product, cudaStream_t
         g = std::max(1, per) * d.sms;
         dev = d.device;
     }
-    k_lb_zspmv<SIDE><<<std::min(g, a.nb), BS, 0, s>>>(a, j, host_product ? 1 : 0);
+    k_lb_zspmv<SIDE><<<std::min(g, a.nb_spmv), BS, 0, s>>>(a, j, host_product ? 1 : 0);
 }
 
 // Enqueue the kernels of one half step.  host_product: the product was
