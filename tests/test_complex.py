@@ -368,8 +368,10 @@ def test_complex_zero_and_tiny_operators(form):
     """Edge cases of both operator forms: an operator with no nonzeros
     annihilates every start vector and both drivers report k zero values
     (INFO 0, as the real drivers and scipy's packaging do); a 7 x 5 dense
-    complex matrix (rows shorter and longer than a warp's run) solves to
-    LAPACK's values."""
+    complex matrix (rows shorter and longer than a warp's run) gives the
+    oracle's values.  There the reference itself stops 4e-8 (sigma_1) and
+    2.6e-6 (sigma_2) from LAPACK's values -- scipy's packaging of PROPACK
+    returns the same -- so the comparison is with the oracle."""
     rng = np.random.default_rng(9)
     Z = sp.csr_array((50, 30), dtype=np.complex128)
     D = sp.csr_array(rng.standard_normal((7, 5)) + 1j * rng.standard_normal((7, 5)))
@@ -378,7 +380,9 @@ def test_complex_zero_and_tiny_operators(form):
         for irl in (True, False):
             u, s, vh, bnd = pg.svdp(Z, 3, irl_mode=irl, kmax=10, rng=np.random.default_rng(0))
             np.testing.assert_array_equal(s, np.zeros(3))
-            u, s, vh, bnd = pg.svdp(D, 2, irl_mode=irl, kmax=4, tol=1e-12, rng=np.random.default_rng(0))
-            np.testing.assert_allclose(s, np.linalg.svd(D.toarray(), compute_uv=False)[:2], rtol=1e-10)
+            u, s, vh, bnd = pg.svdp(D, 2, irl_mode=irl, kmax=5, tol=1e-12, rng=np.random.default_rng(0))
+            so = oracle.svdp(D, 2, irl_mode=irl, kmax=5, tol=1e-12, rng=np.random.default_rng(0))[1]
+            np.testing.assert_allclose(s, so, rtol=1e-10)
+            np.testing.assert_allclose(s, np.linalg.svd(D.toarray(), compute_uv=False)[:2], rtol=1e-5)
     finally:
         pg.set_complex_form("native")
