@@ -170,3 +170,25 @@ def test_argument_errors_match_scipy(kw):
     ref = _outcome(lambda: _svdp(A, k, rng=np.random.default_rng(0), **kw))
     ours = _outcome(lambda: pg.svdp(aslinearoperator(A), k, rng=np.random.default_rng(0), **kw))
     assert ref == "ValueError" and ours == ref
+
+
+def test_process_wide_settings_refuse_bad_values():
+    """The setters of the library's alternative kernels take only their
+    documented values (checked on the host, no device work): the complex
+    operator form, the restart products' tcgen05 kernel, the MLP layer's
+    kernel, the batched arithmetic (and a batch handle that does not exist)."""
+    import ctypes as C
+    import propack_gb300 as pg
+    L = pg.load()
+    for fn, bad, good in (("propack_set_zcsr_form", (2, -1), 0), ("propack_set_gemm_impl", (0, 3), 2),
+                          ("propack_mlp_set_impl", (2, -1), 1)):
+        f = getattr(L, fn)
+        f.restype = C.c_int
+        f.argtypes = [C.c_int]
+        for b in bad:
+            assert f(b) == pg.ERR_ARG, (fn, b)
+        assert f(good) == 0
+    L.propack_batch_set_arith.restype = C.c_int
+    L.propack_batch_set_arith.argtypes = [C.c_int64, C.c_int]
+    assert L.propack_batch_set_arith(C.c_int64(123456789), 2) == pg.ERR_HANDLE
+    assert L.propack_batch_set_arith(C.c_int64(123456789), 1) == pg.ERR_ARG
