@@ -401,8 +401,8 @@ def run_reference(args, wl):
         if it >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
-    # the reference's Fortran as scipy packages it, once (not a step: it is
-    # the second CPU baseline the scope table asks for, beside the port)
+    # the reference's Fortran as scipy packages it, once (not a step: a
+    # second CPU baseline beside the port, the reference's own code)
     try:
         sv, sinfo = scipy_sample(S, L, R, w, wl)
         scipy_line = {"value": sv, "unit": "ms", "kind": "scipy._svdp (reference Fortran, scipy build)",
