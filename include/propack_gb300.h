@@ -207,8 +207,10 @@ int propack_get_profile(double *total_ms, int64_t *launches, int n);
  * each basis column split once into FP32 (hi, lo) planes kept beside the
  * FP64 basis (one more basis-sized array of device memory), the products
  * summed on the FP32 pipe as compensated FP32 pairs (error a few 2^-48 of
- * sum |w x|), then one FP64 FMA per row.  Mode 2 applies to solves whose
- * kmax is at most ~2800 and falls back to mode 0 above that.  Returns 0 or
+ * sum |w x|), then one FP64 FMA per row.  The complex*16 drivers run
+ * mode 2 on planes of the real and imaginary parts and mode 1 as mode 0.
+ * Mode 2 applies to solves whose kmax is at most ~2800 (complex drivers:
+ * ~1500) and falls back to mode 0 above that.  Returns 0 or
  * PROPACK_ERR_ARG. */
 int propack_set_cgs_arith(int mode);
 
