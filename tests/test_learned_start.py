@@ -142,7 +142,11 @@ def test_learned_start_gains_over_random_start():
         rand.append(info_r["nopx"])
         lrn.append(info_l["nopx"])
     assert np.mean(energy) > 0.5, energy
-    assert np.mean(lrn) < np.mean(rand), (lrn, rand)
+    # measured on a GB300: random 65-73 matvecs (mean 69), learned 65 on
+    # every member (5.8 % fewer); the solves and the training are
+    # bit-reproducible, so the margins are not timing-dependent
+    assert all(l <= r for l, r in zip(lrn, rand)), (lrn, rand)
+    assert np.mean(lrn) <= 0.97 * np.mean(rand), (lrn, rand)
     for op in ops:
         op.close()
     model.close()
