@@ -248,14 +248,18 @@ __global__ void k_chunk_count(const int *ptr, int rows, int *cnt)
         cnt[t] = max(1, (e + 31) / 32);
     }
 }
-// entry p of tile t goes to unit tbase[t] + p % C, lane p / C
+// entry p of tile t goes to unit tbase[t] + p % C, lane p / C.  One warp per
+// tile: its lanes read the tile's entries, which are contiguous, with
+// coalesced loads.
 __global__ void k_chunk_scatter(const int *ptr, const int *idx, const double *val, const float *valf, int rows,
                                 const int *tbase, int *cidx, double *cval, float *cvalf)
 {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
-        const int t = r >> 5, eb = ptr[32 * t], t0 = tbase[t], C = tbase[t + 1] - t0;
-        for (int e = ptr[r]; e < ptr[r + 1]; e++) {
-            const int p = e - eb;
+    const int lane = threadIdx.x & 31, ntiles = (rows + 31) / 32;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < ntiles; t += nw) {
+        const int eb = ptr[32 * t], ee = ptr[min(32 * t + 32, rows)], t0 = tbase[t], C = tbase[t + 1] - t0;
+        for (int p = lane; p < ee - eb; p += 32) {
+            const int e = eb + p;
             const size_t pos = ((size_t)t0 + p % C) * 32 + p / C;
             cidx[pos] = idx[e];
             cval[pos] = val[e];
@@ -268,10 +272,12 @@ __global__ void k_chunk_scatter(const int *ptr, const int *idx, const double *va
 __global__ void k_chunk_scatter_z(const int *ptr, const int *idx, const double2 *val, int rows, const int *tbase,
                                   int *cidx, double2 *cval)
 {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
-        const int t = r >> 5, eb = ptr[32 * t], t0 = tbase[t], C = tbase[t + 1] - t0;
-        for (int e = ptr[r]; e < ptr[r + 1]; e++) {
-            const int p = e - eb;
+    const int lane = threadIdx.x & 31, ntiles = (rows + 31) / 32;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < ntiles; t += nw) {
+        const int eb = ptr[32 * t], ee = ptr[min(32 * t + 32, rows)], t0 = tbase[t], C = tbase[t + 1] - t0;
+        for (int p = lane; p < ee - eb; p += 32) {
+            const int e = eb + p;
             const size_t pos = ((size_t)t0 + p % C) * 32 + p / C;
             cidx[pos] = idx[e];
             cval[pos] = val[e];
@@ -294,7 +300,7 @@ static void build_chunks(Csr &A, cudaStream_t s)
     const size_t units = (size_t)scan_excl(cnt, A.tbase, ntiles, s);
     PGB_CUDA(cudaFreeAsync(cnt, s));
     const size_t len = units * 32;
-    const int gr = std::min(4096, std::max(1, (A.rows + 255) / 256));
+    const int gr = std::min(4096, std::max(1, (ntiles + 7) / 8));  // a warp per 32-row tile
     A.cidx = (int *)pool_alloc(sizeof(int) * len, s);
     PGB_CUDA(cudaMemsetAsync(A.cidx, 0, sizeof(int) * len, s));
     if (A.zval) {
@@ -356,19 +362,61 @@ __global__ void k_add_extra(int *tot, const int *cnt, const int *xptr, int cols)
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x)
         tot[c] = cnt[c] + (xptr ? (xptr[c + 1] - xptr[c]) : 0);
 }
-__global__ void k_scatter(const int *ptr, const int *idx, int rows, const int *optr, int *fill,
-                          unsigned long long *key)
+// One warp per 32-row tile: the lanes read the tile's entries (contiguous)
+// with coalesced loads and find each entry's row among the tile's 33 row
+// starts, kept in shared memory.  The order of the atomic slots is
+// arbitrary; the keys (entry, row) are sorted per column afterwards.
+__global__ void __launch_bounds__(256) k_scatter(const int *ptr, const int *idx, int rows, const int *optr,
+                                                 int *fill, unsigned long long *key)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
-        for (int e = ptr[i]; e < ptr[i + 1]; e++) {
+    __shared__ int rbs[8][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, ntiles = (rows + 31) / 32;
+    int *rb = rbs[w];
+    const int nw = gridDim.x * 8;
+    for (int t = blockIdx.x * 8 + w; t < ntiles; t += nw) {
+        rb[lane] = ptr[min(32 * t + lane, rows)];
+        if (lane == 0) rb[32] = ptr[min(32 * t + 32, rows)];
+        __syncwarp();
+        const int eb = rb[0], ee = rb[32];
+        for (int e = eb + lane; e < ee; e += 32) {
+            // the last row of the tile that starts at or before e
+            int k = 0;
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1)
+                if (rb[k + st] <= e) k += st;
+            const int i = 32 * t + k;
             const int c = idx[e];
             const int p = optr[c] + atomicAdd(&fill[c], 1);
             key[p] = ((unsigned long long)(unsigned)e << 32) | (unsigned)i;
         }
+        __syncwarp();
     }
 }
-// one warp per segment of length <= 1024: bitonic sort in shared memory;
-// longer segments are listed for k_segsort_long.
+// segments of at most SEG_SMALL keys (most columns of a sparse matrix): one
+// thread per segment, insertion sort in registers/local memory.  The keys
+// are distinct, so every sort gives the same order.
+constexpr int SEG_SMALL = 32;
+__global__ void k_segsort_small(unsigned long long *key, const int *optr, const int *cnt, int cols)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
+        const int len = cnt[c], off = optr[c];
+        if (len <= 1 || len > SEG_SMALL) continue;
+        unsigned long long v[SEG_SMALL];
+        for (int i = 0; i < len; i++) v[i] = key[off + i];
+        for (int i = 1; i < len; i++) {
+            const unsigned long long x = v[i];
+            int j = i - 1;
+            while (j >= 0 && v[j] > x) {
+                v[j + 1] = v[j];
+                j--;
+            }
+            v[j + 1] = x;
+        }
+        for (int i = 0; i < len; i++) key[off + i] = v[i];
+    }
+}
+// one warp per segment of SEG_SMALL+1 .. 1024 keys: bitonic sort in shared
+// memory; longer segments are listed for k_segsort_long.
 __global__ void k_segsort_warp(unsigned long long *key, const int *optr, const int *cnt, int cols,
                                int *longlist, int *nlong)
 {
@@ -377,7 +425,7 @@ __global__ void k_segsort_warp(unsigned long long *key, const int *optr, const i
     unsigned long long *s = sh[w];
     for (int c = blockIdx.x * 4 + w; c < cols; c += gridDim.x * 4) {
         const int len = cnt[c], off = optr[c];
-        if (len <= 1) continue;
+        if (len <= SEG_SMALL) continue;
         if (len > 1024) {
             if (lane == 0) longlist[atomicAdd(nlong, 1)] = c;
             continue;
@@ -490,8 +538,17 @@ static void transpose_into(Csr &T, const int *ptr, const int *idx, const V *val,
     // not by nnz(A)
     PGB_CUDA(cudaMallocAsync(&key, sizeof(unsigned long long) * std::max(total, 1), s));
     // the scan wrote T.ptr; optr == T.ptr, the A' part of row c is [ptr[c], ptr[c]+cnt[c])
-    if (rows > 0 && nnz > 0) { k_scatter<<<g, 256, 0, s>>>(ptr, idx, rows, T.ptr, fill, key); PGB_LAUNCHED(); }
-    if (cols > 0) { k_segsort_warp<<<g, 128, 0, s>>>(key, T.ptr, cnt, cols, longlist, nlong); PGB_LAUNCHED(); }
+    if (rows > 0 && nnz > 0) {
+        const int gt = std::min(4096, std::max(1, ((rows + 31) / 32 + 7) / 8));  // a warp per 32-row tile
+        k_scatter<<<gt, 256, 0, s>>>(ptr, idx, rows, T.ptr, fill, key);
+        PGB_LAUNCHED();
+    }
+    if (cols > 0) {
+        k_segsort_small<<<g, 256, 0, s>>>(key, T.ptr, cnt, cols);
+        PGB_LAUNCHED();
+        k_segsort_warp<<<g, 128, 0, s>>>(key, T.ptr, cnt, cols, longlist, nlong);
+        PGB_LAUNCHED();
+    }
     int hlong = 0;
     PGB_CUDA(cudaMemcpyAsync(&hlong, nlong, sizeof(int), cudaMemcpyDeviceToHost, s));
     PGB_CUDA(cudaStreamSynchronize(s));
@@ -864,8 +921,18 @@ static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, c
     op->w = dw;
     PGB_CUDA(cudaGetDevice(&op->device));
     const int g = 4096;
-    // fwd = [S | L]
-    {
+    // the transposition's inputs (the uploaded S)
+    const int *tsp = dsp, *tsi = dsi;
+    const double *tsv = dsv;
+    // fwd = [S | L]; without a low-rank term that is S itself, whose
+    // uploaded arrays the operator keeps
+    if (r == 0) {
+        Csr &A = op->fwd;
+        A.rows = m; A.cols = n; A.ncol0 = n;
+        A.ptr = dsp; A.idx = dsi; A.val = dsv; A.nnz = snnz;
+        dsp = nullptr; dsi = nullptr; dsv = nullptr;  // owned by the operator now
+        build_blocks(A, s);
+    } else {
         Csr &A = op->fwd;
         A.rows = m; A.cols = n + r; A.ncol0 = n;
         int *tot = nullptr;
@@ -882,7 +949,7 @@ static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, c
         build_blocks(A, s);
     }
     // adj = [S' | R]
-    transpose_into<double>(op->adj, dsp, dsi, dsv, m, n, snnz, drp, dri, drv, m, r, s);
+    transpose_into<double>(op->adj, tsp, tsi, tsv, m, n, snnz, drp, dri, drv, m, r, s);
     build_blocks(op->adj, s);
     if (r > 0) {
         // thin_r = R' (r x n), thin_l = L' (r x m)
