@@ -590,6 +590,7 @@ def run_ours(args, wl):
         return (time.perf_counter() - t0) * 1e3 / steps, {kk: v / steps for kk, v in ph.items()}
 
     barrier()
+    e2e_run(h_parts, h_w, u_pin, v_pin, 1)  # untimed warm-up step (first-call costs), as for the pageable arrays
     e2e_ms, phases = e2e_run(h_parts, h_w, u_pin, v_pin, e2e_steps)
     # the same with ordinary (pageable) host arrays, as a Fortran or numpy
     # caller has them: allocated once, pages touched by one untimed call
@@ -991,14 +992,19 @@ def run_complex(args, wl):
     v_pin = torch.zeros((kmax, n), dtype=torch.complex128).pin_memory().numpy().T
     lib = pg.load()
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 2))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def e2e_step():
         h = C.c_int64(0)
         rc = lib.propack_zcsr_create(m, n, pg._i64p(hp), pg._ip(hi), C.c_void_p(hv.ctypes.data), C.byref(h))
         assert rc == 0, pg.last_error()
         iparm = np.array([h.value & 0xFFFFFFFF, (h.value >> 32) & 0xFFFFFFFF], dtype=np.uint32).view(np.int32)
         solve(C.cast(lib.propack_gpu_csr_zaprod_, pg.ZAPROD), iparm, u_pin, v_pin)
         lib.propack_csr_destroy(h.value)
+
+    e2e_step()  # untimed warm-up step (first-call costs)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     h2d = hp.nbytes + hi.nbytes + hv.nbytes + m * 16
     d2h = 2 * k * 8 + k * (m + n) * 16

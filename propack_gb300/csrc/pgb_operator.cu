@@ -204,7 +204,7 @@ int scan_excl(const int *in, int *out, int n, cudaStream_t s)
 {
     const int nblk = std::max(1, (n + 4095) / 4096);
     int *bsum = nullptr;
-    PGB_CUDA(cudaMallocAsync(&bsum, sizeof(int) * (nblk + 1), s));
+    bsum = static_cast<decltype(bsum)>(pool_alloc(sizeof(int) * (nblk + 1), s));
     k_scan_blocks<<<nblk, 1024, 0, s>>>(in, n, bsum);
     PGB_LAUNCHED();
     k_scan_sums<<<1, 1024, 0, s>>>(bsum, nblk, out + n);
@@ -213,7 +213,7 @@ int scan_excl(const int *in, int *out, int n, cudaStream_t s)
     PGB_LAUNCHED();
     int total = 0;
     PGB_CUDA(cudaMemcpyAsync(&total, out + n, sizeof(int), cudaMemcpyDeviceToHost, s));
-    PGB_CUDA(cudaFreeAsync(bsum, s));
+    pool_free(bsum, s);
     PGB_CUDA(cudaStreamSynchronize(s));
     return total;
 }
@@ -292,13 +292,13 @@ static void build_chunks(Csr &A, cudaStream_t s)
     if (A.rows == 0 || A.cidx) return;
     const int ntiles = (A.rows + 31) / 32;
     int *cnt = nullptr;
-    PGB_CUDA(cudaMallocAsync(&cnt, sizeof(int) * (ntiles + 1), s));
+    cnt = static_cast<decltype(cnt)>(pool_alloc(sizeof(int) * (ntiles + 1), s));
     A.tbase = (int *)pool_alloc(sizeof(int) * (ntiles + 1), s);
     const int g = std::min(4096, std::max(1, (ntiles + 255) / 256));
     k_chunk_count<<<g, 256, 0, s>>>(A.ptr, A.rows, cnt);
     PGB_LAUNCHED();
     const size_t units = (size_t)scan_excl(cnt, A.tbase, ntiles, s);
-    PGB_CUDA(cudaFreeAsync(cnt, s));
+    pool_free(cnt, s);
     const size_t len = units * 32;
     const int gr = std::min(4096, std::max(1, (ntiles + 7) / 8));  // a warp per 32-row tile
     A.cidx = (int *)pool_alloc(sizeof(int) * len, s);
@@ -332,8 +332,8 @@ static void build_blocks(Csr &A, cudaStream_t s)
     int *flag = nullptr, *pos = nullptr;
     const int rows = A.rows;
     A.short_rows = 0;  // the schedule is chosen after the FP32 values exist (choose_schedule)
-    PGB_CUDA(cudaMallocAsync(&flag, sizeof(int) * (rows + 1), s));
-    PGB_CUDA(cudaMallocAsync(&pos, sizeof(int) * (rows + 1), s));
+    flag = static_cast<decltype(flag)>(pool_alloc(sizeof(int) * (rows + 1), s));
+    pos = static_cast<decltype(pos)>(pool_alloc(sizeof(int) * (rows + 1), s));
     const int g = std::min(4096, std::max(1, (rows + 255) / 256));
     if (rows > 0) {
         k_blk_flags<<<g, 256, 0, s>>>(A.ptr, rows, NNZ_W / 2, flag);
@@ -343,8 +343,8 @@ static void build_blocks(Csr &A, cudaStream_t s)
     A.blk = (int *)pool_alloc(sizeof(int) * (A.nblk + 1), s);
     k_blk_emit<<<g, 256, 0, s>>>(flag, pos, rows, A.blk);
     PGB_LAUNCHED();
-    PGB_CUDA(cudaFreeAsync(flag, s));
-    PGB_CUDA(cudaFreeAsync(pos, s));
+    pool_free(flag, s);
+    pool_free(pos, s);
 }
 
 // -------------------------------------------------------- transpose
@@ -502,6 +502,19 @@ __global__ void k_finish_t(const unsigned long long *key, const int *optr, const
     }
 }
 
+// without appended X entries every key slot p holds an entry of A: one
+// thread per slot (coalesced index and value writes)
+template <typename V>
+__global__ void k_finish_t_flat(const unsigned long long *key, int64_t total, const V *val, int *oidx, V *oval)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long k = key[p];
+        oidx[p] = (int)(k & 0xffffffffull);
+        oval[p] = adj_value(val[(int)(k >> 32)]);
+    }
+}
+
 // A: rows x cols device CSR (ptr/idx/val); X optional (cols rows).  V =
 // double2: a complex A, T = A^H (X must be absent), values into T.zval.
 template <typename V>
@@ -512,11 +525,11 @@ static void transpose_into(Csr &T, const int *ptr, const int *idx, const V *val,
     constexpr bool Z = std::is_same<V, double2>::value;
     int *cnt = nullptr, *tot = nullptr, *fill = nullptr, *longlist = nullptr, *nlong = nullptr;
     unsigned long long *key = nullptr;
-    PGB_CUDA(cudaMallocAsync(&cnt, sizeof(int) * (cols + 1), s));
-    PGB_CUDA(cudaMallocAsync(&tot, sizeof(int) * (cols + 1), s));
-    PGB_CUDA(cudaMallocAsync(&fill, sizeof(int) * (cols + 1), s));
-    PGB_CUDA(cudaMallocAsync(&longlist, sizeof(int) * (cols + 1), s));
-    PGB_CUDA(cudaMallocAsync(&nlong, sizeof(int), s));
+    cnt = static_cast<decltype(cnt)>(pool_alloc(sizeof(int) * (cols + 1), s));
+    tot = static_cast<decltype(tot)>(pool_alloc(sizeof(int) * (cols + 1), s));
+    fill = static_cast<decltype(fill)>(pool_alloc(sizeof(int) * (cols + 1), s));
+    longlist = static_cast<decltype(longlist)>(pool_alloc(sizeof(int) * (cols + 1), s));
+    nlong = static_cast<decltype(nlong)>(pool_alloc(sizeof(int), s));
     PGB_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (cols + 1), s));
     PGB_CUDA(cudaMemsetAsync(fill, 0, sizeof(int) * (cols + 1), s));
     PGB_CUDA(cudaMemsetAsync(nlong, 0, sizeof(int), s));
@@ -536,7 +549,7 @@ static void transpose_into(Csr &T, const int *ptr, const int *idx, const V *val,
     // the sort keys live at the output positions of row c of A', whose
     // offsets T.ptr include the appended X entries: size them by `total`,
     // not by nnz(A)
-    PGB_CUDA(cudaMallocAsync(&key, sizeof(unsigned long long) * std::max(total, 1), s));
+    key = static_cast<decltype(key)>(pool_alloc(sizeof(unsigned long long) * std::max(total, 1), s));
     // the scan wrote T.ptr; optr == T.ptr, the A' part of row c is [ptr[c], ptr[c]+cnt[c])
     if (rows > 0 && nnz > 0) {
         const int gt = std::min(4096, std::max(1, ((rows + 31) / 32 + 7) / 8));  // a warp per 32-row tile
@@ -579,16 +592,21 @@ static void transpose_into(Csr &T, const int *ptr, const int *idx, const V *val,
         PGB_CUDA(cudaFree(doff));
         PGB_CUDA(cudaFree(scr));
     }
-    if (cols > 0) {
+    if (cols > 0 && !xptr) {
+        if (total > 0) {
+            k_finish_t_flat<V><<<g, 256, 0, s>>>(key, total, val, T.idx, tval);
+            PGB_LAUNCHED();
+        }
+    } else if (cols > 0) {
         k_finish_t<V><<<g, 256, 0, s>>>(key, T.ptr, cnt, cols, val, xptr, xidx, xval, rows, T.idx, tval);
         PGB_LAUNCHED();
     }
-    PGB_CUDA(cudaFreeAsync(cnt, s));
-    PGB_CUDA(cudaFreeAsync(tot, s));
-    PGB_CUDA(cudaFreeAsync(fill, s));
-    PGB_CUDA(cudaFreeAsync(longlist, s));
-    PGB_CUDA(cudaFreeAsync(nlong, s));
-    PGB_CUDA(cudaFreeAsync(key, s));
+    pool_free(cnt, s);
+    pool_free(tot, s);
+    pool_free(fill, s);
+    pool_free(longlist, s);
+    pool_free(nlong, s);
+    pool_free(key, s);
     (void)xoff;
 }
 
@@ -745,15 +763,15 @@ static void choose_schedule(Csr &A, const double *z, cudaStream_t s)
     if (A.nnz >= (int64_t)CHUNK_MEAN_MAX * A.rows) return;
     build_chunks(A, s);
     double *x = nullptr, *y = nullptr;
-    PGB_CUDA(cudaMallocAsync(&x, sizeof(double) * std::max(A.ncol0, 1), s));
-    PGB_CUDA(cudaMallocAsync(&y, sizeof(double) * A.rows, s));
+    x = static_cast<decltype(x)>(pool_alloc(sizeof(double) * std::max(A.ncol0, 1), s));
+    y = static_cast<decltype(y)>(pool_alloc(sizeof(double) * A.rows, s));
     PGB_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * std::max(A.ncol0, 1), s));
     A.short_rows = 1;
     const float tc = time_spmv(A, x, z, y, s);
     A.short_rows = 0;
     const float ts = time_spmv(A, x, z, y, s);
-    PGB_CUDA(cudaFreeAsync(x, s));
-    PGB_CUDA(cudaFreeAsync(y, s));
+    pool_free(x, s);
+    pool_free(y, s);
     const bool chunked = rule ? !(ts < 0.95f * tc) : (tc < 0.95f * ts);
     A.short_rows = chunked ? 1 : 0;
     A.tuned_ms[0] = tc;
@@ -936,7 +954,7 @@ static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, c
         Csr &A = op->fwd;
         A.rows = m; A.cols = n + r; A.ncol0 = n;
         int *tot = nullptr;
-        PGB_CUDA(cudaMallocAsync(&tot, sizeof(int) * (m + 1), s));
+        tot = static_cast<decltype(tot)>(pool_alloc(sizeof(int) * (m + 1), s));
         k_count_merge<<<g, 256, 0, s>>>(dsp, dlp, m, tot);
         PGB_LAUNCHED();
         A.ptr = (int *)pool_alloc(sizeof(int) * (m + 1), s);
@@ -945,7 +963,7 @@ static int create_operator(int m, int n, const int64_t *sp, const int32_t *si, c
         A.val = (double *)pool_alloc(sizeof(double) * std::max<int64_t>(A.nnz, 1), s);
         k_merge_rows<<<g, 256, 0, s>>>(dsp, dsi, dsv, dlp, dli, dlv, m, n, A.ptr, A.idx, A.val);
         PGB_LAUNCHED();
-        PGB_CUDA(cudaFreeAsync(tot, s));
+        pool_free(tot, s);
         build_blocks(A, s);
     }
     // adj = [S' | R]
@@ -1347,13 +1365,13 @@ extern "C" void propack_gpu_csr_zaprod_(const char *transa, const int *m, const 
             cudaStream_t s;
             PGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
             double2 *dx = nullptr, *dy = nullptr;
-            PGB_CUDA(cudaMallocAsync(&dx, sizeof(double2) * nin, s));
-            PGB_CUDA(cudaMallocAsync(&dy, sizeof(double2) * nout, s));
+            dx = static_cast<decltype(dx)>(pool_alloc(sizeof(double2) * nin, s));
+            dy = static_cast<decltype(dy)>(pool_alloc(sizeof(double2) * nout, s));
             PGB_CUDA(cudaMemcpyAsync(dx, x, sizeof(double2) * nin, cudaMemcpyHostToDevice, s));
             op_zapply(*op, t, dx, dy, s);
             PGB_CUDA(cudaMemcpyAsync(y, dy, sizeof(double2) * nout, cudaMemcpyDeviceToHost, s));
-            PGB_CUDA(cudaFreeAsync(dx, s));
-            PGB_CUDA(cudaFreeAsync(dy, s));
+            pool_free(dx, s);
+            pool_free(dy, s);
             PGB_CUDA(cudaStreamSynchronize(s));
             PGB_CUDA(cudaStreamDestroy(s));
         } catch (...) {
@@ -1380,13 +1398,13 @@ extern "C" void propack_gpu_csr_aprod_(const char *transa, const int *m, const i
         cudaStream_t s;
         PGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
         double *dx = nullptr, *dy = nullptr;
-        PGB_CUDA(cudaMallocAsync(&dx, sizeof(double) * nin, s));
-        PGB_CUDA(cudaMallocAsync(&dy, sizeof(double) * nout, s));
+        dx = static_cast<decltype(dx)>(pool_alloc(sizeof(double) * nin, s));
+        dy = static_cast<decltype(dy)>(pool_alloc(sizeof(double) * nout, s));
         PGB_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * nin, cudaMemcpyHostToDevice, s));
         op_apply<double>(*op, t, dx, dy, s);
         PGB_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
-        PGB_CUDA(cudaFreeAsync(dx, s));
-        PGB_CUDA(cudaFreeAsync(dy, s));
+        pool_free(dx, s);
+        pool_free(dy, s);
         PGB_CUDA(cudaStreamSynchronize(s));
         PGB_CUDA(cudaStreamDestroy(s));
     } catch (...) {
