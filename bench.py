@@ -129,6 +129,8 @@ def parse():
                     help="shrink m and n by this factor (profiling captures only; not a bench line)")
     ap.add_argument("--cgs-arith", default="planes", choices=["planes", "fp64", "f3"],
                     help="Gram-Schmidt arithmetic of the FP64 form (propack_set_cgs_arith)")
+    ap.add_argument("--spmv-schedule", default=None, choices=["rule", "chunked", "staged", "tuned"],
+                    help="SpMV schedule of the operators built (propack_set_spmv_schedule; default: the library's)")
     ap.add_argument("--gemm-impl", type=int, default=None, choices=[1, 2],
                     help="tcgen05 kernel of the restart/Ritz products (propack_set_gemm_impl; default: the library's)")
     ap.add_argument("--batch-arith", default="fp64", choices=["fp64", "planes"],
@@ -441,6 +443,8 @@ def run_ours(args, wl):
     pg.set_cgs_arith(args.cgs_arith)
     if getattr(args, "gemm_impl", None) is not None:
         pg.load().propack_set_gemm_impl(args.gemm_impl)
+    if getattr(args, "spmv_schedule", None) is not None:
+        pg.set_spmv_schedule(args.spmv_schedule)
     barrier = lambda: None
     dist = None
     if world > 1:

@@ -91,10 +91,10 @@ int propack_csr_create(int m, int n, const int64_t *s_rowptr,
 int propack_csr_destroy(int64_t handle);
 /* SpMV schedule of the operators built after the call (per host process),
  * per direction: 0 (default) a rule on the mean row length -- chunked
- * below 32 nonzeros per row, staged above -- so that a matrix always gets
+ * below 128 nonzeros per row, staged above -- so that a matrix always gets
  * the same schedule and the same summation order; 1 always chunked;
  * 2 always staged; 3 a timed choice -- propack_csr_create builds the
- * run-interleaved copy of any matrix with fewer than 64 nonzeros per row
+ * run-interleaved copy of any matrix with fewer than 512 nonzeros per row
  * on average, times both schedules on the device and keeps the faster
  * (the rule's choice unless the other is more than 5 % faster; a near-tie
  * can go either way between builds).  Results depend only on the matrix

@@ -112,7 +112,7 @@ def get_profile():
 
 def set_spmv_schedule(mode):
     """SpMV schedule of operators built afterwards: "rule" (default: chunked
-    below 32 nonzeros per row), "chunked", "staged" or "tuned" (timed on
+    below 128 nonzeros per row), "chunked", "staged" or "tuned" (timed on
     the device; propack_set_spmv_schedule)."""
     m = {"rule": 0, "chunked": 1, "staged": 2, "tuned": 3}[mode]
     if load().propack_set_spmv_schedule(m) != 0:

@@ -718,8 +718,8 @@ void op_spmv_plain_launch(const Csr &A, const double *x, const double *z, double
 // propack_set_spmv_schedule: 0 the row-length rule (default), 1 chunked,
 // 2 staged, 3 timed choice
 static std::atomic<int> g_sched{0};
-constexpr int CHUNK_RULE_MEAN = 32;  // the rule: chunked below this mean row length
-constexpr int CHUNK_MEAN_MAX = 64;   // the timed choice tries the chunked schedule below this mean row length
+constexpr int CHUNK_RULE_MEAN = 128;  // the rule: chunked below this mean row length
+constexpr int CHUNK_MEAN_MAX = 512;   // the timed choice tries the chunked schedule below this mean row length
 
 // mean device ms of one plain product with the matrix's current schedule
 static float time_spmv(const Csr &A, const double *x, const double *z, double *y, cudaStream_t s)
@@ -741,7 +741,7 @@ static float time_spmv(const Csr &A, const double *x, const double *z, double *y
 
 // Sets A.short_rows (1: chunked, 0: staged).  The default is a rule on the
 // mean row length (chunked below CHUNK_RULE_MEAN, where it measured faster
-// on every workload tried: 7.7 and 20.6 nonzeros per row), so that a given
+// on every workload tried: 7.7, 20.6 and ~83 nonzeros per row), so that a given
 // matrix always gets the same schedule and the same summation order.  The
 // timed choice (mode 3) builds the chunked copy, runs both schedules on the
 // device and keeps the chunked one when it wins; it starts from the rule
