@@ -182,6 +182,20 @@ def run_other_configs(args):
     return out
 
 
+def bind_local_gpu(local):
+    """One GPU per rank, before CUDA is initialised: the rank's entry of an
+    existing CUDA_VISIBLE_DEVICES list (a launcher may export all of the
+    job's devices to every rank), else the device with the local rank's
+    index.  A list of one device is the launcher's own binding and stays."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis is None or vis.strip() == "":
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        return
+    devs = [d.strip() for d in vis.split(",") if d.strip()]
+    if len(devs) > 1 and local < len(devs):
+        os.environ["CUDA_VISIBLE_DEVICES"] = devs[local]
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -436,7 +450,7 @@ def run_reference(args, wl):
 def run_ours(args, wl):
     rank, world, local = dist_env()
     if world > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        bind_local_gpu(local)
     import numpy as np
     import propack_gb300 as pg
     pg.load()
@@ -737,7 +751,7 @@ def run_batched(args, wl):
     if world > 1:
         # independent problems: each rank solves its share, no collective on
         # the data path (gloo only for the closing max / sums)
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        bind_local_gpu(local)
         import torch.distributed as dist
         dist.init_process_group("gloo")
         mine = shard_problems([A.nnz for A in mats], rank, world)

@@ -3,6 +3,7 @@ keys, the two CPU baselines) on a small stand-in workload, and the
 algorithmic-bytes formula of the SpMV roofline."""
 import argparse
 import json
+import os
 
 import pytest
 
@@ -43,3 +44,17 @@ def test_shards_cover_every_problem_once(world):
     costs = [5, 1, 3, 9, 9, 2, 7]
     got = sorted(i for r in range(world) for i in bench.shard_problems(costs, r, world))
     assert got == list(range(len(costs)))
+
+
+@pytest.mark.parametrize("vis,local,want", [(None, 2, "2"), ("0,1,2,3", 2, "2"), ("4,5,6,7", 1, "5"),
+                                            ("3", 1, "3"), ("", 0, "0")])
+def test_each_rank_binds_its_own_gpu(monkeypatch, vis, local, want):
+    """Under torchrun every rank takes its own device: its entry of a
+    CUDA_VISIBLE_DEVICES list exported to all ranks, its local index when
+    none is set, and a launcher's one-device binding as it is."""
+    if vis is None:
+        monkeypatch.delenv("CUDA_VISIBLE_DEVICES", raising=False)
+    else:
+        monkeypatch.setenv("CUDA_VISIBLE_DEVICES", vis)
+    bench.bind_local_gpu(local)
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == want
