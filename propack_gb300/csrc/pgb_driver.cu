@@ -226,6 +226,13 @@ __global__ void k_sum_cols(const T *U, size_t ldu, int m, int ncols, double *out
 }
 
 // ------------------------------------------------------------- context
+// The Ritz products for page-locked host arrays run in row chunks of about
+// RITZ_CHUNK_ROWS (each far above the tensor-core GEMM's 4096-row minimum,
+// so every chunk takes the same kernel and gives the same bits), so that
+// the copy of a finished chunk to the host overlaps the next products.
+constexpr int RITZ_CHUNK_ROWS = 1 << 19;
+constexpr int RITZ_MAX_CHUNKS = 8;
+
 struct Ctx {
     int m = 0, n = 0, kmax = 0, ldu = 0, ldv = 0, es = 8;
     int vw = 1;                             // real scalars per vector element (2: complex*16)
@@ -268,11 +275,15 @@ struct Ctx {
     cudaEvent_t wev[2] = {nullptr, nullptr};
     std::vector<void *> allocs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
-    // the left Ritz vectors are final (recorded by dev_ritzvec): their copy
-    // to the host may run on s2 while the right ones are formed on s
+    // the caller's page-locked U and V (set_host_out): dev_ritzvec forms
+    // the Ritz vectors in row chunks and copies each finished chunk there on
+    // s2 while the next chunks are formed on s; done[side] = columns copied
+    char *hout[2] = {nullptr, nullptr};
+    size_t hpitch[2] = {0, 0};
+    int done[2] = {0, 0};
     cudaStream_t s2 = nullptr;
-    cudaEvent_t ev_u = nullptr, ev_s2 = nullptr;
-    bool u_final = false;
+    cudaEvent_t ev_chunk[2][RITZ_MAX_CHUNKS] = {};
+    cudaEvent_t ev_s2 = nullptr;
 
     // zero-filled device memory from the library's pool
     void *dbytes(size_t bytes)
@@ -294,6 +305,7 @@ struct Ctx {
     T *dalloc(size_t count) { return (T *)dbytes(sizeof(T) * count); }
     ~Ctx()
     {
+        if (s2) cudaStreamSynchronize(s2);  // copies of Ritz chunks read pool memory
         if (s) {
             for (void *p : allocs) pool_free(p, s);
             cudaStreamSynchronize(s);
@@ -309,7 +321,9 @@ struct Ctx {
         if (ev1) cudaEventDestroy(ev1);
         if (evs0) cudaEventDestroy(evs0);
         if (evs1) cudaEventDestroy(evs1);
-        if (ev_u) cudaEventDestroy(ev_u);
+        for (auto &side : ev_chunk)
+            for (cudaEvent_t e : side)
+                if (e) cudaEventDestroy(e);
         if (ev_s2) cudaEventDestroy(ev_s2);
         if (s2) cudaStreamDestroy(s2);
         if (s) cudaStreamDestroy(s);
@@ -1131,43 +1145,78 @@ static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, 
         }
         return;
     } else {
-    // FP64 or complex*16 (sizeof(T) = 16) bases into the caller's arrays.
-    // When the left vectors were final before the right ones were formed,
-    // their copy runs on a second stream, behind that point only, so that
-    // it overlaps the right vectors' product.
-    if (du) {
-        cudaStream_t su = c.s;
-        if (c.u_final && dv) {
-            if (!c.s2) PGB_CUDA(cudaStreamCreateWithFlags(&c.s2, cudaStreamNonBlocking));
-            if (!c.ev_s2) PGB_CUDA(cudaEventCreateWithFlags(&c.ev_s2, cudaEventDisableTiming));
-            PGB_CUDA(cudaStreamWaitEvent(c.s2, c.ev_u, 0));
-            su = c.s2;
-        }
-        d2h_columns((char *)U, sizeof(T) * ldu, (const char *)c.U, sizeof(T) * c.ldu, sizeof(T) * c.m, ncols, su);
-        if (su != c.s) {
-            PGB_CUDA(cudaEventRecord(c.ev_s2, su));
-            PGB_CUDA(cudaStreamWaitEvent(c.s, c.ev_s2, 0));
-        }
-    }
-    if (dv)
+    // FP64 or complex*16 (sizeof(T) = 16) bases into the caller's arrays;
+    // the sides dev_ritzvec already copied chunk by chunk (on s2) are done
+    // once s2 is
+    if (du && c.done[0] < ncols)
+        d2h_columns((char *)U, sizeof(T) * ldu, (const char *)c.U, sizeof(T) * c.ldu, sizeof(T) * c.m, ncols, c.s);
+    if (dv && c.done[1] < ncols)
         d2h_columns((char *)V, sizeof(T) * ldv, (const char *)c.V, sizeof(T) * c.ldv, sizeof(T) * c.n, ncols, c.s);
+    if (c.s2) {
+        PGB_CUDA(cudaEventRecord(c.ev_s2, c.s2));
+        PGB_CUDA(cudaStreamWaitEvent(c.s, c.ev_s2, 0));
+    }
     }
 }
 
-// A(:,0:nc) <- A(:,0:kk) op(B)   (dgemm_ovwr_left)
-// (complex A times the real B: the real GEMM on the (re, im) rows,
-// zdgemm_ovwr_left of complex16/zgemm_ovwr.F)
+// the caller's U and V, when page-locked, receive the Ritz vectors from
+// dev_ritzvec chunk by chunk (the FP64 and complex*16 drivers)
 template <typename T>
-static void ovwr_left(Ctx &c, T *A, int lda, int rows, int nc, int kk, const double *B, int ldb, bool tb)
+static void set_host_out(Ctx &c, double *U, int ldu, double *V, int ldv, bool du, bool dv)
 {
+    if (du && host_pinned(U)) { c.hout[0] = (char *)U; c.hpitch[0] = sizeof(T) * (size_t)ldu; }
+    if (dv && host_pinned(V)) { c.hout[1] = (char *)V; c.hpitch[1] = sizeof(T) * (size_t)ldv; }
+}
+
+// A(:,0:nc) <- A(:,0:kk) op(B)   (dgemm_ovwr_left) on rows r0:r1
+// (complex A times the real B: the real GEMM on the (re, im) rows,
+// zdgemm_ovwr_left of complex16/zgemm_ovwr.F).  Row i of the product
+// reads only row i of A, so a row range can be overwritten once its own
+// product is formed.
+template <typename T>
+static void ovwr_left(Ctx &c, T *A, int lda, int rows, int nc, int kk, const double *B, int ldb, bool tb, int r0 = 0,
+                      int r1 = -1)
+{
+    if (r1 < 0) r1 = rows;
+    const int nr = r1 - r0;
     if constexpr (VecW<T>::w == 2) {
-        gemm<double>(2 * rows, nc, kk, (const double *)A, 2 * lda, false, B, ldb, tb, (double *)c.gout, 2 * lda,
-                     c.s);
-        copy_cols<double>((const double *)c.gout, 2 * lda, (double *)A, 2 * lda, 2 * rows, nc, c.s);
+        const double *Ar = (const double *)A + 2 * (size_t)r0;
+        double *Gr = (double *)c.gout + 2 * (size_t)r0;
+        gemm<double>(2 * nr, nc, kk, Ar, 2 * lda, false, B, ldb, tb, Gr, 2 * lda, c.s);
+        copy_cols<double>(Gr, 2 * lda, (double *)A + 2 * (size_t)r0, 2 * lda, 2 * nr, nc, c.s);
     } else {
-        gemm<T>(rows, nc, kk, A, lda, false, B, ldb, tb, (T *)c.gout, lda, c.s);
-        copy_cols<T>((T *)c.gout, lda, A, lda, rows, nc, c.s);
+        gemm<T>(nr, nc, kk, A + r0, lda, false, B, ldb, tb, (T *)c.gout + r0, lda, c.s);
+        copy_cols<T>((T *)c.gout + r0, lda, A + r0, lda, nr, nc, c.s);
     }
+}
+
+// the Ritz product of one side; with a page-locked host array (FP64 and
+// complex*16 bases) in row chunks, each copied to the host on s2 as soon as
+// it is formed
+template <typename T>
+static void ritz_side(Ctx &c, int side, T *A, int lda, int rows, int nc, int kk, const double *B, int ldb)
+{
+    if (sizeof(T) < 8 || !c.hout[side] || rows < 2 * RITZ_CHUNK_ROWS) {
+        ovwr_left<T>(c, A, lda, rows, nc, kk, B, ldb, true);
+        return;
+    }
+    const int nch = std::min(RITZ_MAX_CHUNKS, (rows + RITZ_CHUNK_ROWS - 1) / RITZ_CHUNK_ROWS);
+    const int per = ((rows + nch - 1) / nch + 127) / 128 * 128;
+    if (!c.s2) PGB_CUDA(cudaStreamCreateWithFlags(&c.s2, cudaStreamNonBlocking));
+    if (!c.ev_s2) PGB_CUDA(cudaEventCreateWithFlags(&c.ev_s2, cudaEventDisableTiming));
+    for (int i = 0; i < nch; i++) {
+        const int r0 = i * per, r1 = std::min(rows, r0 + per);
+        if (r0 >= r1) break;
+        ovwr_left<T>(c, A, lda, rows, nc, kk, B, ldb, true, r0, r1);
+        cudaEvent_t &e = c.ev_chunk[side][i];
+        if (!e) PGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        PGB_CUDA(cudaEventRecord(e, c.s));
+        PGB_CUDA(cudaStreamWaitEvent(c.s2, e, 0));
+        PGB_CUDA(cudaMemcpy2DAsync(c.hout[side] + sizeof(T) * (size_t)r0, c.hpitch[side], A + r0,
+                                   sizeof(T) * (size_t)lda, sizeof(T) * (size_t)(r1 - r0), nc,
+                                   cudaMemcpyDeviceToHost, c.s2));
+    }
+    c.done[side] = nc;
 }
 
 // the bidiagonal analysis; returns the number of converged values
@@ -1213,13 +1262,8 @@ static void dev_ritzvec(Ctx &c, bool small_side, bool du, bool dv, int k, int di
     // X = P' Mt(1:dim, 1:dim+1)   (dim x dim+1, ld dim+1)
     gemm<double>(dim, dp1, dim, c.Pr, dim, true, c.Mt, dp1, false, c.X, dp1, c.s);
     const int mstart = small_side ? dim - k + 1 : 1;
-    if (du) {
-        ovwr_left<T>(c, (T *)c.U, c.ldu, c.m, k, dp1, c.X + (mstart - 1), dp1, true);
-        if (!c.ev_u) PGB_CUDA(cudaEventCreateWithFlags(&c.ev_u, cudaEventDisableTiming));
-        PGB_CUDA(cudaEventRecord(c.ev_u, c.s));
-        c.u_final = true;
-    }
-    if (dv) ovwr_left<T>(c, (T *)c.V, c.ldv, c.n, k, dim, c.Qt + (mstart - 1), dim, true);
+    if (du) ritz_side<T>(c, 0, (T *)c.U, c.ldu, c.m, k, dp1, c.X + (mstart - 1), dp1);
+    if (dv) ritz_side<T>(c, 1, (T *)c.V, c.ldv, c.n, k, dim, c.Qt + (mstart - 1), dim);
 }
 
 struct Timer {
@@ -1444,6 +1488,7 @@ static void irl_plain(const IrlIn &in, propack_aprod_t aprod, double *dparm, pro
     init_ctx<T>(c, in.m, in.n, in.dim);
     if constexpr (VecW<T>::w == 2) setup_zoperator(c, zaprod, zparm, iparm);
     else setup_operator(c, aprod, dparm, iparm);
+    set_host_out<T>(c, U, ldu, V, ldv, in.du, in.dv);
     PGB_CUDA(cudaEventRecord(c.ev0, c.s));
     PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(T) * in.m, cudaMemcpyHostToDevice, c.s));
     PGB_CUDA(cudaEventRecord(c.evs0, c.s));
@@ -1553,6 +1598,7 @@ static void run_irl(const char *which, const char *jobu, const char *jobv, int m
         Ctx c64;
         init_ctx<double>(c64, m, n, in64.dim);
         setup_operator(c64, aprod, dparm, iparm);
+        set_host_out<double>(c64, U, ldu, V, ldv, in.du, in.dv);
         const int nwarm = std::min(std::max(out32.nconv, out32.ritz), in.neig);
         if (nwarm > 0) {
             k_sum_cols<float><<<c64.nb, 256, 0, c64.s>>>(c32.Ucol<float>(0), c32.ldu, m, nwarm, c64.Ucol<double>(0));
@@ -1613,6 +1659,7 @@ static void run_lansvd_t(const char *jobu, const char *jobv, int m, int n, int *
     init_ctx<T>(c, m, n, lanmax);
     if constexpr (cplx) setup_zoperator(c, zaprod, zparm, iparm);
     else setup_operator(c, aprod, dparm, iparm);
+    if constexpr (sizeof(T) >= 8) set_host_out<T>(c, U, ldu, V, ldv, yes(jobu), yes(jobv));
     PGB_CUDA(cudaEventRecord(c.ev0, c.s));
     if constexpr (cplx) {
         PGB_CUDA(cudaMemcpyAsync(c.U, U, sizeof(T) * m, cudaMemcpyHostToDevice, c.s));

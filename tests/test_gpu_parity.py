@@ -372,3 +372,54 @@ def test_mixed_host_callback(golden):
     M = csr_from(golden, "small").toarray()
     u, s, vt, bnd = pg.svdp(aslinearoperator(M), 3, tol=1e-8, rng=rng0(), precision="mixed")
     np.testing.assert_allclose(s, golden["small_irl_lm_sigma"], rtol=1e-8, atol=1e-8)
+
+
+# ------------------------------------------------- Ritz vectors to the host
+@pytest.mark.parametrize("driver", ["irl", "irl_complex", "plain"])
+def test_ritz_vectors_into_page_locked_arrays(driver):
+    """Above 2^20 rows the drivers form the Ritz vectors in row chunks and
+    copy each chunk into a page-locked U, V while the next chunk is formed;
+    the caller gets the same bits as through ordinary arrays (one product
+    and one copy), and the values of the oracle."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    m, n, k = 1_200_000, 2_000, 4
+    cols = (rng.integers(0, n - 3, m)[:, None] + np.arange(3)).ravel()
+    vals = rng.standard_normal(3 * m) * (1.0 + cols) ** -0.5
+    cplx = driver == "irl_complex"
+    if cplx:
+        vals = vals * (1 + 0.5j)
+    S = sp.csr_array((vals, cols, np.arange(0, 3 * m + 1, 3)), shape=(m, n))
+    op = pg.CsrOperator(S)
+    dt, tdt = (np.complex128, torch.complex128) if cplx else (np.float64, torch.float64)
+    dim = 16 if driver != "plain" else 40
+    u0 = np.random.default_rng(0).uniform(size=m)
+    eps = np.finfo(np.float64).eps
+    ioption = np.array([0, 1], dtype=np.int32)
+    outs = []
+    for pinned in (False, True):
+        if pinned:
+            U = torch.zeros((dim + 1, m), dtype=tdt).pin_memory().numpy().T
+            V = torch.zeros((dim, n), dtype=tdt).pin_memory().numpy().T
+        else:
+            U = np.zeros((m, dim + 1), dtype=dt, order="F")
+            V = np.zeros((n, dim), dtype=dt, order="F")
+        U[:, 0] = u0
+        sig, bnd = np.zeros(k), np.zeros(k)
+        if driver == "plain":
+            doption = np.array([np.sqrt(eps), eps ** 0.75, 0.0])
+            nc, info = pg.lansvd(b"Y", b"Y", m, n, k, dim, op.aprod, U, sig, bnd, V, 1e-8, doption, ioption,
+                                 iparm=op.iparm)
+        else:
+            doption = np.array([np.sqrt(eps), eps ** 0.75, 0.0, 0.002])
+            call = pg.zlansvd_irl if cplx else pg.lansvd_irl
+            nc, info = call(b"L", b"Y", b"Y", m, n, dim, dim - k, k, 30, op.aprod, U, sig, bnd, V, 1e-8, doption,
+                            ioption, iparm=op.iparm)
+        assert info == 0 and nc == k
+        outs.append((sig.copy(), np.array(U[:, :k]), np.array(V[:, :k])))
+        del U, V
+    op.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+    ref = oracle.svdp(S, k, irl_mode=driver != "plain", kmax=dim, tol=1e-8, v0=u0, maxiter=30)[1]
+    np.testing.assert_allclose(outs[1][0], ref, rtol=SIG_RTOL)
