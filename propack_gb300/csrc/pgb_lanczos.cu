@@ -72,6 +72,31 @@ __device__ double sum_parts(const double *p, int nb, double *red)
     for (int b = threadIdx.x; b < nb; b += BS) s += p[b];
     return block_sum<BS>(s, red);
 }
+// the same for two (three) arrays, their loads issued together: one round
+// trip instead of two (three), the same sums
+__device__ void sum_parts2(const double *p, const double *q, int nb, double *red, double &sp, double &sq)
+{
+    double s = 0.0, u = 0.0;
+    for (int b = threadIdx.x; b < nb; b += BS) {
+        s += p[b];
+        u += q[b];
+    }
+    sp = block_sum<BS>(s, red);
+    sq = block_sum<BS>(u, red);
+}
+__device__ void sum_parts3(const double *p, const double *q, const double *r, int nb, double *red, double &sp,
+                           double &sq, double &sr)
+{
+    double s = 0.0, u = 0.0, v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += BS) {
+        s += p[b];
+        u += q[b];
+        v += r[b];
+    }
+    sp = block_sum<BS>(s, red);
+    sq = block_sum<BS>(u, red);
+    sr = block_sum<BS>(v, red);
+}
 
 // dset_mu (dlanbpro.F:555-577), thread 0
 __device__ void set_mu(int k, double *mu, const int *index, double val)
@@ -534,15 +559,20 @@ __global__ void __launch_bounds__(BS, SHORT ? SPMV_SHORT_MINB : 3) k_lb_spmv(LbA
     __shared__ ChunkStage<T> cst[SHORT ? SPMV_WARPS : 1];
     __shared__ double sred[32];
     __shared__ Tail t;
-    if (a.ctl->status != 0) return;
+    const Csr &A = SIDE == 0 ? a.adj : a.fwd;
+    // the control words are loaded first and the chunked schedule's tile
+    // search runs while they arrive (neither depends on the other)
+    const int status = a.ctl->status;
     const Pend pin = SIDE == 0 ? a.ctl->pend_u : a.ctl->pend_v;
     const Pend pprev = SIDE == 0 ? a.ctl->pend_v : a.ctl->pend_u;
-    const bool has_prev = SIDE == 1 || j > 1;
     const T coef = (T)(SIDE == 0 ? a.ctl->beta : a.ctl->alpha);
+    int tb0 = -1, tb1 = -1;
+    if (SHORT && !host_product) chunk_warp_tiles(A.tbase, A.rows, tb0, tb1);
+    if (status != 0) return;
+    const bool has_prev = SIDE == 1 || j > 1;
     const T *x = SIDE == 0 ? ucol<T>(a, j - 1) : vcol<T>(a, j - 1);
     T *out = SIDE == 0 ? vcol<T>(a, j - 1) : ucol<T>(a, j);
     T *prev = SIDE == 0 ? (j > 1 ? vcol<T>(a, j - 2) : nullptr) : ucol<T>(a, j - 1);
-    const Csr &A = SIDE == 0 ? a.adj : a.fwd;
     const double *z = a.z;
     const int n0 = A.ncol0;
     // this launch rewrites the output column and (deferred scale) the
@@ -570,7 +600,8 @@ __global__ void __launch_bounds__(BS, SHORT ? SPMV_SHORT_MINB : 3) k_lb_spmv(LbA
     auto pre = [&](int r) -> double { return has_prev ? (double)prev[r] : 0.0; };
     if (!host_product) {
         auto xl = [&](int c) -> T { return c < n0 ? x[c] : (T)z[c - n0]; };
-        if (SHORT) csr_rows_chunked<T, T>(A.ptr, A.tbase, A.cidx, chunk_vals<T>(A), A.rows, xl, pre, epi, cst);
+        if (SHORT)
+            csr_rows_chunked<T, T>(A.ptr, A.tbase, A.cidx, chunk_vals<T>(A), A.rows, xl, pre, epi, cst, tb0, tb1);
         else csr_rows_staged<T, T>(A.ptr, A.idx, csr_vals<T>(A), A.blk, A.nblk, xl, pre, epi, st);
     } else {
         // the caller's APROD already wrote the product into out
@@ -584,8 +615,8 @@ __global__ void __launch_bounds__(BS, SHORT ? SPMV_SHORT_MINB : 3) k_lb_spmv(LbA
     }
     if (last_cta(&a.ctl->ticket)) {
         tail_load(a, t);
-        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
-        const double d2 = sum_parts(a.part_dot, gridDim.x, t.red);
+        double s2, d2;
+        sum_parts2(a.part_sq, a.part_dot, gridDim.x, t.red, s2, d2);
         after_spmv<SIDE>(t, a, j, sqrt(s2), d2);
         tail_store(a, t);
     }
@@ -617,8 +648,8 @@ __global__ void __launch_bounds__(BS) k_lb_elr(LbArgs a, int j)
     }
     if (last_cta(&a.ctl->ticket)) {
         tail_load(a, t);
-        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
-        const double d2 = sum_parts(a.part_dot, gridDim.x, t.red);
+        double s2, d2;
+        sum_parts2(a.part_sq, a.part_dot, gridDim.x, t.red, s2, d2);
         after_elr<SIDE>(t, a, j, sqrt(s2), d2);
         tail_store(a, t);
     }
@@ -1256,9 +1287,8 @@ __global__ void __launch_bounds__(BS) k_lb_zelr(LbArgs a, int j)
     }
     if (last_cta(&a.ctl->ticket)) {
         tail_load(a, t);
-        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
-        const double d2 = sum_parts(a.part_dot, gridDim.x, t.red);
-        const double e2 = sum_parts(a.part_cols, gridDim.x, t.red);
+        double s2, d2, e2;
+        sum_parts3(a.part_sq, a.part_dot, a.part_cols, gridDim.x, t.red, s2, d2, e2);
         if (dot_only) {
             if (threadIdx.x == 0) {
                 t.c.elr_s = d2;
@@ -1288,16 +1318,20 @@ __global__ void __launch_bounds__(BS, ZSPMV_MINB) k_lb_zspmv(LbArgs a, int j, in
     __shared__ ChunkStage<double2> cst[SPMV_WARPS];
     __shared__ double sred[32];
     __shared__ Tail t;
-    if (a.ctl->status != 0) return;
+    const Csr &A = SIDE == 0 ? a.zadj : a.zfwd;
+    // control words first; the tile search runs while they arrive
+    const int status = a.ctl->status;
     const Pend pin = SIDE == 0 ? a.ctl->pend_u : a.ctl->pend_v;
     const Pend pprev = SIDE == 0 ? a.ctl->pend_v : a.ctl->pend_u;
-    const bool has_prev = SIDE == 1 || j > 1;
     const double coef = SIDE == 0 ? a.ctl->beta : a.ctl->alpha;
+    int tb0 = -1, tb1 = -1;
+    if (!host_product) chunk_warp_tiles(A.tbase, A.rows, tb0, tb1);
+    if (status != 0) return;
+    const bool has_prev = SIDE == 1 || j > 1;
     const double2 *x = reinterpret_cast<const double2 *>(SIDE == 0 ? ucol<double>(a, j - 1) : vcol<double>(a, j - 1));
     double2 *out = reinterpret_cast<double2 *>(SIDE == 0 ? vcol<double>(a, j - 1) : ucol<double>(a, j));
     double2 *prev = has_prev ? reinterpret_cast<double2 *>(SIDE == 0 ? vcol<double>(a, j - 2) : ucol<double>(a, j - 1))
                              : nullptr;
-    const Csr &A = SIDE == 0 ? a.zadj : a.zfwd;
     // this launch rewrites the output column and (deferred scale) the
     // previous one: their planes no longer hold them
     if (a.okU && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1325,7 +1359,8 @@ __global__ void __launch_bounds__(BS, ZSPMV_MINB) k_lb_zspmv(LbArgs a, int j, in
     auto pre = [&](int r) -> double2 { return has_prev ? prev[r] : make_double2(0.0, 0.0); };
     if (!host_product) {
         auto xl = [&](int c) -> double2 { return x[c]; };
-        csr_rows_chunked<double2, double2, ZSPMV_UNROLL>(A.ptr, A.tbase, A.cidx, A.czval, A.rows, xl, pre, epi, cst);
+        csr_rows_chunked<double2, double2, ZSPMV_UNROLL>(A.ptr, A.tbase, A.cidx, A.czval, A.rows, xl, pre, epi, cst,
+                                                         tb0, tb1);
     } else {
         const int rows = (SIDE == 0 ? a.adj.rows : a.fwd.rows) / 2;
         for (int r = blockIdx.x * BS + threadIdx.x; r < rows; r += gridDim.x * BS) epi(r, out[r], pre(r));
@@ -1340,9 +1375,8 @@ __global__ void __launch_bounds__(BS, ZSPMV_MINB) k_lb_zspmv(LbArgs a, int j, in
     }
     if (last_cta(&a.ctl->ticket)) {
         tail_load(a, t);
-        const double s2 = sum_parts(a.part_sq, gridDim.x, t.red);
-        const double d2 = sum_parts(a.part_dot, gridDim.x, t.red);
-        const double e2 = sum_parts(a.part_cols, gridDim.x, t.red);
+        double s2, d2, e2;
+        sum_parts3(a.part_sq, a.part_dot, a.part_cols, gridDim.x, t.red, s2, d2, e2);
         after_spmv<SIDE>(t, a, j, sqrt(s2), d2, e2, true);
         tail_store(a, t);
     }

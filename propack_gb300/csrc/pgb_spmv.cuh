@@ -180,17 +180,18 @@ struct ChunkStage {
     int bnd[33];  // row bounds of the tile, relative to its first entry
 };
 
-// first i in [0, n) with t[i] + kappa i >= key (non-decreasing in i, and
-// >= key at n-1), by a 32-way search of the whole warp
-__device__ __forceinline__ int warp_lower_bound(const int *__restrict__ t, int n, long long key, int kappa)
+// warp_lower_bound2: for two keys, the first i in [0, n) with
+// t[i] + kappa i >= key (non-decreasing in i, and >= key at n-1), each by a
+// 32-way search of the whole warp.
+// The two searches run in lockstep: each round issues both probes' loads
+// before either ballot, so the pair costs the round trips of one search.
+__device__ __forceinline__ void warp_lower_bound2(const int *__restrict__ t, int n, long long key0, long long key1,
+                                                  int kappa, int &r0, int &r1)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    auto ge = [&](int i) { return (long long)t[i] + (long long)kappa * i >= key; };
-    int lo = 0, hi = n;  // the answer lies in [lo, hi]
-    while (hi - lo > 32) {
-        const int step = (hi - lo + 31) / 32;
-        const unsigned m = __ballot_sync(FULL, ge(min(lo + lane * step, hi - 1)));
+    auto ge = [&](int i, int v, long long key) { return (long long)v + (long long)kappa * i >= key; };
+    auto narrow = [&](int &lo, int &hi, int step, unsigned m) {
         if (m == 0) {
             lo = min(lo + 31 * step + 1, hi);
         } else {
@@ -199,29 +200,52 @@ __device__ __forceinline__ int warp_lower_bound(const int *__restrict__ t, int n
             lo = f > 0 ? lo + (f - 1) * step + 1 : lo;
             hi = nhi;
         }
+    };
+    int lo0 = 0, hi0 = n, lo1 = 0, hi1 = n;
+    while (hi0 - lo0 > 32 || hi1 - lo1 > 32) {
+        const bool a0 = hi0 - lo0 > 32, a1 = hi1 - lo1 > 32;  // warp-uniform
+        const int st0 = (hi0 - lo0 + 31) / 32, st1 = (hi1 - lo1 + 31) / 32;
+        const int i0 = min(lo0 + lane * st0, hi0 - 1), i1 = min(lo1 + lane * st1, hi1 - 1);
+        const int v0 = a0 ? t[i0] : 0, v1 = a1 ? t[i1] : 0;
+        const unsigned m0 = __ballot_sync(FULL, a0 && ge(i0, v0, key0));
+        const unsigned m1 = __ballot_sync(FULL, a1 && ge(i1, v1, key1));
+        if (a0) narrow(lo0, hi0, st0, m0);
+        if (a1) narrow(lo1, hi1, st1, m1);
     }
     // a window of exactly 32 may hold its answer at hi (no lane probes it)
-    const unsigned m = __ballot_sync(FULL, lo + lane < hi ? ge(lo + lane) : true);
-    return m ? lo + __ffs(m) - 1 : hi;
+    const bool in0 = lo0 + lane < hi0, in1 = lo1 + lane < hi1;
+    const int v0 = in0 ? t[lo0 + lane] : 0, v1 = in1 ? t[lo1 + lane] : 0;
+    const unsigned m0 = __ballot_sync(FULL, in0 ? ge(lo0 + lane, v0, key0) : true);
+    const unsigned m1 = __ballot_sync(FULL, in1 ? ge(lo1 + lane, v1, key1) : true);
+    r0 = m0 ? lo0 + __ffs(m0) - 1 : hi0;
+    r1 = m1 ? lo1 + __ffs(m1) - 1 : hi1;
 }
 
+// the chunked schedule's tiles of this warp: a contiguous range holding an
+// equal share of the work, counted as the tiles' units plus
+// CHUNK_TILE_COST per tile (bounds, combine, epilogue), so that no warp of
+// a CTA waits long for the others at the closing reductions.  Kernels call
+// it before their first dependent load, so that its round trips overlap
+// those of their control words.
+__device__ __forceinline__ void chunk_warp_tiles(const int *__restrict__ tbase, int nrows, int &tb0, int &tb1)
+{
+    const int nwarps = gridDim.x * SPMV_WARPS;
+    const int ntiles = (nrows + 31) / 32;
+    const long long gw = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
+    const long long work = (long long)tbase[ntiles] + (long long)CHUNK_TILE_COST * ntiles;
+    warp_lower_bound2(tbase, ntiles + 1, work * gw / nwarps, work * (gw + 1) / nwarps, CHUNK_TILE_COST, tb0, tb1);
+}
+
+// tb0 < 0: the warp's tiles are found here (chunk_warp_tiles)
 template <typename VT, typename AT, int UNROLL = CHUNK_UNROLL, typename XF, typename PF, typename EPI>
 __device__ __forceinline__ void csr_rows_chunked(const int *__restrict__ ptr, const int *__restrict__ tbase,
                                                  const int *__restrict__ cidx, const VT *__restrict__ cval,
-                                                 int nrows, XF xload, PF pre_load, EPI epi, ChunkStage<AT> *stages)
+                                                 int nrows, XF xload, PF pre_load, EPI epi, ChunkStage<AT> *stages,
+                                                 int tb0 = -1, int tb1 = -1)
 {
     const int lane = threadIdx.x & 31;
     ChunkStage<AT> &cs = stages[threadIdx.x >> 5];
-    const int nwarps = gridDim.x * SPMV_WARPS;
-    const int ntiles = (nrows + 31) / 32;
-    // each warp takes a contiguous range of tiles holding an equal share of
-    // the work, counted as the tiles' units plus CHUNK_TILE_COST per tile
-    // (bounds, combine, epilogue), so that no warp of a CTA waits long for
-    // the others at the closing reductions
-    const long long gw = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
-    const long long work = (long long)tbase[ntiles] + (long long)CHUNK_TILE_COST * ntiles;
-    const int tb0 = warp_lower_bound(tbase, ntiles + 1, work * gw / nwarps, CHUNK_TILE_COST);
-    const int tb1 = warp_lower_bound(tbase, ntiles + 1, work * (gw + 1) / nwarps, CHUNK_TILE_COST);
+    if (tb0 < 0) chunk_warp_tiles(tbase, nrows, tb0, tb1);
     // a tile's bounds: lane l's row start (rows past the end are empty),
     // lane 31 also the tile's end, and the tile's units; those of the next
     // tile are loaded while the current one runs
