@@ -251,13 +251,16 @@ __global__ void k_chunk_count(const int *ptr, int rows, int *cnt)
 // entry p of tile t goes to unit tbase[t] + p % C, lane p / C.  One warp per
 // tile: its lanes read the tile's entries, which are contiguous, with
 // coalesced loads.
-__global__ void k_chunk_scatter(const int *ptr, const int *idx, const double *val, const float *valf, int rows,
-                                const int *tbase, int *cidx, double *cval, float *cvalf)
+__global__ void k_chunk_scatter(const int *__restrict__ ptr, const int *__restrict__ idx,
+                                const double *__restrict__ val, const float *__restrict__ valf, int rows,
+                                const int *__restrict__ tbase, int *__restrict__ cidx, double *__restrict__ cval,
+                                float *__restrict__ cvalf)
 {
     const int lane = threadIdx.x & 31, ntiles = (rows + 31) / 32;
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < ntiles; t += nw) {
         const int eb = ptr[32 * t], ee = ptr[min(32 * t + 32, rows)], t0 = tbase[t], C = tbase[t + 1] - t0;
+#pragma unroll 4
         for (int p = lane; p < ee - eb; p += 32) {
             const int e = eb + p;
             const size_t pos = ((size_t)t0 + p % C) * 32 + p / C;
@@ -269,13 +272,15 @@ __global__ void k_chunk_scatter(const int *ptr, const int *idx, const double *va
 }
 
 // the same for complex values (native complex operators)
-__global__ void k_chunk_scatter_z(const int *ptr, const int *idx, const double2 *val, int rows, const int *tbase,
-                                  int *cidx, double2 *cval)
+__global__ void k_chunk_scatter_z(const int *__restrict__ ptr, const int *__restrict__ idx,
+                                  const double2 *__restrict__ val, int rows, const int *__restrict__ tbase,
+                                  int *__restrict__ cidx, double2 *__restrict__ cval)
 {
     const int lane = threadIdx.x & 31, ntiles = (rows + 31) / 32;
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < ntiles; t += nw) {
         const int eb = ptr[32 * t], ee = ptr[min(32 * t + 32, rows)], t0 = tbase[t], C = tbase[t + 1] - t0;
+#pragma unroll 4
         for (int p = lane; p < ee - eb; p += 32) {
             const int e = eb + p;
             const size_t pos = ((size_t)t0 + p % C) * 32 + p / C;
@@ -366,8 +371,13 @@ __global__ void k_add_extra(int *tot, const int *cnt, const int *xptr, int cols)
 // with coalesced loads and find each entry's row among the tile's 33 row
 // starts, kept in shared memory.  The order of the atomic slots is
 // arbitrary; the keys (entry, row) are sorted per column afterwards.
-__global__ void __launch_bounds__(256) k_scatter(const int *ptr, const int *idx, int rows, const int *optr,
-                                                 int *fill, unsigned long long *key)
+// Each lane takes SCATTER_BATCH entries at a time: their index loads, then
+// their atomics, then their key stores, so that the round trips of a batch
+// overlap.
+constexpr int SCATTER_BATCH = 4;
+__global__ void __launch_bounds__(256) k_scatter(const int *__restrict__ ptr, const int *__restrict__ idx, int rows,
+                                                 const int *__restrict__ optr, int *__restrict__ fill,
+                                                 unsigned long long *__restrict__ key)
 {
     __shared__ int rbs[8][33];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, ntiles = (rows + 31) / 32;
@@ -378,16 +388,27 @@ __global__ void __launch_bounds__(256) k_scatter(const int *ptr, const int *idx,
         if (lane == 0) rb[32] = ptr[min(32 * t + 32, rows)];
         __syncwarp();
         const int eb = rb[0], ee = rb[32];
-        for (int e = eb + lane; e < ee; e += 32) {
-            // the last row of the tile that starts at or before e
-            int k = 0;
+        for (int e0 = eb + lane; e0 < ee; e0 += 32 * SCATTER_BATCH) {
+            int c[SCATTER_BATCH], p[SCATTER_BATCH];
 #pragma unroll
-            for (int st = 16; st > 0; st >>= 1)
-                if (rb[k + st] <= e) k += st;
-            const int i = 32 * t + k;
-            const int c = idx[e];
-            const int p = optr[c] + atomicAdd(&fill[c], 1);
-            key[p] = ((unsigned long long)(unsigned)e << 32) | (unsigned)i;
+            for (int u = 0; u < SCATTER_BATCH; u++) {
+                const int e = e0 + 32 * u;
+                c[u] = e < ee ? idx[e] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < SCATTER_BATCH; u++)
+                p[u] = e0 + 32 * u < ee ? optr[c[u]] + atomicAdd(&fill[c[u]], 1) : 0;
+#pragma unroll
+            for (int u = 0; u < SCATTER_BATCH; u++) {
+                const int e = e0 + 32 * u;
+                if (e >= ee) break;
+                // the last row of the tile that starts at or before e
+                int k = 0;
+#pragma unroll
+                for (int st = 16; st > 0; st >>= 1)
+                    if (rb[k + st] <= e) k += st;
+                key[p[u]] = ((unsigned long long)(unsigned)e << 32) | (unsigned)(32 * t + k);
+            }
         }
         __syncwarp();
     }
@@ -401,6 +422,25 @@ __global__ void k_segsort_small(unsigned long long *key, const int *optr, const 
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
         const int len = cnt[c], off = optr[c];
         if (len <= 1 || len > SEG_SMALL) continue;
+        if (len <= 8) {
+            // the common case, in registers: an odd-even transposition
+            // network over eight keys padded with the largest key
+            unsigned long long r[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) r[i] = i < len ? key[off + i] : ~0ull;
+#pragma unroll
+            for (int round = 0; round < 8; round++)
+#pragma unroll
+                for (int i = round & 1; i + 1 < 8; i += 2) {
+                    const unsigned long long a = r[i], b = r[i + 1];
+                    r[i] = a < b ? a : b;
+                    r[i + 1] = a < b ? b : a;
+                }
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (i < len) key[off + i] = r[i];
+            continue;
+        }
         unsigned long long v[SEG_SMALL];
         for (int i = 0; i < len; i++) v[i] = key[off + i];
         for (int i = 1; i < len; i++) {
@@ -504,14 +544,28 @@ __global__ void k_finish_t(const unsigned long long *key, const int *optr, const
 
 // without appended X entries every key slot p holds an entry of A: one
 // thread per slot (coalesced index and value writes)
+// (four slots per thread and round, so that four value gathers are in
+// flight)
 template <typename V>
-__global__ void k_finish_t_flat(const unsigned long long *key, int64_t total, const V *val, int *oidx, V *oval)
+__global__ void k_finish_t_flat(const unsigned long long *__restrict__ key, int64_t total, const V *__restrict__ val,
+                                int *__restrict__ oidx, V *__restrict__ oval)
 {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total;
-         p += (int64_t)gridDim.x * blockDim.x) {
-        const unsigned long long k = key[p];
-        oidx[p] = (int)(k & 0xffffffffull);
-        oval[p] = adj_value(val[(int)(k >> 32)]);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < total; p0 += 4 * stride) {
+        unsigned long long k[4];
+        V v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) k[u] = p0 + u * stride < total ? key[p0 + u * stride] : 0ull;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (p0 + u * stride < total) v[u] = val[(int)(k[u] >> 32)];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t p = p0 + u * stride;
+            if (p >= total) break;
+            oidx[p] = (int)(k[u] & 0xffffffffull);
+            oval[p] = adj_value(v[u]);
+        }
     }
 }
 
