@@ -375,12 +375,13 @@ def test_mixed_host_callback(golden):
 
 
 # ------------------------------------------------- Ritz vectors to the host
-@pytest.mark.parametrize("driver", ["irl", "irl_complex", "plain"])
+@pytest.mark.parametrize("driver", ["irl", "irl_complex", "plain", "irl_mixed"])
 def test_ritz_vectors_into_page_locked_arrays(driver):
     """Above 2^20 rows the drivers form the Ritz vectors in row chunks and
     copy each chunk into a page-locked U, V while the next chunk is formed;
     the caller gets the same bits as through ordinary arrays (one product
-    and one copy), and the values of the oracle."""
+    and one copy), and the values of the oracle (the mixed form: its FP64
+    refinement's products)."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(21)
     m, n, k = 1_200_000, 2_000, 4
@@ -413,8 +414,15 @@ def test_ritz_vectors_into_page_locked_arrays(driver):
         else:
             doption = np.array([np.sqrt(eps), eps ** 0.75, 0.0, 0.002])
             call = pg.zlansvd_irl if cplx else pg.lansvd_irl
-            nc, info = call(b"L", b"Y", b"Y", m, n, dim, dim - k, k, 30, op.aprod, U, sig, bnd, V, 1e-8, doption,
-                            ioption, iparm=op.iparm)
+            if driver == "irl_mixed":
+                pg.set_precision("mixed")
+            try:
+                nc, info = call(b"L", b"Y", b"Y", m, n, dim, dim - k, k, 30, op.aprod, U, sig, bnd, V, 1e-8,
+                                doption, ioption, iparm=op.iparm)
+            finally:
+                pg.set_precision("fp64")
+            if driver == "irl_mixed":
+                assert pg.get_stats()["nopx_low"] > 0, "the FP32 phase did not run"
         assert info == 0 and nc == k
         outs.append((sig.copy(), np.array(U[:, :k]), np.array(V[:, :k])))
         del U, V
@@ -422,4 +430,4 @@ def test_ritz_vectors_into_page_locked_arrays(driver):
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
     ref = oracle.svdp(S, k, irl_mode=driver != "plain", kmax=dim, tol=1e-8, v0=u0, maxiter=30)[1]
-    np.testing.assert_allclose(outs[1][0], ref, rtol=SIG_RTOL)
+    np.testing.assert_allclose(outs[1][0], ref, rtol=MIXED_SIG_RTOL if driver == "irl_mixed" else SIG_RTOL)
