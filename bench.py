@@ -719,6 +719,9 @@ def run_ours(args, wl):
             "error_vs_fp64": sig_err,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "phases_ms": phases, "host_buffers": "pinned",
+                    "phases_note": ("solve_device (the driver's solve events) includes the Ritz products, formed "
+                                    "in row chunks whose copies to the page-locked U, V run meanwhile; "
+                                    "each chunk's error-flag read waits behind the copy in flight"),
                     "pageable": {"value": e2e_pg_ms, "unit": "ms", "phases_ms": phases_pg,
                                  "host_buffers": "ordinary numpy arrays (CSR inputs, U and V), allocated once"}},
             "gpu_launches": int(sum(results[f]["launches"] for f in forms)), "roofline": dominant,
