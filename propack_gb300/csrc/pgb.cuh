@@ -413,6 +413,8 @@ const Dev &device_info();
 // gives it back.
 cudaMemPool_t lib_pool();
 void release_bounce_buffers();  // the idle pinned bounce buffers of pageable result copies
+// host -> device copy on s; pageable sources go through the bounce buffers
+void h2d_bytes(void *dst, const void *src, size_t bytes, cudaStream_t s);
 void *pool_alloc(size_t bytes, cudaStream_t s);  // zero bytes allowed; never returns null
 inline void pool_free(void *p, cudaStream_t s)
 {

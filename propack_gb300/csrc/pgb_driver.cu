@@ -1125,6 +1125,39 @@ static void d2h_columns(char *dst, size_t dpitch, const char *src, size_t spitch
     }
 }
 
+// bytes from host src to device dst on stream s: straight when src is
+// pinned (or small); otherwise through the bounce buffer, each 64 MB piece
+// copied into a half by the host pool while the other half's copy to the
+// device runs.  Returns when the buffer is free again (its last copies
+// done); the device copies are ordered on s.
+void h2d_bytes(void *dst, const void *src, size_t bytes, cudaStream_t s)
+{
+    if (bytes == 0) return;
+    if (bytes < ((size_t)4 << 20) || host_pinned(src)) {
+        PGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+        return;
+    }
+    BounceLease lease;
+    Bounce &b = lease.b;
+    HostPool &pool = HostPool::get();
+    const size_t np = (bytes + BOUNCE_BYTES - 1) / BOUNCE_BYTES;
+    for (size_t i = 0; i < np; i++) {
+        const size_t off = i * BOUNCE_BYTES, len = std::min(BOUNCE_BYTES, bytes - off);
+        char *half = b.buf + (i & 1) * BOUNCE_BYTES;
+        if (i >= 2) PGB_CUDA(cudaEventSynchronize(b.ev[i & 1]));  // piece i-2 has left this half
+        const int parts = (int)std::min<size_t>((size_t)pool.threads() * 2, std::max<size_t>(1, len >> 20));
+        const size_t step = (len + parts - 1) / parts;
+        const char *from = (const char *)src + off;
+        pool.run(parts, [&](int q) {
+            const size_t a = (size_t)q * step, e = std::min(len, a + step);
+            if (a < e) memcpy(half + a, from + a, e - a);
+        });
+        PGB_CUDA(cudaMemcpyAsync((char *)dst + off, half, len, cudaMemcpyHostToDevice, s));
+        PGB_CUDA(cudaEventRecord(b.ev[i & 1], s));
+    }
+    for (size_t h = 0; h < 2 && h < np; h++) PGB_CUDA(cudaEventSynchronize(b.ev[h]));
+}
+
 template <typename T>
 static void copy_out(Ctx &c, double *U, int ldu, double *V, int ldv, int ncols, bool du, bool dv)
 {

@@ -924,7 +924,7 @@ template <typename T>
 static T *upload(const T *p, int64_t n, cudaStream_t s)
 {
     T *d = (T *)pool_alloc(sizeof(T) * std::max<int64_t>(n, 1), s);
-    if (n > 0) PGB_CUDA(cudaMemcpyAsync(d, p, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+    if (n > 0) h2d_bytes(d, p, sizeof(T) * n, s);
     return d;
 }
 static int *upload_ptr(const int64_t *p, int rows, int64_t nnz, int *flag, cudaStream_t s)
@@ -1086,7 +1086,7 @@ static int create_zoperator(int m, int n, const int64_t *sp, const int32_t *si, 
     int *dsi = upload<int>(si, nnz, s);
     // propack_z16 is (re, im) doubles, the layout of double2
     double2 *dsv = (double2 *)pool_alloc(sizeof(double2) * std::max<int64_t>(nnz, 1), s);
-    if (nnz > 0) PGB_CUDA(cudaMemcpyAsync(dsv, sv, sizeof(double2) * nnz, cudaMemcpyHostToDevice, s));
+    if (nnz > 0) h2d_bytes(dsv, sv, sizeof(double2) * nnz, s);
     check_idx(dsi, nnz, n, dflag, s);
     int hflag = 0;
     PGB_CUDA(cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, s));
