@@ -429,5 +429,10 @@ def test_ritz_vectors_into_page_locked_arrays(driver):
     op.close()
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
+    # no misplaced rows: every chunk's vectors satisfy A v = sigma u
+    sig, Uk, Vk = outs[1]
+    for i in range(k):
+        r = S @ Vk[:, i] - sig[i] * Uk[:, i]
+        assert np.linalg.norm(r) <= 1e-7 * sig[0], (i, np.linalg.norm(r))
     ref = oracle.svdp(S, k, irl_mode=driver != "plain", kmax=dim, tol=1e-8, v0=u0, maxiter=30)[1]
     np.testing.assert_allclose(outs[1][0], ref, rtol=MIXED_SIG_RTOL if driver == "irl_mixed" else SIG_RTOL)
